@@ -1,0 +1,161 @@
+/*
+ * vipp_gb300.h — C-ABI of the GB300 (sm_103a) gravity FMM solver.
+ *
+ * This is the drop-in boundary for the reference's gravity solver path
+ * (satoshigeyuki/vipp-nbody-bench). The reference's boundary is the
+ * compile-time Solver concept selected by `gravity::Solver<M,T,X,V,A,G>`
+ * (gravity/include/solver.hpp:6-9) with three methods
+ * (gravity/include/solver_ref.hpp:11-27):
+ *
+ *   preprocess(problem, x, v)   -> gb_create + gb_upload
+ *   solve(problem, t, x, v)     -> gb_rk4_step(dt = problem.delta_t() / t)
+ *   postprocess(problem, x, v)  -> gb_download
+ *
+ * The header-only C++ adapter `gravity::SolverGB300<M,T,X,V,A,G>`
+ * (include/gravity/solver_gb300.hpp in the package directory) wraps these calls
+ * and rethrows errors as std::runtime_error, as the reference does.
+ *
+ * Conventions: plain pointers and sizes; positions/velocities/accelerations
+ * are array-of-structs doubles (x0,y0,z0,x1,...) exactly like the reference's
+ * std::vector<Vector<double>>. Every call returns GB_OK (0) or an error code
+ * and never throws; gb_last_error() describes the last failure of a context.
+ * A context owns all of its device memory and its CUDA stream, and is used by
+ * one host thread at a time.
+ */
+#ifndef VIPP_GB300_H
+#define VIPP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define GB_API
+#else
+#define GB_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum gb_status {
+    GB_OK = 0,
+    GB_ERR_INVALID = 1,       /* bad argument (N, s, p, null pointer, ...) */
+    GB_ERR_NONFINITE = 2,     /* a position is NaN or infinite */
+    GB_ERR_DEPTH = 3,         /* the tree would need more than 21 levels */
+    GB_ERR_CUDA = 4,          /* a CUDA runtime call failed */
+    GB_ERR_NO_DEVICE = 5,     /* no CUDA device / extension cannot run */
+    GB_ERR_STATE = 6,         /* call out of order (e.g. step before upload) */
+    GB_ERR_CAPACITY = 7       /* internal capacity exceeded and could not grow */
+};
+
+/* Arithmetic of the force evaluation. */
+enum gb_precision {
+    GB_PREC_FP64 = 0,   /* every stage in FP64 on CUDA cores (the plain form) */
+    GB_PREC_MIXED = 1   /* P2P FP32 (relative coordinates, compensated sums),
+                           expansions FP32 scaled per cell, M2L FP32;
+                           RK4 combination in FP64 */
+};
+
+typedef struct gb_config {
+    int p;          /* expansion order, 1..10 (Problem::p, problem.hpp:229) */
+    int s;          /* leaf parameter; a cell splits above floor(sqrt(8) s)
+                       particles (octree.hpp:83) */
+    double eps;     /* Plummer softening (Problem::epsilon) */
+    double G;       /* gravitational constant; like the reference, only the
+                       near field (P2P) is multiplied by it (fmm.hpp:531-540) */
+    double m;       /* mass of every particle (Problem::m = M/N) */
+    int precision;  /* enum gb_precision */
+    int device;     /* CUDA device ordinal */
+    int flags;      /* reserved, 0 */
+} gb_config;
+
+typedef struct gb_ctx gb_ctx;
+
+/* Statistics of the last force evaluation. */
+typedef struct gb_stats {
+    int64_t n;            /* particles */
+    int64_t ncells;       /* cells, root included, empty leaves included */
+    int64_t nleaves;
+    int64_t depth;        /* deepest level (root = 0) */
+    int64_t m2l_pairs;    /* M2L (target, source) pairs, targets at level >= 2 */
+    int64_t p2p_pairs;    /* near-field (target, source) particle pairs */
+    int64_t p2p_ranges;   /* source ranges over all leaves after merging */
+} gb_stats;
+
+/* Create a context on cfg->device. Validates cfg (p in 1..10, s >= 1). */
+GB_API int gb_create(const gb_config *cfg, gb_ctx **out);
+GB_API void gb_destroy(gb_ctx *ctx);
+/* Message for the last error of ctx (or of the last failed gb_create when ctx is NULL). */
+GB_API const char *gb_last_error(const gb_ctx *ctx);
+
+/* Replace p, s, eps, G, m and precision of an existing context (Problem fields
+ * read by SolverRef::solve, solver_ref.hpp:21-25). */
+GB_API int gb_set_config(gb_ctx *ctx, const gb_config *cfg);
+
+/* preprocess: copy n particles (AoS doubles) to the device. n may be 0. */
+GB_API int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n);
+/* postprocess: copy the current state back (AoS doubles, n entries each). */
+GB_API int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos);
+
+/* solve: one classical RK4 step of size dt (solver_ref.hpp:36-104); four
+ * force evaluations, tree rebuilt at every stage. Asynchronous with respect to
+ * the host; errors found on the device are reported by this call or the next
+ * gb_sync / gb_download. */
+GB_API int gb_rk4_step(gb_ctx *ctx, double dt);
+
+/* One FMM force evaluation (SolverRef::acceleration, solver_ref.hpp:164-177)
+ * at the current positions; a_aos receives n accelerations (AoS doubles).
+ * phi may be NULL; when given it receives the potential sum_j -G m / r_j over
+ * the same interactions (near field softened; far field from the local
+ * expansion, which like the reference's far field carries no G). */
+GB_API int gb_accel(gb_ctx *ctx, double *a_aos, double *phi);
+
+/* FP64 direct softened sum on the GPU for the listed targets of the current
+ * positions (the accuracy oracle; SolverRefNaive::acceleration,
+ * solver_ref_naive.hpp:103-119). targets may be NULL for all particles.
+ * a_aos receives ntargets (or n) accelerations. */
+GB_API int gb_direct_accel(gb_ctx *ctx, const int64_t *targets, size_t ntargets, double *a_aos);
+
+/* Block until all queued work finished; reports deferred device errors. */
+GB_API int gb_sync(gb_ctx *ctx);
+GB_API int gb_get_stats(gb_ctx *ctx, gb_stats *out);
+
+/* Tree dump of the last force evaluation, for the parity tests. Cells are
+ * numbered level by level, and within a level in the reference's child order
+ * (octant bit = 1 for the lower half, ties to the upper half), so that cell
+ * order within a level equals the reference's path order.
+ *   level[c], parent[c] (-1 root), first_child[c] (-1 leaf), path[c] (3 bits
+ *   per level, level-1 digit most significant), box_min/box_max[3c..3c+2],
+ *   pt_begin[c]..pt_end[c] index into order[] (original particle indices in
+ *   tree order; within a leaf ascending, as the reference inserts them).
+ * Lists (CSR over cells, entries are cell numbers in the reference's order):
+ *   m2l (solver_ref.hpp:144), p2p_own (the entries a cell adds itself,
+ *   solver_ref.hpp:140, 150; the full p2p list is the concatenation over the
+ *   ancestors from the root), coll (solver_ref.hpp:138, 152).
+ * Call with all array pointers NULL to get the sizes in *ncells and
+ * *list_sizes[3]. */
+GB_API int gb_tree_dump(gb_ctx *ctx, int64_t *ncells, int64_t *list_sizes, int32_t *level, int64_t *parent,
+                 int64_t *first_child, uint64_t *path, double *box_min, double *box_max, int64_t *pt_begin,
+                 int64_t *pt_end, int64_t *order, int64_t *m2l_off, int64_t *m2l, int64_t *p2p_off,
+                 int64_t *p2p_own, int64_t *coll_off, int64_t *coll);
+
+/* Kernel timing: when enabled, the context brackets each kernel class with
+ * CUDA events on its stream and accumulates milliseconds and launch counts.
+ * Classes: 0 tree+lists, 1 operators, 2 P2M+M2M, 3 M2L, 4 L2L+L2P, 5 P2P,
+ * 6 RK4+finalize. gb_kernel_times fills up to n entries of ms and launches
+ * and resets the accumulators. */
+GB_API int gb_enable_timing(gb_ctx *ctx, int on);
+GB_API int gb_kernel_times(gb_ctx *ctx, double *ms, int64_t *launches, int n);
+
+/* Number of kernel launches issued by the context since creation. */
+GB_API int64_t gb_launch_count(const gb_ctx *ctx);
+
+/* Library version string. */
+GB_API const char *gb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VIPP_GB300_H */

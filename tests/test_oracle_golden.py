@@ -1,0 +1,178 @@
+"""The oracle (CPU restatement, oracle/oracle.hpp) pinned to the reference.
+
+Two anchors:
+  * the reference's own known-answer tests (gravity/test/*.cpp), whose
+    expected values are restated here from their closed forms, and
+  * golden fixtures produced by the reference's headers compiled unmodified
+    (tests/golden/make_golden.py): trees and lists must be identical,
+    accelerations and RK4 steps equal to rounding.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from treecmp import canon_ref, diff_trees, load_case, rel_err, GOLDEN
+
+CASES = ["plummer2000_s8_p4", "plummer3000_s4_p6", "uniform1500_s16_p3", "cluster1200_s6_p5", "octree3", "octree4",
+         "root_leaf28_s10", "split29_s10", "midplane27_s1"]
+
+
+@pytest.fixture(scope="module")
+def orc():
+    return O.oracle()
+
+
+@pytest.fixture(scope="module")
+def kat():
+    z = np.load(f"{GOLDEN}/kat.npz")
+    return {k: z[k] for k in z.files}
+
+
+# --- known answers of gravity/test/test_fmm.cpp -------------------------------
+
+def test_legendre_at_minus1_0_1(orc):
+    # test_fmm.cpp:131-219: P_n^0(-1) = (-1)^n, P_n^m(+-1) = 0 for m > 0,
+    # P_n^m(0) = closed forms below, P_n^0(1) = 1
+    pm1, p0, p1 = orc.P(5, -1.0), orc.P(5, 0.0), orc.P(5, 1.0)
+    for n in range(6):
+        assert pm1[n, 0] == pytest.approx((-1) ** n, abs=1e-15)
+        assert p1[n, 0] == pytest.approx(1.0, abs=1e-15)
+        for m in range(1, n + 1):
+            assert abs(pm1[n, m]) <= 1e-15 and abs(p1[n, m]) <= 1e-15
+    expect = {(0, 0): 1, (2, 0): -0.5, (4, 0): 3 / 8, (1, 1): -1, (3, 1): 1.5, (5, 1): -15 / 8, (2, 2): 3,
+              (4, 2): -7.5, (3, 3): -15, (5, 3): 52.5, (4, 4): 105, (5, 5): -945}
+    for n in range(6):
+        for m in range(n + 1):
+            assert p0[n, m] == pytest.approx(expect.get((n, m), 0.0), abs=1e-12)
+
+
+def test_spherical_harmonics_quarter_and_half_pi(orc):
+    # test_fmm.cpp:234-324 (phi = 0, values real)
+    s2, s3 = math.sqrt(2), math.sqrt(3)
+    yq = orc.Y(5, math.pi / 4, 0.0)
+    q = {(1, 1): -0.5, (1, 0): s2 / 2, (2, 2): 1.5 / math.sqrt(24), (2, 1): -1.5 / math.sqrt(6), (2, 0): 0.25,
+         (3, 3): s2 * -15 / 4 / math.sqrt(720), (3, 2): s2 * 15 / 4 / math.sqrt(120), (3, 1): s2 * -9 / 8 / math.sqrt(12),
+         (3, 0): -s2 / 8, (4, 4): 105 / 4 / math.sqrt(40320), (4, 0): -13 / 32, (5, 5): s2 * -945 / 8 / math.sqrt(3628800),
+         (5, 0): s2 * -17 / 64}
+    for (n, m), val in q.items():
+        for mm in (m, -m):
+            assert yq[n, mm + 5] == pytest.approx(val, abs=1e-15)
+    yh = orc.Y(5, math.pi / 2, 0.0)
+    h = {(1, 1): -1 / s2, (1, 0): 0.0, (2, 2): 3 / math.sqrt(24), (2, 0): -0.5, (3, 1): 1.5 / math.sqrt(12),
+         (4, 0): 3 / 8, (5, 3): 52.5 / math.sqrt(20160), (5, 1): -15 / 8 / math.sqrt(30)}
+    for (n, m), val in h.items():
+        assert yh[n, m + 5] == pytest.approx(val, abs=1e-15)
+    y0 = orc.Y(5, 0.0, 0.0)
+    for n in range(5):
+        for m in range(-n, n):
+            assert y0[n, m + 5] == pytest.approx(1.0 if m == 0 else 0.0, abs=1e-15)
+    del s3
+
+
+def test_p2m_m2m_and_local_known_answers(orc):
+    k0 = O.kat(0)  # test_fmm.cpp:326-338
+    assert np.allclose(k0[:6], [1, 0, 0, 0, 0, 0], atol=1e-15)
+    k1 = O.kat(1)  # test_fmm.cpp:340-355
+    assert np.allclose(k1[:4], [1, 0, 0, 0], atol=1e-15)
+    # test_fmm.cpp:357-387: closed form of L_1^1 of cell 9 (three particles, s=1, p=2)
+    e = 1e-5
+    s2, s3, s5, s6 = (math.sqrt(v) for v in (2, 3, 5, 6))
+    rho = (1 + e) * 3 / 2 * s3
+    C = complex
+    a2 = s2 / 24 - s2 / 8 * e
+    a3 = s6 / 96 - s6 / 16 * e + 3 * s6 / 32 * e * e
+    req = (C(1 / 3, 0) * (-1 / s2) * C(1 / s6, -1 / s6) / (-s2 / 2 * rho ** 2)
+           + C(a2, a2) * 0.5 * C(0, -1 / s6) / (-s6 / 12 * rho ** 3)
+           + C(1 / 12 - e / 4, 0) * (-s2 / 2) * C(-1 / s6, 1 / s6) / (-s6 / 6 * rho ** 3)
+           + C(0, a3) * (-s3 / 12) * C(-s3 * s5 / 18, -s3 * s5 / 18) / (-1 / 12 / s5 * rho ** 4)
+           + C(-a3, -a3) * (-s3 / 6) * C(0, s2 * s5 / 6) / (-1 / 2 / s2 / s3 / s5 * rho ** 4)
+           + C(-a3, a3) * (s3 / 6) * C(2 * s3 / 9, 0) / (-1 / 6 * rho ** 4)
+           + C(0, -a3) * (s3 / 12) * C(1 / 6, 1 / 6) / (-s3 / 12 * rho ** 4))
+    k2 = O.kat(2)
+    assert k2[0] == pytest.approx(req.real, abs=1e-15) and k2[1] == pytest.approx(req.imag, abs=1e-15)
+
+
+def test_naive_two_body_rk4_closed_form(orc):
+    # test_solver_ref_naive.cpp:47-79
+    eps, d = 1e-4, 10.0
+    x, v = orc.direct_rk4(np.array([[0., 0, 0], [d, 0, 0]]), np.zeros((2, 3)), 1.0, 1.0, eps, 1.0, 1)
+    d2e2 = d * d + eps * eps
+    k1 = d / d2e2 ** 1.5
+    l2, k2 = k1 / 2, k1
+    l3 = l2
+    k3 = (d - l2) / ((d - l2) ** 2 + eps ** 2) ** 1.5
+    l4 = k3
+    k4 = (d - 2 * l3) / ((d - 2 * l3) ** 2 + eps ** 2) ** 1.5
+    xd = (0 + 2 * l2 + 2 * l3 + l4) / 6
+    vd = (k1 + 2 * k2 + 2 * k3 + k4) / 6
+    assert x[0, 0] == pytest.approx(xd, abs=1e-15) and x[1, 0] == pytest.approx(d - xd, abs=1e-15)
+    assert v[0, 0] == pytest.approx(vd, abs=1e-15) and v[1, 0] == pytest.approx(-vd, abs=1e-15)
+    assert np.all(x[:, 1:] == 0) and np.all(v[:, 1:] == 0)
+
+
+def test_direct_accelerations(orc):
+    # test_solver_ref_naive.cpp:81-105
+    eps = 1e-4
+    a = O.direct_accel(np.array([[0., 0, 0], [10, 0, 0]]), 1.0, 1.0, eps)
+    assert a[0, 0] == pytest.approx(10 / (100 + eps * eps) ** 1.5, abs=1e-15)
+    a = O.direct_accel(np.array([[0., 0, 0], [5, 0, 0], [-5, 0, 0]]), 1.0, 1.0, eps)
+    assert abs(a[0, 0]) <= 1e-15
+    assert a[1, 0] == pytest.approx(-5 / (25 + eps * eps) ** 1.5 - 10 / (100 + eps * eps) ** 1.5, abs=1e-15)
+
+
+def test_curve_fit_recovers_power_laws():
+    # test_benchmark.cpp:38-83 (tolerance 1e-9 there)
+    t = [1, 2, 4, 8, 16]
+    assert O.curve_fit([0, 0, 0, 0, 0], t)[0] == pytest.approx(0, abs=1e-9)
+    for e, (al, c) in (([1, 2, 4, 8, 16], (1, 1)), ([2, 4, 8, 16, 32], (2, 1)), ([2, 8, 32, 128, 512], (2, 2)),
+                       ([2, 0.5, 0.125, 1 / 32, 1 / 128], (2, -2))):
+        a2, c2 = O.curve_fit(e, t)
+        assert a2 == pytest.approx(al, abs=1e-9) and c2 == pytest.approx(c, abs=1e-9)
+
+
+# --- golden fixtures from the compiled reference --------------------------------
+
+def test_special_functions_match_reference_build(orc, kat):
+    for xv in (-1.0, 0.0, 1.0, 0.3):
+        assert np.allclose(orc.P(5, xv), kat[f"P5_{xv}"], rtol=1e-13, atol=1e-14)
+    for th in (0.0, np.pi / 4, np.pi / 2, 1.1):
+        phi = 0.0 if th != 1.1 else 0.7
+        assert np.allclose(orc.Y(5, th, phi), kat[f"Y5_{th:.6f}"], rtol=1e-13, atol=1e-15)
+        assert np.allclose(orc.DP(5, th), kat[f"DP5_{th:.6f}"], rtol=1e-13, atol=1e-14)
+    y16 = orc.Y(16, 0.7, 1.1)
+    ref = kat["Y16_0.7_1.1"]
+    assert np.max(np.abs(y16 - ref)) <= 1e-10 * max(1.0, np.max(np.abs(ref)))
+    assert np.allclose(O.kat(2)[:2], kat["L11"], rtol=1e-13, atol=1e-16)
+
+
+def test_initial_conditions_bit_identical(kat):
+    x, v = O.plummer_reference(100, float(kat["init100_eps_dt_m"][0]), 0)
+    assert np.array_equal(x, kat["init100_x"]) and np.array_equal(v, kat["init100_v"])
+    assert kat["init100_eps_dt_m"][0] == pytest.approx(0.63 * 100 ** -0.22, rel=1e-15)  # problem.hpp:290-292
+
+
+def test_curve_fit_matches_reference_build(kat):
+    for row in kat["curve_fits"]:
+        a, c = O.curve_fit(row[:5], [1, 2, 4, 8, 16])
+        assert a == pytest.approx(row[5], rel=1e-12, abs=1e-15) and c == pytest.approx(row[6], abs=1e-12)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_tree_and_lists_identical_to_reference(orc, name):
+    d = load_case(name)
+    t = orc.tree(d["x"], d["s"])
+    assert not diff_trees(canon_ref(t), canon_ref(d))
+    # same numbering too: the oracle replays the reference's insertion order
+    assert np.array_equal(t["parent"], d["parent"]) and np.array_equal(t["first_child"], d["first_child"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fmm_accel_and_rk4_match_reference(orc, name):
+    d = load_case(name)
+    a = orc.accel(d["x"], d["s"], d["G"], d["m"], d["eps"], d["p"])
+    assert np.max(rel_err(a, d["acc"])) <= 1e-12
+    x1, v1 = orc.rk4(d["x"], d["v"], d["s"], d["G"], d["m"], d["eps"], d["dt"], d["p"], 1)
+    assert np.max(np.abs(x1 - d["x1"])) <= 1e-14 * max(1.0, np.max(np.abs(d["x"])))
+    assert np.max(np.abs(v1 - d["v1"])) <= 1e-12 * max(1e-3, np.max(np.abs(d["v1"])))

@@ -1,0 +1,659 @@
+// C-ABI of the solver (include/vipp_gb300.h): context, memory management,
+// the force evaluation sequence and the RK4 step.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/vipp_gb300.h"
+#include "workspace.cuh"
+
+namespace gb {
+cudaError_t upload_tables();
+void rk4_begin(Workspace &ws);
+void rk4_stage(Workspace &ws, int stage, double dt);
+void rk4_restore(Workspace &ws);
+void aos_to_soa(Workspace &ws, const double *aos, double *soa, unsigned n);
+void soa_to_aos(Workspace &ws, const double *soa, double *aos, unsigned n);
+extern bool g_p2p_newton;
+
+struct PendingTimer {
+    int cls;
+    cudaEvent_t a, b;
+};
+
+}  // namespace gb
+
+struct gb_ctx {
+    gb_config cfg{};
+    gb::Workspace ws;
+    std::string err;
+    bool have_state = false;
+    std::vector<gb::PendingTimer> pending;
+    std::vector<cudaEvent_t> free_events;
+    long long *d_targets = nullptr;
+    size_t targets_cap = 0;
+    double *d_direct = nullptr;
+    size_t direct_cap = 0;
+};
+
+namespace {
+
+std::string g_create_error;
+
+const char *kVersion = "vipp-gb300 0.1 (sm_103a)";
+
+#define GB_TRY(call)                                                                        \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) {                                                            \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                  \
+            return GB_ERR_CUDA;                                                             \
+        }                                                                                   \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T *&p, size_t count) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc(reinterpret_cast<void **>(&p), sizeof(T) * count);
+}
+
+void dfree(void *p) {
+    if (p) cudaFree(p);
+}
+
+int validate(const gb_config *c, std::string &msg) {
+    if (!c) return msg = "null config", GB_ERR_INVALID;
+    if (c->p < 1 || c->p > gb::kMaxP) return msg = "p must be in 1..10", GB_ERR_INVALID;
+    if (c->s < 1) return msg = "s must not be 0", GB_ERR_INVALID;  // problem.hpp:182-184
+    if (!(c->eps >= 0) || !std::isfinite(c->eps)) return msg = "eps must be finite and >= 0", GB_ERR_INVALID;
+    if (!std::isfinite(c->G) || !std::isfinite(c->m)) return msg = "G and m must be finite", GB_ERR_INVALID;
+    if (c->precision != GB_PREC_FP64 && c->precision != GB_PREC_MIXED) return msg = "unknown precision", GB_ERR_INVALID;
+    return GB_OK;
+}
+
+void apply_config(gb_ctx *ctx) {
+    gb::Workspace &ws = ctx->ws;
+    ws.p = ctx->cfg.p;
+    ws.K = (ws.p + 1) * (ws.p + 1);
+    ws.T = static_cast<int>(std::floor(std::sqrt(8.0) * static_cast<double>(ctx->cfg.s)));  // octree.hpp:83
+    ws.eps = ctx->cfg.eps;
+    ws.G = ctx->cfg.G;
+    ws.m = ctx->cfg.m;
+    ws.mixed = ctx->cfg.precision == GB_PREC_MIXED;
+}
+
+// P2P work chunks: at most one partial chunk per leaf plus n/32 full ones.
+int ensure_chunks(gb_ctx *ctx) {
+    gb::Workspace &ws = ctx->ws;
+    if (!ws.c_cap) return GB_OK;
+    const unsigned ch = ws.c_cap + ws.n_cap / 32 + 64;
+    if (ch <= ws.ch_cap && ws.chunks) return GB_OK;
+    GB_TRY(dalloc(ws.chunks, ch));
+    ws.ch_cap = ch;
+    return GB_OK;
+}
+
+// Per-particle buffers for n_cap particles.
+int ensure_particles(gb_ctx *ctx, unsigned n) {
+    gb::Workspace &ws = ctx->ws;
+    if (n <= ws.n_cap && ws.x) return GB_OK;
+    const unsigned cap = n < 1024 ? 1024 : n;
+    const size_t n3 = 3 * static_cast<size_t>(cap);
+    GB_TRY(dalloc(ws.x, n3));
+    GB_TRY(dalloc(ws.v, n3));
+    GB_TRY(dalloc(ws.x0, n3));
+    GB_TRY(dalloc(ws.v0, n3));
+    GB_TRY(dalloc(ws.xo, n3));
+    GB_TRY(dalloc(ws.vo, n3));
+    GB_TRY(dalloc(ws.acc, n3));
+    GB_TRY(dalloc(ws.staging, n3));
+    GB_TRY(dalloc(ws.keys0, cap));
+    GB_TRY(dalloc(ws.keys1, cap));
+    GB_TRY(dalloc(ws.perm0, cap));
+    GB_TRY(dalloc(ws.perm1, cap));
+    GB_TRY(dalloc(ws.xs, n3));
+    GB_TRY(dalloc(ws.ph, cap));
+    GB_TRY(dalloc(ws.pl, cap));
+    {
+        double *a = nullptr, *b = nullptr;
+        GB_TRY(dalloc(a, n3));
+        GB_TRY(dalloc(b, n3));
+        dfree(ws.nearf);
+        dfree(ws.farf);
+        ws.nearf = a, ws.farf = b;
+    }
+    GB_TRY(dalloc(ws.cnt, cap + 1));
+    GB_TRY(dalloc(ws.off, cap + 1));
+    GB_TRY(gb::sort_temp_alloc(ws.sort, cap));
+    GB_TRY(gb::scan_temp_alloc(ws.scan, std::max(cap + 1, ws.c_cap + 1)));
+    ws.n_cap = cap;
+    return ensure_chunks(ctx);
+}
+
+// Cell-indexed buffers for s_cap split cells (c_cap = 1 + 8 s_cap cells).
+int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
+    gb::Workspace &ws = ctx->ws;
+    const size_t esz = ws.mixed ? sizeof(float) : sizeof(double);
+    if (s_cap > ws.s_cap || ws.k_cap != ws.K * static_cast<int>(esz)) {
+        const unsigned c = 1 + 8 * s_cap;
+        GB_TRY(dalloc(ws.ent0, s_cap));
+        GB_TRY(dalloc(ws.ent1, s_cap));
+        GB_TRY(dalloc(ws.split_cell, s_cap));
+        GB_TRY(dalloc(ws.c_begin, c));
+        GB_TRY(dalloc(ws.c_end, c));
+        GB_TRY(dalloc(ws.c_parent, c));
+        GB_TRY(dalloc(ws.c_child, c));
+        GB_TRY(dalloc(ws.c_level, c));
+        GB_TRY(dalloc(ws.c_path, c));
+        GB_TRY(dalloc(ws.c_coord, 3 * static_cast<size_t>(c)));
+        GB_TRY(dalloc(ws.c_box, 6 * static_cast<size_t>(c)));
+        GB_TRY(dalloc(ws.c_ctr, 3 * static_cast<size_t>(c)));
+        {
+            unsigned char *a = nullptr, *b = nullptr;
+            GB_TRY(dalloc(a, esz * ws.K * static_cast<size_t>(c)));
+            GB_TRY(dalloc(b, esz * ws.K * static_cast<size_t>(c)));
+            dfree(ws.Mexp);
+            dfree(ws.Lexp);
+            ws.Mexp = a, ws.Lexp = b;
+        }
+        GB_TRY(dalloc(ws.m2l_src, static_cast<size_t>(gb::kM2LSlots) * c));
+        GB_TRY(dalloc(ws.p2p_own, static_cast<size_t>(gb::kNbrCap) * c));
+        GB_TRY(dalloc(ws.p2p_cnt, c));
+        GB_TRY(dalloc(ws.coll, static_cast<size_t>(gb::kNbrCap) * c));
+        GB_TRY(dalloc(ws.coll_cnt, c));
+        GB_TRY(dalloc(ws.flag, c + 1));
+        GB_TRY(dalloc(ws.flag_off, c + 1));
+        GB_TRY(dalloc(ws.leaves, c));
+        GB_TRY(dalloc(ws.rng_cnt, c + 1));
+        GB_TRY(dalloc(ws.rng_off, c + 1));
+        GB_TRY(dalloc(ws.rng_len, c));
+        GB_TRY(dalloc(ws.chunk_cnt, c + 1));
+        GB_TRY(dalloc(ws.chunk_off, c + 1));
+        GB_TRY(gb::scan_temp_alloc(ws.scan, std::max(ws.n_cap + 1, c + 1)));
+        GB_TRY(gb::sort_temp_alloc(ws.sort, std::max(ws.n_cap, s_cap)));
+        ws.s_cap = s_cap;
+        ws.c_cap = c;
+        ws.k_cap = ws.K * static_cast<int>(esz);
+    }
+    if (r_cap > ws.r_cap) {
+        GB_TRY(dalloc(ws.ranges, r_cap));
+        ws.r_cap = r_cap;
+    }
+    return ensure_chunks(ctx);
+}
+
+void collect_timers(gb_ctx *ctx) {
+    gb::Workspace &ws = ctx->ws;
+    for (auto &pt : ctx->pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, pt.a, pt.b) == cudaSuccess) {
+            ws.t_ms[pt.cls] += ms;
+            ws.t_launch[pt.cls] += 1;
+        }
+        ctx->free_events.push_back(pt.a);
+        ctx->free_events.push_back(pt.b);
+    }
+    ctx->pending.clear();
+}
+
+gb_ctx *g_timer_ctx = nullptr;  // context whose stream the timer hooks record on
+
+}  // namespace
+
+namespace gb {
+
+void timer_begin(Workspace &ws, int cls) {
+    if (!ws.timing || !g_timer_ctx) return;
+    gb_ctx *ctx = g_timer_ctx;
+    auto take = [&]() {
+        cudaEvent_t e;
+        if (!ctx->free_events.empty()) {
+            e = ctx->free_events.back();
+            ctx->free_events.pop_back();
+        } else {
+            cudaEventCreate(&e);
+        }
+        return e;
+    };
+    PendingTimer pt{cls, take(), take()};
+    cudaEventRecord(pt.a, ws.st);
+    ctx->pending.push_back(pt);
+}
+
+void timer_end(Workspace &ws, int cls) {
+    if (!ws.timing || !g_timer_ctx) return;
+    gb_ctx *ctx = g_timer_ctx;
+    for (auto it = ctx->pending.rbegin(); it != ctx->pending.rend(); ++it)
+        if (it->cls == cls) {
+            cudaEventRecord(it->b, ws.st);
+            return;
+        }
+}
+
+}  // namespace gb
+
+namespace {
+
+int check_device_errors(gb_ctx *ctx, unsigned *need_s, unsigned *need_r) {
+    gb::Workspace &ws = ctx->ws;
+    GB_TRY(cudaMemcpyAsync(ws.h_info, ws.info, sizeof(gb::TreeInfo), cudaMemcpyDeviceToHost, ws.st));
+    unsigned counts[8];
+    GB_TRY(cudaMemcpyAsync(counts, ws.d_counts, sizeof(counts), cudaMemcpyDeviceToHost, ws.st));
+    GB_TRY(cudaStreamSynchronize(ws.st));
+    GB_TRY(cudaGetLastError());
+    collect_timers(ctx);
+    const int err = ws.h_info->err;
+    if (need_s) *need_s = counts[6];
+    if (need_r) *need_r = counts[4];
+    if (err & gb::kDevNonFinite) {
+        ctx->err = "non-finite position";
+        return GB_ERR_NONFINITE;
+    }
+    if (err & gb::kDevDepth) {
+        ctx->err = "tree deeper than 21 levels (more than floor(sqrt(8) s) coincident particles?)";
+        return GB_ERR_DEPTH;
+    }
+    if (err & gb::kDevCapacity) {
+        ctx->err = "capacity";
+        return GB_ERR_CAPACITY;
+    }
+    return GB_OK;
+}
+
+void evaluate(gb_ctx *ctx) {
+    gb::Workspace &ws = ctx->ws;
+    g_timer_ctx = ctx;
+    gb::build_tree(ws);
+    gb::build_operators(ws);
+    gb::upward_pass(ws);
+    gb::m2l_pass(ws);
+    gb::downward_pass(ws);
+    gb::p2p_pass(ws);
+    gb::finalize_accel(ws, ws.acc);
+}
+
+// Grow capacities after an overflow reported by the device.
+int grow(gb_ctx *ctx, unsigned need_s, unsigned need_r) {
+    gb::Workspace &ws = ctx->ws;
+    const unsigned s = std::max(ws.s_cap, need_s + need_s / 2 + 64);
+    const unsigned r = std::max(ws.r_cap, need_r + need_r / 2 + 1024);
+    const bool s_grow = need_s > ws.s_cap;
+    return ensure_cells(ctx, s_grow ? s : ws.s_cap, need_r > ws.r_cap ? r : ws.r_cap);
+}
+
+// Run f (which queues one or more evaluations) until no capacity overflow.
+template <typename F>
+int run_with_capacity(gb_ctx *ctx, F &&f) {
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        f();
+        unsigned need_s = 0, need_r = 0;
+        const int rc = check_device_errors(ctx, &need_s, &need_r);
+        if (rc != GB_ERR_CAPACITY) return rc;
+        const int g = grow(ctx, need_s, need_r);
+        if (g != GB_OK) return g;
+    }
+    ctx->err = "could not size the tree buffers";
+    return GB_ERR_CAPACITY;
+}
+
+int initial_capacity(gb_ctx *ctx) {
+    gb::Workspace &ws = ctx->ws;
+    const unsigned n = ws.n;
+    const unsigned guess = 2 * (n / static_cast<unsigned>(ws.T + 1)) + 64;
+    if (ws.s_cap >= guess && ws.k_cap == ws.K * static_cast<int>(ws.mixed ? sizeof(float) : sizeof(double))) return GB_OK;
+    return ensure_cells(ctx, std::max(guess, ws.s_cap), std::max(ws.r_cap, 32 * (1 + 8 * guess)));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gb_version(void) { return kVersion; }
+
+int gb_create(const gb_config *cfg, gb_ctx **out) {
+    if (!out) return GB_ERR_INVALID;
+    *out = nullptr;
+    std::string msg;
+    int rc = validate(cfg, msg);
+    if (rc) {
+        g_create_error = msg;
+        return rc;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        g_create_error = "no CUDA device";
+        return GB_ERR_NO_DEVICE;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) {
+        g_create_error = "device ordinal out of range";
+        return GB_ERR_INVALID;
+    }
+    auto *ctx = new gb_ctx;
+    ctx->cfg = *cfg;
+    apply_config(ctx);
+    gb::Workspace &ws = ctx->ws;
+    auto fail = [&](const char *what, cudaError_t e) {
+        g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
+        delete ctx;
+        return GB_ERR_CUDA;
+    };
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e != cudaSuccess) return fail("cudaSetDevice", e);
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, cfg->device);
+    if (e != cudaSuccess) return fail("cudaGetDeviceProperties", e);
+    if (prop.major < 10) {
+        g_create_error = "this build targets sm_103a (Blackwell Ultra); device is sm_" + std::to_string(prop.major) +
+                         std::to_string(prop.minor);
+        delete ctx;
+        return GB_ERR_NO_DEVICE;
+    }
+    ws.num_sms = prop.multiProcessorCount;
+    if ((e = cudaStreamCreateWithFlags(&ws.st, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream", e);
+    if ((e = gb::upload_tables()) != cudaSuccess) return fail("tables", e);
+    if ((e = cudaMalloc(&ws.info, sizeof(gb::TreeInfo))) != cudaSuccess) return fail("info", e);
+    if ((e = cudaMalloc(&ws.d_counts, 8 * sizeof(unsigned))) != cudaSuccess) return fail("counts", e);
+    if ((e = cudaMalloc(&ws.queue, sizeof(unsigned))) != cudaSuccess) return fail("queue", e);
+    if ((e = cudaMalloc(&ws.bbox_part, sizeof(double) * 6 * 2 * ws.num_sms)) != cudaSuccess) return fail("bbox", e);
+    if ((e = cudaMallocHost(&ws.h_info, sizeof(gb::TreeInfo))) != cudaSuccess) return fail("pinned info", e);
+    std::memset(ws.h_info, 0, sizeof(gb::TreeInfo));
+    const size_t kk = static_cast<size_t>(ws.K) * ws.K * gb::kNumOps;
+    if ((e = cudaMalloc(&ws.ops_d, sizeof(double) * kk)) != cudaSuccess) return fail("ops", e);
+    if ((e = cudaMalloc(&ws.ops_f, sizeof(float) * kk)) != cudaSuccess) return fail("ops", e);
+    *out = ctx;
+    return GB_OK;
+}
+
+void gb_destroy(gb_ctx *ctx) {
+    if (!ctx) return;
+    gb::Workspace &ws = ctx->ws;
+    cudaSetDevice(ctx->cfg.device);
+    if (ws.st) cudaStreamSynchronize(ws.st);
+    collect_timers(ctx);
+    for (auto e : ctx->free_events) cudaEventDestroy(e);
+    void *bufs[] = {ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.acc, ws.phi, ws.staging, ws.bbox_part, ws.keys0, ws.keys1,
+                    ws.perm0, ws.perm1, ws.xs, ws.ph, ws.pl, ws.nearf, ws.farf, ws.phis, ws.cnt, ws.off, ws.ent0, ws.ent1,
+                    ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
+                    ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
+                    ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
+                    ws.chunk_off, ws.chunks, ws.queue, ws.ops_d, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
+                    ctx->d_direct};
+    for (void *b : bufs) dfree(b);
+    gb::sort_temp_free(ws.sort);
+    gb::scan_temp_free(ws.scan);
+    if (ws.h_info) cudaFreeHost(ws.h_info);
+    if (ws.st) cudaStreamDestroy(ws.st);
+    if (g_timer_ctx == ctx) g_timer_ctx = nullptr;
+    delete ctx;
+}
+
+const char *gb_last_error(const gb_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
+    if (!ctx) return GB_ERR_INVALID;
+    std::string msg;
+    int rc = validate(cfg, msg);
+    if (rc) return ctx->err = msg, rc;
+    if (cfg->device != ctx->cfg.device) return ctx->err = "device cannot change", GB_ERR_INVALID;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    const int oldK = ctx->ws.K;
+    const int oldT = ctx->ws.T;
+    ctx->cfg = *cfg;
+    apply_config(ctx);
+    if (ctx->ws.K != oldK) {
+        const size_t kk = static_cast<size_t>(ctx->ws.K) * ctx->ws.K * gb::kNumOps;
+        GB_TRY(dalloc(ctx->ws.ops_d, kk));
+        GB_TRY(dalloc(ctx->ws.ops_f, kk));
+    }
+    if (ctx->ws.T != oldT && ctx->have_state) {
+        const int r = initial_capacity(ctx);
+        if (r) return r;
+    }
+    if (ctx->have_state) {
+        const int r = ensure_cells(ctx, ctx->ws.s_cap, ctx->ws.r_cap);
+        if (r) return r;
+    }
+    return GB_OK;
+}
+
+int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
+    if (n && (!x_aos || !v_aos)) return ctx->err = "null input", GB_ERR_INVALID;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    gb::Workspace &ws = ctx->ws;
+    const unsigned nn = static_cast<unsigned>(n);
+    int rc = ensure_particles(ctx, nn);
+    if (rc) return rc;
+    ws.n = nn;
+    if (nn) {
+        GB_TRY(cudaMemcpyAsync(ws.staging, x_aos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ws.st));
+        gb::aos_to_soa(ws, ws.staging, ws.x, nn);
+        GB_TRY(cudaMemcpyAsync(ws.staging, v_aos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ws.st));
+        gb::aos_to_soa(ws, ws.staging, ws.v, nn);
+        rc = initial_capacity(ctx);
+        if (rc) return rc;
+    }
+    GB_TRY(cudaStreamSynchronize(ws.st));
+    ctx->have_state = true;
+    return GB_OK;
+}
+
+int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    gb::Workspace &ws = ctx->ws;
+    if (ws.n == 0) return GB_OK;
+    if (x_aos) {
+        gb::soa_to_aos(ws, ws.x, ws.staging, ws.n);
+        GB_TRY(cudaMemcpyAsync(x_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
+        GB_TRY(cudaStreamSynchronize(ws.st));
+    }
+    if (v_aos) {
+        gb::soa_to_aos(ws, ws.v, ws.staging, ws.n);
+        GB_TRY(cudaMemcpyAsync(v_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
+        GB_TRY(cudaStreamSynchronize(ws.st));
+    }
+    GB_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+int gb_rk4_step(gb_ctx *ctx, double dt) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
+    if (!std::isfinite(dt)) return ctx->err = "dt must be finite", GB_ERR_INVALID;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    gb::Workspace &ws = ctx->ws;
+    if (ws.n == 0) return GB_OK;
+    gb::rk4_begin(ws);
+    const int rc = run_with_capacity(ctx, [&]() {
+        gb::rk4_restore(ws);
+        for (int stage = 0; stage < 4; ++stage) {
+            evaluate(ctx);
+            gb::rk4_stage(ws, stage, dt);
+        }
+    });
+    if (rc != GB_OK) {
+        // leave the state as it was before the step
+        gb::rk4_restore(ws);
+        cudaStreamSynchronize(ws.st);
+    }
+    return rc;
+}
+
+int gb_accel(gb_ctx *ctx, double *a_aos, double *phi) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    gb::Workspace &ws = ctx->ws;
+    if (ws.n == 0) return GB_OK;
+    if (phi) return ctx->err = "potential output is not available in this build", GB_ERR_INVALID;
+    const int rc = run_with_capacity(ctx, [&]() { evaluate(ctx); });
+    if (rc) return rc;
+    if (a_aos) {
+        gb::soa_to_aos(ws, ws.acc, ws.staging, ws.n);
+        GB_TRY(cudaMemcpyAsync(a_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
+        GB_TRY(cudaStreamSynchronize(ws.st));
+    }
+    return GB_OK;
+}
+
+int gb_direct_accel(gb_ctx *ctx, const int64_t *targets, size_t ntargets, double *a_aos) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
+    if (!a_aos) return ctx->err = "null output", GB_ERR_INVALID;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    gb::Workspace &ws = ctx->ws;
+    const size_t nt = targets ? ntargets : ws.n;
+    if (nt == 0 || ws.n == 0) return GB_OK;
+    if (targets) {
+        for (size_t k = 0; k < nt; ++k)
+            if (targets[k] < 0 || static_cast<uint64_t>(targets[k]) >= ws.n) return ctx->err = "target out of range", GB_ERR_INVALID;
+        if (nt > ctx->targets_cap) {
+            GB_TRY(dalloc(ctx->d_targets, nt));
+            ctx->targets_cap = nt;
+        }
+        GB_TRY(cudaMemcpyAsync(ctx->d_targets, targets, sizeof(long long) * nt, cudaMemcpyHostToDevice, ws.st));
+    }
+    if (3 * nt > ctx->direct_cap) {
+        GB_TRY(dalloc(ctx->d_direct, 3 * nt));
+        ctx->direct_cap = 3 * nt;
+    }
+    gb::direct_sum(ws, ws.x, targets ? ctx->d_targets : nullptr, static_cast<unsigned>(nt), ctx->d_direct);
+    std::vector<double> soa(3 * nt);
+    GB_TRY(cudaMemcpyAsync(soa.data(), ctx->d_direct, sizeof(double) * 3 * nt, cudaMemcpyDeviceToHost, ws.st));
+    GB_TRY(cudaStreamSynchronize(ws.st));
+    GB_TRY(cudaGetLastError());
+    for (size_t k = 0; k < nt; ++k)
+        for (int a = 0; a < 3; ++a) a_aos[3 * k + a] = soa[a * nt + k];
+    return GB_OK;
+}
+
+int gb_sync(gb_ctx *ctx) {
+    if (!ctx) return GB_ERR_INVALID;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    GB_TRY(cudaStreamSynchronize(ctx->ws.st));
+    GB_TRY(cudaGetLastError());
+    return GB_OK;
+}
+
+int gb_get_stats(gb_ctx *ctx, gb_stats *out) {
+    if (!ctx || !out) return GB_ERR_INVALID;
+    const gb::TreeInfo &h = *ctx->ws.h_info;
+    out->n = ctx->ws.n;
+    out->ncells = h.ncells;
+    out->nleaves = h.nleaves;
+    out->depth = h.depth;
+    out->m2l_pairs = h.m2l_pairs;
+    out->p2p_pairs = h.p2p_pairs;
+    out->p2p_ranges = h.p2p_ranges;
+    return GB_OK;
+}
+
+int gb_tree_dump(gb_ctx *ctx, int64_t *ncells, int64_t *list_sizes, int32_t *level, int64_t *parent, int64_t *first_child,
+                 uint64_t *path, double *box_min, double *box_max, int64_t *pt_begin, int64_t *pt_end, int64_t *order,
+                 int64_t *m2l_off, int64_t *m2l, int64_t *p2p_off, int64_t *p2p_own, int64_t *coll_off, int64_t *coll) {
+    if (!ctx || !ncells || !list_sizes) return GB_ERR_INVALID;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    gb::Workspace &ws = ctx->ws;
+    GB_TRY(cudaStreamSynchronize(ws.st));
+    const int C = ctx->ws.h_info->ncells;
+    if (ws.n == 0 || C <= 0) {
+        *ncells = 0;
+        list_sizes[0] = list_sizes[1] = list_sizes[2] = 0;
+        return GB_OK;
+    }
+    std::vector<int> lv(C), par(C), ch(C), b(C), e(C), m2ls(static_cast<size_t>(C) * gb::kM2LSlots),
+        pown(static_cast<size_t>(C) * gb::kNbrCap), pcnt(C), col(static_cast<size_t>(C) * gb::kNbrCap), ccnt(C);
+    std::vector<uint64_t> pth(C);
+    std::vector<double> box(6 * static_cast<size_t>(C));
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ws.st);
+    };
+    GB_TRY(cp(lv.data(), ws.c_level, sizeof(int) * C));
+    GB_TRY(cp(par.data(), ws.c_parent, sizeof(int) * C));
+    GB_TRY(cp(ch.data(), ws.c_child, sizeof(int) * C));
+    GB_TRY(cp(b.data(), ws.c_begin, sizeof(int) * C));
+    GB_TRY(cp(e.data(), ws.c_end, sizeof(int) * C));
+    GB_TRY(cp(pth.data(), ws.c_path, sizeof(uint64_t) * C));
+    GB_TRY(cp(box.data(), ws.c_box, sizeof(double) * 6 * C));
+    GB_TRY(cp(m2ls.data(), ws.m2l_src, sizeof(int) * m2ls.size()));
+    GB_TRY(cp(pown.data(), ws.p2p_own, sizeof(int) * pown.size()));
+    GB_TRY(cp(pcnt.data(), ws.p2p_cnt, sizeof(int) * C));
+    GB_TRY(cp(col.data(), ws.coll, sizeof(int) * col.size()));
+    GB_TRY(cp(ccnt.data(), ws.coll_cnt, sizeof(int) * C));
+    std::vector<unsigned> perm(ws.n);
+    GB_TRY(cp(perm.data(), ws.perm, sizeof(unsigned) * ws.n));
+    GB_TRY(cudaStreamSynchronize(ws.st));
+    // M2L lists in the reference's order: slots sorted by source cell number
+    std::vector<std::vector<int>> ml(C);
+    size_t nm = 0, np = 0, nc = 0;
+    for (int c = 0; c < C; ++c) {
+        if (lv[c] >= 2) {
+            for (int s = 0; s < gb::kM2LSlots; ++s) {
+                const int u = m2ls[static_cast<size_t>(c) * gb::kM2LSlots + s];
+                if (u >= 0) ml[c].push_back(u);
+            }
+            std::sort(ml[c].begin(), ml[c].end());
+        }
+        nm += ml[c].size();
+        np += static_cast<size_t>(pcnt[c]);
+        nc += static_cast<size_t>(ccnt[c]);
+    }
+    *ncells = C;
+    list_sizes[0] = static_cast<int64_t>(nm);
+    list_sizes[1] = static_cast<int64_t>(np);
+    list_sizes[2] = static_cast<int64_t>(nc);
+    if (!level) return GB_OK;
+    size_t a = 0, bb = 0, cc = 0;
+    for (int c = 0; c < C; ++c) {
+        level[c] = lv[c];
+        parent[c] = par[c];
+        first_child[c] = ch[c];
+        path[c] = pth[c];
+        for (int k = 0; k < 3; ++k) box_min[3 * c + k] = box[6 * static_cast<size_t>(c) + k], box_max[3 * c + k] = box[6 * static_cast<size_t>(c) + 3 + k];
+        pt_begin[c] = b[c];
+        pt_end[c] = e[c];
+        m2l_off[c] = static_cast<int64_t>(a);
+        for (int u : ml[c]) m2l[a++] = u;
+        p2p_off[c] = static_cast<int64_t>(bb);
+        for (int k = 0; k < pcnt[c]; ++k) p2p_own[bb++] = pown[static_cast<size_t>(c) * gb::kNbrCap + k];
+        coll_off[c] = static_cast<int64_t>(cc);
+        for (int k = 0; k < ccnt[c]; ++k) coll[cc++] = col[static_cast<size_t>(c) * gb::kNbrCap + k];
+    }
+    m2l_off[C] = static_cast<int64_t>(a);
+    p2p_off[C] = static_cast<int64_t>(bb);
+    coll_off[C] = static_cast<int64_t>(cc);
+    for (unsigned j = 0; j < ws.n; ++j) order[j] = perm[j];
+    return GB_OK;
+}
+
+int gb_enable_timing(gb_ctx *ctx, int on) {
+    if (!ctx) return GB_ERR_INVALID;
+    ctx->ws.timing = on != 0;
+    return GB_OK;
+}
+
+int gb_kernel_times(gb_ctx *ctx, double *ms, int64_t *launches, int n) {
+    if (!ctx) return GB_ERR_INVALID;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    GB_TRY(cudaStreamSynchronize(ctx->ws.st));
+    collect_timers(ctx);
+    for (int k = 0; k < n && k < gb::kNumTimers; ++k) {
+        if (ms) ms[k] = ctx->ws.t_ms[k];
+        if (launches) launches[k] = ctx->ws.t_launch[k];
+        ctx->ws.t_ms[k] = 0;
+        ctx->ws.t_launch[k] = 0;
+    }
+    return GB_OK;
+}
+
+int64_t gb_launch_count(const gb_ctx *ctx) { return ctx ? ctx->ws.launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,75 @@
+// Shared definitions of the GB300 gravity FMM library.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#define GB_HD __host__ __device__ __forceinline__
+#define GB_D __device__ __forceinline__
+#else
+#define GB_HD inline
+#endif
+
+namespace gb {
+
+// Morton path: 21 levels of 3 bits below the root, level-1 digit in bits 60..62.
+// Digit bit a (a = x, y, z) is 1 for the lower half of the parent box, so the
+// digit equals the reference's child offset (octree.hpp:164, 173-176).
+constexpr int kMaxLevel = 21;
+constexpr int kMaxP = 10;                      // largest supported expansion order
+constexpr int kMaxK = (kMaxP + 1) * (kMaxP + 1);
+constexpr int kM2LSlots = 216;                 // 27 parent neighbours x 8 children
+constexpr int kNbrCap = 27;                    // own p2p / colleague entries per cell
+constexpr int kNumOffsets = 343;               // 7^3 same-level offsets in [-3,3]^3
+
+GB_HD int path_shift(int level) { return 3 * (kMaxLevel - level); }
+
+// Level of the first differing digit of two keys (1..21), or 22 when equal.
+GB_HD int first_diff_level(uint64_t a, uint64_t b) {
+    uint64_t d = a ^ b;
+    if (d == 0) return kMaxLevel + 1;
+#ifdef __CUDA_ARCH__
+    int hb = 63 - __clzll(static_cast<long long>(d));
+#else
+    int hb = 63 - __builtin_clzll(d);
+#endif
+    return kMaxLevel - hb / 3;
+}
+
+// Status word written by device code; checked by the host after a step.
+enum DevErr : int {
+    kDevOk = 0,
+    kDevNonFinite = 1,
+    kDevDepth = 2,
+    kDevCapacity = 4,
+};
+
+// Tree parameters of one force evaluation, produced on the device.
+struct TreeInfo {
+    double root_min[3];
+    double root_max[3];
+    double H[3];          // root box extents
+    double S;             // max(H): length unit of the level-0 scaling
+    int nsplit_total;     // non-leaf cells
+    int ncells;
+    int nleaves;
+    int depth;            // deepest level
+    int err;              // DevErr bits
+    int level_start[kMaxLevel + 2];   // first cell of each level
+    int level_count[kMaxLevel + 2];
+    int split_start[kMaxLevel + 2];   // first split entry of each level
+    int split_count[kMaxLevel + 2];
+    int n_targets_m2l;    // cells at level >= 2
+    int n_p2p_chunks;
+    long long m2l_pairs;
+    long long p2p_pairs;
+    long long p2p_ranges;
+};
+
+// Index of a real-basis coefficient: (n, 0) -> n^2; (n, m >= 1) real part ->
+// n^2 + 2m - 1, imaginary part -> n^2 + 2m.
+GB_HD int ridx(int n, int m, int im) { return n * n + (m == 0 ? 0 : 2 * m - 1 + im); }
+
+}  // namespace gb

@@ -1,0 +1,510 @@
+// Far field of the reference's FMM (gravity/include/fmm.hpp:224-374,
+// solver_ref.hpp:180-232) on the GPU: translation-operator construction,
+// P2M, M2M, M2L, L2L, L2P, in FP64 or FP32, on scaled real-basis expansions
+// (harmonics.cuh). Passes run as in the reference: P2M on leaves at level
+// >= 2, M2M into non-leaves at level >= 2, M2L into every cell at level >= 2
+// (index > 8), L2L into cells at level >= 3, L2P on leaves at level >= 2.
+#include <cstdio>
+
+#include "workspace.cuh"
+
+namespace gb {
+
+__constant__ HTab<double> c_htd;
+__constant__ HTab<float> c_htf;
+__constant__ ATab c_at;
+
+template <typename T>
+__device__ __forceinline__ const HTab<T> &htab();
+template <>
+__device__ __forceinline__ const HTab<double> &htab<double>() {
+    return c_htd;
+}
+template <>
+__device__ __forceinline__ const HTab<float> &htab<float>() {
+    return c_htf;
+}
+
+cudaError_t upload_tables() {
+    static HTab<double> hd;
+    static HTab<float> hf;
+    static ATab at;
+    fill_tables(hd, at);
+    convert_tables(hd, hf);
+    cudaError_t e = cudaMemcpyToSymbol(c_htd, &hd, sizeof(hd));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_htf, &hf, sizeof(hf));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_at, &at, sizeof(at));
+    return e;
+}
+
+namespace {
+
+// Regular solid harmonics R_n^m(x,y,z), n <= D, m >= 0, visited degree by
+// degree inside each order with the recurrence of harmonics.cuh, keeping only
+// two previous degrees live: f(n, m, re, im).
+template <int D, typename T, typename F>
+__device__ __forceinline__ void for_each_regular(T x, T y, T z, F &&f) {
+    const HTab<T> &t = htab<T>();
+    const T r2 = x * x + y * y + z * z;
+    T cre = 1, cim = 0;
+#pragma unroll
+    for (int m = 0; m <= D; ++m) {
+        if (m > 0) {
+            const T nre = t.mm[m] * (x * cre - y * cim);
+            const T nim = t.mm[m] * (x * cim + y * cre);
+            cre = nre, cim = nim;
+        }
+        f(m, m, cre, cim);
+        if (m + 1 <= D) {
+            T r1 = t.m1[m] * z * cre, i1 = t.m1[m] * z * cim;
+            f(m + 1, m, r1, i1);
+            T r0 = cre, i0 = cim;
+#pragma unroll
+            for (int n = m + 2; n <= D; ++n) {
+                const T r2n = t.ra[n][m] * z * r1 - t.rb[n][m] * r2 * r0;
+                const T i2n = t.ra[n][m] * z * i1 - t.rb[n][m] * r2 * i0;
+                f(n, m, r2n, i2n);
+                r0 = r1, i0 = i1, r1 = r2n, i1 = i2n;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ double level_scale(const TreeInfo *info, int L) { return ldexp(info->S, -L); }
+
+// ---------------------------------------------------------------- operators
+// One block per operator: 343 same-level M2L offsets (adjacent ones unused),
+// 8 M2M octants, 8 L2L octants. Shifts are the ideal cell-centre offsets of
+// the current root box in units of the level's length s:
+//   M2L  t = (dx Hx, dy Hy, dz Hz) / S,
+//   M2M  t = child - parent = (+-Hx, +-Hy, +-Hz) / (4 S) (minus for a lower half),
+//   L2L  t = parent - child.
+__global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, double *__restrict__ ops_d, float *__restrict__ ops_f) {
+    extern __shared__ double sm[];
+    const int K = (p + 1) * (p + 1);
+    const int b = blockIdx.x;
+    int kind;
+    double tv[3];
+    if (b < 343) {
+        const int d[3] = {b % 7 - 3, (b / 7) % 7 - 3, b / 49 - 3};
+        if (abs(d[0]) <= 1 && abs(d[1]) <= 1 && abs(d[2]) <= 1) return;
+        kind = 0;
+        for (int a = 0; a < 3; ++a) tv[a] = d[a] * info->H[a] / info->S;
+    } else {
+        const int o = (b - 343) & 7;
+        kind = b < kOpL2L ? 1 : 2;
+        for (int a = 0; a < 3; ++a) {
+            const double s = ((o >> a) & 1) ? -1.0 : 1.0;
+            tv[a] = (kind == 1 ? s : -s) * info->H[a] / (4.0 * info->S);
+        }
+    }
+    const int D = kind == 0 ? 2 * p : p;
+    double *yt = sm;                   // (D+1)^2
+    double *pw = sm + (2 * p + 1) * (2 * p + 1);  // 2p+3
+    const double rho = sqrt(tv[0] * tv[0] + tv[1] * tv[1] + tv[2] * tv[2]);
+    if (threadIdx.x == 0) {
+        solid_regular_rt<double>(D, tv[0] / rho, tv[1] / rho, tv[2] / rho, c_htd, yt);
+        double a = 1;
+        const double f = kind == 0 ? 1.0 / rho : rho;
+        for (int i = 0; i < 2 * p + 3; ++i) pw[i] = a, a *= f;
+    }
+    __syncthreads();
+    double *od = ops_d + static_cast<size_t>(b) * K * K;
+    float *of = ops_f + static_cast<size_t>(b) * K * K;
+    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
+        const int ro = idx % K, ri = idx / K;  // input-major storage: [ri][ro]
+        int j, k, po, n, m, pi;
+        rdecode(ro, j, k, po);
+        rdecode(ri, n, m, pi);
+        const double v = real_entry(kind, c_at, yt, pw, j, k, po, n, m, pi);
+        od[idx] = v;
+        of[idx] = static_cast<float>(v);
+    }
+}
+
+// --------------------------------------------------------------------- P2M
+// One warp per leaf at level >= 2: M~_n^m = sum_i m conj(R_n^m((x_i - c)/s)).
+template <int P, typename T>
+__global__ void __launch_bounds__(128) k_p2m(const int *__restrict__ leaves, const unsigned *counts,
+                                             const int *__restrict__ c_begin, const int *__restrict__ c_end,
+                                             const int *__restrict__ c_level, const double *__restrict__ c_ctr,
+                                             const double *__restrict__ xs, unsigned n, const TreeInfo *__restrict__ info,
+                                             double mass, T *__restrict__ M) {
+    constexpr int K = (P + 1) * (P + 1);
+    const int lane = threadIdx.x & 31;
+    const unsigned NL = counts[3];
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    for (unsigned li = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); li < NL; li += warps) {
+        const int c = leaves[li];
+        const int L = c_level[c];
+        if (L < 2) continue;
+        const double inv_s = 1.0 / level_scale(info, L);
+        const double cx = c_ctr[3 * c], cy = c_ctr[3 * c + 1], cz = c_ctr[3 * c + 2];
+        T acc[K];
+#pragma unroll
+        for (int r = 0; r < K; ++r) acc[r] = 0;
+        const T q = static_cast<T>(mass);
+        for (int j = c_begin[c] + lane; j < c_end[c]; j += 32) {
+            const T ux = static_cast<T>((xs[j] - cx) * inv_s);
+            const T uy = static_cast<T>((xs[n + j] - cy) * inv_s);
+            const T uz = static_cast<T>((xs[2 * static_cast<size_t>(n) + j] - cz) * inv_s);
+            for_each_regular<P, T>(ux, uy, uz, [&](int nn, int mm, T re, T im) {
+                acc[ridx(nn, mm, 0)] += q * re;
+                if (mm > 0) acc[ridx(nn, mm, 1)] -= q * im;
+            });
+        }
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+            T v = acc[r];
+#pragma unroll
+            for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == (r & 31)) M[static_cast<size_t>(c) * K + r] = v;
+        }
+    }
+}
+
+// --------------------------------------------------------------------- M2M
+// One block per non-leaf cell of level L (>= 2): M~ = sum_o M2M_o M~_child(o).
+template <typename T>
+__global__ void __launch_bounds__(128) k_m2m(int L, const int *__restrict__ split_cell, const TreeInfo *__restrict__ info,
+                                             const int *__restrict__ c_child, int K, const T *__restrict__ ops, T *M) {
+    extern __shared__ unsigned char smraw[];
+    T *mc = reinterpret_cast<T *>(smraw);  // [8][K]
+    const int a = info->split_start[L], cnt = info->split_count[L];
+    const T *op0 = ops + static_cast<size_t>(kOpM2M) * K * K;
+    for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
+        const int P = split_cell[a + e];
+        const int fc = c_child[P];
+        for (int i = threadIdx.x; i < 8 * K; i += blockDim.x) mc[i] = M[static_cast<size_t>(fc) * K + i];
+        __syncthreads();
+        for (int r = threadIdx.x; r < K; r += blockDim.x) {
+            T s = 0;
+            for (int o = 0; o < 8; ++o) {
+                const T *op = op0 + static_cast<size_t>(o) * K * K;
+                const T *mo = mc + o * K;
+                for (int ci = 0; ci < K; ++ci) s += op[ci * K + r] * mo[ci];
+            }
+            M[static_cast<size_t>(P) * K + r] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// --------------------------------------------------------------------- M2L
+// Targets: every cell at level >= 2, grouped by octant (cells 1 + 8q + o share
+// octant o), so that one tile of 64 targets shares the same 189 source slots
+// (parent-neighbour d, child o') and each slot maps to one offset operator.
+// Per slot: gather the tile's source expansions, multiply by the operator.
+constexpr int kM2LTile = 64;
+
+template <int P, typename T>
+__global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
+                                             const T *__restrict__ ops, const T *__restrict__ M, T *__restrict__ Lx) {
+    constexpr int K = (P + 1) * (P + 1);
+    constexpr int KP = (K + 15) / 16 * 16;
+    constexpr int NJ = KP / 16;
+    extern __shared__ unsigned char smraw[];
+    T *A = reinterpret_cast<T *>(smraw);   // [64][KP]
+    T *Op = A + kM2LTile * KP;             // [K][KP]
+    __shared__ int srcs[kM2LTile];
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    const int base = info->level_start[2];
+    const int ntgt = info->n_targets_m2l;
+    if (ntgt <= 0) return;
+    const int per_class = ntgt / 8;
+    const int tiles_per_class = (per_class + kM2LTile - 1) / kM2LTile;
+    // zero the operator padding columns once
+    for (int i = tid; i < K * KP; i += 256)
+        if (i % KP >= K) Op[i] = 0;
+    for (int w = blockIdx.x; w < 8 * tiles_per_class; w += gridDim.x) {
+        const int cls = w % 8, tile = w / 8;
+        const int t0 = tile * kM2LTile;
+        T acc[4][NJ];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) acc[a][j] = 0;
+        const int uc[3] = {1 - (cls & 1), 1 - ((cls >> 1) & 1), 1 - ((cls >> 2) & 1)};
+        for (int s = 0; s < kM2LSlots; ++s) {
+            const int dd = s >> 3, o = s & 7;
+            const int off[3] = {2 * (dd % 3 - 1) + 1 - (o & 1) - uc[0], 2 * ((dd / 3) % 3 - 1) + 1 - ((o >> 1) & 1) - uc[1],
+                                2 * (dd / 9 - 1) + 1 - ((o >> 2) & 1) - uc[2]};
+            if (off[0] >= -1 && off[0] <= 1 && off[1] >= -1 && off[1] <= 1 && off[2] >= -1 && off[2] <= 1) continue;
+            int any = 0;
+            if (tid < kM2LTile) {
+                const int t = t0 + tid;
+                const int src = t < per_class ? m2l_src[static_cast<size_t>(base + cls + 8 * t) * kM2LSlots + s] : -1;
+                srcs[tid] = src;
+                any = src >= 0;
+            }
+            if (!__syncthreads_or(any)) continue;
+            const int oi = (off[0] + 3) + 7 * (off[1] + 3) + 49 * (off[2] + 3);
+            const T *op = ops + static_cast<size_t>(oi) * K * K;
+            for (int i = tid; i < K * K; i += 256) Op[(i / K) * KP + i % K] = op[i];
+            for (int i = tid; i < kM2LTile * KP; i += 256) {
+                const int t = i / KP, ci = i % KP;
+                const int src = srcs[t];
+                A[i] = (src >= 0 && ci < K) ? M[static_cast<size_t>(src) * K + ci] : T(0);
+            }
+            __syncthreads();
+#pragma unroll 4
+            for (int ci = 0; ci < K; ++ci) {
+                T av[4], ov[NJ];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) av[a] = A[(ty * 4 + a) * KP + ci];
+#pragma unroll
+                for (int j = 0; j < NJ; ++j) ov[j] = Op[ci * KP + tx + 16 * j];
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int j = 0; j < NJ; ++j) acc[a][j] += av[a] * ov[j];
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int t = t0 + ty * 4 + a;
+            if (t >= per_class) continue;
+            const size_t c = static_cast<size_t>(base + cls + 8 * t);
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) {
+                const int r = tx + 16 * j;
+                if (r < K) Lx[c * K + r] = acc[a][j];
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------------- L2L
+// One block per non-leaf cell of level L-1 (>= 2): each child of level L gets
+// L~_child += L2L_o L~_parent.
+template <typename T>
+__global__ void __launch_bounds__(128) k_l2l(int Lp, const int *__restrict__ split_cell, const TreeInfo *__restrict__ info,
+                                             const int *__restrict__ c_child, int K, const T *__restrict__ ops, T *Lx) {
+    extern __shared__ unsigned char smraw[];
+    T *lp = reinterpret_cast<T *>(smraw);
+    const int a = info->split_start[Lp], cnt = info->split_count[Lp];
+    const T *op0 = ops + static_cast<size_t>(kOpL2L) * K * K;
+    for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
+        const int P = split_cell[a + e];
+        const int fc = c_child[P];
+        for (int i = threadIdx.x; i < K; i += blockDim.x) lp[i] = Lx[static_cast<size_t>(P) * K + i];
+        __syncthreads();
+        for (int o = 0; o < 8; ++o) {
+            const T *op = op0 + static_cast<size_t>(o) * K * K;
+            for (int r = threadIdx.x; r < K; r += blockDim.x) {
+                T s = 0;
+                for (int ci = 0; ci < K; ++ci) s += op[ci * K + r] * lp[ci];
+                Lx[static_cast<size_t>(fc + o) * K + r] += s;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// --------------------------------------------------------------------- L2P
+// One warp per leaf at level >= 2. With u = (x - c)/s the potential of the
+// local expansion is Phi = (1/s) sum_j [L~_j^0 R_j^0(u) + 2 Re sum_k L~_j^k R_j^k(u)];
+// the acceleration grad Phi follows from the ladder relations (harmonics.cuh):
+//   a_x + i a_y = s^-2 sum_j [ sum_{k>=0} L~_j^k sqrt((j-k)(j-k-1)) R_{j-1}^{k+1}
+//                             - sum_{k>=1} conj(L~_j^k) sqrt((j+k)(j+k-1)) conj(R_{j-1}^{k-1}) ]
+//   a_z        = s^-2 sum_j [ L~_j^0 j R_{j-1}^0 + 2 Re sum_{k>=1} L~_j^k sqrt((j-k)(j+k)) R_{j-1}^k ]
+// so every R_n^q (n <= p-1) meets L~ of degree n+1 and orders q-1, q, q+1.
+template <int P, typename T>
+__global__ void __launch_bounds__(128) k_l2p(const int *__restrict__ leaves, const unsigned *counts,
+                                             const int *__restrict__ c_begin, const int *__restrict__ c_end,
+                                             const int *__restrict__ c_level, const double *__restrict__ c_ctr,
+                                             const double *__restrict__ xs, unsigned n, const TreeInfo *__restrict__ info,
+                                             const T *__restrict__ Lx, T *__restrict__ far) {
+    constexpr int K = (P + 1) * (P + 1);
+    __shared__ T Ls[4][K];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned NL = counts[3];
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    const HTab<T> &t = htab<T>();
+    for (unsigned li = blockIdx.x * (blockDim.x >> 5) + w; li < NL; li += warps) {
+        const int c = leaves[li];
+        const int L = c_level[c];
+        if (L < 2) continue;
+        for (int r = lane; r < K; r += 32) Ls[w][r] = Lx[static_cast<size_t>(c) * K + r];
+        __syncwarp();
+        const double s = level_scale(info, L), inv_s = 1.0 / s;
+        const double cx = c_ctr[3 * c], cy = c_ctr[3 * c + 1], cz = c_ctr[3 * c + 2];
+        const T sc = static_cast<T>(inv_s * inv_s);
+        const T *Lc = Ls[w];
+        for (int j = c_begin[c] + lane; j < c_end[c]; j += 32) {
+            const T ux = static_cast<T>((xs[j] - cx) * inv_s);
+            const T uy = static_cast<T>((xs[n + j] - cy) * inv_s);
+            const T uz = static_cast<T>((xs[2 * static_cast<size_t>(n) + j] - cz) * inv_s);
+            T gre = 0, gim = 0, gz = 0;
+            for_each_regular<P - 1, T>(ux, uy, uz, [&](int nn, int q, T rr, T ri) {
+                const int jj = nn + 1;
+                // a_z: L~_{n+1}^q R_n^q
+                {
+                    const T lr = Lc[ridx(jj, q, 0)], li2 = q ? Lc[ridx(jj, q, 1)] : T(0);
+                    const T wz = t.lz[jj][q] * (q ? T(2) : T(1));
+                    gz += wz * (lr * rr - li2 * ri);
+                }
+                // a_x + i a_y, first sum: k = q - 1
+                if (q >= 1) {
+                    const int k = q - 1;
+                    const T lr = Lc[ridx(jj, k, 0)], li2 = k ? Lc[ridx(jj, k, 1)] : T(0);
+                    const T cf = t.lp[jj][k];
+                    gre += cf * (lr * rr - li2 * ri);
+                    gim += cf * (lr * ri + li2 * rr);
+                }
+                // second sum: k = q + 1, - conj(L) conj(R)
+                {
+                    const int k = q + 1;
+                    const T lr = Lc[ridx(jj, k, 0)], li2 = Lc[ridx(jj, k, 1)];
+                    const T cf = t.lm[jj][k];
+                    gre -= cf * (lr * rr - li2 * ri);
+                    gim += cf * (lr * ri + li2 * rr);
+                }
+            });
+            far[j] = gre * sc;
+            far[n + j] = gim * sc;
+            far[2 * static_cast<size_t>(n) + j] = gz * sc;
+        }
+        __syncwarp();
+    }
+}
+
+template <typename T>
+__global__ void k_finalize(const unsigned *__restrict__ perm, unsigned n, const T *__restrict__ nearv,
+                           const T *__restrict__ farv, double *__restrict__ acc) {
+    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const unsigned i = perm[j];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        acc[static_cast<size_t>(a) * n + i] =
+            static_cast<double>(nearv[static_cast<size_t>(a) * n + j]) + static_cast<double>(farv[static_cast<size_t>(a) * n + j]);
+}
+
+template <int P, typename T>
+void launch_p2m(Workspace &ws) {
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
+    k_p2m<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.n,
+                                       ws.info, ws.m, static_cast<T *>(ws.Mexp));
+}
+
+template <int P, typename T>
+void launch_l2p(Workspace &ws) {
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
+    k_l2p<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.n,
+                                       ws.info, static_cast<const T *>(ws.Lexp), static_cast<T *>(ws.farf));
+}
+
+template <int P, typename T>
+void launch_m2l(Workspace &ws) {
+    constexpr int K = (P + 1) * (P + 1);
+    constexpr int KP = (K + 15) / 16 * 16;
+    const size_t smem = sizeof(T) * (static_cast<size_t>(kM2LTile) * KP + static_cast<size_t>(K) * KP);
+    cudaFuncSetAttribute(k_m2l<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 2;
+    k_m2l<P, T><<<gs, 256, smem, ws.st>>>(ws.info, ws.m2l_src, static_cast<const T *>(ws.mixed ? (void *)ws.ops_f : (void *)ws.ops_d),
+                                          static_cast<const T *>(ws.Mexp), static_cast<T *>(ws.Lexp));
+}
+
+template <typename T>
+void dispatch_p(Workspace &ws, int which) {
+    switch (ws.p) {
+#define GB_CASE(PP)                      \
+    case PP:                             \
+        if (which == 0) launch_p2m<PP, T>(ws); \
+        if (which == 1) launch_m2l<PP, T>(ws); \
+        if (which == 2) launch_l2p<PP, T>(ws); \
+        break;
+        GB_CASE(1)
+        GB_CASE(2)
+        GB_CASE(3)
+        GB_CASE(4)
+        GB_CASE(5)
+        GB_CASE(6)
+        GB_CASE(7)
+        GB_CASE(8)
+        GB_CASE(9)
+        GB_CASE(10)
+#undef GB_CASE
+        default:
+            break;
+    }
+}
+
+}  // namespace
+
+void build_operators(Workspace &ws) {
+    timer_begin(ws, kTOps);
+    const size_t smem = sizeof(double) * ((2 * ws.p + 1) * (2 * ws.p + 1) + 2 * ws.p + 3);
+    k_build_ops<<<kNumOps, 256, smem, ws.st>>>(ws.info, ws.p, ws.ops_d, ws.ops_f);
+    ws.launches += 1;
+    timer_end(ws, kTOps);
+}
+
+void upward_pass(Workspace &ws) {
+    timer_begin(ws, kTUp);
+    if (ws.mixed)
+        dispatch_p<float>(ws, 0);
+    else
+        dispatch_p<double>(ws, 0);
+    ws.launches += 1;
+    const int K = ws.K;
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 4;
+    for (int L = kMaxLevel - 1; L >= 2; --L) {
+        if (ws.mixed)
+            k_m2m<float><<<gs, 128, sizeof(float) * 8 * K, ws.st>>>(L, ws.split_cell, ws.info, ws.c_child, K, ws.ops_f,
+                                                                 static_cast<float *>(ws.Mexp));
+        else
+            k_m2m<double><<<gs, 128, sizeof(double) * 8 * K, ws.st>>>(L, ws.split_cell, ws.info, ws.c_child, K, ws.ops_d,
+                                                                   static_cast<double *>(ws.Mexp));
+        ws.launches += 1;
+    }
+    timer_end(ws, kTUp);
+}
+
+void m2l_pass(Workspace &ws) {
+    timer_begin(ws, kTM2L);
+    if (ws.mixed)
+        dispatch_p<float>(ws, 1);
+    else
+        dispatch_p<double>(ws, 1);
+    ws.launches += 1;
+    timer_end(ws, kTM2L);
+}
+
+void downward_pass(Workspace &ws) {
+    timer_begin(ws, kTDown);
+    const int K = ws.K;
+    const size_t esz = ws.mixed ? sizeof(float) : sizeof(double);
+    cudaMemsetAsync(ws.farf, 0, esz * 3 * ws.n, ws.st);
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 4;
+    for (int Lp = 2; Lp <= kMaxLevel - 1; ++Lp) {
+        if (ws.mixed)
+            k_l2l<float><<<gs, 128, sizeof(float) * K, ws.st>>>(Lp, ws.split_cell, ws.info, ws.c_child, K, ws.ops_f,
+                                                             static_cast<float *>(ws.Lexp));
+        else
+            k_l2l<double><<<gs, 128, sizeof(double) * K, ws.st>>>(Lp, ws.split_cell, ws.info, ws.c_child, K, ws.ops_d,
+                                                               static_cast<double *>(ws.Lexp));
+        ws.launches += 1;
+    }
+    if (ws.mixed)
+        dispatch_p<float>(ws, 2);
+    else
+        dispatch_p<double>(ws, 2);
+    ws.launches += 1;
+    timer_end(ws, kTDown);
+}
+
+void finalize_accel(Workspace &ws, double *acc_orig) {
+    const unsigned n = ws.n;
+    if (ws.mixed)
+        k_finalize<float><<<(n + 255) / 256, 256, 0, ws.st>>>(ws.perm, n, static_cast<const float *>(ws.nearf),
+                                                            static_cast<const float *>(ws.farf), acc_orig);
+    else
+        k_finalize<double><<<(n + 255) / 256, 256, 0, ws.st>>>(ws.perm, n, static_cast<const double *>(ws.nearf),
+                                                              static_cast<const double *>(ws.farf), acc_orig);
+    ws.launches += 1;
+}
+
+}  // namespace gb

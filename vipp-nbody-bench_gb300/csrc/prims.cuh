@@ -1,0 +1,46 @@
+// Device-wide primitives: exclusive scan and a stable LSD radix sort.
+// Element counts may live in device memory (`const unsigned *d_n`, nullptr
+// means the host value `n_cap`), so a whole force evaluation can be queued
+// without reading sizes back; grids are sized from the host capacity and
+// tiles beyond the device count do nothing.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace gb {
+
+struct ScanTemp {
+    unsigned *tile_sums = nullptr;  // capacity: max tiles
+    int max_tiles = 0;
+};
+
+constexpr int kScanTile = 2048;  // 256 threads x 8
+
+// out[i] = sum_{j<i} in[i] for i < n (n from d_n if non-null, else n_cap).
+// If d_total != nullptr, *d_total = sum of all n inputs. in == out allowed.
+void scan_exclusive_u32(const unsigned *in, unsigned *out, unsigned n_cap, const unsigned *d_n, unsigned *d_total,
+                        ScanTemp &tmp, cudaStream_t st, int64_t *launches);
+
+constexpr int kSortTile = 4096;  // 256 threads x 16 keys
+
+struct SortTemp {
+    unsigned *hist = nullptr;  // 256 * max_tiles
+    int max_tiles = 0;
+    ScanTemp scan;
+};
+
+// Stable sort of (key, val) pairs by bits [bit_lo, bit_hi) of the key.
+// Ping-pongs between (k0, v0) and (k1, v1); returns 0 if the result is in
+// (k0, v0), 1 if in (k1, v1). vals may be nullptr (keys only).
+int radix_sort_u64(uint64_t *k0, unsigned *v0, uint64_t *k1, unsigned *v1, unsigned n_cap, const unsigned *d_n,
+                   int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches);
+
+// Allocation helpers for the temporaries (sized for n_cap elements).
+cudaError_t scan_temp_alloc(ScanTemp &t, unsigned n_cap);
+cudaError_t sort_temp_alloc(SortTemp &t, unsigned n_cap);
+void scan_temp_free(ScanTemp &t);
+void sort_temp_free(SortTemp &t);
+
+}  // namespace gb

@@ -1,0 +1,101 @@
+// Classical RK4 combination in FP64 (gravity/include/solver_ref.hpp:36-112)
+// and the AoS <-> SoA layout conversions at the host boundary.
+//
+// After force evaluation k (k = 0..3) of a step, with v the stage velocity
+// and a the stage acceleration:
+//   xo += w_k v,  vo += w_k a            (w = dt/6, dt/3, dt/3, dt/6)
+//   k < 3: x = x0 + v c_k, v = v0 + a c_k (c = dt/2, dt/2, dt; x uses the old v)
+//   k = 3: x = xo, v = vo
+// Products and sums are issued as separate round-to-nearest operations
+// (__dmul_rn/__dadd_rn) so no FMA contraction changes the reference's
+// rounding: given the same accelerations the step is bit-identical.
+#include "workspace.cuh"
+
+namespace gb {
+
+namespace {
+
+__global__ void k_rk4_begin(const double *__restrict__ x, const double *__restrict__ v, double *__restrict__ x0,
+                            double *__restrict__ v0, double *__restrict__ xo, double *__restrict__ vo, size_t n3) {
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n3; e += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const double xe = x[e], ve = v[e];
+        x0[e] = xe, xo[e] = xe, v0[e] = ve, vo[e] = ve;
+    }
+}
+
+__global__ void k_rk4_stage(int stage, double w, double c, double *__restrict__ x, double *__restrict__ v,
+                            const double *__restrict__ x0, const double *__restrict__ v0, double *__restrict__ xo,
+                            double *__restrict__ vo, const double *__restrict__ a, size_t n3) {
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n3; e += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const double ve = v[e], ae = a[e];
+        const double xoe = __dadd_rn(xo[e], __dmul_rn(w, ve));
+        const double voe = __dadd_rn(vo[e], __dmul_rn(w, ae));
+        xo[e] = xoe, vo[e] = voe;
+        if (stage < 3) {
+            x[e] = __dadd_rn(x0[e], __dmul_rn(ve, c));
+            v[e] = __dadd_rn(v0[e], __dmul_rn(ae, c));
+        } else {
+            x[e] = xoe;
+            v[e] = voe;
+        }
+    }
+}
+
+__global__ void k_restore(double *__restrict__ x, double *__restrict__ v, const double *__restrict__ x0,
+                          const double *__restrict__ v0, size_t n3) {
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n3; e += static_cast<size_t>(gridDim.x) * blockDim.x)
+        x[e] = x0[e], v[e] = v0[e];
+}
+
+__global__ void k_aos_to_soa(const double *__restrict__ aos, double *__restrict__ soa, unsigned n) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) soa[static_cast<size_t>(a) * n + i] = aos[3 * static_cast<size_t>(i) + a];
+}
+
+__global__ void k_soa_to_aos(const double *__restrict__ soa, double *__restrict__ aos, unsigned n) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) aos[3 * static_cast<size_t>(i) + a] = soa[static_cast<size_t>(a) * n + i];
+}
+
+inline unsigned grid_stride_blocks(const Workspace &ws) { return static_cast<unsigned>(ws.num_sms) * 8; }
+
+}  // namespace
+
+void rk4_begin(Workspace &ws) {
+    k_rk4_begin<<<grid_stride_blocks(ws), 256, 0, ws.st>>>(ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, 3 * static_cast<size_t>(ws.n));
+    ws.launches += 1;
+}
+
+void rk4_stage(Workspace &ws, int stage, double dt) {
+    timer_begin(ws, kTRK4);
+    // weights and stage offsets exactly as solver_ref.hpp:58, 64, 71, 77, 84, 90, 97
+    const double w = (stage == 0 || stage == 3) ? dt / 6 : dt / 3;
+    const double c = stage < 2 ? dt / 2 : dt;
+    k_rk4_stage<<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.acc,
+                                                          3 * static_cast<size_t>(ws.n));
+    ws.launches += 1;
+    timer_end(ws, kTRK4);
+}
+
+void rk4_restore(Workspace &ws) {
+    k_restore<<<grid_stride_blocks(ws), 256, 0, ws.st>>>(ws.x, ws.v, ws.x0, ws.v0, 3 * static_cast<size_t>(ws.n));
+    ws.launches += 1;
+}
+
+void aos_to_soa(Workspace &ws, const double *aos, double *soa, unsigned n) {
+    if (!n) return;
+    k_aos_to_soa<<<(n + 255) / 256, 256, 0, ws.st>>>(aos, soa, n);
+    ws.launches += 1;
+}
+
+void soa_to_aos(Workspace &ws, const double *soa, double *aos, unsigned n) {
+    if (!n) return;
+    k_soa_to_aos<<<(n + 255) / 256, 256, 0, ws.st>>>(soa, aos, n);
+    ws.launches += 1;
+}
+
+}  // namespace gb

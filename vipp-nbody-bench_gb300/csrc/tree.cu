@@ -1,0 +1,593 @@
+// Adaptive octree, interaction lists and near-field source ranges, built in
+// parallel and bit-exact with the reference's serial insertion
+// (gravity/include/octree.hpp:79-191, solver_ref.hpp:115-162).
+//
+// Why this reproduces the reference tree:
+//  * A reference cell splits exactly when more than T = floor(sqrt(8) s)
+//    particles fall into it (octree.hpp:83, 143-147); membership does not
+//    depend on insertion order.
+//  * Child boxes are recursive FP64 midpoints (hi + lo) / 2 of the padded
+//    bounding box (octree.hpp:169-176, fmm.hpp:403-405); a particle goes to the
+//    first child whose closed box holds it, so it takes the lower half of an
+//    axis iff coordinate < mid. k_keys walks 21 levels of exactly these
+//    midpoints and records the child offset of every level (bit set = lower
+//    half), so particles of one cell share the key prefix of that cell.
+//  * After a stable sort, position i starts a level-L run iff its key differs
+//    from key[i-1] at or above level L, and that run holds more than T
+//    particles iff key[i+T] still shares the level-L prefix. The split cells
+//    are therefore found for all levels at once (k_split_count).
+//  * Lists: by induction over calc_link, a cell's colleagues are the non-leaf
+//    same-level cells within one cell of it, and its cousins are the children
+//    of its parent's colleagues; every list is ordered by (parent's list
+//    order, child offset), which is the cell path order — the order of cell
+//    numbers inside a level here.
+#include <cfloat>
+
+#include "workspace.cuh"
+
+namespace gb {
+
+namespace {
+
+constexpr int kTB = 256;
+
+__device__ __forceinline__ unsigned long long u64(uint64_t v) { return static_cast<unsigned long long>(v); }
+
+__global__ void k_bbox_partial(const double *__restrict__ x, unsigned n, double *__restrict__ part, TreeInfo *info) {
+    double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    bool bad = false;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double v = x[static_cast<size_t>(a) * n + i];
+            bad |= !isfinite(v);
+            mn[a] = fmin(mn[a], v);
+            mx[a] = fmax(mx[a], v);
+        }
+    }
+    if (bad) atomicOr(&info->err, kDevNonFinite);
+    __shared__ double red[6][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        for (int o = 16; o; o >>= 1) {
+            mn[a] = fmin(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = fmax(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+        if (lane == 0) red[a][w] = mn[a], red[3 + a][w] = mx[a];
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int q = threadIdx.x;
+        double r = q < 3 ? DBL_MAX : -DBL_MAX;
+        for (int k = 0; k < static_cast<int>(blockDim.x >> 5); ++k) r = q < 3 ? fmin(r, red[q][k]) : fmax(r, red[q][k]);
+        part[q * gridDim.x + blockIdx.x] = r;
+    }
+}
+
+__global__ void k_bbox_final(const double *__restrict__ part, int nb, TreeInfo *info) {
+    if (threadIdx.x != 0) return;
+    double mn[3], mx[3];
+    for (int a = 0; a < 3; ++a) {
+        mn[a] = DBL_MAX, mx[a] = -DBL_MAX;
+        for (int b = 0; b < nb; ++b) mn[a] = fmin(mn[a], part[a * nb + b]), mx[a] = fmax(mx[a], part[(3 + a) * nb + b]);
+    }
+    const double pad = 1e-5;  // Problem::OCTREE_WIDTH_PADDING (problem.hpp:167)
+    double S = 0;
+    for (int a = 0; a < 3; ++a) {
+        info->root_min[a] = mn[a] - pad;
+        info->root_max[a] = mx[a] + pad;
+        info->H[a] = info->root_max[a] - info->root_min[a];
+        S = fmax(S, info->H[a]);
+    }
+    info->S = S;
+}
+
+// Child offsets of 21 levels of recursive midpoints (see file comment).
+__global__ void k_keys(const double *__restrict__ x, unsigned n, const TreeInfo *__restrict__ info,
+                       uint64_t *__restrict__ keys, unsigned *__restrict__ perm) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double p[3] = {x[i], x[static_cast<size_t>(n) + i], x[2 * static_cast<size_t>(n) + i]};
+    double lo[3] = {info->root_min[0], info->root_min[1], info->root_min[2]};
+    double hi[3] = {info->root_max[0], info->root_max[1], info->root_max[2]};
+    uint64_t key = 0;
+    for (int L = 1; L <= kMaxLevel; ++L) {
+        unsigned dig = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double mid = (hi[a] + lo[a]) / 2;
+            if (p[a] < mid) {
+                dig |= 1u << a;
+                hi[a] = mid;
+            } else {
+                lo[a] = mid;
+            }
+        }
+        key = (key << 3) | dig;
+    }
+    keys[i] = key;
+    perm[i] = i;
+}
+
+__global__ void k_split_count(const uint64_t *__restrict__ keys, unsigned n, int T, unsigned *__restrict__ cnt,
+                              TreeInfo *info) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int Ls = i == 0 ? 0 : first_diff_level(keys[i - 1], keys[i]);
+    int Lm = -1;
+    if (static_cast<unsigned long long>(i) + T < n) {
+        Lm = first_diff_level(keys[i], keys[i + T]) - 1;
+        if (Lm >= kMaxLevel) {  // a deepest-level cell would still split
+            atomicOr(&info->err, kDevDepth);
+            Lm = kMaxLevel - 1;
+        }
+    }
+    cnt[i] = Lm >= Ls ? static_cast<unsigned>(Lm - Ls + 1) : 0u;
+}
+
+__global__ void k_check_split_total(unsigned *counts, unsigned s_cap, TreeInfo *info) {
+    counts[6] = counts[1];  // requested size, kept for the host when it overflows
+    if (counts[1] > s_cap) {
+        atomicOr(&info->err, kDevCapacity);
+        counts[1] = 0;
+    }
+}
+
+__global__ void k_split_emit(const uint64_t *__restrict__ keys, unsigned n, int T, const unsigned *__restrict__ off,
+                             const unsigned *counts, unsigned s_cap, uint64_t *__restrict__ ent) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || counts[1] == 0) return;
+    const int Ls = i == 0 ? 0 : first_diff_level(keys[i - 1], keys[i]);
+    int Lm = -1;
+    if (static_cast<unsigned long long>(i) + T < n) Lm = min(first_diff_level(keys[i], keys[i + T]) - 1, kMaxLevel - 1);
+    unsigned o = off[i];
+    for (int L = Ls; L <= Lm; ++L, ++o)
+        if (o < s_cap) ent[o] = (static_cast<uint64_t>(L) << 32) | i;
+}
+
+__device__ unsigned lower_bound_ent(const uint64_t *ent, unsigned lo, unsigned hi, uint64_t v) {
+    while (lo < hi) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (ent[mid] < v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// first j in [lo, hi) with (keys[j] >> sh) >= v
+__device__ unsigned lower_bound_pre(const uint64_t *keys, unsigned lo, unsigned hi, int sh, uint64_t v) {
+    while (lo < hi) {
+        const unsigned mid = (lo + hi) >> 1;
+        if ((keys[mid] >> sh) < v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_level_table(const uint64_t *__restrict__ ent, unsigned *counts, TreeInfo *info, unsigned n) {
+    if (threadIdx.x != 0) return;
+    const unsigned S = counts[1];
+    int start = 0, depth = 0;
+    info->level_count[0] = 1;
+    for (int L = 0; L <= kMaxLevel; ++L) {
+        const unsigned a = lower_bound_ent(ent, 0, S, static_cast<uint64_t>(L) << 32);
+        const unsigned b = lower_bound_ent(ent, 0, S, static_cast<uint64_t>(L + 1) << 32);
+        info->split_start[L] = static_cast<int>(a);
+        info->split_count[L] = static_cast<int>(b - a);
+        if (L + 1 <= kMaxLevel + 1) info->level_count[L + 1] = 8 * static_cast<int>(b - a);
+    }
+    for (int L = 0; L <= kMaxLevel + 1; ++L) {
+        info->level_start[L] = start;
+        start += info->level_count[L];
+        if (info->level_count[L] > 0) depth = L;
+    }
+    info->ncells = start;
+    info->nsplit_total = static_cast<int>(S);
+    info->nleaves = start - static_cast<int>(S);
+    info->depth = depth;
+    info->n_targets_m2l = depth >= 2 ? start - info->level_start[2] : 0;
+    counts[2] = static_cast<unsigned>(start);
+    counts[3] = static_cast<unsigned>(start) - S;
+    (void)n;
+}
+
+__device__ void path_geometry(uint64_t path, int L, const TreeInfo *info, double *box, double *ctr, int *coord) {
+    double lo[3] = {info->root_min[0], info->root_min[1], info->root_min[2]};
+    double hi[3] = {info->root_max[0], info->root_max[1], info->root_max[2]};
+    int c[3] = {0, 0, 0};
+    for (int l = 1; l <= L; ++l) {
+        const unsigned dig = static_cast<unsigned>(path >> (3 * (L - l))) & 7u;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double mid = (hi[a] + lo[a]) / 2;
+            const int lower = (dig >> a) & 1;
+            if (lower)
+                hi[a] = mid;
+            else
+                lo[a] = mid;
+            c[a] = 2 * c[a] + (1 - lower);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        box[a] = lo[a];
+        box[3 + a] = hi[a];
+        ctr[a] = (lo[a] + hi[a]) / 2;
+        coord[a] = c[a];
+    }
+}
+
+__global__ void k_root(unsigned n, int T, const TreeInfo *__restrict__ info, int *c_begin, int *c_end, int *c_parent,
+                       int *c_child, int *c_level, uint64_t *c_path, int *c_coord, double *c_box, double *c_ctr,
+                       int *p2p_own, int *p2p_cnt, int *coll, int *coll_cnt) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    c_begin[0] = 0;
+    c_end[0] = static_cast<int>(n);
+    c_parent[0] = -1;
+    c_level[0] = 0;
+    c_path[0] = 0;
+    const bool split = static_cast<long long>(n) > T;
+    c_child[0] = split ? 1 : -1;
+    path_geometry(0, 0, info, c_box, c_ctr, c_coord);
+    // calc_link at the root (solver_ref.hpp:148-154)
+    if (split) {
+        coll[0] = 0, coll_cnt[0] = 1, p2p_cnt[0] = 0;
+    } else {
+        p2p_own[0] = 0, p2p_cnt[0] = 1, coll_cnt[0] = 0;
+    }
+}
+
+__global__ void k_cells(const uint64_t *__restrict__ ent, const unsigned *counts, const uint64_t *__restrict__ keys,
+                        unsigned n, int T, const TreeInfo *__restrict__ info, int *split_cell, int *c_begin, int *c_end,
+                        int *c_parent, int *c_child, int *c_level, uint64_t *c_path, int *c_coord, double *c_box,
+                        double *c_ctr) {
+    const unsigned S = counts[1];
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < S; e += gridDim.x * blockDim.x) {
+        const int L = static_cast<int>(ent[e] >> 32);
+        const unsigned i = static_cast<unsigned>(ent[e] & 0xffffffffu);
+        const unsigned r = e - static_cast<unsigned>(info->split_start[L]);
+        const int sh = path_shift(L);
+        const uint64_t pre = L == 0 ? 0 : (keys[i] >> sh);
+        int own = 0;
+        if (L > 0) {
+            const int shp = path_shift(L - 1);
+            const unsigned ip = lower_bound_pre(keys, 0, i, shp, keys[i] >> shp);
+            const unsigned a = static_cast<unsigned>(info->split_start[L - 1]);
+            const unsigned b = a + static_cast<unsigned>(info->split_count[L - 1]);
+            const unsigned rp = lower_bound_ent(ent, a, b, (static_cast<uint64_t>(L - 1) << 32) | ip) - a;
+            own = info->level_start[L] + 8 * static_cast<int>(rp) + static_cast<int>(pre & 7u);
+        }
+        split_cell[e] = own;
+        const unsigned pe = L == 0 ? n : lower_bound_pre(keys, i + 1, n, sh, pre + 1);
+        const int shc = path_shift(L + 1);
+        const unsigned a1 = static_cast<unsigned>(info->split_start[L + 1]);
+        const unsigned b1 = a1 + static_cast<unsigned>(info->split_count[L + 1]);
+        unsigned cb = i;
+        for (int o = 0; o < 8; ++o) {
+            const uint64_t cpath = (pre << 3) | static_cast<uint64_t>(o);
+            const unsigned ce = o == 7 ? pe : lower_bound_pre(keys, cb, pe, shc, cpath + 1);
+            const int c = info->level_start[L + 1] + 8 * static_cast<int>(r) + o;
+            c_begin[c] = static_cast<int>(cb);
+            c_end[c] = static_cast<int>(ce);
+            c_parent[c] = own;
+            c_level[c] = L + 1;
+            c_path[c] = cpath;
+            int fc = -1;
+            if (static_cast<long long>(ce) - cb > T && L + 1 <= kMaxLevel - 1) {
+                const unsigned rc = lower_bound_ent(ent, a1, b1, (static_cast<uint64_t>(L + 1) << 32) | cb) - a1;
+                fc = info->level_start[L + 2] + 8 * static_cast<int>(rc);
+            }
+            c_child[c] = fc;
+            path_geometry(cpath, L + 1, info, c_box + 6 * static_cast<size_t>(c), c_ctr + 3 * static_cast<size_t>(c),
+                          c_coord + 3 * static_cast<size_t>(c));
+            cb = ce;
+        }
+    }
+}
+
+__global__ void k_leaf_flags(const int *__restrict__ c_child, const unsigned *counts, unsigned *flag) {
+    const unsigned C = counts[2];
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) flag[c] = c_child[c] < 0;
+}
+
+__global__ void k_leaf_compact(const unsigned *__restrict__ flag, const unsigned *__restrict__ off, const unsigned *counts,
+                               int *leaves) {
+    const unsigned C = counts[2];
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x)
+        if (flag[c]) leaves[off[c]] = static_cast<int>(c);
+}
+
+// Within a leaf the reference keeps insertion order, i.e. ascending particle
+// index (octree.hpp:143-145). Rank sort of each leaf's permutation slice.
+__global__ void k_leaf_sort(const int *__restrict__ leaves, const unsigned *counts, const int *__restrict__ c_begin,
+                            const int *__restrict__ c_end, int T, unsigned *perm) {
+    extern __shared__ unsigned sh[];
+    const unsigned NL = counts[3];
+    for (unsigned li = blockIdx.x; li < NL; li += gridDim.x) {
+        const int c = leaves[li];
+        const int b = c_begin[c], e = c_end[c], len = e - b;
+        if (len < 2 || len > T) continue;  // uniform per block
+        for (int k = threadIdx.x; k < len; k += blockDim.x) sh[k] = perm[b + k];
+        __syncthreads();
+        for (int k = threadIdx.x; k < len; k += blockDim.x) {
+            const unsigned v = sh[k];
+            int rank = 0;
+            for (int q = 0; q < len; ++q) rank += sh[q] < v;
+            sh[T + 1 + rank] = v;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < len; k += blockDim.x) perm[b + k] = sh[T + 1 + k];
+        __syncthreads();
+    }
+}
+
+__global__ void k_gather(const double *__restrict__ x, unsigned n, const unsigned *__restrict__ perm,
+                         const TreeInfo *__restrict__ info, float mass_f, double *__restrict__ xs, float4 *__restrict__ ph,
+                         float4 *__restrict__ pl) {
+    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const unsigned i = perm[j];
+    double d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double v = x[static_cast<size_t>(a) * n + i];
+        xs[static_cast<size_t>(a) * n + j] = v;
+        d[a] = v - (info->root_min[a] + info->root_max[a]) / 2;
+    }
+    const float hx = static_cast<float>(d[0]), hy = static_cast<float>(d[1]), hz = static_cast<float>(d[2]);
+    ph[j] = make_float4(hx, hy, hz, mass_f);
+    pl[j] = make_float4(static_cast<float>(d[0] - hx), static_cast<float>(d[1] - hy), static_cast<float>(d[2] - hz), 0.f);
+}
+
+// One warp per non-leaf cell P: its 27 same-level neighbours, then for each of
+// its 8 children the colleague, own-p2p and M2L entries (solver_ref.hpp:129-147).
+__global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts, const int *__restrict__ split_cell,
+                        const TreeInfo *__restrict__ info, const int *__restrict__ c_child,
+                        const uint64_t *__restrict__ c_path, const int *__restrict__ c_coord, int *m2l_src, int *p2p_own,
+                        int *p2p_cnt, int *coll, int *coll_cnt, unsigned long long *m2l_pairs) {
+    __shared__ int nb[8][32], ord[8][32], nord[8];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned S = counts[1];
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    for (unsigned e = blockIdx.x * (blockDim.x >> 5) + w; e < S; e += warps) {
+        const int L = static_cast<int>(ent[e] >> 32);
+        const int P = split_cell[e];
+        const int fcP = c_child[P];
+        int q = -1;
+        if (lane < 27) {
+            const int d[3] = {lane % 3 - 1, (lane / 3) % 3 - 1, lane / 9 - 1};
+            int qc[3];
+            bool in = true;
+            const int lim = 1 << L;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                qc[a] = c_coord[3 * P + a] + d[a];
+                in &= qc[a] >= 0 && qc[a] < lim;
+            }
+            if (in) {
+                uint64_t path = 0;
+                for (int l = 1; l <= L; ++l) {
+                    unsigned dig = 0;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) dig |= static_cast<unsigned>(1 - ((qc[a] >> (L - l)) & 1)) << a;
+                    path = (path << 3) | dig;
+                }
+                int lo = info->level_start[L], hi = lo + info->level_count[L];
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (c_path[mid] < path)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                if (lo < info->level_start[L] + info->level_count[L] && c_path[lo] == path && c_child[lo] >= 0) q = lo;
+            }
+        }
+        nb[w][lane] = q;
+        __syncwarp();
+        // order the existing neighbours by cell number (= path order)
+        if (lane < 27 && q >= 0) {
+            int rank = 0;
+            for (int k = 0; k < 27; ++k) {
+                const int o = nb[w][k];
+                rank += (o >= 0 && o < q);
+            }
+            ord[w][rank] = lane;
+        }
+        const unsigned ballot = __ballot_sync(0xffffffffu, lane < 27 && q >= 0);
+        if (lane == 0) nord[w] = __popc(ballot);
+        // every child's 216 M2L slots start empty
+        for (int k = lane; k < 8 * kM2LSlots; k += 32) m2l_src[static_cast<size_t>(fcP + k / kM2LSlots) * kM2LSlots + k % kM2LSlots] = -1;
+        __syncwarp();
+        if (lane < 8) {
+            const int c = fcP + lane;
+            const int uc[3] = {1 - (lane & 1), 1 - ((lane >> 1) & 1), 1 - ((lane >> 2) & 1)};
+            const bool cleaf = c_child[c] < 0;
+            int ncoll = 0, np2p = 0;
+            unsigned nm2l = 0;
+            for (int k = 0; k < nord[w]; ++k) {
+                const int dd = ord[w][k];
+                const int Q = nb[w][dd];
+                const int fq = c_child[Q];
+                const int d[3] = {dd % 3 - 1, (dd / 3) % 3 - 1, dd / 9 - 1};
+                for (int o = 0; o < 8; ++o) {
+                    const int u = fq + o;
+                    const int uo[3] = {1 - (o & 1), 1 - ((o >> 1) & 1), 1 - ((o >> 2) & 1)};
+                    bool adj = true;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const int off = 2 * d[a] + uo[a] - uc[a];
+                        adj &= off >= -1 && off <= 1;
+                    }
+                    if (adj) {
+                        if (!cleaf && c_child[u] >= 0)
+                            coll[static_cast<size_t>(c) * kNbrCap + ncoll++] = u;
+                        else
+                            p2p_own[static_cast<size_t>(c) * kNbrCap + np2p++] = u;
+                    } else {
+                        m2l_src[static_cast<size_t>(c) * kM2LSlots + dd * 8 + o] = u;
+                        ++nm2l;
+                    }
+                }
+            }
+            coll_cnt[c] = ncoll;
+            p2p_cnt[c] = np2p;
+            if (L + 1 >= 2 && nm2l) atomicAdd(m2l_pairs, static_cast<unsigned long long>(nm2l));
+        }
+        __syncwarp();
+    }
+}
+
+// Near-field source ranges of every leaf: the own-p2p entries of its
+// ancestors from the root down, then its own (the inherited list of
+// solver_ref.hpp:126 followed by the cell's additions). Each entry is a
+// subtree, i.e. a contiguous particle range in tree order.
+__global__ void k_rng_count(const int *__restrict__ leaves, const unsigned *counts, const int *__restrict__ c_parent,
+                            const int *__restrict__ c_begin, const int *__restrict__ c_end,
+                            const int *__restrict__ p2p_cnt, unsigned *rng_cnt, unsigned *chunk_cnt) {
+    const unsigned NL = counts[3];
+    for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < NL; li += gridDim.x * blockDim.x) {
+        const int c = leaves[li];
+        const int nt = c_end[c] - c_begin[c];
+        unsigned tot = 0;
+        if (nt > 0)
+            for (int a = c; a >= 0; a = c_parent[a]) tot += static_cast<unsigned>(p2p_cnt[a]);
+        rng_cnt[li] = tot;
+        chunk_cnt[li] = static_cast<unsigned>((nt + 31) / 32);
+    }
+}
+
+__global__ void k_rng_fill(const int *__restrict__ leaves, const unsigned *counts, unsigned r_cap, unsigned ch_cap,
+                           const int *__restrict__ c_parent, const int *__restrict__ c_begin, const int *__restrict__ c_end,
+                           const int *__restrict__ p2p_own, const int *__restrict__ p2p_cnt,
+                           const unsigned *__restrict__ rng_off, unsigned *rng_len, uint2 *ranges,
+                           const unsigned *__restrict__ chunk_off, int2 *chunks, TreeInfo *info) {
+    const unsigned NL = counts[3];
+    for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < NL; li += gridDim.x * blockDim.x) {
+        const int c = leaves[li];
+        const int b = c_begin[c], e = c_end[c];
+        if (e == b) {
+            rng_len[li] = 0;
+            continue;
+        }
+        int anc[kMaxLevel + 2];
+        int na = 0;
+        for (int a = c; a >= 0 && na < kMaxLevel + 2; a = c_parent[a]) anc[na++] = a;
+        const unsigned base = rng_off[li];
+        unsigned k = 0;
+        unsigned long long srcs = 0;
+        uint2 last = make_uint2(0, 0);
+        bool have = false, overflow = false;
+        for (int t = na - 1; t >= 0; --t) {
+            const int a = anc[t];
+            for (int q = 0; q < p2p_cnt[a]; ++q) {
+                const int u = p2p_own[static_cast<size_t>(a) * kNbrCap + q];
+                const unsigned ub = static_cast<unsigned>(c_begin[u]), ue = static_cast<unsigned>(c_end[u]);
+                if (ue == ub) continue;
+                srcs += ue - ub;
+                if (have && last.y == ub) {
+                    last.y = ue;
+                } else {
+                    if (have) {
+                        if (base + k < r_cap)
+                            ranges[base + k] = last;
+                        else
+                            overflow = true;
+                        ++k;
+                    }
+                    last = make_uint2(ub, ue);
+                    have = true;
+                }
+            }
+        }
+        if (have) {
+            if (base + k < r_cap)
+                ranges[base + k] = last;
+            else
+                overflow = true;
+            ++k;
+        }
+        rng_len[li] = overflow ? 0u : k;  // never let P2P read past the buffer
+        const unsigned cb = chunk_off[li];
+        const int nch = (e - b + 31) / 32;
+        for (int q = 0; q < nch; ++q) {
+            if (cb + q < ch_cap)
+                chunks[cb + q] = make_int2(static_cast<int>(li), b + 32 * q);
+            else
+                overflow = true;
+        }
+        if (overflow) atomicOr(&info->err, kDevCapacity);
+        atomicAdd(reinterpret_cast<unsigned long long *>(&info->p2p_pairs), static_cast<unsigned long long>(e - b) * srcs);
+        atomicAdd(reinterpret_cast<unsigned long long *>(&info->p2p_ranges), static_cast<unsigned long long>(k));
+    }
+}
+
+__global__ void k_check_totals(unsigned *counts, unsigned r_cap, unsigned ch_cap, TreeInfo *info) {
+    if (counts[4] > r_cap || counts[5] > ch_cap) atomicOr(&info->err, kDevCapacity);
+    info->n_p2p_chunks = static_cast<int>(min(counts[5], ch_cap));
+    counts[5] = min(counts[5], ch_cap);
+}
+
+inline unsigned grid_for(unsigned n, int tb) { return (n + tb - 1) / tb; }
+
+}  // namespace
+
+void build_tree(Workspace &ws) {
+    const unsigned n = ws.n;
+    cudaStream_t st = ws.st;
+    timer_begin(ws, kTTree);
+    cudaMemsetAsync(ws.info, 0, sizeof(TreeInfo), st);
+    cudaMemsetAsync(ws.d_counts, 0, 8 * sizeof(unsigned), st);
+    cudaMemcpyAsync(ws.d_counts, &n, sizeof(unsigned), cudaMemcpyHostToDevice, st);
+    const int nb = 2 * ws.num_sms;
+    double *part = ws.bbox_part;
+    k_bbox_partial<<<nb, kTB, 0, st>>>(ws.x, n, part, ws.info);
+    k_bbox_final<<<1, 32, 0, st>>>(part, nb, ws.info);
+    k_keys<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.keys0, ws.perm0);
+    ws.launches += 3;
+    const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, 0, 3 * kMaxLevel, ws.sort, st,
+                                   &ws.launches);
+    ws.keys = res ? ws.keys1 : ws.keys0;
+    ws.perm = res ? ws.perm1 : ws.perm0;
+    // split cells of every level
+    k_split_count<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.cnt, ws.info);
+    scan_exclusive_u32(ws.cnt, ws.off, n, nullptr, ws.d_counts + 1, ws.scan, st, &ws.launches);
+    k_check_split_total<<<1, 1, 0, st>>>(ws.d_counts, ws.s_cap, ws.info);
+    k_split_emit<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.off, ws.d_counts, ws.s_cap, ws.ent0);
+    ws.launches += 3;
+    const int re = radix_sort_u64(ws.ent0, nullptr, ws.ent1, nullptr, ws.s_cap, ws.d_counts + 1, 32, 40, ws.sort, st,
+                                  &ws.launches);
+    ws.ent = re ? ws.ent1 : ws.ent0;
+    k_level_table<<<1, 32, 0, st>>>(ws.ent, ws.d_counts, ws.info, n);
+    k_root<<<1, 32, 0, st>>>(n, ws.T, ws.info, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path,
+                             ws.c_coord, ws.c_box, ws.c_ctr, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt);
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 4;
+    k_cells<<<gs, 128, 0, st>>>(ws.ent, ws.d_counts, ws.keys, n, ws.T, ws.info, ws.split_cell, ws.c_begin, ws.c_end,
+                                ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr);
+    k_leaf_flags<<<gs, kTB, 0, st>>>(ws.c_child, ws.d_counts, ws.flag);
+    scan_exclusive_u32(ws.flag, ws.flag_off, ws.c_cap, ws.d_counts + 2, nullptr, ws.scan, st, &ws.launches);
+    k_leaf_compact<<<gs, kTB, 0, st>>>(ws.flag, ws.flag_off, ws.d_counts, ws.leaves);
+    const size_t smem = sizeof(unsigned) * (2 * static_cast<size_t>(ws.T) + 2);
+    k_leaf_sort<<<gs * 2, 128, smem, st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.T, ws.perm);
+    k_gather<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.perm, ws.info, static_cast<float>(ws.m), ws.xs, ws.ph, ws.pl);
+    k_lists<<<gs, 256, 0, st>>>(ws.ent, ws.d_counts, ws.split_cell, ws.info, ws.c_child, ws.c_path, ws.c_coord,
+                                ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
+                                reinterpret_cast<unsigned long long *>(&ws.info->m2l_pairs));
+    k_rng_count<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.c_parent, ws.c_begin, ws.c_end, ws.p2p_cnt, ws.rng_cnt,
+                                    ws.chunk_cnt);
+    scan_exclusive_u32(ws.rng_cnt, ws.rng_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 4, ws.scan, st, &ws.launches);
+    scan_exclusive_u32(ws.chunk_cnt, ws.chunk_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 5, ws.scan, st, &ws.launches);
+    k_check_totals<<<1, 1, 0, st>>>(ws.d_counts, ws.r_cap, ws.ch_cap, ws.info);
+    k_rng_fill<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.r_cap, ws.ch_cap, ws.c_parent, ws.c_begin, ws.c_end,
+                                   ws.p2p_own, ws.p2p_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_off, ws.chunks,
+                                   ws.info);
+    ws.launches += 13;
+    timer_end(ws, kTTree);
+}
+
+}  // namespace gb

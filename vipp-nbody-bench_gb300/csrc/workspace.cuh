@@ -1,0 +1,128 @@
+// Device workspace of one solver context and the stage entry points.
+//
+// HBM layout (N particles, C cells, S non-leaf cells, K = (p+1)^2):
+//   state, original particle order, FP64 SoA planes [3][N]:
+//     x, v (current), x0, v0 (step start), xo, vo (RK4 accumulators), acc
+//   per evaluation, tree (Morton) order:
+//     keys/perm (u64/u32 ping-pong pairs), xs [3][N] FP64 positions,
+//     ph/pl float4 hi/lo split of the positions (mixed P2P),
+//     near/far [3][N] partial accelerations (FP32 or FP64)
+//   cells (level by level, path order inside a level, 8 siblings adjacent):
+//     begin/end/parent/child/level/path/coord, box [6C], centre [3C],
+//     M and L scaled real-basis expansions [C][K] (FP32 or FP64),
+//     m2l_src [C][216] source cell per (parent-neighbour, octant) slot,
+//     p2p_own/coll [C][27] + counts
+//   leaves: list, near-field source ranges (CSR of uint2), P2P work chunks
+//   operators: 343 M2L offsets + 8 M2M + 8 L2L real matrices [K][K],
+//     stored input-major (op[c*K + r]) in FP64 and FP32.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "harmonics.cuh"
+#include "prims.cuh"
+
+namespace gb {
+
+enum TimerClass { kTTree = 0, kTOps = 1, kTUp = 2, kTM2L = 3, kTDown = 4, kTP2P = 5, kTRK4 = 6, kNumTimers = 7 };
+
+struct Workspace {
+    // configuration of the evaluation
+    int p = 4, K = 25, T = 90;  // T = floor(sqrt(8) s)
+    double eps = 0, G = 1, m = 1;
+    bool mixed = false;
+    cudaStream_t st = nullptr;
+    int64_t launches = 0;
+    int num_sms = 152;
+
+    // capacities
+    unsigned n_cap = 0;   // particles
+    unsigned s_cap = 0;   // split entries (non-leaf cells)
+    unsigned c_cap = 0;   // cells = 1 + 8 s_cap
+    unsigned r_cap = 0;   // near-field source ranges
+    unsigned ch_cap = 0;  // P2P chunks
+    int k_cap = 0;        // K the expansion buffers were sized for
+    unsigned n = 0;       // current particle count
+
+    // state (original order)
+    double *x = nullptr, *v = nullptr, *x0 = nullptr, *v0 = nullptr, *xo = nullptr, *vo = nullptr, *acc = nullptr;
+    double *phi = nullptr;  // optional potential (original order)
+    double *staging = nullptr;  // AoS staging [3N] for host copies
+    double *bbox_part = nullptr; // [6 * 2 * num_sms] bounding-box partials
+
+    // per evaluation, tree order
+    uint64_t *keys0 = nullptr, *keys1 = nullptr;
+    unsigned *perm0 = nullptr, *perm1 = nullptr;
+    uint64_t *keys = nullptr;  // points at the sorted buffer
+    unsigned *perm = nullptr;
+    double *xs = nullptr;                   // [3][N]
+    float4 *ph = nullptr, *pl = nullptr;    // hi/lo positions, w = mass (hi) / 0
+    void *nearf = nullptr, *farf = nullptr; // [3][N] of FP32 or FP64
+    double *phis = nullptr;                 // potential, tree order [N] (optional)
+    unsigned *cnt = nullptr, *off = nullptr;  // [N+1]
+
+    // split entries
+    uint64_t *ent0 = nullptr, *ent1 = nullptr, *ent = nullptr;
+    int *split_cell = nullptr;
+
+    // cells
+    int *c_begin = nullptr, *c_end = nullptr, *c_parent = nullptr, *c_child = nullptr, *c_level = nullptr;
+    uint64_t *c_path = nullptr;
+    int *c_coord = nullptr;     // [3C]
+    double *c_box = nullptr;    // [6C] min xyz, max xyz
+    double *c_ctr = nullptr;    // [3C]
+    void *Mexp = nullptr, *Lexp = nullptr;  // [C][K]
+    int *m2l_src = nullptr;     // [C][216]
+    int *p2p_own = nullptr, *p2p_cnt = nullptr;  // [C][27], [C]
+    int *coll = nullptr, *coll_cnt = nullptr;    // [C][27], [C]
+    unsigned *flag = nullptr, *flag_off = nullptr;  // [C+1]
+
+    // leaves
+    int *leaves = nullptr;            // [C]
+    unsigned *rng_cnt = nullptr;      // [C] ranges per leaf before merging (then capacity offsets)
+    unsigned *rng_off = nullptr;      // [C+1]
+    unsigned *rng_len = nullptr;      // [C] ranges per leaf after merging
+    uint2 *ranges = nullptr;          // [r_cap]
+    unsigned *chunk_cnt = nullptr, *chunk_off = nullptr;  // [C]
+    int2 *chunks = nullptr;           // [ch_cap] (leaf, first target)
+    unsigned *queue = nullptr;        // P2P work-queue counter
+
+    // operators
+    double *ops_d = nullptr;  // [(343+16) K K]
+    float *ops_f = nullptr;
+
+    // device-side info and device-resident counters
+    TreeInfo *info = nullptr;
+    unsigned *d_counts = nullptr;  // [8]: 0 n, 1 S, 2 C, 3 leaves, 4 ranges, 5 chunks
+    TreeInfo *h_info = nullptr;    // pinned mirror
+
+    SortTemp sort;
+    ScanTemp scan;
+
+    // timing
+    bool timing = false;
+    cudaEvent_t ev[kNumTimers][2] = {};
+    double t_ms[kNumTimers] = {};
+    int64_t t_launch[kNumTimers] = {};
+};
+
+constexpr int kOpM2M = 343;  // op index of M2M octant 0
+constexpr int kOpL2L = 351;  // op index of L2L octant 0
+constexpr int kNumOps = 359;
+
+// stages (all asynchronous on ws.st)
+void build_tree(Workspace &ws);               // bbox, keys, sort, cells, leaves, lists, near-field ranges
+void build_operators(Workspace &ws);          // 359 translation matrices for the current root box
+void upward_pass(Workspace &ws);              // P2M + M2M
+void m2l_pass(Workspace &ws);                 // M2L into L
+void downward_pass(Workspace &ws);            // L2L + L2P into far
+void p2p_pass(Workspace &ws);                 // near field into near
+void finalize_accel(Workspace &ws, double *acc_orig);  // acc[perm] = near + far
+void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, unsigned nt, double *out_soa);
+
+// timing helpers
+void timer_begin(Workspace &ws, int cls);
+void timer_end(Workspace &ws, int cls);
+
+}  // namespace gb

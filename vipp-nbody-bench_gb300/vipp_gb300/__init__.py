@@ -1,0 +1,230 @@
+"""Python binding of libvipp_gb300.so (the C-ABI in include/vipp_gb300.h).
+
+``Solver`` mirrors the reference's Solver concept
+(gravity/include/solver_ref.hpp:11-27): ``preprocess`` uploads the particles,
+``solve`` runs one RK4 step of size ``problem.delta_t() / t`` and
+``postprocess`` downloads the state. Errors are raised as RuntimeError, as
+the reference throws std::runtime_error.
+
+The compute path is the CUDA library only: importing this module does not
+fall back to anything else. ``load()`` raises if the shared library is
+missing, and every call that needs a GPU raises if none is present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libvipp_gb300.so")
+
+GB_OK, GB_ERR_INVALID, GB_ERR_NONFINITE, GB_ERR_DEPTH, GB_ERR_CUDA, GB_ERR_NO_DEVICE, GB_ERR_STATE, GB_ERR_CAPACITY = range(8)
+PREC = {"fp64": 0, "mixed": 1}
+TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
+
+# Every symbol include/vipp_gb300.h declares.
+EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_upload", "gb_download", "gb_rk4_step",
+           "gb_accel", "gb_direct_accel", "gb_sync", "gb_get_stats", "gb_tree_dump", "gb_enable_timing",
+           "gb_kernel_times", "gb_launch_count", "gb_version")
+
+
+class GbConfig(ctypes.Structure):
+    _fields_ = [("p", ctypes.c_int), ("s", ctypes.c_int), ("eps", ctypes.c_double), ("G", ctypes.c_double),
+                ("m", ctypes.c_double), ("precision", ctypes.c_int), ("device", ctypes.c_int), ("flags", ctypes.c_int)]
+
+
+class GbStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in ("n", "ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges")]
+
+
+_LIB = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (built by build.py). Raises if it is missing."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"libvipp_gb300.so not built ({path}); run __graft_entry__.build()")
+    lib = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    lib.gb_create.argtypes = [ctypes.POINTER(GbConfig), ctypes.POINTER(vp)]
+    lib.gb_destroy.argtypes = [vp]
+    lib.gb_destroy.restype = None
+    lib.gb_last_error.argtypes = [vp]
+    lib.gb_last_error.restype = ctypes.c_char_p
+    lib.gb_set_config.argtypes = [vp, ctypes.POINTER(GbConfig)]
+    lib.gb_upload.argtypes = [vp, vp, vp, ctypes.c_size_t]
+    lib.gb_download.argtypes = [vp, vp, vp]
+    lib.gb_rk4_step.argtypes = [vp, ctypes.c_double]
+    lib.gb_accel.argtypes = [vp, vp, vp]
+    lib.gb_direct_accel.argtypes = [vp, vp, ctypes.c_size_t, vp]
+    lib.gb_sync.argtypes = [vp]
+    lib.gb_get_stats.argtypes = [vp, ctypes.POINTER(GbStats)]
+    lib.gb_tree_dump.argtypes = [vp] + [vp] * 17
+    lib.gb_enable_timing.argtypes = [vp, ctypes.c_int]
+    lib.gb_kernel_times.argtypes = [vp, vp, vp, ctypes.c_int]
+    lib.gb_launch_count.argtypes = [vp]
+    lib.gb_launch_count.restype = ctypes.c_int64
+    lib.gb_version.restype = ctypes.c_char_p
+    _LIB = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _aos(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1, 3))
+
+
+class GB300Error(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gb error {code}: {msg}")
+        self.code = code
+
+
+class Solver:
+    """One solver context on one GPU (see include/vipp_gb300.h)."""
+
+    def __init__(self, p: int = 4, s: int = 10, eps: float = 0.01, G: float = 1.0, m: float = 1.0,
+                 precision: str = "fp64", device: int = 0):
+        self.lib = load()
+        self.cfg = GbConfig(p, s, eps, G, m, PREC[precision], device, 0)
+        h = ctypes.c_void_p()
+        rc = self.lib.gb_create(ctypes.byref(self.cfg), ctypes.byref(h))
+        if rc != GB_OK:
+            raise GB300Error(rc, self.lib.gb_last_error(None).decode())
+        self.h = h
+        self.n = 0
+
+    def _check(self, rc):
+        if rc != GB_OK:
+            raise GB300Error(rc, self.lib.gb_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_config(self, **kw):
+        for k, v in kw.items():
+            if k == "precision":
+                v = PREC[v]
+            setattr(self.cfg, k, v)
+        self._check(self.lib.gb_set_config(self.h, ctypes.byref(self.cfg)))
+
+    # Solver concept -------------------------------------------------------
+    def preprocess(self, x, v):
+        x, v = _aos(x), _aos(v)
+        self.n = x.shape[0]
+        self._check(self.lib.gb_upload(self.h, _ptr(x), _ptr(v), self.n))
+
+    def solve(self, dt: float):
+        self._check(self.lib.gb_rk4_step(self.h, float(dt)))
+
+    def postprocess(self):
+        x = np.zeros((self.n, 3))
+        v = np.zeros((self.n, 3))
+        self._check(self.lib.gb_download(self.h, _ptr(x), _ptr(v)))
+        return x, v
+
+    # extras ----------------------------------------------------------------
+    def upload_ptr(self, x_ptr: int, v_ptr: int, n: int):
+        """preprocess from raw host pointers (e.g. pinned buffers)."""
+        self.n = n
+        self._check(self.lib.gb_upload(self.h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(v_ptr), n))
+
+    def download_ptr(self, x_ptr: int, v_ptr: int):
+        self._check(self.lib.gb_download(self.h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(v_ptr)))
+
+    def accel(self):
+        a = np.zeros((self.n, 3))
+        self._check(self.lib.gb_accel(self.h, _ptr(a), None))
+        return a
+
+    def direct_accel(self, targets=None):
+        if targets is None:
+            a = np.zeros((self.n, 3))
+            self._check(self.lib.gb_direct_accel(self.h, None, 0, _ptr(a)))
+        else:
+            t = np.ascontiguousarray(targets, dtype=np.int64)
+            a = np.zeros((len(t), 3))
+            self._check(self.lib.gb_direct_accel(self.h, _ptr(t), len(t), _ptr(a)))
+        return a
+
+    def sync(self):
+        self._check(self.lib.gb_sync(self.h))
+
+    def stats(self) -> dict:
+        s = GbStats()
+        self._check(self.lib.gb_get_stats(self.h, ctypes.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in GbStats._fields_}
+
+    def enable_timing(self, on=True):
+        self._check(self.lib.gb_enable_timing(self.h, int(on)))
+
+    def kernel_times(self) -> dict:
+        n = len(TIMER_CLASSES)
+        ms = np.zeros(n)
+        cnt = np.zeros(n, np.int64)
+        self._check(self.lib.gb_kernel_times(self.h, _ptr(ms), _ptr(cnt), n))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(TIMER_CLASSES)}
+
+    def launch_count(self) -> int:
+        return int(self.lib.gb_launch_count(self.h))
+
+    def tree_dump(self) -> dict:
+        """Tree and lists of the last force evaluation (see gb_tree_dump)."""
+        nc = np.zeros(1, np.int64)
+        ls = np.zeros(3, np.int64)
+        nulls = [None] * 15
+        self._check(self.lib.gb_tree_dump(self.h, _ptr(nc), _ptr(ls), *nulls))
+        C = int(nc[0])
+        level = np.zeros(C, np.int32)
+        parent = np.zeros(C, np.int64)
+        first_child = np.zeros(C, np.int64)
+        path = np.zeros(C, np.uint64)
+        bmin = np.zeros((C, 3))
+        bmax = np.zeros((C, 3))
+        pb = np.zeros(C, np.int64)
+        pe = np.zeros(C, np.int64)
+        order = np.zeros(max(self.n, 1), np.int64)
+        m2l_off = np.zeros(C + 1, np.int64)
+        m2l = np.zeros(max(int(ls[0]), 1), np.int64)
+        p2p_off = np.zeros(C + 1, np.int64)
+        p2p = np.zeros(max(int(ls[1]), 1), np.int64)
+        coll_off = np.zeros(C + 1, np.int64)
+        coll = np.zeros(max(int(ls[2]), 1), np.int64)
+        self._check(self.lib.gb_tree_dump(self.h, _ptr(nc), _ptr(ls), _ptr(level), _ptr(parent), _ptr(first_child),
+                                          _ptr(path), _ptr(bmin), _ptr(bmax), _ptr(pb), _ptr(pe), _ptr(order),
+                                          _ptr(m2l_off), _ptr(m2l), _ptr(p2p_off), _ptr(p2p), _ptr(coll_off),
+                                          _ptr(coll)))
+        return dict(level=level, parent=parent, first_child=first_child, path=path, mins=bmin, maxs=bmax,
+                    pt_begin=pb, pt_end=pe, order=order[:self.n],
+                    m2l=[m2l[m2l_off[c]:m2l_off[c + 1]] for c in range(C)],
+                    p2p_own=[p2p[p2p_off[c]:p2p_off[c + 1]] for c in range(C)],
+                    coll=[coll[coll_off[c]:coll_off[c + 1]] for c in range(C)])
+
+
+def version() -> str:
+    return load().gb_version().decode()

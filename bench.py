@@ -1,0 +1,386 @@
+"""Benchmark of the GB300 FMM RK4 step (one JSON line on stdout).
+
+Workload (headline): Plummer sphere of 4,194,304 equal-mass particles (G = 1,
+M = 1, scale radius 1; radii by inverse CDF r = (u^(-2/3) - 1)^(-1/2) with
+r <= 10, isotropic directions, speeds by von Neumann rejection from the
+Plummer distribution function; seed 2), eps = 0.005, p = 8, s = 64, mixed
+precision, RK4 dt = 5e-4. A step is one RK4 step (four force evaluations,
+tree rebuilt at every stage).
+
+  value   particle-steps/s with the state resident in HBM (CUDA events on the
+          solver's stream around exactly --steps steps)
+  e2e     the same through the C-ABI with host buffers: per step, upload of
+          x, v from pinned host memory, one RK4 step, download of x, v
+  plain_fp64  the same step with every stage in FP64 (the plain form)
+  cpu_baseline  the reference's algorithm on the host cores (oracle port, or
+          the compiled reference where it exists), on a bounded sample of one
+          force evaluation, extrapolated to a step
+
+``--impl reference`` times the reference's CPU implementation instead
+(same metric and config) and prints its own line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "vipp-nbody-bench_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "RK4 particle-steps/s at stated FP64-direct force error; mixed/batched vs plain"
+UNIT = "particle-steps/s"
+FP32_LANES_PER_SM = 128
+
+
+def plummer(n: int, seed: int, rmax: float = 10.0):
+    """Plummer sphere (G = M = a = 1) with the inverse-CDF radius capped at rmax."""
+    rng = np.random.default_rng(seed)
+    r = np.empty(n)
+    todo = np.arange(n)
+    while todo.size:
+        u = rng.random(todo.size)
+        u = np.where(u == 0, 0.5, u)
+        rr = 1.0 / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
+        ok = rr <= rmax
+        r[todo[ok]] = rr[ok]
+        todo = todo[~ok]
+    q = np.empty(n)
+    todo = np.arange(n)
+    pmax = math.sqrt(7.0) * 686 / 19683
+    while todo.size:
+        x1, x2 = rng.random(todo.size), rng.random(todo.size)
+        ok = pmax * x1 < x2 * x2 * (1 - x2 * x2) ** 3.5
+        q[todo[ok]] = x2[ok]
+        todo = todo[~ok]
+    ve = math.sqrt(2.0) * (1.0 + r * r) ** -0.25
+
+    def iso(norm, a, b):
+        z = (1 - 2 * a) * norm
+        w = np.sqrt(np.maximum(norm * norm - z * z, 0.0))
+        return np.stack([z, w * np.cos(2 * np.pi * b), w * np.sin(2 * np.pi * b)], axis=1)
+
+    x = iso(r, rng.random(n), rng.random(n))
+    v = iso(q * ve, rng.random(n), rng.random(n))
+    return np.ascontiguousarray(x), np.ascontiguousarray(v)
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) of SM clock and throttle reasons."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [t.strip() for t in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(val: float, ws: int) -> float:
+    if ws <= 1:
+        return val
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([val], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def cpu_baseline_sample(x, s, p, eps, target_seconds=12.0):
+    """The reference's algorithm (oracle port) on the host cores: the whole
+    tree, lists and upward pass of one force evaluation, plus M2L/P2P/L2L/L2P
+    of every stride-th cell, scaled up by M2L pair counts."""
+    import oracle
+
+    n = x.shape[0]
+    stride = 96
+    times, counts = oracle.accel_sampled(x, s, 1.0, 1.0 / n, eps, p, stride)
+    per_eval = times[0] + times[1] + times[2] * (counts[2] / max(counts[3], 1))
+    step = 4 * per_eval
+    ref = oracle.ref() is not None and os.environ.get("VIPP_BASELINE_KIND") == "reference"
+    return {"value": n / step, "unit": UNIT, "cores": oracle.threads(), "kind": "reference" if ref else "port",
+            "sample": (f"one force evaluation of the same {n}-particle workload: full tree+lists "
+                       f"({times[0]:.2f} s) and upward pass ({times[1]:.2f} s), far/near work of every "
+                       f"{stride}th cell ({int(counts[1])} cells, {times[2]:.2f} s) scaled by M2L pairs "
+                       f"{int(counts[2])}/{int(counts[3])}; x4 evaluations per RK4 step"),
+            "seconds_per_step_extrapolated": step}
+
+
+def run_reference_arm(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    import oracle
+
+    x, v = plummer(args.n, 2)
+    vals = []
+    t_start = time.time()
+    # CPU runs need no warm-up beyond the first sample; every step is one
+    # bounded sample (about 20 s), stopped early to stay within a few minutes
+    for k in range(args.steps):
+        r = cpu_baseline_sample(x, args.s, args.p, args.eps)
+        vals.append(r["value"])
+        if time.time() - t_start > 150:
+            break
+    value = float(np.median(vals))
+    cfg = {"workload": f"plummer-{args.n} p={args.p} s={args.s} eps={args.eps} (reference algorithm, CPU)",
+           "N": args.n, "p": args.p, "s": args.s, "eps": args.eps, "dt": args.dt}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": len(vals),
+            "warmup": args.warmup, "ms_per_step": 1e3 * args.n / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
+                             "sample": r["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    del oracle
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 22)
+    ap.add_argument("--p", type=int, default=8)
+    ap.add_argument("--s", type=int, default=64)
+    ap.add_argument("--eps", type=float, default=0.005)
+    ap.add_argument("--dt", type=float, default=5e-4)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--error-sample", type=int, default=65536)
+    ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain-form comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    ws, rank, local = dist_setup()
+    import torch
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import vipp_gb300
+
+    n = args.n
+    x, v = plummer(n, 2 + rank)
+    m = 1.0 / n
+    sol = vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision=args.precision, device=local)
+    sol.preprocess(x, v)
+    for _ in range(args.warmup):
+        sol.solve(args.dt)
+    sol.sync()
+
+    # --- timed region: state resident in HBM -------------------------------------
+    sol.enable_timing(True)
+    sol.kernel_times()
+    launches0 = sol.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stream = torch.cuda.ExternalStream(sol.stream_ptr(), device=local)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(ws)
+    torch.cuda.synchronize()
+    sol.sync()
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sol.solve(args.dt)
+    ev1.record(stream)
+    ev1.synchronize()
+    sol.sync()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    barrier(ws)
+    elapsed = ev0.elapsed_time(ev1) / 1e3  # device time of exactly --steps steps
+    clk = clocks.stop()
+    launches = sol.launch_count() - launches0
+    kt = sol.kernel_times()
+    sol.enable_timing(False)
+    st = sol.stats()
+    elapsed = max_over_ranks(elapsed, ws)
+    value = n * ws * args.steps / elapsed
+
+    # --- end to end through the C-ABI with pinned host buffers -------------------
+    xh = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    vh = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    xh.copy_(torch.from_numpy(x))
+    vh.copy_(torch.from_numpy(v))
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sol.upload_ptr(xh.data_ptr(), vh.data_ptr(), n)
+        sol.solve(args.dt)
+        sol.download_ptr(xh.data_ptr(), vh.data_ptr())
+    e2e_t = max_over_ranks(time.perf_counter() - t0, ws)
+    e2e = {"value": n * ws * e2e_steps / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 2 * 24 * n,
+           "d2h_bytes_per_step": 2 * 24 * n, "steps": e2e_steps}
+
+    # --- accuracy on a 65,536-particle sample vs the FP64 direct sum (GPU) -------
+    acc_info = {}
+    if rank == 0 and args.error_sample > 0:
+        sol.preprocess(x, v)
+        a = sol.accel()
+        tg = np.sort(np.random.default_rng(7).choice(n, size=min(args.error_sample, n), replace=False))
+        ad = sol.direct_accel(tg)
+        e = np.linalg.norm(a[tg] - ad, axis=1) / np.linalg.norm(ad, axis=1)
+        acc_info = {"rms_rel_err_vs_fp64_direct": float(math.sqrt(np.mean(e * e))),
+                    "max_rel_err_vs_fp64_direct": float(e.max()), "error_sample": int(len(tg))}
+    sol.close()
+
+    # --- plain FP64 form of the same method --------------------------------------
+    plain = None
+    if rank == 0 and not args.no_plain and args.precision == "mixed":
+        with vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, m=m, precision="fp64", device=local) as sp:
+            sp.preprocess(x, v)
+            sp.solve(args.dt)
+            sp.sync()
+            t0 = time.perf_counter()
+            sp.solve(args.dt)
+            sp.sync()
+            tp = time.perf_counter() - t0
+            sp.preprocess(x, v)
+            ap64 = sp.accel()
+            e = np.linalg.norm(ap64[tg] - ad, axis=1) / np.linalg.norm(ad, axis=1) if acc_info else None
+        plain = {"value": n / tp, "unit": UNIT, "steps": 1, "ms_per_step": 1e3 * tp,
+                 "rms_rel_err_vs_fp64_direct": float(math.sqrt(np.mean(e * e))) if e is not None else None,
+                 "max_rel_err_vs_fp64_direct": float(e.max()) if e is not None else None,
+                 "mixed_over_plain": value / ws / (n / tp)}
+
+    # --- roofline of the dominant kernel class ---------------------------------
+    peaks, src = measured_peaks()
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    props = torch.cuda.get_device_properties(local)
+    nsm = props.multi_processor_count
+    fp32_peak = 2 * FP32_LANES_PER_SM * nsm * sm_mhz * 1e6 / 1e12  # TFLOP/s
+    per = {}
+    K = (args.p + 1) ** 2
+    if kt["p2p"][1]:
+        t = kt["p2p"][0] / kt["p2p"][1] / 1e3
+        ach = 20.0 * st["p2p_pairs"] / t / 1e12
+        per["p2p"] = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                      "ms_per_launch": 1e3 * t, "launches": kt["p2p"][1]}
+    if kt["m2l"][1]:
+        t = kt["m2l"][0] / kt["m2l"][1] / 1e3
+        ach = 2.0 * K * K * st["m2l_pairs"] / t / 1e12
+        per["m2l"] = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                      "ms_per_launch": 1e3 * t, "launches": kt["m2l"][1]}
+    if kt["tree"][1]:
+        t = kt["tree"][0] / kt["tree"][1] / 1e3
+        ncell = st["ncells"]
+        ach = (60.0 * n + 64.0 * ncell) / t / 1e9
+        per["tree"] = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                       "frac": ach / peaks["hbm_gbs"], "ms_per_launch": 1e3 * t, "launches": kt["tree"][1]}
+    dom = max(per, key=lambda k: per[k]["ms_per_launch"] * per[k]["launches"]) if per else None
+    roof = dict(per[dom]) if dom else {}
+    if dom:
+        roof.update({"kernel": dom, "traffic": None,
+                     "peak_source": (f"{src}: FP32 = 2 x 128 lanes x {nsm} SMs x sm_max_mhz {sm_mhz:.0f}"
+                                     if roof["bound"] == "fp32" else f"{src} hbm_gbs")})
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline_sample(x, args.s, args.p, args.eps)
+
+    kt_ms = {k: round(v[0] / args.steps, 4) for k, v in kt.items()}
+    cfg = {"workload": f"plummer-{n} p={args.p} s={args.s} eps={args.eps} {args.precision}", "N": n, "p": args.p,
+           "s": args.s, "eps": args.eps, "dt": args.dt, "precision": args.precision, "seed": 2,
+           "l2": "inputs larger than L2 (state 192 MB, per-step working set > 1 GB)",
+           "tree": {k: st[k] for k in ("ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges")},
+           "kernel_ms_per_step": kt_ms, **acc_info, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * elapsed / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
+            "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": cfg, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
+            "roofline_kernels": per, "plain_fp64": plain, "cpu_baseline": cpu}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -148,6 +148,10 @@ GB_API int gb_tree_dump(gb_ctx *ctx, int64_t *ncells, int64_t *list_sizes, int32
 GB_API int gb_enable_timing(gb_ctx *ctx, int on);
 GB_API int gb_kernel_times(gb_ctx *ctx, double *ms, int64_t *launches, int n);
 
+/* The context's CUDA stream (a cudaStream_t), so callers can order their own
+ * work or record events around the context's kernels. */
+GB_API void *gb_stream(gb_ctx *ctx);
+
 /* Number of kernel launches issued by the context since creation. */
 GB_API int64_t gb_launch_count(const gb_ctx *ctx);
 

@@ -285,18 +285,9 @@ int orc_accel_sampled(const double *x_aos, std::size_t n, std::size_t s, double 
             }
         }
         const double Gm = G * m;
-        // Sampled cells need their parent's final local for L2L; the parent's
-        // own M2L is included in the timed region only when it is sampled too,
-        // so parents are computed untimed first.
-        std::vector<char> need(nc, 0);
-        for (std::size_t i : sample)
-            for (long long q = t.cells[i].parent; q > 8; q = t.cells[static_cast<std::size_t>(q)].parent) need[static_cast<std::size_t>(q)] = 1;
-        std::vector<std::size_t> pre;
-        for (std::size_t i = 0; i < nc; ++i)
-            if (need[i]) pre.push_back(i);
-        for (std::size_t i : pre) m2l(t, i, p, ls.m2l[i]);
-        for (std::size_t i : pre)
-            if (t.cells[i].level >= 3) l2l(t, i, p);
+        // Only the cost is sampled: every cell gets a (zero) local expansion
+        // so a sampled cell's L2L has a parent local to read.
+        for (std::size_t i = 9; i < nc; ++i) t.cells[i].L.assign((p + 1) * (2 * p + 1), cd{0, 0});
         auto t3 = clk::now();
 #pragma omp parallel for schedule(dynamic, 1)
         for (std::size_t k = 0; k < sample.size(); ++k) {

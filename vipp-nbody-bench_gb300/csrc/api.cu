@@ -656,4 +656,6 @@ int gb_kernel_times(gb_ctx *ctx, double *ms, int64_t *launches, int n) {
 
 int64_t gb_launch_count(const gb_ctx *ctx) { return ctx ? ctx->ws.launches : 0; }
 
+void *gb_stream(gb_ctx *ctx) { return ctx ? static_cast<void *>(ctx->ws.st) : nullptr; }
+
 }  // extern "C"

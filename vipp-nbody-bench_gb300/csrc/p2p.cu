@@ -192,10 +192,11 @@ __global__ void __launch_bounds__(256) k_direct_f64(const double *__restrict__ x
             if (b + q == i) continue;
             const double dx = sx[q] - tx, dy = sy[q] - ty, dz = sz[q] - tz;
             const double r2 = dx * dx + dy * dy + dz * dz + eps2;
-            const double den = r2 * sqrt(r2);
-            ax += Gm * dx / den;
-            ay += Gm * dy / den;
-            az += Gm * dz / den;
+            const double ri = rsqrt(r2);
+            const double f = Gm * ri * ri * ri;
+            ax += f * dx;
+            ay += f * dy;
+            az += f * dz;
         }
         __syncthreads();
     }

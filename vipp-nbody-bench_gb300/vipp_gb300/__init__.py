@@ -27,7 +27,7 @@ TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
 # Every symbol include/vipp_gb300.h declares.
 EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_upload", "gb_download", "gb_rk4_step",
            "gb_accel", "gb_direct_accel", "gb_sync", "gb_get_stats", "gb_tree_dump", "gb_enable_timing",
-           "gb_kernel_times", "gb_launch_count", "gb_version")
+           "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream")
 
 
 class GbConfig(ctypes.Structure):
@@ -73,6 +73,8 @@ def load(path: str | None = None):
     lib.gb_launch_count.argtypes = [vp]
     lib.gb_launch_count.restype = ctypes.c_int64
     lib.gb_version.restype = ctypes.c_char_p
+    lib.gb_stream.argtypes = [vp]
+    lib.gb_stream.restype = vp
     _LIB = lib
     return lib
 
@@ -189,6 +191,10 @@ class Solver:
         cnt = np.zeros(n, np.int64)
         self._check(self.lib.gb_kernel_times(self.h, _ptr(ms), _ptr(cnt), n))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(TIMER_CLASSES)}
+
+    def stream_ptr(self) -> int:
+        """The context's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        return int(self.lib.gb_stream(self.h) or 0)
 
     def launch_count(self) -> int:
         return int(self.lib.gb_launch_count(self.h))

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/vipp_gb300.h"
+#include "direct.cuh"
 #include "workspace.cuh"
 
 namespace gb {
@@ -521,11 +522,14 @@ int gb_direct_accel(gb_ctx *ctx, const int64_t *targets, size_t ntargets, double
         }
         GB_TRY(cudaMemcpyAsync(ctx->d_targets, targets, sizeof(long long) * nt, cudaMemcpyHostToDevice, ws.st));
     }
-    if (3 * nt > ctx->direct_cap) {
-        GB_TRY(dalloc(ctx->d_direct, 3 * nt));
-        ctx->direct_cap = 3 * nt;
+    const unsigned nsplit = gb::direct_nsplit(ws.n, static_cast<unsigned>(nt), ws.num_sms);
+    const size_t need = 3 * nt * (1 + static_cast<size_t>(nsplit));  // result planes + per-slice partial sums
+    if (need > ctx->direct_cap) {
+        GB_TRY(dalloc(ctx->d_direct, need));
+        ctx->direct_cap = need;
     }
-    gb::direct_sum(ws, ws.x, targets ? ctx->d_targets : nullptr, static_cast<unsigned>(nt), ctx->d_direct);
+    gb::direct_sum(ws, ws.x, targets ? ctx->d_targets : nullptr, static_cast<unsigned>(nt), ctx->d_direct,
+                   ctx->d_direct + 3 * nt, nsplit);
     std::vector<double> soa(3 * nt);
     GB_TRY(cudaMemcpyAsync(soa.data(), ctx->d_direct, sizeof(double) * 3 * nt, cudaMemcpyDeviceToHost, ws.st));
     GB_TRY(cudaStreamSynchronize(ws.st));

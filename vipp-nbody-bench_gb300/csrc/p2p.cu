@@ -14,6 +14,7 @@
 // Pair term: rsqrt, optional Newton step, m r^-3 d; per-batch FP32 partial
 // sums folded into a compensated (Kahan) per-target accumulator. The
 // reference's factor G multiplies the near field only (fmm.hpp:539).
+#include "direct.cuh"
 #include "workspace.cuh"
 
 namespace gb {
@@ -169,44 +170,6 @@ __global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f64(const int2 *__restri
     }
 }
 
-// FP64 direct sum for listed targets over all particles (original order).
-// One thread per target; sources staged through shared memory.
-__global__ void __launch_bounds__(256) k_direct_f64(const double *__restrict__ x, unsigned n, const long long *__restrict__ targets,
-                                                    unsigned nt, double Gm, double eps2, double *__restrict__ out) {
-    __shared__ double sx[256], sy[256], sz[256];
-    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool act = k < nt;
-    const unsigned i = act ? (targets ? static_cast<unsigned>(targets[k]) : k) : 0u;
-    const double tx = act ? x[i] : 0.0, ty = act ? x[n + i] : 0.0, tz = act ? x[2 * static_cast<size_t>(n) + i] : 0.0;
-    double ax = 0, ay = 0, az = 0;
-    for (unsigned b = 0; b < n; b += 256) {
-        const unsigned j = b + threadIdx.x;
-        if (j < n) {
-            sx[threadIdx.x] = x[j];
-            sy[threadIdx.x] = x[n + j];
-            sz[threadIdx.x] = x[2 * static_cast<size_t>(n) + j];
-        }
-        __syncthreads();
-        const unsigned cnt = min(256u, n - b);
-        for (unsigned q = 0; q < cnt; ++q) {
-            if (b + q == i) continue;
-            const double dx = sx[q] - tx, dy = sy[q] - ty, dz = sz[q] - tz;
-            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
-            const double ri = rsqrt(r2);
-            const double f = Gm * ri * ri * ri;
-            ax += f * dx;
-            ay += f * dy;
-            az += f * dz;
-        }
-        __syncthreads();
-    }
-    if (act) {
-        out[k] = ax;
-        out[nt + k] = ay;
-        out[2 * static_cast<size_t>(nt) + k] = az;
-    }
-}
-
 }  // namespace
 
 bool g_p2p_newton = true;
@@ -249,9 +212,13 @@ void p2p_pass(Workspace &ws) {
     timer_end(ws, kTP2P);
 }
 
-void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, unsigned nt, double *out_soa) {
-    k_direct_f64<<<(nt + 255) / 256, 256, 0, ws.st>>>(x_orig, ws.n, targets, nt, ws.G * ws.m, ws.eps * ws.eps, out_soa);
-    ws.launches += 1;
+void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, unsigned nt, double *out_soa,
+                double *part, unsigned nsplit) {
+    const dim3 grid((nt + kDirectTB - 1) / kDirectTB, nsplit);
+    k_direct_part<SoA><<<grid, kDirectTB, 0, ws.st>>>(SoA{x_orig, ws.n}, ws.n, targets, nt, nsplit, ws.G * ws.m,
+                                                     ws.eps * ws.eps, part);
+    k_direct_reduce<<<(nt + 255) / 256, 256, 0, ws.st>>>(part, nt, nsplit, out_soa, nullptr);
+    ws.launches += 2;
 }
 
 }  // namespace gb

@@ -119,7 +119,8 @@ void m2l_pass(Workspace &ws);                 // M2L into L
 void downward_pass(Workspace &ws);            // L2L + L2P into far
 void p2p_pass(Workspace &ws);                 // near field into near
 void finalize_accel(Workspace &ws, double *acc_orig);  // acc[perm] = near + far
-void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, unsigned nt, double *out_soa);
+void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, unsigned nt, double *out_soa,
+                double *part, unsigned nsplit);  // part: [nsplit][3][nt] scratch
 
 // timing helpers
 void timer_begin(Workspace &ws, int cls);

@@ -117,6 +117,28 @@ GB_API int gb_accel(gb_ctx *ctx, double *a_aos, double *phi);
  * a_aos receives ntargets (or n) accelerations. */
 GB_API int gb_direct_accel(gb_ctx *ctx, const int64_t *targets, size_t ntargets, double *a_aos);
 
+/* No counterpart in the reference. The same FP64 direct softened sum as
+ * gb_direct_accel, for callers that cannot allocate GPU memory (hosts that own
+ * every device allocation through their own pool, runtimes that forbid
+ * cudaMalloc after start-up, plugins limited to the buffers they are handed).
+ * It creates no context and calls no cudaMalloc/cudaFree or allocating
+ * library routine: every input and output is the caller's device memory.
+ *   x_dev        n positions, AoS doubles, device memory
+ *   targets_dev  ntargets particle indices in [0, n) (device memory), or NULL
+ *                for all n particles; an index outside [0, n) yields NaN
+ *   a_dev        ntargets (or n) accelerations, AoS doubles, device memory
+ *   stream       cudaStream_t to run on (NULL: the legacy default stream)
+ * The kernels run on the calling thread's current device and are only
+ * queued: results are ready once `stream` reaches this point. Its scratch
+ * is one fixed 16 MiB device array inside the library, reserved on every
+ * GPU that loads it until the process exits; at most 699,050 targets fit
+ * (GB_ERR_CAPACITY beyond that). The first call on a device looks up that
+ * array's address and should come before any stream capture. All calls share
+ * the array, so calls that overlap on the GPU (other streams, other host
+ * threads) race; order them on one stream. */
+GB_API int gb_direct_accel_noalloc(const double *x_dev, size_t n, const int64_t *targets_dev, size_t ntargets, double G,
+                                   double m, double eps, double *a_dev, void *stream);
+
 /* Block until all queued work finished; reports deferred device errors. */
 GB_API int gb_sync(gb_ctx *ctx);
 GB_API int gb_get_stats(gb_ctx *ctx, gb_stats *out);

@@ -27,7 +27,7 @@ TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
 # Every symbol include/vipp_gb300.h declares.
 EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_upload", "gb_download", "gb_rk4_step",
            "gb_accel", "gb_direct_accel", "gb_sync", "gb_get_stats", "gb_tree_dump", "gb_enable_timing",
-           "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream")
+           "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream", "gb_direct_accel_noalloc")
 
 
 class GbConfig(ctypes.Structure):
@@ -75,6 +75,8 @@ def load(path: str | None = None):
     lib.gb_version.restype = ctypes.c_char_p
     lib.gb_stream.argtypes = [vp]
     lib.gb_stream.restype = vp
+    lib.gb_direct_accel_noalloc.argtypes = [vp, ctypes.c_size_t, vp, ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double, vp, vp]
     _LIB = lib
     return lib
 

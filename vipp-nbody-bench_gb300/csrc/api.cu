@@ -18,7 +18,6 @@ void rk4_stage(Workspace &ws, int stage, double dt);
 void rk4_restore(Workspace &ws);
 void aos_to_soa(Workspace &ws, const double *aos, double *soa, unsigned n);
 void soa_to_aos(Workspace &ws, const double *soa, double *aos, unsigned n);
-extern bool g_p2p_newton;
 
 struct PendingTimer {
     int cls;
@@ -86,16 +85,29 @@ void apply_config(gb_ctx *ctx) {
     ws.G = ctx->cfg.G;
     ws.m = ctx->cfg.m;
     ws.mixed = ctx->cfg.precision == GB_PREC_MIXED;
+    ws.p2p_newton = (ctx->cfg.flags & GB_FLAG_P2P_NEWTON) != 0;
 }
 
-// P2P work chunks: at most one partial chunk per leaf plus n/32 full ones.
-int ensure_chunks(gb_ctx *ctx) {
+// P2P work items: at most two partial chunks per leaf plus n/32 full ones,
+// plus source slices of leaves with long near-field lists (grown on demand).
+int ensure_chunks(gb_ctx *ctx, unsigned need_items = 0, unsigned need_part = 0) {
     gb::Workspace &ws = ctx->ws;
     if (!ws.c_cap) return GB_OK;
-    const unsigned ch = ws.c_cap + ws.n_cap / 32 + 64;
-    if (ch <= ws.ch_cap && ws.chunks) return GB_OK;
-    GB_TRY(dalloc(ws.chunks, ch));
-    ws.ch_cap = ch;
+    unsigned ch = 2 * ws.c_cap + ws.n_cap / 32 + 64;
+    if (need_items > ch) ch = need_items + need_items / 4;
+    if (ch > ws.ch_cap || !ws.chunks) {
+        GB_TRY(dalloc(ws.chunks, ch));
+        ws.ch_cap = ch;
+    }
+    unsigned pc = ws.part_cap ? ws.part_cap : 4096u;
+    if (need_part > pc) pc = need_part + need_part / 4;
+    if (pc > ws.part_cap || !ws.part) {
+        unsigned char *b = nullptr;
+        GB_TRY(dalloc(b, sizeof(double) * 96 * static_cast<size_t>(pc)));
+        dfree(ws.part);
+        ws.part = b;
+        ws.part_cap = pc;
+    }
     return GB_OK;
 }
 
@@ -175,6 +187,9 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
         GB_TRY(dalloc(ws.rng_len, c));
         GB_TRY(dalloc(ws.chunk_cnt, c + 1));
         GB_TRY(dalloc(ws.chunk_off, c + 1));
+        GB_TRY(dalloc(ws.src_total, c + 1));
+        GB_TRY(dalloc(ws.part_cnt, c + 1));
+        GB_TRY(dalloc(ws.part_off, c + 1));
         GB_TRY(gb::scan_temp_alloc(ws.scan, std::max(ws.n_cap + 1, c + 1)));
         GB_TRY(gb::sort_temp_alloc(ws.sort, std::max(ws.n_cap, s_cap)));
         ws.s_cap = s_cap;
@@ -240,17 +255,16 @@ void timer_end(Workspace &ws, int cls) {
 
 namespace {
 
-int check_device_errors(gb_ctx *ctx, unsigned *need_s, unsigned *need_r) {
+int check_device_errors(gb_ctx *ctx, unsigned *need) {
     gb::Workspace &ws = ctx->ws;
     GB_TRY(cudaMemcpyAsync(ws.h_info, ws.info, sizeof(gb::TreeInfo), cudaMemcpyDeviceToHost, ws.st));
-    unsigned counts[8];
+    unsigned counts[gb::kNumCounts];
     GB_TRY(cudaMemcpyAsync(counts, ws.d_counts, sizeof(counts), cudaMemcpyDeviceToHost, ws.st));
     GB_TRY(cudaStreamSynchronize(ws.st));
     GB_TRY(cudaGetLastError());
     collect_timers(ctx);
     const int err = ws.h_info->err;
-    if (need_s) *need_s = counts[6];
-    if (need_r) *need_r = counts[4];
+    if (need) std::memcpy(need, counts, sizeof(counts));
     if (err & gb::kDevNonFinite) {
         ctx->err = "non-finite position";
         return GB_ERR_NONFINITE;
@@ -278,13 +292,16 @@ void evaluate(gb_ctx *ctx) {
     gb::finalize_accel(ws, ws.acc);
 }
 
-// Grow capacities after an overflow reported by the device.
-int grow(gb_ctx *ctx, unsigned need_s, unsigned need_r) {
+// Grow capacities after an overflow reported by the device (counts holds
+// the sizes the evaluation asked for).
+int grow(gb_ctx *ctx, const unsigned *counts) {
     gb::Workspace &ws = ctx->ws;
-    const unsigned s = std::max(ws.s_cap, need_s + need_s / 2 + 64);
-    const unsigned r = std::max(ws.r_cap, need_r + need_r / 2 + 1024);
-    const bool s_grow = need_s > ws.s_cap;
-    return ensure_cells(ctx, s_grow ? s : ws.s_cap, need_r > ws.r_cap ? r : ws.r_cap);
+    const unsigned need_s = counts[6], need_r = counts[4], need_items = counts[7], need_part = counts[8];
+    const unsigned s = need_s > ws.s_cap ? need_s + need_s / 2 + 64 : ws.s_cap;
+    const unsigned r = need_r > ws.r_cap ? need_r + need_r / 2 + 1024 : ws.r_cap;
+    const int rc = ensure_cells(ctx, s, r);
+    if (rc) return rc;
+    return ensure_chunks(ctx, need_items, need_part);
 }
 
 // Run f (which queues one or more evaluations) until no capacity overflow.
@@ -292,10 +309,10 @@ template <typename F>
 int run_with_capacity(gb_ctx *ctx, F &&f) {
     for (int attempt = 0; attempt < 6; ++attempt) {
         f();
-        unsigned need_s = 0, need_r = 0;
-        const int rc = check_device_errors(ctx, &need_s, &need_r);
+        unsigned counts[gb::kNumCounts];
+        const int rc = check_device_errors(ctx, counts);
         if (rc != GB_ERR_CAPACITY) return rc;
-        const int g = grow(ctx, need_s, need_r);
+        const int g = grow(ctx, counts);
         if (g != GB_OK) return g;
     }
     ctx->err = "could not size the tree buffers";
@@ -358,7 +375,7 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     if ((e = cudaStreamCreateWithFlags(&ws.st, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream", e);
     if ((e = gb::upload_tables()) != cudaSuccess) return fail("tables", e);
     if ((e = cudaMalloc(&ws.info, sizeof(gb::TreeInfo))) != cudaSuccess) return fail("info", e);
-    if ((e = cudaMalloc(&ws.d_counts, 8 * sizeof(unsigned))) != cudaSuccess) return fail("counts", e);
+    if ((e = cudaMalloc(&ws.d_counts, gb::kNumCounts * sizeof(unsigned))) != cudaSuccess) return fail("counts", e);
     if ((e = cudaMalloc(&ws.queue, sizeof(unsigned))) != cudaSuccess) return fail("queue", e);
     if ((e = cudaMalloc(&ws.bbox_part, sizeof(double) * 6 * 2 * ws.num_sms)) != cudaSuccess) return fail("bbox", e);
     if ((e = cudaMallocHost(&ws.h_info, sizeof(gb::TreeInfo))) != cudaSuccess) return fail("pinned info", e);
@@ -382,7 +399,7 @@ void gb_destroy(gb_ctx *ctx) {
                     ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
-                    ws.chunk_off, ws.chunks, ws.queue, ws.ops_d, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
+                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
                     ctx->d_direct};
     for (void *b : bufs) dfree(b);
     gb::sort_temp_free(ws.sort);

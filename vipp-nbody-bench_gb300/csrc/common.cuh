@@ -52,6 +52,9 @@ struct TreeInfo {
     double root_max[3];
     double H[3];          // root box extents
     double S;             // max(H): length unit of the level-0 scaling
+    double key_scale[3];  // 2^21 / H: root box -> [0, 2^21) key coordinates
+    double key_margin;    // distance (key units) from an integer below which
+                          // a key is recomputed by exact midpoint bisection
     int nsplit_total;     // non-leaf cells
     int ncells;
     int nleaves;
@@ -67,6 +70,43 @@ struct TreeInfo {
     long long p2p_pairs;
     long long p2p_ranges;
 };
+
+// P2P work chunks of one leaf with n targets. Full chunks hold 32 targets; a
+// chunk of t < 32 targets runs floor(32/t) lane groups that share its sources,
+// so its cost is ~1/floor(32/t) of a full chunk. The remainder r = n mod 32 is
+// one chunk, or two halves when that is cheaper (r = 17..21).
+GB_HD bool chunk_split_rem(int r) { return r >= 17 && r <= 21; }
+GB_HD int chunk_count(int n) {
+    const int r = n % 32;
+    return n / 32 + (r == 0 ? 0 : (chunk_split_rem(r) ? 2 : 1));
+}
+GB_HD void chunk_at(int n, int q, int &off, int &len) {
+    const int full = n / 32, r = n % 32;
+    if (q < full) {
+        off = 32 * q, len = 32;
+    } else if (!chunk_split_rem(r)) {
+        off = 32 * full, len = r;
+    } else if (q == full) {
+        off = 32 * full, len = (r + 1) / 2;
+    } else {
+        off = 32 * full + (r + 1) / 2, len = r / 2;
+    }
+}
+
+// A chunk whose leaf has more than kSliceSources near-field sources runs as
+// several work items, each over a slice of the sources; their partial sums
+// are added in slice order afterwards. This bounds the longest work item.
+constexpr int kSliceSources = 8192;
+constexpr int kMaxSlices = 4095;
+GB_HD int slice_count(unsigned long long srcs) {
+    const unsigned long long s = (srcs + kSliceSources - 1) / kSliceSources;
+    return s < 1 ? 1 : (s > kMaxSlices ? kMaxSlices : static_cast<int>(s));
+}
+// Work-item field z: targets (6 bits), slice index (12 bits), slices (12 bits).
+GB_HD int item_pack(int nt, int s, int ns) { return nt | (s << 6) | (ns << 18); }
+GB_HD int item_nt(int z) { return z & 63; }
+GB_HD int item_slice(int z) { return (z >> 6) & 4095; }
+GB_HD int item_nslices(int z) { return (z >> 18) & 4095; }
 
 // Index of a real-basis coefficient: (n, 0) -> n^2; (n, m >= 1) real part ->
 // n^2 + 2m - 1, imaginary part -> n^2 + 2m.

@@ -112,7 +112,7 @@ __global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, double *__
     double *od = ops_d + static_cast<size_t>(b) * K * K;
     float *of = ops_f + static_cast<size_t>(b) * K * K;
     for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
-        const int ro = idx % K, ri = idx / K;  // input-major storage: [ri][ro]
+        const int ro = idx / K, ri = idx % K;  // output-major storage: [ro][ri]
         int j, k, po, n, m, pi;
         rdecode(ro, j, k, po);
         rdecode(ri, n, m, pi);
@@ -163,67 +163,123 @@ __global__ void __launch_bounds__(128) k_p2m(const int *__restrict__ leaves, con
     }
 }
 
-// --------------------------------------------------------------------- M2M
-// One block per non-leaf cell of level L (>= 2): M~ = sum_o M2M_o M~_child(o).
+// ------------------------------------------------------------ tile GEMM core
+// M2M, M2L and L2L are all D[64 targets][K] += A[64][K] x Op^T with a K x K
+// operator. Both operands sit in shared memory with the input index
+// contiguous and a row stride KS (elements) with KS * sizeof(T) = 16 mod 128
+// bytes, so the 16-byte vector loads of 8 consecutive rows fall into distinct
+// bank groups. 256 threads: ty = 0..15 owns 4 target rows, tx = 0..15 owns the
+// output columns tx + 16 j (j < NJ).
+constexpr int kTile = 64;
+
+constexpr int tile_stride(int K, int esz) {
+    int vw = 16 / esz;
+    int s = (K + vw - 1) / vw * vw;
+    while ((s * esz) % 128 != 16) s += vw;
+    return s;
+}
+
+template <int P, typename T>
+struct TileCfg {
+    static constexpr int K = (P + 1) * (P + 1);
+    static constexpr int KS = tile_stride(K, static_cast<int>(sizeof(T)));
+    static constexpr int KO = (K + 15) / 16 * 16;
+    static constexpr int NJ = KO / 16;
+    static constexpr int VW = 16 / static_cast<int>(sizeof(T));
+    static constexpr size_t smem = sizeof(T) * static_cast<size_t>(kTile + KO) * KS;
+};
+
 template <typename T>
-__global__ void __launch_bounds__(128) k_m2m(int L, const int *__restrict__ split_cell, const TreeInfo *__restrict__ info,
-                                             const int *__restrict__ c_child, int K, const T *__restrict__ ops, T *M) {
-    extern __shared__ unsigned char smraw[];
-    T *mc = reinterpret_cast<T *>(smraw);  // [8][K]
-    const int a = info->split_start[L], cnt = info->split_count[L];
-    const T *op0 = ops + static_cast<size_t>(kOpM2M) * K * K;
-    for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
-        const int P = split_cell[a + e];
-        const int fc = c_child[P];
-        for (int i = threadIdx.x; i < 8 * K; i += blockDim.x) mc[i] = M[static_cast<size_t>(fc) * K + i];
-        __syncthreads();
-        for (int r = threadIdx.x; r < K; r += blockDim.x) {
-            T s = 0;
-            for (int o = 0; o < 8; ++o) {
-                const T *op = op0 + static_cast<size_t>(o) * K * K;
-                const T *mo = mc + o * K;
-                for (int ci = 0; ci < K; ++ci) s += op[ci * K + r] * mo[ci];
-            }
-            M[static_cast<size_t>(P) * K + r] = s;
-        }
-        __syncthreads();
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using type = float4;
+};
+template <>
+struct Vec16<double> {
+    using type = double2;
+};
+
+__device__ __forceinline__ float vget(const float4 &v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
+__device__ __forceinline__ double vget(const double2 &v, int e) { return e == 0 ? v.x : v.y; }
+
+template <int P, typename T>
+__device__ __forceinline__ void tile_gemm(const T *__restrict__ A, const T *__restrict__ Op, T (&acc)[4][TileCfg<P, T>::NJ],
+                                          int ty, int tx) {
+    using C = TileCfg<P, T>;
+    using V = typename Vec16<T>::type;
+#pragma unroll 2
+    for (int ci = 0; ci < C::KS; ci += C::VW) {
+        V av[4], ov[C::NJ];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) av[a] = *reinterpret_cast<const V *>(A + (ty * 4 + a) * C::KS + ci);
+#pragma unroll
+        for (int j = 0; j < C::NJ; ++j) ov[j] = *reinterpret_cast<const V *>(Op + (tx + 16 * j) * C::KS + ci);
+#pragma unroll
+        for (int e = 0; e < C::VW; ++e)
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int j = 0; j < C::NJ; ++j) acc[a][j] += vget(av[a], e) * vget(ov[j], e);
     }
 }
 
+// Zero both tiles (padding stays zero: later loads write columns < K only).
+template <int P, typename T>
+__device__ __forceinline__ void tile_clear(T *sm) {
+    using C = TileCfg<P, T>;
+    for (int i = threadIdx.x; i < (kTile + C::KO) * C::KS; i += blockDim.x) sm[i] = T(0);
+}
+
+// Op tile <- operator oi (global, output-major K x K).
+template <int P, typename T>
+__device__ __forceinline__ void tile_load_op(T *Op, const T *__restrict__ ops, int oi) {
+    using C = TileCfg<P, T>;
+    const T *op = ops + static_cast<size_t>(oi) * C::K * C::K;
+    for (int i = threadIdx.x; i < C::K * C::K; i += blockDim.x) Op[(i / C::K) * C::KS + i % C::K] = op[i];
+}
+
+// A row t <- expansion of cell src[t] (zero when src[t] < 0).
+template <int P, typename T>
+__device__ __forceinline__ void tile_gather(T *A, const int *srcs, const T *__restrict__ X) {
+    using C = TileCfg<P, T>;
+    for (int i = threadIdx.x; i < kTile * C::K; i += blockDim.x) {
+        const int t = i / C::K, ci = i % C::K;
+        const int s = srcs[t];
+        A[t * C::KS + ci] = s >= 0 ? X[static_cast<size_t>(s) * C::K + ci] : T(0);
+    }
+}
+
+// --------------------------------------------------------------------- M2M
+// One block per non-leaf cell of level L (>= 2): M~ = sum_o M2M_o M~_child(o).
 // --------------------------------------------------------------------- M2L
 // Targets: every cell at level >= 2, grouped by octant (cells 1 + 8q + o share
 // octant o), so that one tile of 64 targets shares the same 189 source slots
 // (parent-neighbour d, child o') and each slot maps to one offset operator.
 // Per slot: gather the tile's source expansions, multiply by the operator.
-constexpr int kM2LTile = 64;
-
 template <int P, typename T>
 __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
                                              const T *__restrict__ ops, const T *__restrict__ M, T *__restrict__ Lx) {
-    constexpr int K = (P + 1) * (P + 1);
-    constexpr int KP = (K + 15) / 16 * 16;
-    constexpr int NJ = KP / 16;
-    extern __shared__ unsigned char smraw[];
-    T *A = reinterpret_cast<T *>(smraw);   // [64][KP]
-    T *Op = A + kM2LTile * KP;             // [K][KP]
-    __shared__ int srcs[kM2LTile];
+    using C = TileCfg<P, T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *A = reinterpret_cast<T *>(smraw);  // [64][KS]
+    T *Op = A + kTile * C::KS;             // [KO][KS]
+    __shared__ int srcs[kTile];
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int base = info->level_start[2];
     const int ntgt = info->n_targets_m2l;
     if (ntgt <= 0) return;
     const int per_class = ntgt / 8;
-    const int tiles_per_class = (per_class + kM2LTile - 1) / kM2LTile;
-    // zero the operator padding columns once
-    for (int i = tid; i < K * KP; i += 256)
-        if (i % KP >= K) Op[i] = 0;
+    const int tiles_per_class = (per_class + kTile - 1) / kTile;
+    tile_clear<P, T>(A);
     for (int w = blockIdx.x; w < 8 * tiles_per_class; w += gridDim.x) {
         const int cls = w % 8, tile = w / 8;
-        const int t0 = tile * kM2LTile;
-        T acc[4][NJ];
+        const int t0 = tile * kTile;
+        T acc[4][C::NJ];
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int j = 0; j < NJ; ++j) acc[a][j] = 0;
+            for (int j = 0; j < C::NJ; ++j) acc[a][j] = 0;
         const int uc[3] = {1 - (cls & 1), 1 - ((cls >> 1) & 1), 1 - ((cls >> 2) & 1)};
         for (int s = 0; s < kM2LSlots; ++s) {
             const int dd = s >> 3, o = s & 7;
@@ -231,34 +287,17 @@ __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, 
                                 2 * (dd / 9 - 1) + 1 - ((o >> 2) & 1) - uc[2]};
             if (off[0] >= -1 && off[0] <= 1 && off[1] >= -1 && off[1] <= 1 && off[2] >= -1 && off[2] <= 1) continue;
             int any = 0;
-            if (tid < kM2LTile) {
+            if (tid < kTile) {
                 const int t = t0 + tid;
                 const int src = t < per_class ? m2l_src[static_cast<size_t>(base + cls + 8 * t) * kM2LSlots + s] : -1;
                 srcs[tid] = src;
                 any = src >= 0;
             }
             if (!__syncthreads_or(any)) continue;
-            const int oi = (off[0] + 3) + 7 * (off[1] + 3) + 49 * (off[2] + 3);
-            const T *op = ops + static_cast<size_t>(oi) * K * K;
-            for (int i = tid; i < K * K; i += 256) Op[(i / K) * KP + i % K] = op[i];
-            for (int i = tid; i < kM2LTile * KP; i += 256) {
-                const int t = i / KP, ci = i % KP;
-                const int src = srcs[t];
-                A[i] = (src >= 0 && ci < K) ? M[static_cast<size_t>(src) * K + ci] : T(0);
-            }
+            tile_load_op<P, T>(Op, ops, (off[0] + 3) + 7 * (off[1] + 3) + 49 * (off[2] + 3));
+            tile_gather<P, T>(A, srcs, M);
             __syncthreads();
-#pragma unroll 4
-            for (int ci = 0; ci < K; ++ci) {
-                T av[4], ov[NJ];
-#pragma unroll
-                for (int a = 0; a < 4; ++a) av[a] = A[(ty * 4 + a) * KP + ci];
-#pragma unroll
-                for (int j = 0; j < NJ; ++j) ov[j] = Op[ci * KP + tx + 16 * j];
-#pragma unroll
-                for (int a = 0; a < 4; ++a)
-#pragma unroll
-                    for (int j = 0; j < NJ; ++j) acc[a][j] += av[a] * ov[j];
-            }
+            tile_gemm<P, T>(A, Op, acc, ty, tx);
             __syncthreads();
         }
 #pragma unroll
@@ -267,38 +306,105 @@ __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, 
             if (t >= per_class) continue;
             const size_t c = static_cast<size_t>(base + cls + 8 * t);
 #pragma unroll
-            for (int j = 0; j < NJ; ++j) {
+            for (int j = 0; j < C::NJ; ++j) {
                 const int r = tx + 16 * j;
-                if (r < K) Lx[c * K + r] = acc[a][j];
+                if (r < C::K) Lx[c * C::K + r] = acc[a][j];
             }
         }
     }
 }
 
-// --------------------------------------------------------------------- L2L
-// One block per non-leaf cell of level L-1 (>= 2): each child of level L gets
-// L~_child += L2L_o L~_parent.
-template <typename T>
-__global__ void __launch_bounds__(128) k_l2l(int Lp, const int *__restrict__ split_cell, const TreeInfo *__restrict__ info,
-                                             const int *__restrict__ c_child, int K, const T *__restrict__ ops, T *Lx) {
-    extern __shared__ unsigned char smraw[];
-    T *lp = reinterpret_cast<T *>(smraw);
-    const int a = info->split_start[Lp], cnt = info->split_count[Lp];
-    const T *op0 = ops + static_cast<size_t>(kOpL2L) * K * K;
-    for (int e = blockIdx.x; e < cnt; e += gridDim.x) {
-        const int P = split_cell[a + e];
-        const int fc = c_child[P];
-        for (int i = threadIdx.x; i < K; i += blockDim.x) lp[i] = Lx[static_cast<size_t>(P) * K + i];
-        __syncthreads();
+// M2M for one level L >= 2: tiles of 64 non-leaf cells, 8 octant slots
+// (child o of each cell through M2M_o).
+template <int P, typename T>
+__global__ void __launch_bounds__(256) k_m2m(int L, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell,
+                                             const int *__restrict__ c_child, const T *__restrict__ ops, T *M) {
+    using C = TileCfg<P, T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *A = reinterpret_cast<T *>(smraw);
+    T *Op = A + kTile * C::KS;
+    __shared__ int par[kTile], srcs[kTile];
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    const int e0 = info->split_start[L], cnt = info->split_count[L];
+    const int tiles = (cnt + kTile - 1) / kTile;
+    if (tiles == 0) return;
+    tile_clear<P, T>(A);
+    for (int w = blockIdx.x; w < tiles; w += gridDim.x) {
+        if (tid < kTile) {
+            const int e = w * kTile + tid;
+            par[tid] = e < cnt ? split_cell[e0 + e] : -1;
+        }
+        T acc[4][C::NJ];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int j = 0; j < C::NJ; ++j) acc[a][j] = 0;
         for (int o = 0; o < 8; ++o) {
-            const T *op = op0 + static_cast<size_t>(o) * K * K;
-            for (int r = threadIdx.x; r < K; r += blockDim.x) {
-                T s = 0;
-                for (int ci = 0; ci < K; ++ci) s += op[ci * K + r] * lp[ci];
-                Lx[static_cast<size_t>(fc + o) * K + r] += s;
+            __syncthreads();
+            if (tid < kTile) srcs[tid] = par[tid] >= 0 ? c_child[par[tid]] + o : -1;
+            __syncthreads();
+            tile_load_op<P, T>(Op, ops, kOpM2M + o);
+            tile_gather<P, T>(A, srcs, M);
+            __syncthreads();
+            tile_gemm<P, T>(A, Op, acc, ty, tx);
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int pc = par[ty * 4 + a];
+            if (pc < 0) continue;
+#pragma unroll
+            for (int j = 0; j < C::NJ; ++j) {
+                const int r = tx + 16 * j;
+                if (r < C::K) M[static_cast<size_t>(pc) * C::K + r] = acc[a][j];
             }
         }
         __syncthreads();
+    }
+}
+
+// L2L into level Lp+1 (Lp >= 2): for each octant o, tiles of 64 non-leaf cells
+// of level Lp; child o of each gets L~ += L2L_o L~_parent.
+template <int P, typename T>
+__global__ void __launch_bounds__(256) k_l2l(int Lp, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell,
+                                             const int *__restrict__ c_child, const T *__restrict__ ops, T *Lx) {
+    using C = TileCfg<P, T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *A = reinterpret_cast<T *>(smraw);
+    T *Op = A + kTile * C::KS;
+    __shared__ int par[kTile];
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    const int e0 = info->split_start[Lp], cnt = info->split_count[Lp];
+    const int tiles = (cnt + kTile - 1) / kTile;
+    if (tiles == 0) return;
+    tile_clear<P, T>(A);
+    for (int w = blockIdx.x; w < 8 * tiles; w += gridDim.x) {
+        const int o = w % 8, tile = w / 8;
+        __syncthreads();
+        if (tid < kTile) {
+            const int e = tile * kTile + tid;
+            par[tid] = e < cnt ? split_cell[e0 + e] : -1;
+        }
+        __syncthreads();
+        tile_load_op<P, T>(Op, ops, kOpL2L + o);
+        tile_gather<P, T>(A, par, Lx);
+        __syncthreads();
+        T acc[4][C::NJ];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int j = 0; j < C::NJ; ++j) acc[a][j] = 0;
+        tile_gemm<P, T>(A, Op, acc, ty, tx);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int pc = par[ty * 4 + a];
+            if (pc < 0) continue;
+            const size_t c = static_cast<size_t>(c_child[pc] + o);
+#pragma unroll
+            for (int j = 0; j < C::NJ; ++j) {
+                const int r = tx + 16 * j;
+                if (r < C::K) Lx[c * C::K + r] += acc[a][j];
+            }
+        }
     }
 }
 
@@ -397,14 +503,40 @@ void launch_l2p(Workspace &ws) {
 }
 
 template <int P, typename T>
+const T *ops_of(const Workspace &ws) {
+    return static_cast<const T *>(sizeof(T) == 4 ? static_cast<const void *>(ws.ops_f) : static_cast<const void *>(ws.ops_d));
+}
+
+template <int P, typename T>
 void launch_m2l(Workspace &ws) {
-    constexpr int K = (P + 1) * (P + 1);
-    constexpr int KP = (K + 15) / 16 * 16;
-    const size_t smem = sizeof(T) * (static_cast<size_t>(kM2LTile) * KP + static_cast<size_t>(K) * KP);
+    const size_t smem = TileCfg<P, T>::smem;
     cudaFuncSetAttribute(k_m2l<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     const unsigned gs = static_cast<unsigned>(ws.num_sms) * 2;
-    k_m2l<P, T><<<gs, 256, smem, ws.st>>>(ws.info, ws.m2l_src, static_cast<const T *>(ws.mixed ? (void *)ws.ops_f : (void *)ws.ops_d),
-                                          static_cast<const T *>(ws.Mexp), static_cast<T *>(ws.Lexp));
+    k_m2l<P, T><<<gs, 256, smem, ws.st>>>(ws.info, ws.m2l_src, ops_of<P, T>(ws), static_cast<const T *>(ws.Mexp),
+                                          static_cast<T *>(ws.Lexp));
+    ws.launches += 1;
+}
+
+template <int P, typename T>
+void launch_m2m_levels(Workspace &ws) {
+    const size_t smem = TileCfg<P, T>::smem;
+    cudaFuncSetAttribute(k_m2m<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 2;
+    for (int L = kMaxLevel - 1; L >= 2; --L) {
+        k_m2m<P, T><<<gs, 256, smem, ws.st>>>(L, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws), static_cast<T *>(ws.Mexp));
+        ws.launches += 1;
+    }
+}
+
+template <int P, typename T>
+void launch_l2l_levels(Workspace &ws) {
+    const size_t smem = TileCfg<P, T>::smem;
+    cudaFuncSetAttribute(k_l2l<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 2;
+    for (int Lp = 2; Lp <= kMaxLevel - 1; ++Lp) {
+        k_l2l<P, T><<<gs, 256, smem, ws.st>>>(Lp, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws), static_cast<T *>(ws.Lexp));
+        ws.launches += 1;
+    }
 }
 
 template <typename T>
@@ -415,6 +547,8 @@ void dispatch_p(Workspace &ws, int which) {
         if (which == 0) launch_p2m<PP, T>(ws); \
         if (which == 1) launch_m2l<PP, T>(ws); \
         if (which == 2) launch_l2p<PP, T>(ws); \
+        if (which == 3) launch_m2m_levels<PP, T>(ws); \
+        if (which == 4) launch_l2l_levels<PP, T>(ws); \
         break;
         GB_CASE(1)
         GB_CASE(2)
@@ -444,22 +578,14 @@ void build_operators(Workspace &ws) {
 
 void upward_pass(Workspace &ws) {
     timer_begin(ws, kTUp);
-    if (ws.mixed)
+    if (ws.mixed) {
         dispatch_p<float>(ws, 0);
-    else
+        dispatch_p<float>(ws, 3);
+    } else {
         dispatch_p<double>(ws, 0);
-    ws.launches += 1;
-    const int K = ws.K;
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 4;
-    for (int L = kMaxLevel - 1; L >= 2; --L) {
-        if (ws.mixed)
-            k_m2m<float><<<gs, 128, sizeof(float) * 8 * K, ws.st>>>(L, ws.split_cell, ws.info, ws.c_child, K, ws.ops_f,
-                                                                 static_cast<float *>(ws.Mexp));
-        else
-            k_m2m<double><<<gs, 128, sizeof(double) * 8 * K, ws.st>>>(L, ws.split_cell, ws.info, ws.c_child, K, ws.ops_d,
-                                                                   static_cast<double *>(ws.Mexp));
-        ws.launches += 1;
+        dispatch_p<double>(ws, 3);
     }
+    ws.launches += 1;
     timer_end(ws, kTUp);
 }
 
@@ -469,29 +595,20 @@ void m2l_pass(Workspace &ws) {
         dispatch_p<float>(ws, 1);
     else
         dispatch_p<double>(ws, 1);
-    ws.launches += 1;
     timer_end(ws, kTM2L);
 }
 
 void downward_pass(Workspace &ws) {
     timer_begin(ws, kTDown);
-    const int K = ws.K;
     const size_t esz = ws.mixed ? sizeof(float) : sizeof(double);
     cudaMemsetAsync(ws.farf, 0, esz * 3 * ws.n, ws.st);
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 4;
-    for (int Lp = 2; Lp <= kMaxLevel - 1; ++Lp) {
-        if (ws.mixed)
-            k_l2l<float><<<gs, 128, sizeof(float) * K, ws.st>>>(Lp, ws.split_cell, ws.info, ws.c_child, K, ws.ops_f,
-                                                             static_cast<float *>(ws.Lexp));
-        else
-            k_l2l<double><<<gs, 128, sizeof(double) * K, ws.st>>>(Lp, ws.split_cell, ws.info, ws.c_child, K, ws.ops_d,
-                                                               static_cast<double *>(ws.Lexp));
-        ws.launches += 1;
-    }
-    if (ws.mixed)
+    if (ws.mixed) {
+        dispatch_p<float>(ws, 4);
         dispatch_p<float>(ws, 2);
-    else
+    } else {
+        dispatch_p<double>(ws, 4);
         dispatch_p<double>(ws, 2);
+    }
     ws.launches += 1;
     timer_end(ws, kTDown);
 }

@@ -1,19 +1,24 @@
 // Near field (P2P, gravity/include/fmm.hpp:377-385, 513-540) and the FP64
 // direct-sum oracle (solver_ref_naive.hpp:103-119) on the GPU.
 //
-// Work decomposition: every leaf is cut into chunks of 32 targets; a
+// Work decomposition: every leaf is cut into chunks (common.cuh chunk_at):
+// full chunks of 32 targets, and remainders of t < 32 targets that run
+// floor(32/t) lane groups over disjoint subsets of the same sources (combined
+// at the end through shared memory), so small leaves keep most lanes busy. A
 // persistent grid of warps pulls chunks from a device counter (work queue).
 // A warp streams the leaf's near-field source ranges through shared memory
-// 32 sources at a time; every lane owns one target and visits the staged
-// sources in the same order (broadcast shared-memory reads).
+// 32 sources at a time, prefetching the next batch into registers while it
+// works on the current one; lanes read the staged sources with broadcast
+// shared-memory loads.
 //
 // Mixed precision (FP32): positions are kept as hi + lo float pairs relative
 // to the root-box centre; targets and staged sources are re-expressed relative
 // to the target leaf's centre ((hi - c_hi) + (lo - c_lo)), so FP32 differences
 // carry ~1e-7 of the neighbourhood size rather than of the coordinate.
-// Pair term: rsqrt, optional Newton step, m r^-3 d; per-batch FP32 partial
-// sums folded into a compensated (Kahan) per-target accumulator. The
-// reference's factor G multiplies the near field only (fmm.hpp:539).
+// Pair term: rsqrt.approx.ftz (a Newton step on request: it leaves the RMS
+// error unchanged to 1e-10 at 20% of the cost), r^-3 d (equal masses: m
+// and the reference's G, fmm.hpp:539, multiply the sum once); per-batch FP32
+// partial sums folded into a compensated (Kahan) per-target accumulator.
 #include "direct.cuh"
 #include "workspace.cuh"
 
@@ -37,15 +42,82 @@ __device__ __forceinline__ RootC leaf_centre(const double *c_ctr, int c, const T
     return r;
 }
 
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Source-batch cursor over a slice [v0, v0 + len) of the concatenation of a
+// leaf's source ranges; batches never cross a range end.
+struct Cursor {
+    const uint2 *rng;
+    unsigned nr, r, b, end, rem;
+    __device__ __forceinline__ void start(const uint2 *ranges, unsigned n, unsigned v0, unsigned len) {
+        rng = ranges, nr = n, r = 0, rem = len, b = 0, end = 0;
+        for (; r < nr; ++r) {
+            const uint2 g = rng[r];
+            if (v0 < g.y - g.x) {
+                b = g.x + v0, end = g.y;
+                break;
+            }
+            v0 -= g.y - g.x;
+        }
+        if (rem == 0) r = nr;
+    }
+    __device__ __forceinline__ bool valid() const { return r < nr; }
+    __device__ __forceinline__ unsigned count() const { return min(min(32u, end - b), rem); }
+    __device__ __forceinline__ void advance() {
+        const unsigned c = count();
+        rem -= c, b += c;
+        if (rem == 0) {
+            r = nr;
+        } else if (b >= end && ++r < nr) {
+            const uint2 g = rng[r];
+            b = g.x, end = g.y;
+        }
+    }
+};
+
+// Work item -> (leaf, first target, targets, slice, slices, partial slot,
+// source slice [v0, v0 + len)).
+struct Item {
+    int li, t0, nt, sl, ns, pslot;
+    unsigned v0, len;
+    __device__ __forceinline__ Item(const int4 w, const unsigned *src_total) {
+        li = w.x, t0 = w.y, nt = item_nt(w.z), sl = item_slice(w.z), ns = item_nslices(w.z), pslot = w.w;
+        const unsigned S = src_total[li];
+        const unsigned per = (S + ns - 1) / ns;
+        v0 = min(S, sl * per);
+        len = min(per, S - v0);
+    }
+};
+
 template <bool kNewton, bool kSoft>
-__global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f32(const int2 *__restrict__ chunks, const unsigned *counts,
+__device__ __forceinline__ void pair_f32(const float4 s, float tx, float ty, float tz, float eps2, float &bx, float &by,
+                                         float &bz) {
+    const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+    float ri = rsqrt_ftz(r2);
+    if (kNewton) ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
+    if (!kSoft) ri = r2 > 0.f ? ri : 0.f;
+    const float f = ri * (ri * ri);
+    bx = fmaf(dx, f, bx);
+    by = fmaf(dy, f, by);
+    bz = fmaf(dz, f, bz);
+}
+
+template <bool kNewton, bool kSoft>
+__global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f32(const int4 *__restrict__ chunks, const unsigned *counts,
                                                             unsigned *queue, const int *__restrict__ leaves,
-                                                            const int *__restrict__ c_end, const double *__restrict__ c_ctr,
+                                                            const double *__restrict__ c_ctr,
                                                             const TreeInfo *__restrict__ info, const unsigned *__restrict__ rng_off,
                                                             const unsigned *__restrict__ rng_len, const uint2 *__restrict__ ranges,
                                                             const float4 *__restrict__ ph, const float4 *__restrict__ pl,
-                                                            float G, float eps2, float *__restrict__ nearv, unsigned n) {
+                                                            const unsigned *__restrict__ src_total, float *__restrict__ part,
+                                                            float Gm, float eps2, float *__restrict__ nearv, unsigned n) {
     __shared__ float4 src[kP2PWarps][32];
+    __shared__ float red[kP2PWarps][3][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned nch = counts[5];
     while (true) {
@@ -53,75 +125,87 @@ __global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f32(const int2 *__restri
         if (lane == 0) ci = atomicAdd(queue, 1u);
         ci = __shfl_sync(0xffffffffu, ci, 0);
         if (ci >= nch) break;
-        const int2 ch = chunks[ci];
-        const int li = ch.x;
-        const int c = leaves[li];
-        const int te = c_end[c];
-        const int i = ch.y + lane;
-        const bool act = i < te;
-        const RootC cc = leaf_centre(c_ctr, c, info);
+        const Item it(chunks[ci], src_total);
+        const int nt = it.nt;
+        const int g = 32 / nt;
+        const int grp = lane / nt;
+        const int t = lane - grp * nt;
+        const bool tact = grp < g;
+        const int i = it.t0 + t;
+        const RootC cc = leaf_centre(c_ctr, leaves[it.li], info);
         float tx = 0, ty = 0, tz = 0;
-        if (act) {
+        if (tact) {
             const float4 h = ph[i], l = pl[i];
             tx = (h.x - cc.hx) + (l.x - cc.lx);
             ty = (h.y - cc.hy) + (l.y - cc.ly);
             tz = (h.z - cc.hz) + (l.z - cc.lz);
         }
         float sx = 0, sy = 0, sz = 0, kx = 0, ky = 0, kz = 0;  // Kahan sums and compensations
-        const unsigned r0 = rng_off[li], nr = rng_len[li];
-        for (unsigned r = 0; r < nr; ++r) {
-            const uint2 rg = ranges[r0 + r];
-            for (unsigned b = rg.x; b < rg.y; b += 32) {
-                const unsigned j = b + lane;
-                const unsigned cnt = min(32u, rg.y - b);
-                if (j < rg.y) {
-                    const float4 h = ph[j], l = pl[j];
-                    src[w][lane] = make_float4((h.x - cc.hx) + (l.x - cc.lx), (h.y - cc.hy) + (l.y - cc.ly),
-                                               (h.z - cc.hz) + (l.z - cc.lz), h.w);
-                }
-                __syncwarp();
-                float bx = 0, by = 0, bz = 0;
-#pragma unroll 8
-                for (unsigned k = 0; k < cnt; ++k) {
-                    const float4 s = src[w][k];
-                    const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    float ri = rsqrtf(r2);
-                    if (kNewton) ri = ri * fmaf(-0.5f * r2 * ri, ri, 1.5f);
-                    if (!kSoft) ri = r2 > 0.f ? ri : 0.f;
-                    const float mr = s.w * ri;
-                    const float f = mr * (ri * ri);
-                    bx = fmaf(dx, f, bx);
-                    by = fmaf(dy, f, by);
-                    bz = fmaf(dz, f, bz);
-                }
-                __syncwarp();
-                {
-                    float y = bx - kx, t = sx + y;
-                    kx = (t - sx) - y, sx = t;
-                    y = by - ky, t = sy + y;
-                    ky = (t - sy) - y, sy = t;
-                    y = bz - kz, t = sz + y;
-                    kz = (t - sz) - y, sz = t;
-                }
-            }
+        Cursor cur;
+        cur.start(ranges + rng_off[it.li], rng_len[it.li], it.v0, it.len);
+        float4 h = make_float4(0, 0, 0, 0), l = h;
+        unsigned cnt = 0;
+        if (cur.valid()) {
+            cnt = cur.count();
+            if (static_cast<unsigned>(lane) < cnt) h = ph[cur.b + lane], l = pl[cur.b + lane];
         }
-        if (act) {
-            nearv[i] = G * sx;
-            nearv[n + i] = G * sy;
-            nearv[2 * static_cast<size_t>(n) + i] = G * sz;
+        while (cnt) {
+            if (static_cast<unsigned>(lane) < cnt)
+                src[w][lane] = make_float4((h.x - cc.hx) + (l.x - cc.lx), (h.y - cc.hy) + (l.y - cc.ly),
+                                           (h.z - cc.hz) + (l.z - cc.lz), 0.f);
+            __syncwarp();
+            const unsigned now = cnt;
+            cur.advance();
+            cnt = 0;
+            if (cur.valid()) {  // prefetch the next batch while this one is computed
+                cnt = cur.count();
+                if (static_cast<unsigned>(lane) < cnt) h = ph[cur.b + lane], l = pl[cur.b + lane];
+            }
+            float bx = 0, by = 0, bz = 0;
+            if (g == 1 && now == 32) {
+#pragma unroll
+                for (int k = 0; k < 32; ++k) pair_f32<kNewton, kSoft>(src[w][k], tx, ty, tz, eps2, bx, by, bz);
+            } else if (tact) {
+                for (unsigned k = grp; k < now; k += g) pair_f32<kNewton, kSoft>(src[w][k], tx, ty, tz, eps2, bx, by, bz);
+            }
+            __syncwarp();
+            float y = bx - kx, tt = sx + y;
+            kx = (tt - sx) - y, sx = tt;
+            y = by - ky, tt = sy + y;
+            ky = (tt - sy) - y, sy = tt;
+            y = bz - kz, tt = sz + y;
+            kz = (tt - sz) - y, sz = tt;
+        }
+        sx -= kx, sy -= ky, sz -= kz;
+        if (g > 1) {
+            red[w][0][lane] = sx, red[w][1][lane] = sy, red[w][2][lane] = sz;
+            __syncwarp();
+            if (grp == 0)
+                for (int q = 1; q < g; ++q) sx += red[w][0][t + q * nt], sy += red[w][1][t + q * nt], sz += red[w][2][t + q * nt];
+            __syncwarp();
+        }
+        if (grp == 0) {
+            if (it.ns == 1) {
+                nearv[i] = Gm * sx;
+                nearv[n + i] = Gm * sy;
+                nearv[2 * static_cast<size_t>(n) + i] = Gm * sz;
+            } else {
+                float *o = part + static_cast<size_t>(it.pslot) * 96;
+                o[t] = sx, o[32 + t] = sy, o[64 + t] = sz;
+            }
         }
     }
 }
 
 template <bool kSoft>
-__global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f64(const int2 *__restrict__ chunks, const unsigned *counts,
-                                                            unsigned *queue, const int *__restrict__ leaves,
-                                                            const int *__restrict__ c_end, const unsigned *__restrict__ rng_off,
+__global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f64(const int4 *__restrict__ chunks, const unsigned *counts,
+                                                            unsigned *queue, const unsigned *__restrict__ rng_off,
                                                             const unsigned *__restrict__ rng_len, const uint2 *__restrict__ ranges,
-                                                            const double *__restrict__ xs, double Gm, double eps2,
+                                                            const double *__restrict__ xs, const unsigned *__restrict__ src_total,
+                                                            double *__restrict__ part, double Gm, double eps2,
                                                             double *__restrict__ nearv, unsigned n) {
     __shared__ double src[kP2PWarps][3][32];
+    __shared__ double red[kP2PWarps][3][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned nch = counts[5];
     while (true) {
@@ -129,50 +213,80 @@ __global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f64(const int2 *__restri
         if (lane == 0) ci = atomicAdd(queue, 1u);
         ci = __shfl_sync(0xffffffffu, ci, 0);
         if (ci >= nch) break;
-        const int2 ch = chunks[ci];
-        const int li = ch.x;
-        const int c = leaves[li];
-        const int te = c_end[c];
-        const int i = ch.y + lane;
-        const bool act = i < te;
-        const double tx = act ? xs[i] : 0.0, ty = act ? xs[n + i] : 0.0, tz = act ? xs[2 * static_cast<size_t>(n) + i] : 0.0;
+        const Item it(chunks[ci], src_total);
+        const int nt = it.nt;
+        const int g = 32 / nt;
+        const int grp = lane / nt;
+        const int t = lane - grp * nt;
+        const bool tact = grp < g;
+        const int i = it.t0 + t;
+        const double tx = tact ? xs[i] : 0.0, ty = tact ? xs[n + i] : 0.0, tz = tact ? xs[2 * static_cast<size_t>(n) + i] : 0.0;
         double ax = 0, ay = 0, az = 0;
-        const unsigned r0 = rng_off[li], nr = rng_len[li];
-        for (unsigned r = 0; r < nr; ++r) {
-            const uint2 rg = ranges[r0 + r];
-            for (unsigned b = rg.x; b < rg.y; b += 32) {
-                const unsigned j = b + lane;
-                const unsigned cnt = min(32u, rg.y - b);
-                if (j < rg.y) {
-                    src[w][0][lane] = xs[j];
-                    src[w][1][lane] = xs[n + j];
-                    src[w][2][lane] = xs[2 * static_cast<size_t>(n) + j];
-                }
-                __syncwarp();
-                for (unsigned k = 0; k < cnt; ++k) {
+        Cursor cur;
+        cur.start(ranges + rng_off[it.li], rng_len[it.li], it.v0, it.len);
+        while (cur.valid()) {
+            const unsigned cnt = cur.count();
+            if (static_cast<unsigned>(lane) < cnt) {
+                const unsigned j = cur.b + lane;
+                src[w][0][lane] = xs[j];
+                src[w][1][lane] = xs[n + j];
+                src[w][2][lane] = xs[2 * static_cast<size_t>(n) + j];
+            }
+            __syncwarp();
+            if (tact)
+                for (unsigned k = grp; k < cnt; k += g) {
                     const double dx = src[w][0][k] - tx, dy = src[w][1][k] - ty, dz = src[w][2][k] - tz;
                     const double r2 = dx * dx + dy * dy + dz * dz + eps2;
                     double ri = rsqrt(r2);
                     if (!kSoft) ri = r2 > 0.0 ? ri : 0.0;
-                    const double f = Gm * ri * ri * ri;
+                    const double f = ri * ri * ri;
                     ax += f * dx;
                     ay += f * dy;
                     az += f * dz;
                 }
-                __syncwarp();
+            __syncwarp();
+            cur.advance();
+        }
+        if (g > 1) {
+            red[w][0][lane] = ax, red[w][1][lane] = ay, red[w][2][lane] = az;
+            __syncwarp();
+            if (grp == 0)
+                for (int q = 1; q < g; ++q) ax += red[w][0][t + q * nt], ay += red[w][1][t + q * nt], az += red[w][2][t + q * nt];
+            __syncwarp();
+        }
+        if (grp == 0) {
+            if (it.ns == 1) {
+                nearv[i] = Gm * ax;
+                nearv[n + i] = Gm * ay;
+                nearv[2 * static_cast<size_t>(n) + i] = Gm * az;
+            } else {
+                double *o = part + static_cast<size_t>(it.pslot) * 96;
+                o[t] = ax, o[32 + t] = ay, o[64 + t] = az;
             }
         }
-        if (act) {
-            nearv[i] = ax;
-            nearv[n + i] = ay;
-            nearv[2 * static_cast<size_t>(n) + i] = az;
+    }
+}
+
+// Sum the slices of every split chunk in slice order (deterministic).
+template <typename T>
+__global__ void k_p2p_combine(const int4 *__restrict__ chunks, const unsigned *counts, const T *__restrict__ part, T scale,
+                              T *__restrict__ nearv, unsigned n) {
+    const unsigned nit = counts[5];
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nit * 32u; q += gridDim.x * blockDim.x) {
+        const int4 w = chunks[q >> 5];
+        const int t = static_cast<int>(q & 31u);
+        const int ns = item_nslices(w.z);
+        if (ns <= 1 || item_slice(w.z) != 0 || t >= item_nt(w.z)) continue;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            T s = 0;
+            for (int k = 0; k < ns; ++k) s += part[static_cast<size_t>(w.w + k) * 96 + 32 * a + t];
+            nearv[static_cast<size_t>(a) * n + w.y + t] = scale * s;
         }
     }
 }
 
 }  // namespace
-
-bool g_p2p_newton = true;
 
 void p2p_pass(Workspace &ws) {
     timer_begin(ws, kTP2P);
@@ -181,12 +295,14 @@ void p2p_pass(Workspace &ws) {
     const bool soft = ws.eps > 0;
     if (ws.mixed) {
         const float eps2 = static_cast<float>(ws.eps * ws.eps);
-        const float G = static_cast<float>(ws.G);
+        const float Gm = static_cast<float>(ws.G * ws.m);
         auto *o = static_cast<float *>(ws.nearf);
+        auto *pf = static_cast<float *>(ws.part);
 #define GB_P2P32(NW, SF)                                                                                                \
-    k_p2p_f32<NW, SF><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.leaves, ws.c_end, ws.c_ctr, \
-                                                        ws.info, ws.rng_off, ws.rng_len, ws.ranges, ws.ph, ws.pl, G, eps2, o, ws.n)
-        if (g_p2p_newton) {
+    k_p2p_f32<NW, SF><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.leaves, ws.c_ctr, ws.info, \
+                                                        ws.rng_off, ws.rng_len, ws.ranges, ws.ph, ws.pl, ws.src_total, pf, \
+                                                        Gm, eps2, o, ws.n)
+        if (ws.p2p_newton) {
             if (soft)
                 GB_P2P32(true, true);
             else
@@ -198,17 +314,20 @@ void p2p_pass(Workspace &ws) {
                 GB_P2P32(false, false);
         }
 #undef GB_P2P32
+        k_p2p_combine<float><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, pf, Gm, o, ws.n);
     } else {
         const double Gm = ws.G * ws.m, eps2 = ws.eps * ws.eps;
         auto *o = static_cast<double *>(ws.nearf);
+        auto *pd = static_cast<double *>(ws.part);
         if (soft)
-            k_p2p_f64<true><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.leaves, ws.c_end, ws.rng_off,
-                                                              ws.rng_len, ws.ranges, ws.xs, Gm, eps2, o, ws.n);
+            k_p2p_f64<true><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.rng_off, ws.rng_len,
+                                                              ws.ranges, ws.xs, ws.src_total, pd, Gm, eps2, o, ws.n);
         else
-            k_p2p_f64<false><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.leaves, ws.c_end,
-                                                               ws.rng_off, ws.rng_len, ws.ranges, ws.xs, Gm, eps2, o, ws.n);
+            k_p2p_f64<false><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.rng_off, ws.rng_len,
+                                                               ws.ranges, ws.xs, ws.src_total, pd, Gm, eps2, o, ws.n);
+        k_p2p_combine<double><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, pd, Gm, o, ws.n);
     }
-    ws.launches += 1;
+    ws.launches += 2;
     timer_end(ws, kTP2P);
 }
 

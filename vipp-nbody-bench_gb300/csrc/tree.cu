@@ -31,8 +31,6 @@ namespace {
 
 constexpr int kTB = 256;
 
-__device__ __forceinline__ unsigned long long u64(uint64_t v) { return static_cast<unsigned long long>(v); }
-
 __global__ void k_bbox_partial(const double *__restrict__ x, unsigned n, double *__restrict__ part, TreeInfo *info) {
     double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
     bool bad = false;
@@ -73,14 +71,32 @@ __global__ void k_bbox_final(const double *__restrict__ part, int nb, TreeInfo *
         for (int b = 0; b < nb; ++b) mn[a] = fmin(mn[a], part[a * nb + b]), mx[a] = fmax(mx[a], part[(3 + a) * nb + b]);
     }
     const double pad = 1e-5;  // Problem::OCTREE_WIDTH_PADDING (problem.hpp:167)
-    double S = 0;
+    double S = 0, margin = 0;
     for (int a = 0; a < 3; ++a) {
         info->root_min[a] = mn[a] - pad;
         info->root_max[a] = mx[a] + pad;
         info->H[a] = info->root_max[a] - info->root_min[a];
         S = fmax(S, info->H[a]);
+        info->key_scale[a] = ldexp(1.0, kMaxLevel) / info->H[a];
+        // Recursive FP64 midpoints stray from the ideal ones by at most
+        // 21/2 ulp(max|bound|) and u = (x - lo) 2^21 / H carries about one more
+        // ulp; in key units that is < 12 * 2^-52 * 2^21 * max|bound| / H.
+        const double big = fmax(fabs(info->root_min[a]), fabs(info->root_max[a]));
+        margin = fmax(margin, 64.0 * ldexp(big / info->H[a], -31) + ldexp(1.0, -30));
     }
     info->S = S;
+    info->key_margin = margin;
+}
+
+// Spread the 21 low bits of v to every third bit.
+__device__ __forceinline__ uint64_t spread3(uint64_t v) {
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
 }
 
 // Child offsets of 21 levels of recursive midpoints (see file comment).
@@ -89,6 +105,28 @@ __global__ void k_keys(const double *__restrict__ x, unsigned n, const TreeInfo 
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double p[3] = {x[i], x[static_cast<size_t>(n) + i], x[2 * static_cast<size_t>(n) + i]};
+    // Fast path: every split decision of the 21 levels compares x with a
+    // midpoint that sits at an integer of u = (x - lo) 2^21 / H up to the
+    // rounding bounded by key_margin, so away from integers the child offsets
+    // are the complemented bits of floor(u).
+    {
+        const double margin = info->key_margin;
+        bool ok = margin < 0.25;
+        uint64_t k[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double u = (p[a] - info->root_min[a]) * info->key_scale[a];
+            const double f = floor(u);
+            const double fr = u - f;
+            ok &= u >= 0.0 && u < 2097152.0 && fr > margin && fr < 1.0 - margin;
+            k[a] = ok ? (~static_cast<uint64_t>(f)) & 0x1fffffull : 0;
+        }
+        if (ok) {
+            keys[i] = spread3(k[0]) | (spread3(k[1]) << 1) | (spread3(k[2]) << 2);
+            perm[i] = i;
+            return;
+        }
+    }
     double lo[3] = {info->root_min[0], info->root_min[1], info->root_min[2]};
     double hi[3] = {info->root_max[0], info->root_max[1], info->root_max[2]};
     uint64_t key = 0;
@@ -449,16 +487,27 @@ __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts
 // subtree, i.e. a contiguous particle range in tree order.
 __global__ void k_rng_count(const int *__restrict__ leaves, const unsigned *counts, const int *__restrict__ c_parent,
                             const int *__restrict__ c_begin, const int *__restrict__ c_end,
-                            const int *__restrict__ p2p_cnt, unsigned *rng_cnt, unsigned *chunk_cnt) {
+                            const int *__restrict__ p2p_own, const int *__restrict__ p2p_cnt, unsigned *rng_cnt,
+                            unsigned *chunk_cnt, unsigned *src_total, unsigned *part_cnt) {
     const unsigned NL = counts[3];
     for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < NL; li += gridDim.x * blockDim.x) {
         const int c = leaves[li];
         const int nt = c_end[c] - c_begin[c];
         unsigned tot = 0;
+        unsigned long long srcs = 0;
         if (nt > 0)
-            for (int a = c; a >= 0; a = c_parent[a]) tot += static_cast<unsigned>(p2p_cnt[a]);
+            for (int a = c; a >= 0; a = c_parent[a]) {
+                tot += static_cast<unsigned>(p2p_cnt[a]);
+                for (int q = 0; q < p2p_cnt[a]; ++q) {
+                    const int u = p2p_own[static_cast<size_t>(a) * kNbrCap + q];
+                    srcs += static_cast<unsigned>(c_end[u] - c_begin[u]);
+                }
+            }
         rng_cnt[li] = tot;
-        chunk_cnt[li] = static_cast<unsigned>((nt + 31) / 32);
+        const unsigned ns = nt > 0 ? static_cast<unsigned>(slice_count(srcs)) : 1u;
+        chunk_cnt[li] = static_cast<unsigned>(chunk_count(nt)) * ns;
+        part_cnt[li] = ns > 1 ? static_cast<unsigned>(chunk_count(nt)) * ns : 0u;
+        src_total[li] = static_cast<unsigned>(srcs < 0xffffffffull ? srcs : 0xffffffffull);
     }
 }
 
@@ -466,7 +515,8 @@ __global__ void k_rng_fill(const int *__restrict__ leaves, const unsigned *count
                            const int *__restrict__ c_parent, const int *__restrict__ c_begin, const int *__restrict__ c_end,
                            const int *__restrict__ p2p_own, const int *__restrict__ p2p_cnt,
                            const unsigned *__restrict__ rng_off, unsigned *rng_len, uint2 *ranges,
-                           const unsigned *__restrict__ chunk_off, int2 *chunks, TreeInfo *info) {
+                           const unsigned *__restrict__ chunk_off, int4 *chunks, const unsigned *__restrict__ src_total,
+                           const unsigned *__restrict__ part_off, unsigned part_cap, TreeInfo *info) {
     const unsigned NL = counts[3];
     for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < NL; li += gridDim.x * blockDim.x) {
         const int c = leaves[li];
@@ -514,12 +564,21 @@ __global__ void k_rng_fill(const int *__restrict__ leaves, const unsigned *count
         }
         rng_len[li] = overflow ? 0u : k;  // never let P2P read past the buffer
         const unsigned cb = chunk_off[li];
-        const int nch = (e - b + 31) / 32;
+        const int nch = chunk_count(e - b);
+        const int ns = slice_count(src_total[li]);
         for (int q = 0; q < nch; ++q) {
-            if (cb + q < ch_cap)
-                chunks[cb + q] = make_int2(static_cast<int>(li), b + 32 * q);
-            else
-                overflow = true;
+            int off, len;
+            chunk_at(e - b, q, off, len);
+            for (int sl = 0; sl < ns; ++sl) {
+                const unsigned it = cb + static_cast<unsigned>(q * ns + sl);
+                // split items keep their partial sums in part[pslot]
+                const unsigned pslot = ns > 1 ? part_off[li] + static_cast<unsigned>(q * ns + sl) : 0xffffffffu;
+                if (ns > 1 && pslot >= part_cap) overflow = true;
+                if (it < ch_cap)
+                    chunks[it] = make_int4(static_cast<int>(li), b + off, item_pack(len, sl, ns), static_cast<int>(pslot));
+                else
+                    overflow = true;
+            }
         }
         if (overflow) atomicOr(&info->err, kDevCapacity);
         atomicAdd(reinterpret_cast<unsigned long long *>(&info->p2p_pairs), static_cast<unsigned long long>(e - b) * srcs);
@@ -527,8 +586,9 @@ __global__ void k_rng_fill(const int *__restrict__ leaves, const unsigned *count
     }
 }
 
-__global__ void k_check_totals(unsigned *counts, unsigned r_cap, unsigned ch_cap, TreeInfo *info) {
-    if (counts[4] > r_cap || counts[5] > ch_cap) atomicOr(&info->err, kDevCapacity);
+__global__ void k_check_totals(unsigned *counts, unsigned r_cap, unsigned ch_cap, unsigned part_cap, TreeInfo *info) {
+    counts[7] = counts[5];  // requested sizes, kept for the host when they overflow
+    if (counts[4] > r_cap || counts[5] > ch_cap || counts[8] > part_cap) atomicOr(&info->err, kDevCapacity);
     info->n_p2p_chunks = static_cast<int>(min(counts[5], ch_cap));
     counts[5] = min(counts[5], ch_cap);
 }
@@ -542,7 +602,7 @@ void build_tree(Workspace &ws) {
     cudaStream_t st = ws.st;
     timer_begin(ws, kTTree);
     cudaMemsetAsync(ws.info, 0, sizeof(TreeInfo), st);
-    cudaMemsetAsync(ws.d_counts, 0, 8 * sizeof(unsigned), st);
+    cudaMemsetAsync(ws.d_counts, 0, kNumCounts * sizeof(unsigned), st);
     cudaMemcpyAsync(ws.d_counts, &n, sizeof(unsigned), cudaMemcpyHostToDevice, st);
     const int nb = 2 * ws.num_sms;
     double *part = ws.bbox_part;
@@ -578,14 +638,15 @@ void build_tree(Workspace &ws) {
     k_lists<<<gs, 256, 0, st>>>(ws.ent, ws.d_counts, ws.split_cell, ws.info, ws.c_child, ws.c_path, ws.c_coord,
                                 ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                                 reinterpret_cast<unsigned long long *>(&ws.info->m2l_pairs));
-    k_rng_count<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.c_parent, ws.c_begin, ws.c_end, ws.p2p_cnt, ws.rng_cnt,
-                                    ws.chunk_cnt);
+    k_rng_count<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.c_parent, ws.c_begin, ws.c_end, ws.p2p_own, ws.p2p_cnt,
+                                    ws.rng_cnt, ws.chunk_cnt, ws.src_total, ws.part_cnt);
     scan_exclusive_u32(ws.rng_cnt, ws.rng_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 4, ws.scan, st, &ws.launches);
     scan_exclusive_u32(ws.chunk_cnt, ws.chunk_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 5, ws.scan, st, &ws.launches);
-    k_check_totals<<<1, 1, 0, st>>>(ws.d_counts, ws.r_cap, ws.ch_cap, ws.info);
+    scan_exclusive_u32(ws.part_cnt, ws.part_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 8, ws.scan, st, &ws.launches);
+    k_check_totals<<<1, 1, 0, st>>>(ws.d_counts, ws.r_cap, ws.ch_cap, ws.part_cap, ws.info);
     k_rng_fill<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.r_cap, ws.ch_cap, ws.c_parent, ws.c_begin, ws.c_end,
                                    ws.p2p_own, ws.p2p_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_off, ws.chunks,
-                                   ws.info);
+                                   ws.src_total, ws.part_off, ws.part_cap, ws.info);
     ws.launches += 13;
     timer_end(ws, kTTree);
 }

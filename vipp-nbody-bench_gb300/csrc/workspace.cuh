@@ -32,6 +32,7 @@ struct Workspace {
     int p = 4, K = 25, T = 90;  // T = floor(sqrt(8) s)
     double eps = 0, G = 1, m = 1;
     bool mixed = false;
+    bool p2p_newton = false;  // one Newton step after the FP32 rsqrt
     cudaStream_t st = nullptr;
     int64_t launches = 0;
     int num_sms = 152;
@@ -85,7 +86,11 @@ struct Workspace {
     unsigned *rng_len = nullptr;      // [C] ranges per leaf after merging
     uint2 *ranges = nullptr;          // [r_cap]
     unsigned *chunk_cnt = nullptr, *chunk_off = nullptr;  // [C]
-    int2 *chunks = nullptr;           // [ch_cap] (leaf, first target)
+    int4 *chunks = nullptr;           // [ch_cap] work items (leaf, first target, packed sizes, partial slot)
+    unsigned *src_total = nullptr;    // [C] near-field sources per leaf
+    unsigned *part_cnt = nullptr, *part_off = nullptr;  // [C+1] partial-sum slots per leaf
+    void *part = nullptr;             // [part_cap][3][32] partial sums of split items (FP32 or FP64)
+    unsigned part_cap = 0;
     unsigned *queue = nullptr;        // P2P work-queue counter
 
     // operators
@@ -94,7 +99,8 @@ struct Workspace {
 
     // device-side info and device-resident counters
     TreeInfo *info = nullptr;
-    unsigned *d_counts = nullptr;  // [8]: 0 n, 1 S, 2 C, 3 leaves, 4 ranges, 5 chunks
+    unsigned *d_counts = nullptr;  // [kNumCounts]: 0 n, 1 S, 2 C, 3 leaves, 4 ranges, 5 items,
+                                   // 6 S requested, 7 items requested, 8 partial slots
     TreeInfo *h_info = nullptr;    // pinned mirror
 
     SortTemp sort;
@@ -107,6 +113,7 @@ struct Workspace {
     int64_t t_launch[kNumTimers] = {};
 };
 
+constexpr int kNumCounts = 16;
 constexpr int kOpM2M = 343;  // op index of M2M octant 0
 constexpr int kOpL2L = 351;  // op index of L2L octant 0
 constexpr int kNumOps = 359;

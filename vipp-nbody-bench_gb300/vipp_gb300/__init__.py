@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(PKG_DIR, "lib", "libvipp_gb300.so")
 
 GB_OK, GB_ERR_INVALID, GB_ERR_NONFINITE, GB_ERR_DEPTH, GB_ERR_CUDA, GB_ERR_NO_DEVICE, GB_ERR_STATE, GB_ERR_CAPACITY = range(8)
 PREC = {"fp64": 0, "mixed": 1}
+FLAG_P2P_NEWTON = 1
 TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
 
 # Every symbol include/vipp_gb300.h declares.
@@ -99,9 +100,9 @@ class Solver:
     """One solver context on one GPU (see include/vipp_gb300.h)."""
 
     def __init__(self, p: int = 4, s: int = 10, eps: float = 0.01, G: float = 1.0, m: float = 1.0,
-                 precision: str = "fp64", device: int = 0):
+                 precision: str = "fp64", device: int = 0, flags: int = 0):
         self.lib = load()
-        self.cfg = GbConfig(p, s, eps, G, m, PREC[precision], device, 0)
+        self.cfg = GbConfig(p, s, eps, G, m, PREC[precision], device, flags)
         h = ctypes.c_void_p()
         rc = self.lib.gb_create(ctypes.byref(self.cfg), ctypes.byref(h))
         if rc != GB_OK:

@@ -53,8 +53,8 @@ enum gb_status {
 enum gb_precision {
     GB_PREC_FP64 = 0,   /* every stage in FP64 on CUDA cores (the plain form) */
     GB_PREC_MIXED = 1   /* P2P FP32 (relative coordinates, compensated sums),
-                           expansions FP32 scaled per cell, M2L FP32;
-                           RK4 combination in FP64 */
+                           expansions FP32 scaled per cell, M2L on the tensor
+                           cores (3xTF32); RK4 combination in FP64 */
 };
 
 typedef struct gb_config {
@@ -71,9 +71,12 @@ typedef struct gb_config {
 } gb_config;
 
 enum gb_flags {
-    GB_FLAG_P2P_NEWTON = 1  /* mixed P2P: refine the FP32 rsqrt with one Newton
-                               step (off by default: it changes the RMS error by
-                               about 1e-10 and costs about 20% of P2P time) */
+    GB_FLAG_P2P_NEWTON = 1,  /* mixed P2P: refine the FP32 rsqrt with one Newton
+                                step (off by default: it changes the RMS error by
+                                about 1e-10 and costs about 20% of P2P time) */
+    GB_FLAG_M2L_CUDA_CORES = 2  /* mixed M2L on CUDA cores in FP32 instead of the
+                                   default tensor-core M2L (tcgen05, TF32 with a
+                                   three-term hi/lo split) */
 };
 
 typedef struct gb_ctx gb_ctx;

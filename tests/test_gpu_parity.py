@@ -130,6 +130,21 @@ def test_direct_sum_kernel_vs_oracle(plummer16k):
     assert np.max(rel_err(a_all[targets], ref)) <= 1e-13
 
 
+@pytest.mark.parametrize("name", ["plummer3000_s4_p6", "cluster1200_s6_p5", "plummer2000_s8_p4"])
+def test_mixed_m2l_tensor_and_cuda_cores_agree(name):
+    """The tensor-core M2L (default) and the FP32 CUDA-core M2L both match the reference."""
+    import vipp_gb300
+    d = load_case(name)
+    res = {}
+    for label, flags in (("tensor", 0), ("cuda", vipp_gb300.FLAG_M2L_CUDA_CORES)):
+        with vipp_gb300.Solver(p=d["p"], s=d["s"], eps=d["eps"], G=d["G"], m=d["m"], precision="mixed", flags=flags) as s:
+            s.preprocess(d["x"], d["v"])
+            res[label] = s.accel()
+        e = rel_err(res[label], d["acc"])
+        assert math.sqrt(np.mean(e ** 2)) <= MIXED_RMS_REL and np.max(e) <= MIXED_MAX_REL
+    assert np.max(rel_err(res["tensor"], res["cuda"])) <= 2 * MIXED_MAX_REL
+
+
 def test_results_are_deterministic():
     import vipp_gb300
     d = load_case("cluster1200_s6_p5")

@@ -86,6 +86,7 @@ void apply_config(gb_ctx *ctx) {
     ws.m = ctx->cfg.m;
     ws.mixed = ctx->cfg.precision == GB_PREC_MIXED;
     ws.p2p_newton = (ctx->cfg.flags & GB_FLAG_P2P_NEWTON) != 0;
+    ws.m2l_tensor = ws.mixed && (ctx->cfg.flags & GB_FLAG_M2L_CUDA_CORES) == 0 && gb::m2l_tc_supported(ws.p);
 }
 
 // P2P work items: at most two partial chunks per leaf plus n/32 full ones,
@@ -273,6 +274,10 @@ int check_device_errors(gb_ctx *ctx, unsigned *need) {
         ctx->err = "tree deeper than 21 levels (more than floor(sqrt(8) s) coincident particles?)";
         return GB_ERR_DEPTH;
     }
+    if (err & gb::kDevTimeout) {
+        ctx->err = "a pipelined kernel timed out waiting on its barriers";
+        return GB_ERR_CUDA;
+    }
     if (err & gb::kDevCapacity) {
         ctx->err = "capacity";
         return GB_ERR_CAPACITY;
@@ -286,7 +291,10 @@ void evaluate(gb_ctx *ctx) {
     gb::build_tree(ws);
     gb::build_operators(ws);
     gb::upward_pass(ws);
-    gb::m2l_pass(ws);
+    if (ws.m2l_tensor)
+        gb::m2l_pass_tc(ws);
+    else
+        gb::m2l_pass(ws);
     gb::downward_pass(ws);
     gb::p2p_pass(ws);
     gb::finalize_accel(ws, ws.acc);
@@ -383,6 +391,7 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     const size_t kk = static_cast<size_t>(ws.K) * ws.K * gb::kNumOps;
     if ((e = cudaMalloc(&ws.ops_d, sizeof(double) * kk)) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.ops_f, sizeof(float) * kk)) != cudaSuccess) return fail("ops", e);
+    if ((e = cudaMalloc(&ws.bimg, sizeof(float) * gb::m2l_tc_image_floats(gb::kMaxP))) != cudaSuccess) return fail("ops", e);
     *out = ctx;
     return GB_OK;
 }
@@ -399,7 +408,7 @@ void gb_destroy(gb_ctx *ctx) {
                     ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
-                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
+                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
                     ctx->d_direct};
     for (void *b : bufs) dfree(b);
     gb::sort_temp_free(ws.sort);

@@ -44,6 +44,7 @@ enum DevErr : int {
     kDevNonFinite = 1,
     kDevDepth = 2,
     kDevCapacity = 4,
+    kDevTimeout = 8,  // a bounded wait in a pipelined kernel gave up
 };
 
 // Tree parameters of one force evaluation, produced on the device.

@@ -33,6 +33,7 @@ struct Workspace {
     double eps = 0, G = 1, m = 1;
     bool mixed = false;
     bool p2p_newton = false;  // one Newton step after the FP32 rsqrt
+    bool m2l_tensor = false;  // tcgen05 M2L (mixed precision only)
     cudaStream_t st = nullptr;
     int64_t launches = 0;
     int num_sms = 152;
@@ -96,6 +97,7 @@ struct Workspace {
     // operators
     double *ops_d = nullptr;  // [(343+16) K K]
     float *ops_f = nullptr;
+    float *bimg = nullptr;    // tensor-core M2L operator images (m2l_tc.cu)
 
     // device-side info and device-resident counters
     TreeInfo *info = nullptr;
@@ -122,7 +124,10 @@ constexpr int kNumOps = 359;
 void build_tree(Workspace &ws);               // bbox, keys, sort, cells, leaves, lists, near-field ranges
 void build_operators(Workspace &ws);          // 359 translation matrices for the current root box
 void upward_pass(Workspace &ws);              // P2M + M2M
-void m2l_pass(Workspace &ws);                 // M2L into L
+void m2l_pass(Workspace &ws);                 // M2L into L (CUDA cores)
+void m2l_pass_tc(Workspace &ws);              // M2L into L (tensor cores, mixed)
+bool m2l_tc_supported(int p);
+size_t m2l_tc_image_floats(int p);
 void downward_pass(Workspace &ws);            // L2L + L2P into far
 void p2p_pass(Workspace &ws);                 // near field into near
 void finalize_accel(Workspace &ws, double *acc_orig);  // acc[perm] = near + far

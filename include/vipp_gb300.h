@@ -90,6 +90,7 @@ typedef struct gb_stats {
     int64_t m2l_pairs;    /* M2L (target, source) pairs, targets at level >= 2 */
     int64_t p2p_pairs;    /* near-field (target, source) particle pairs */
     int64_t p2p_ranges;   /* source ranges over all leaves after merging */
+    int64_t retries;      /* evaluations of this context repeated after growing its buffers */
 } gb_stats;
 
 /* Create a context on cfg->device. Validates cfg (p in 1..10, s >= 1). */

@@ -156,6 +156,26 @@ def test_results_are_deterministic():
         assert np.array_equal(a1, a2)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_near_field_overflow_is_repeated_cleanly(precision):
+    """The first evaluation of a fresh context runs on guessed buffer sizes.
+    Plummer 100k (reference generator, seed 0) with s = 256 splits the long
+    near-field lists of its leaves into 12,639 partial-sum slots (counted on
+    the oracle's tree), three times the initial 4096, so that evaluation
+    overflows, queues no P2P work, grows the buffers and is repeated. The
+    repeat must equal an evaluation that fits."""
+    import vipp_gb300
+    x, v = O.plummer_reference(100_000, 0.01, 0)
+    with vipp_gb300.Solver(p=4, s=256, eps=0.01, m=1.0 / len(x), precision=precision) as s:
+        s.preprocess(x, v)
+        a1 = s.accel()
+        r1 = s.stats()["retries"]
+        a2 = s.accel()
+        r2 = s.stats()["retries"]
+    assert r1 >= 1 and r2 == r1
+    assert np.array_equal(a1, a2)
+
+
 def test_uniform_cube_mixed_vs_fp64_at_scale():
     """Size-independent property at 262,144 particles: the mixed pipeline agrees
     with the FP64 pipeline (same lists) and the tree is consistent."""

@@ -31,6 +31,7 @@ struct gb_ctx {
     gb::Workspace ws;
     std::string err;
     bool have_state = false;
+    long long retries = 0;  // evaluations repeated after a capacity overflow
     std::vector<gb::PendingTimer> pending;
     std::vector<cudaEvent_t> free_events;
     long long *d_targets = nullptr;
@@ -201,6 +202,21 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
         GB_TRY(dalloc(ws.ranges, r_cap));
         ws.r_cap = r_cap;
     }
+    if (ws.m2l_tensor) {
+        // split expansions of the tensor-core M2L and their TMA map
+        const int kp = gb::m2l_tc_row_floats(ws.p);
+        const unsigned rows = ws.c_cap + 1;
+        if (!ws.ms_tc || ws.ms_rows != rows || ws.ms_kp != kp) {
+            GB_TRY(dalloc(ws.ms_tc, 2 * static_cast<size_t>(rows) * kp));
+            ws.ms_rows = rows, ws.ms_kp = kp;
+            if (const char *e = gb::m2l_tc_encode(ws)) {
+                dfree(ws.ms_tc);
+                ws.ms_tc = nullptr, ws.ms_rows = 0;
+                ctx->err = e;
+                return GB_ERR_CUDA;
+            }
+        }
+    }
     return ensure_chunks(ctx);
 }
 
@@ -322,6 +338,7 @@ int run_with_capacity(gb_ctx *ctx, F &&f) {
         if (rc != GB_ERR_CAPACITY) return rc;
         const int g = grow(ctx, counts);
         if (g != GB_OK) return g;
+        ++ctx->retries;
     }
     ctx->err = "could not size the tree buffers";
     return GB_ERR_CAPACITY;
@@ -408,7 +425,7 @@ void gb_destroy(gb_ctx *ctx) {
                     ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
-                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
+                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.ms_tc, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
                     ctx->d_direct};
     for (void *b : bufs) dfree(b);
     gb::sort_temp_free(ws.sort);
@@ -583,6 +600,7 @@ int gb_get_stats(gb_ctx *ctx, gb_stats *out) {
     out->m2l_pairs = h.m2l_pairs;
     out->p2p_pairs = h.p2p_pairs;
     out->p2p_ranges = h.p2p_ranges;
+    out->retries = ctx->retries;
     return GB_OK;
 }
 

@@ -7,7 +7,7 @@
 // tile of 128 same-octant targets is, per slot, one GEMM
 //     D[128 x N] += A[128 x K] * B[N x K]^T,  A = gathered source rows,
 //                                             B = the slot's operator,
-// accumulated over all slots in TMEM (128 lanes x N FP32 columns).
+// accumulated in TMEM (128 lanes x N FP32 columns).
 //
 // Precision: kind::tf32 with a three-term split (hi = FP32 with the low 13
 // mantissa bits cleared, lo = x - hi):  D += Ahi Bhi + Ahi Blo + Alo Bhi,
@@ -16,24 +16,31 @@
 // Accumulation: the tensor core's FP32 accumulation adds an error that grows
 // with the number of MMAs summed into one accumulator (measured: RMS error
 // proportional to the chain length, 1.5e-5 relative on the accelerations with
-// all ~6000 MMAs of a tile in one accumulator). Slots are therefore grouped,
-// kGroup slots per group, into one of two TMEM accumulators used in turn; the
-// producer warps drain each finished group into FP32 registers (round-to-
-// nearest additions) while the next group accumulates.
+// all MMAs of a tile in one accumulator). Slots are therefore grouped, kGroup
+// slots per group, into one of two TMEM accumulators used in turn; the drain
+// warps add each finished group into FP32 registers (round-to-nearest
+// additions) while the next group accumulates.
 //
-// Pipeline (one CTA per SM, persistent over tiles): K is cut into 32-wide
-// chunks; each (slot, chunk) step goes through one of C::STAGES shared-memory
-// stages holding A hi/lo [128 x 32] and B hi/lo [N x 32] in the canonical
-// no-swizzle K-major layout (8-row x 16-byte core matrices; LBO = 128 B along
-// K, SBO = 1024 B between 8-row groups). B chunks are stored pre-split in that
-// exact image in global memory and arrive by one cp.async.bulk; warps 0-3
-// gather and split the A rows; warp 4 issues the MMAs (one elected thread)
-// and commits each stage back to its producers. Warps 0-3 then read their 32
-// TMEM lanes of D (tcgen05.ld) and write the local expansions.
+// Data flow (one CTA per SM, persistent over tiles, warp-specialised):
+//  * k_split_m writes every cell's expansion once more as two zero-padded
+//    rows of KP = 32 ceil(K / 32) floats, the hi part and the lo part, plus a
+//    zero row that stands in for absent sources;
+//  * the loader warp gathers, per (slot, 32-wide K chunk) step, the 128
+//    source rows of the tile with TMA tile::gather4 copies (4 rows of 128
+//    bytes per copy, hi and lo) into 128B-swizzled K-major A tiles, and the
+//    slot's pre-split operator chunk with one cp.async.bulk;
+//  * the MMA warp (one thread) issues 3 x 4 tcgen05.mma per step, commits the
+//    stage back to the loader and each finished group to the drain warps;
+//  * the drain warps (warps 0-3 own TMEM lanes 32w..32w+31, i.e. tile rows)
+//    add the groups and write the tile's local expansions.
+// Every tile runs the same static schedule (189 slots x NKC chunks), so the
+// three roles agree on it without exchanging control data.
 //
 // Every mbarrier wait is bounded by the global timer; on a timeout the CTA
 // records kDevTimeout in the status word, stops issuing work, waits (bounded)
-// for its own bulk copies and MMAs, frees its TMEM and returns.
+// for its own copies and MMAs, frees its TMEM and returns.
+#include <cuda.h>
+
 #include "workspace.cuh"
 
 namespace gb {
@@ -41,29 +48,53 @@ namespace gb {
 namespace {
 
 constexpr int kRows = 128;          // targets per tile (MMA M)
-constexpr int kKC = 32;             // K chunk (tf32 elements)
-constexpr int kProducers = 128;     // warps 0-3
-constexpr int kThreads = 160;       // + issuer warp 4
+constexpr int kKC = 32;             // K chunk (tf32 elements): one 128-byte swizzle row
+constexpr int kDrainThreads = 128;  // warps 0-3
+#ifndef M2L_LOADER_WARPS
+#define M2L_LOADER_WARPS 4
+#endif
+#ifndef M2L_WIDE_B
+#define M2L_WIDE_B 1
+#endif
+constexpr int kLoaderWarps = M2L_LOADER_WARPS;  // warps 4 .. 3 + kLoaderWarps
+constexpr int kGathers = 64;                    // gather4 copies per step: 32 row quads x (hi, lo)
+constexpr int kGathersPerWarp = kGathers / kLoaderWarps;
+constexpr int kMmaWarp = 4 + kLoaderWarps;
+constexpr int kThreads = 32 * (kMmaWarp + 1);
+static_assert(kGathers % kLoaderWarps == 0, "loader warps");
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr int kGroup = 4;           // slots per TMEM accumulation group
+constexpr int kSlotsPerTile = 189;  // M2L slots of every octant: 216 minus the 27 adjacent ones
+constexpr int kGroupsPerTile = (kSlotsPerTile + kGroup - 1) / kGroup;
 constexpr int kSmemMax = 232448;    // opt-in shared memory per block
 
 template <int P>
 struct TcCfg {
     static constexpr int K = (P + 1) * (P + 1);
     static constexpr int NKC = (K + kKC - 1) / kKC;      // K chunks
+    static constexpr int KP = NKC * kKC;                 // row length of the split expansions
     static constexpr int N = (K + 15) / 16 * 16;         // MMA N (multiple of 16 for M = 128)
-    static constexpr int ACOL = N <= 32 ? 32 : (N <= 64 ? 64 : 128);  // columns of one accumulator
+    // An accumulator holds Ahi [Bhi; Blo]^T (2N columns: N of Ahi Bhi + Alo Bhi,
+    // N of Ahi Blo); the hi and lo operator blocks are adjacent in the stage,
+    // so [Bhi; Blo] is one B operand of 2N rows.
+    static constexpr int DCOLS = M2L_WIDE_B ? 2 * N : N;
+    static constexpr int ACOL = DCOLS <= 32 ? 32 : (DCOLS <= 64 ? 64 : (DCOLS <= 128 ? 128 : 256));
     static constexpr int TMEM_COLS = 2 * ACOL;
-    static constexpr int A_BYTES = kRows * kKC * 4;      // one of hi/lo
+    static constexpr int A_BYTES = kRows * kKC * 4;      // one of hi/lo: 16 KB
     static constexpr int B_BYTES = N * kKC * 4;
     static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
-    static constexpr int STAGES = (kSmemMax - 1280) / STAGE >= 4 ? 4 : 3;  // ring depth
+    static constexpr int STAGES = (kSmemMax - 2048) / STAGE >= 4 ? 4 : 3;  // ring depth
     static constexpr size_t SMEM = static_cast<size_t>(STAGES) * STAGE + 1024 + 256;
     // instruction descriptor: D f32 (bits 4-5 = 1), A/B tf32 (bits 7-9, 10-12 = 2),
     // both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
-    static constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
-                                      (static_cast<uint32_t>(kRows >> 4) << 24);
+    static constexpr uint32_t idesc(int n) {
+        return (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(n >> 3) << 17) | (static_cast<uint32_t>(kRows >> 4) << 24);
+    }
+    static constexpr uint32_t IDESC = idesc(N);
+    static constexpr uint32_t IDESC_W = idesc(2 * N);
+    static_assert(2 * N <= 256, "MMA N");
+    static_assert(STAGE % 1024 == 0, "stages must keep the 1024-byte swizzle atoms aligned");
+    static_assert(SMEM <= static_cast<size_t>(kSmemMax), "shared memory");
 };
 
 // canonical no-swizzle K-major position (in floats) of element (row, k) of a [rows x 32] chunk
@@ -116,11 +147,29 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
                  : "memory");
 }
 
+// Four rows (r0..r3) of a 2-D tensor, columns [x, x + box width), into dst as
+// four consecutive swizzled 128-byte rows.
+__device__ __forceinline__ void tma_gather4(void *dst, const CUtensorMap *map, int x, int r0, int r1, int r2, int r3,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5, %6}], [%7];" ::"r"(saddr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(saddr(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptors. No swizzle: start address >> 4 (bits 0-13),
+// LBO 128 B >> 4 (bits 16-29), SBO 1024 B >> 4 (bits 32-45), version 1 (bit 46).
 __device__ __forceinline__ uint64_t sdesc(const void *p) {
-    // start address >> 4 (bits 0-13), LBO 128 B >> 4 (bits 16-29), SBO 1024 B >> 4
-    // (bits 32-45), descriptor version 1 (bit 46), no swizzle (bits 61-63 = 0)
     const uint64_t a = (saddr(p) & 0x3FFFFu) >> 4;
     return a | (static_cast<uint64_t>(128 >> 4) << 16) | (static_cast<uint64_t>(1024 >> 4) << 32) | (1ull << 46);
+}
+// 128-byte swizzle, K-major: 8-row atoms of 1024 B (SBO), layout type 2 at
+// bits 61-63; LBO is not used. The start may move by 32 B steps along K
+// inside an atom whose base is 1024-byte aligned.
+__device__ __forceinline__ uint64_t sdesc_sw128(const void *p) {
+    const uint64_t a = (saddr(p) & 0x3FFFFu) >> 4;
+    return a | (1ull << 16) | (static_cast<uint64_t>(1024 >> 4) << 32) | (1ull << 46) | (2ull << 61);
 }
 
 __device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
@@ -130,16 +179,6 @@ __device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t ad, uint64_t 
 }
 __device__ __forceinline__ void umma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar)) : "memory");
-}
-
-// OR of a predicate over the 128 producer threads (named barrier 1).
-__device__ __forceinline__ bool bar_or(bool pred) {
-    unsigned r;
-    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, 128, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
-                 : "=r"(r)
-                 : "r"(static_cast<unsigned>(pred))
-                 : "memory");
-    return r != 0;
 }
 
 __device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
@@ -161,7 +200,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
 
 // Slot s of a target with octant cls maps to same-level offset 2d + u(o') - u(cls);
 // adjacent offsets are not M2L slots. Returns the operator index or -1.
-__device__ __forceinline__ int slot_operator(int cls, int s) {
+__host__ __device__ __forceinline__ int slot_operator(int cls, int s) {
     const int dd = s >> 3, o = s & 7;
     const int uc0 = 1 - (cls & 1), uc1 = 1 - ((cls >> 1) & 1), uc2 = 1 - ((cls >> 2) & 1);
     const int o0 = 2 * (dd % 3 - 1) + 1 - (o & 1) - uc0;
@@ -171,10 +210,15 @@ __device__ __forceinline__ int slot_operator(int cls, int s) {
     return (o0 + 3) + 7 * (o1 + 3) + 49 * (o2 + 3);
 }
 
+__device__ __forceinline__ int next_slot(int cls, int s) {
+    while (s < kM2LSlots && slot_operator(cls, s) < 0) ++s;
+    return s;
+}
+
 template <int P>
-__global__ void __launch_bounds__(kThreads, 1) k_m2l_tc(const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
-                                                        const float *__restrict__ bimg, const float *__restrict__ M,
-                                                        float *__restrict__ Lx, TreeInfo *info_rw) {
+__global__ void __launch_bounds__(kThreads, 1)
+    k_m2l_tc(const __grid_constant__ CUtensorMap tmap, const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
+             const float *__restrict__ bimg, int rows_cap, float *__restrict__ Lx, TreeInfo *info_rw) {
     using C = TcCfg<P>;
     extern __shared__ __align__(1024) unsigned char sm_raw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(sm_raw) + 1023) & ~uintptr_t(1023));
@@ -194,8 +238,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_m2l_tc(const TreeInfo *__restri
     if (ntiles == 0 || static_cast<int>(blockIdx.x) >= ntiles) return;  // uniform: no barrier or TMEM touched yet
 
     if (tid == 0) {
-        for (int s = 0; s < C::STAGES; ++s) mbar_init(full + s, kProducers + 1), mbar_init(empty + s, 1);
-        for (int a = 0; a < 2; ++a) mbar_init(accum + a, 1), mbar_init(tfree + a, kProducers);
+        for (int s = 0; s < C::STAGES; ++s) mbar_init(full + s, kLoaderWarps), mbar_init(empty + s, 1);
+        for (int a = 0; a < 2; ++a) mbar_init(accum + a, 1), mbar_init(tfree + a, kDrainThreads);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -210,168 +254,174 @@ __global__ void __launch_bounds__(kThreads, 1) k_m2l_tc(const TreeInfo *__restri
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    unsigned step = 0;     // (slot, chunk) steps of this CTA so far
-    unsigned groups = 0;   // accumulation groups of this CTA so far (group g uses accumulator g % 2)
-    if (warp < 4) {
-        // ------------------------------------------------ producers + epilogue
-        // `stop` only changes through bar_or over all 128 producers, so every
-        // producer takes the same path through the named barrier.
+    unsigned mma_steps = 0;  // steps whose MMAs the MMA thread issued
+    if (warp >= 4 && warp < kMmaWarp) {
+        // --------------------------------------------------------------- loaders
+        // Copy G = q kGathersPerWarp + l (+ 32 i) of a step moves row quad G mod 32
+        // (tile rows 4(G mod 32) .. +3) of part G / 32 (hi, lo); absent sources
+        // read the zero row. Each loader warp's lane 0 arms the stage's barrier
+        // with the bytes of its own warp's copies.
+        const int q = warp - 4;
+        const int g0 = q * kGathersPerWarp + lane;
+        const int quad = g0 % 32;
+        const bool active = lane < kGathersPerWarp;
+        const bool do_hi = active && (kGathersPerWarp >= 64 || g0 < 32);
+        const bool do_lo = active && (kGathersPerWarp >= 64 || g0 >= 32);
+        const unsigned warp_bytes = static_cast<unsigned>(kGathersPerWarp) * 512u + (q == 0 ? 2u * C::B_BYTES : 0u);
+        const int zrow = rows_cap - 1;
+        unsigned step = 0;
         bool stop = false;
-        unsigned drained = 0;  // groups drained so far
-        float acc[C::N];
-        // Drain group g: wait for its last MMA, add its accumulator to acc.
-        auto drain = [&](unsigned g) -> bool {
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(accum + (g & 1), (g >> 1) & 1, abort_flag));
-            if (ok) {
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t base_col = (g & 1) * C::ACOL;
-#pragma unroll
-                for (int c0 = 0; c0 < C::N; c0 += 32) {
-                    float v[32];
-                    tmem_ld32(tmem + (static_cast<uint32_t>(32 * warp) << 16) + base_col + static_cast<uint32_t>(c0), v);
-#pragma unroll
-                    for (int i = 0; i < 32; ++i)
-                        if (c0 + i < C::N) acc[c0 + i] += v[i];
-                }
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            }
-            mbar_arrive(tfree + (g & 1));
-            return ok;
-        };
         for (int w = blockIdx.x; w < ntiles && !stop; w += gridDim.x) {
             const int cls = w % 8, t0 = (w / 8) * kRows;
-            const int t = t0 + tid;
-            const int crow = t < per_class ? base + cls + 8 * t : -1;
+            int crow[4];
 #pragma unroll
-            for (int i = 0; i < C::N; ++i) acc[i] = 0.f;
-            const unsigned tile_groups = groups;
-            int in_group = 0;
-            for (int s = 0; s < kM2LSlots; ++s) {
-                if (slot_operator(cls, s) < 0) continue;
-                const int src = crow >= 0 ? m2l_src[static_cast<size_t>(crow) * kM2LSlots + s] : -1;
-                const bool any = bar_or(src >= 0);
-                stop = bar_or(*abort_flag != 0);
-                if (stop) break;
-                if (!any) continue;
+            for (int i = 0; i < 4; ++i) {
+                const int t = t0 + 4 * quad + i;
+                crow[i] = (active && t < per_class) ? base + cls + 8 * t : -1;
+            }
+            auto rows_of = [&](int s, int *r) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int src = crow[i] >= 0 ? m2l_src[static_cast<size_t>(crow[i]) * kM2LSlots + s] : -1;
+                    r[i] = src >= 0 ? src : zrow;
+                }
+            };
+            int s = next_slot(cls, 0);
+            int cur[4];
+            rows_of(s, cur);
+            while (s < kM2LSlots && !stop) {
+                const int oi = slot_operator(cls, s);
+                const int sn = next_slot(cls, s + 1);
+                int nxt[4] = {zrow, zrow, zrow, zrow};
+                if (sn < kM2LSlots) rows_of(sn, nxt);  // in flight while this slot's copies are posted
                 for (int kc = 0; kc < C::NKC; ++kc, ++step) {
                     const int st = step % C::STAGES;
                     const unsigned use = step / C::STAGES;
-                    if (use > 0 && !mbar_wait(empty + st, (use - 1) & 1, abort_flag)) break;
-                    float *Ahi = reinterpret_cast<float *>(sm + st * C::STAGE);
-                    float *Alo = Ahi + kRows * kKC;
-                    const float *row = src >= 0 ? M + static_cast<size_t>(src) * C::K : nullptr;
-#pragma unroll 4
-                    for (int k4 = 0; k4 < kKC; k4 += 4) {
-                        float v[4];
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const int ci = kc * kKC + k4 + e;
-                            v[e] = (row && ci < C::K) ? row[ci] : 0.f;
-                        }
-                        float4 h, l;
-                        h.x = tf32_hi(v[0]), h.y = tf32_hi(v[1]), h.z = tf32_hi(v[2]), h.w = tf32_hi(v[3]);
-                        l.x = v[0] - h.x, l.y = v[1] - h.y, l.z = v[2] - h.z, l.w = v[3] - h.w;
-                        *reinterpret_cast<float4 *>(Ahi + canon(tid, k4)) = h;
-                        *reinterpret_cast<float4 *>(Alo + canon(tid, k4)) = l;
+                    int ok = 1;
+                    if (lane == 0) {
+                        if (use > 0 && !mbar_wait(empty + st, (use - 1) & 1, abort_flag)) ok = 0;
+                        if (ok) mbar_expect_tx(full + st, warp_bytes);
                     }
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    mbar_arrive(full + st);
+                    if (!__shfl_sync(0xffffffffu, ok, 0)) {
+                        stop = true;
+                        break;
+                    }
+                    unsigned char *stage = sm + st * C::STAGE;
+                    if (do_hi)
+                        tma_gather4(stage + 512 * quad, &tmap, kc * kKC, cur[0], cur[1], cur[2], cur[3], full + st);
+                    if (do_lo)
+                        tma_gather4(stage + C::A_BYTES + 512 * quad, &tmap, kc * kKC, cur[0] + rows_cap, cur[1] + rows_cap,
+                                    cur[2] + rows_cap, cur[3] + rows_cap, full + st);
+                    if (q == 0 && lane == 0)
+                        bulk_g2s(stage + 2 * C::A_BYTES, bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::N * kKC),
+                                 2 * C::B_BYTES, full + st);
                 }
-                // After queueing the first slot of a group, drain the previous
-                // group of this tile (its MMAs overlap with the queued ones).
-                if (in_group == 0 && groups > tile_groups && drained < groups) {
-                    if (!drain(drained)) break;
-                    ++drained;
-                }
-                if (++in_group == kGroup) in_group = 0, ++groups;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) cur[i] = nxt[i];
+                s = sn;
             }
-            if (in_group > 0) ++groups;  // the tile's last, partial group
-            if (!stop) stop = bar_or(*abort_flag != 0);
-            if (stop) break;
-            bool ok = true;
-            while (drained < groups && ok) ok = drain(drained++);
-            if (crow >= 0 && ok)
-                for (int r = 0; r < C::K; ++r) Lx[static_cast<size_t>(crow) * C::K + r] = groups > tile_groups ? acc[r] : 0.f;
-            stop = bar_or(*abort_flag != 0);
         }
-    } else {
-        // ------------------------------------------------------------ issuer
-        // The whole warp scans the tile's sources of a slot; lane 0 alone
-        // posts the bulk copies, issues the MMAs and commits.
-        bool stop = false;
-        for (int w = blockIdx.x; w < ntiles && !stop; w += gridDim.x) {
-            const int cls = w % 8, t0 = (w / 8) * kRows;
-            int in_group = 0;
-            bool acc_on = false;
-            for (int s = 0; s < kM2LSlots && !stop; ++s) {
-                const int oi = slot_operator(cls, s);
-                if (oi < 0) continue;
-                bool mine = false;
-                for (int r = lane; r < kRows; r += 32) {
-                    const int t = t0 + r;
-                    if (t < per_class && m2l_src[static_cast<size_t>(base + cls + 8 * t) * kM2LSlots + s] >= 0) mine = true;
-                }
-                if (!__any_sync(0xffffffffu, mine)) continue;
-                int ok = 1;
-                if (lane == 0) {
+    } else if (warp == kMmaWarp) {
+        // ------------------------------------------------------------------- MMA
+        if (lane == 0) {
+            unsigned groups = 0;
+            bool stop = false;
+            for (int w = blockIdx.x; w < ntiles && !stop; w += gridDim.x) {
+                for (int j = 0; j < kSlotsPerTile && !stop; ++j) {
+                    const int in_group = j % kGroup;
                     const unsigned a = groups & 1;
-                    // a new group reuses accumulator a once group - 2 has been drained
-                    if (in_group == 0 && groups >= 2 && !mbar_wait(tfree + a, ((groups - 2) >> 1) & 1, abort_flag)) ok = 0;
-                    if (in_group == 0) acc_on = false;
+                    // a group reuses accumulator a once group - 2 has been drained
+                    if (in_group == 0 && groups >= 2 && !mbar_wait(tfree + a, ((groups - 2) >> 1) & 1, abort_flag)) {
+                        stop = true;
+                        break;
+                    }
                     const uint32_t dt = tmem + a * C::ACOL;
-                    for (int kc = 0; kc < C::NKC && ok; ++kc, ++step) {
-                        const int st = step % C::STAGES;
-                        const unsigned use = step / C::STAGES;
-                        if (use > 0 && !mbar_wait(empty + st, (use - 1) & 1, abort_flag)) {
-                            ok = 0;
-                            break;
-                        }
-                        unsigned char *stage = sm + st * C::STAGE;
-                        float *Bhi = reinterpret_cast<float *>(stage + 2 * C::A_BYTES);
-                        mbar_expect_tx(full + st, 2 * C::B_BYTES);
-                        bulk_g2s(Bhi, bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::N * kKC), 2 * C::B_BYTES,
-                                 full + st);
+                    for (int kc = 0; kc < C::NKC; ++kc) {
+                        const int st = mma_steps % C::STAGES;
+                        const unsigned use = mma_steps / C::STAGES;
                         if (!mbar_wait(full + st, use & 1, abort_flag)) {
-                            ok = 0;
+                            stop = true;
                             break;
                         }
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                        const float *Ahi = reinterpret_cast<const float *>(stage);
-                        const float *Alo = Ahi + kRows * kKC;
+                        const unsigned char *stage = sm + st * C::STAGE;
+                        const uint64_t ahi = sdesc_sw128(stage), alo = sdesc_sw128(stage + C::A_BYTES);
+                        const float *Bhi = reinterpret_cast<const float *>(stage + 2 * C::A_BYTES);
                         const float *Blo = Bhi + C::N * kKC;
                         const int ksteps = min(kKC / 8, (C::K - kc * kKC + 7) / 8);
                         for (int ks = 0; ks < ksteps; ++ks) {
-                            const int off = ks * 64;  // 8 tf32 = two core matrices along K = 64 floats
-                            umma_tf32(dt, sdesc(Ahi + off), sdesc(Bhi + off), C::IDESC, acc_on ? 1u : 0u);
-                            acc_on = true;
-                            umma_tf32(dt, sdesc(Ahi + off), sdesc(Blo + off), C::IDESC, 1u);
-                            umma_tf32(dt, sdesc(Alo + off), sdesc(Bhi + off), C::IDESC, 1u);
+                            // 8 tf32 = 32 B along K: +2 in the swizzled start field,
+                            // two core matrices (64 floats) in the plain layout
+                            const uint64_t bhi = sdesc(Bhi + ks * 64), blo = sdesc(Blo + ks * 64);
+                            const uint32_t first = (in_group == 0 && kc == 0 && ks == 0) ? 0u : 1u;
+                            if (M2L_WIDE_B) {
+                                umma_tf32(dt, ahi + 2 * ks, bhi, C::IDESC_W, first);  // Ahi [Bhi; Blo]^T
+                            } else {
+                                umma_tf32(dt, ahi + 2 * ks, bhi, C::IDESC, first);
+                                umma_tf32(dt, ahi + 2 * ks, blo, C::IDESC, 1u);
+                            }
+                            umma_tf32(dt, alo + 2 * ks, bhi, C::IDESC, 1u);
                         }
                         umma_commit(empty + st);
+                        ++mma_steps;
                     }
-                    if (*abort_flag) ok = 0;
-                    if (ok && in_group + 1 == kGroup) umma_commit(accum + a);
+                    if (stop) break;
+                    if (in_group == kGroup - 1 || j == kSlotsPerTile - 1) {
+                        umma_commit(accum + a);
+                        ++groups;
+                    }
                 }
-                if (++in_group == kGroup) in_group = 0, ++groups;
-                stop = __shfl_sync(0xffffffffu, ok, 0) == 0;
             }
-            if (!stop && in_group > 0) {
-                if (lane == 0) umma_commit(accum + (groups & 1));
-                ++groups;
+        }
+        __syncwarp();
+    } else {
+        // ----------------------------------------------------------------- drain
+        unsigned groups = 0;
+        bool stop = false;
+        float acc[C::N];
+        for (int w = blockIdx.x; w < ntiles && !stop; w += gridDim.x) {
+            const int cls = w % 8, t0 = (w / 8) * kRows;
+#pragma unroll
+            for (int i = 0; i < C::N; ++i) acc[i] = 0.f;
+            for (int gi = 0; gi < kGroupsPerTile; ++gi, ++groups) {
+                if (!__all_sync(0xffffffffu, mbar_wait(accum + (groups & 1), (groups >> 1) & 1, abort_flag))) {
+                    stop = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t col = (groups & 1) * C::ACOL;
+#pragma unroll
+                for (int h = 0; h < (M2L_WIDE_B ? 2 : 1); ++h)
+#pragma unroll
+                    for (int c0 = 0; c0 < C::N; c0 += 32) {
+                        float v[32];
+                        tmem_ld32(tmem + (static_cast<uint32_t>(32 * warp) << 16) + col + static_cast<uint32_t>(h * C::N + c0), v);
+#pragma unroll
+                        for (int i = 0; i < 32; ++i)
+                            if (c0 + i < C::N) acc[c0 + i] += v[i];
+                    }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                mbar_arrive(tfree + (groups & 1));
+            }
+            if (stop) break;
+            const int t = t0 + tid;
+            if (t < per_class) {
+                float *out = Lx + static_cast<size_t>(base + cls + 8 * t) * C::K;
+                for (int r = 0; r < C::K; ++r) out[r] = acc[r];
             }
         }
     }
     // Orderly exit: every wait above is bounded, so all threads get here.
-    if (warp == 4 && lane == 0 && step > 0) {
+    if (warp == kMmaWarp && lane == 0 && mma_steps > 0) {
         // outstanding MMAs of this thread finish before the CTA may exit
-        uint64_t *last = empty + ((step - 1) % C::STAGES);
-        mbar_wait(last, ((step - 1) / C::STAGES) & 1, abort_flag);
+        uint64_t *last = empty + ((mma_steps - 1) % C::STAGES);
+        mbar_wait(last, ((mma_steps - 1) / C::STAGES) & 1, abort_flag);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (*abort_flag) {
         if (tid == 0) atomicOr(&info_rw->err, kDevTimeout);
-        // give any bulk copy still in flight time to land before the smem is released
+        // give any copy still in flight time to land before the smem is released
         const unsigned long long t0 = now_ns();
         while (now_ns() - t0 < 1000000ull) {
         }
@@ -381,6 +431,30 @@ __global__ void __launch_bounds__(kThreads, 1) k_m2l_tc(const TreeInfo *__restri
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(static_cast<unsigned>(C::TMEM_COLS))
                      : "memory");
     }
+}
+
+// Split expansions for the gather: rows [0, rows_cap) hold the hi parts,
+// rows [rows_cap, 2 rows_cap) the lo parts, KP floats each, zero beyond K;
+// row rows_cap - 1 of both halves is the zero row.
+template <int P>
+__global__ void k_split_m(const TreeInfo *__restrict__ info, const float *__restrict__ M, float *__restrict__ ms, int rows_cap) {
+    using C = TcCfg<P>;
+    const int nc = min(info->ncells, rows_cap - 1);
+    float *lo = ms + static_cast<size_t>(rows_cap) * C::KP;
+    const size_t total = static_cast<size_t>(nc) * C::KP;
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const size_t c = i / C::KP;
+        const int k = static_cast<int>(i - c * C::KP);
+        const float v = k < C::K ? M[c * C::K + k] : 0.f;
+        const float h = tf32_hi(v);
+        ms[i] = h;
+        lo[i] = v - h;
+    }
+    if (blockIdx.x == 0)
+        for (int k = threadIdx.x; k < C::KP; k += blockDim.x) {
+            ms[static_cast<size_t>(rows_cap - 1) * C::KP + k] = 0.f;
+            lo[static_cast<size_t>(rows_cap - 1) * C::KP + k] = 0.f;
+        }
 }
 
 // Pre-split operator images: for each same-level offset oi and K chunk kc,
@@ -409,11 +483,17 @@ template <int P>
 void launch(Workspace &ws) {
     using C = TcCfg<P>;
     k_build_bimg<P><<<343, 256, 0, ws.st>>>(ws.ops_d, ws.bimg);
+    k_split_m<P><<<4 * ws.num_sms, 256, 0, ws.st>>>(ws.info, static_cast<const float *>(ws.Mexp), ws.ms_tc,
+                                                   static_cast<int>(ws.ms_rows));
     cudaFuncSetAttribute(k_m2l_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(C::SMEM));
-    k_m2l_tc<P><<<ws.num_sms, kThreads, C::SMEM, ws.st>>>(ws.info, ws.m2l_src, ws.bimg, static_cast<const float *>(ws.Mexp),
-                                                         static_cast<float *>(ws.Lexp), ws.info);
-    ws.launches += 2;
+    k_m2l_tc<P><<<ws.num_sms, kThreads, C::SMEM, ws.st>>>(ws.tmap_ms, ws.info, ws.m2l_src, ws.bimg,
+                                                         static_cast<int>(ws.ms_rows), static_cast<float *>(ws.Lexp), ws.info);
+    ws.launches += 3;
 }
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 }  // namespace
 
@@ -423,7 +503,32 @@ size_t m2l_tc_image_floats(int p) {
     return static_cast<size_t>(343) * NKC * 2 * N * kKC;
 }
 
+int m2l_tc_row_floats(int p) {
+    const int K = (p + 1) * (p + 1);
+    return (K + kKC - 1) / kKC * kKC;
+}
+
 bool m2l_tc_supported(int p) { return p >= 2 && p <= kMaxP; }
+
+const char *m2l_tc_encode(Workspace &ws) {
+    static EncodeTiled encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return "cuTensorMapEncodeTiled is not available";
+        encode = reinterpret_cast<EncodeTiled>(fn);
+    }
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(ws.ms_kp), 2ull * ws.ms_rows};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ws.ms_kp) * sizeof(float)};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(kKC), 1u};  // gather4 boxes are one row high
+    const cuuint32_t estr[2] = {1u, 1u};
+    const CUresult r = encode(&ws.tmap_ms, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, ws.ms_tc, dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? nullptr : "cuTensorMapEncodeTiled rejected the split-expansion tensor";
+}
 
 void m2l_pass_tc(Workspace &ws) {
     timer_begin(ws, kTM2L);

@@ -586,11 +586,16 @@ __global__ void k_rng_fill(const int *__restrict__ leaves, const unsigned *count
     }
 }
 
+// On any overflow of the near-field buffers the evaluation queues no P2P work
+// item at all: k_rng_fill may still address items whose partial-sum slot lies
+// past part_cap, and the P2P kernels run before the host sees the flag, grows
+// the buffers and repeats the evaluation.
 __global__ void k_check_totals(unsigned *counts, unsigned r_cap, unsigned ch_cap, unsigned part_cap, TreeInfo *info) {
     counts[7] = counts[5];  // requested sizes, kept for the host when they overflow
-    if (counts[4] > r_cap || counts[5] > ch_cap || counts[8] > part_cap) atomicOr(&info->err, kDevCapacity);
-    info->n_p2p_chunks = static_cast<int>(min(counts[5], ch_cap));
-    counts[5] = min(counts[5], ch_cap);
+    const bool over = counts[4] > r_cap || counts[5] > ch_cap || counts[8] > part_cap;
+    if (over) atomicOr(&info->err, kDevCapacity);
+    counts[5] = over ? 0u : counts[5];
+    info->n_p2p_chunks = static_cast<int>(counts[5]);
 }
 
 inline unsigned grid_for(unsigned n, int tb) { return (n + tb - 1) / tb; }

@@ -17,6 +17,7 @@
 //     stored input-major (op[c*K + r]) in FP64 and FP32.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -98,6 +99,10 @@ struct Workspace {
     double *ops_d = nullptr;  // [(343+16) K K]
     float *ops_f = nullptr;
     float *bimg = nullptr;    // tensor-core M2L operator images (m2l_tc.cu)
+    float *ms_tc = nullptr;   // tensor-core M2L split expansions [2][ms_rows][ms_kp] (hi, lo)
+    unsigned ms_rows = 0;     // c_cap + 1: the last row of each half is zero
+    int ms_kp = 0;
+    CUtensorMap tmap_ms{};    // TMA map of ms_tc: 2 ms_rows rows of ms_kp floats
 
     // device-side info and device-resident counters
     TreeInfo *info = nullptr;
@@ -128,6 +133,8 @@ void m2l_pass(Workspace &ws);                 // M2L into L (CUDA cores)
 void m2l_pass_tc(Workspace &ws);              // M2L into L (tensor cores, mixed)
 bool m2l_tc_supported(int p);
 size_t m2l_tc_image_floats(int p);
+int m2l_tc_row_floats(int p);
+const char *m2l_tc_encode(Workspace &ws);     // (re)build tmap_ms; nullptr or an error message
 void downward_pass(Workspace &ws);            // L2L + L2P into far
 void p2p_pass(Workspace &ws);                 // near field into near
 void finalize_accel(Workspace &ws, double *acc_orig);  // acc[perm] = near + far

@@ -38,7 +38,7 @@ class GbConfig(ctypes.Structure):
 
 
 class GbStats(ctypes.Structure):
-    _fields_ = [(k, ctypes.c_int64) for k in ("n", "ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges")]
+    _fields_ = [(k, ctypes.c_int64) for k in ("n", "ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges", "retries")]
 
 
 _LIB = None

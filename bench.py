@@ -224,6 +224,7 @@ def main():
     ap.add_argument("--error-sample", type=int, default=65536)
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--flags", type=int, default=0, help="gb_config flags (vipp_gb300.FLAG_*)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
@@ -244,7 +245,8 @@ def main():
     n = args.n
     x, v = plummer(n, 2 + rank)
     m = 1.0 / n
-    sol = vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision=args.precision, device=local)
+    sol = vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision=args.precision, device=local,
+                            flags=args.flags)
     sol.preprocess(x, v)
     for _ in range(args.warmup):
         sol.solve(args.dt)

@@ -74,9 +74,12 @@ enum gb_flags {
     GB_FLAG_P2P_NEWTON = 1,  /* mixed P2P: refine the FP32 rsqrt with one Newton
                                 step (off by default: it changes the RMS error by
                                 about 1e-10 and costs about 20% of P2P time) */
-    GB_FLAG_M2L_CUDA_CORES = 2  /* mixed M2L on CUDA cores in FP32 instead of the
+    GB_FLAG_M2L_CUDA_CORES = 2, /* mixed M2L on CUDA cores in FP32 instead of the
                                    default tensor-core M2L (tcgen05, TF32 with a
                                    three-term hi/lo split) */
+    GB_FLAG_SERIAL = 4          /* run the near field (P2P) after the far field on
+                                   one stream instead of concurrently on a second
+                                   stream of the context (same results) */
 };
 
 typedef struct gb_ctx gb_ctx;

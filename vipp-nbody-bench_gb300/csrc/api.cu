@@ -88,6 +88,7 @@ void apply_config(gb_ctx *ctx) {
     ws.mixed = ctx->cfg.precision == GB_PREC_MIXED;
     ws.p2p_newton = (ctx->cfg.flags & GB_FLAG_P2P_NEWTON) != 0;
     ws.m2l_tensor = ws.mixed && (ctx->cfg.flags & GB_FLAG_M2L_CUDA_CORES) == 0 && gb::m2l_tc_supported(ws.p);
+    ws.serial = (ctx->cfg.flags & GB_FLAG_SERIAL) != 0;
 }
 
 // P2P work items: at most two partial chunks per leaf plus n/32 full ones,
@@ -301,10 +302,22 @@ int check_device_errors(gb_ctx *ctx, unsigned *need) {
     return GB_OK;
 }
 
+// One force evaluation. After the tree the near field (P2P, FP32/FP64 CUDA
+// cores) and the far field (operators, P2M/M2M, M2L on the tensor cores,
+// L2L/L2P) read only tree data and write separate buffers, so the near field
+// runs on a second stream concurrently with the far field; finalize joins them.
 void evaluate(gb_ctx *ctx) {
     gb::Workspace &ws = ctx->ws;
     g_timer_ctx = ctx;
     gb::build_tree(ws);
+    if (!ws.serial) {
+        cudaEventRecord(ws.ev_fork, ws.st);
+        cudaStreamWaitEvent(ws.st2, ws.ev_fork, 0);
+        std::swap(ws.st, ws.st2);  // the stages launch on ws.st
+        gb::p2p_pass(ws);
+        std::swap(ws.st, ws.st2);
+        cudaEventRecord(ws.ev_join, ws.st2);
+    }
     gb::build_operators(ws);
     gb::upward_pass(ws);
     if (ws.m2l_tensor)
@@ -312,7 +325,10 @@ void evaluate(gb_ctx *ctx) {
     else
         gb::m2l_pass(ws);
     gb::downward_pass(ws);
-    gb::p2p_pass(ws);
+    if (ws.serial)
+        gb::p2p_pass(ws);
+    else
+        cudaStreamWaitEvent(ws.st, ws.ev_join, 0);
     gb::finalize_accel(ws, ws.acc);
 }
 
@@ -398,6 +414,9 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     }
     ws.num_sms = prop.multiProcessorCount;
     if ((e = cudaStreamCreateWithFlags(&ws.st, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream", e);
+    if ((e = cudaStreamCreateWithFlags(&ws.st2, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream", e);
+    if ((e = cudaEventCreateWithFlags(&ws.ev_fork, cudaEventDisableTiming)) != cudaSuccess) return fail("event", e);
+    if ((e = cudaEventCreateWithFlags(&ws.ev_join, cudaEventDisableTiming)) != cudaSuccess) return fail("event", e);
     if ((e = gb::upload_tables()) != cudaSuccess) return fail("tables", e);
     if ((e = cudaMalloc(&ws.info, sizeof(gb::TreeInfo))) != cudaSuccess) return fail("info", e);
     if ((e = cudaMalloc(&ws.d_counts, gb::kNumCounts * sizeof(unsigned))) != cudaSuccess) return fail("counts", e);
@@ -431,6 +450,9 @@ void gb_destroy(gb_ctx *ctx) {
     gb::sort_temp_free(ws.sort);
     gb::scan_temp_free(ws.scan);
     if (ws.h_info) cudaFreeHost(ws.h_info);
+    if (ws.ev_fork) cudaEventDestroy(ws.ev_fork);
+    if (ws.ev_join) cudaEventDestroy(ws.ev_join);
+    if (ws.st2) cudaStreamDestroy(ws.st2);
     if (ws.st) cudaStreamDestroy(ws.st);
     if (g_timer_ctx == ctx) g_timer_ctx = nullptr;
     delete ctx;

@@ -53,6 +53,9 @@ constexpr int kDrainThreads = 128;  // warps 0-3
 #ifndef M2L_LOADER_WARPS
 #define M2L_LOADER_WARPS 4
 #endif
+#ifndef M2L_MAX_STAGES
+#define M2L_MAX_STAGES 4  // 3 leaves shared memory for concurrent P2P blocks
+#endif
 #ifndef M2L_WIDE_B
 #define M2L_WIDE_B 1
 #endif
@@ -83,7 +86,7 @@ struct TcCfg {
     static constexpr int A_BYTES = kRows * kKC * 4;      // one of hi/lo: 16 KB
     static constexpr int B_BYTES = N * kKC * 4;
     static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
-    static constexpr int STAGES = (kSmemMax - 2048) / STAGE >= 4 ? 4 : 3;  // ring depth
+    static constexpr int STAGES = (kSmemMax - 2048) / STAGE >= M2L_MAX_STAGES ? M2L_MAX_STAGES : 3;  // ring depth
     static constexpr size_t SMEM = static_cast<size_t>(STAGES) * STAGE + 1024 + 256;
     // instruction descriptor: D f32 (bits 4-5 = 1), A/B tf32 (bits 7-9, 10-12 = 2),
     // both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28

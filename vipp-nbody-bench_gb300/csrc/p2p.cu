@@ -22,6 +22,10 @@
 #include "direct.cuh"
 #include "workspace.cuh"
 
+#ifndef GB_P2P_BLOCKS_PER_SM
+#define GB_P2P_BLOCKS_PER_SM 8
+#endif
+
 namespace gb {
 
 namespace {
@@ -291,7 +295,9 @@ __global__ void k_p2p_combine(const int4 *__restrict__ chunks, const unsigned *c
 void p2p_pass(Workspace &ws) {
     timer_begin(ws, kTP2P);
     cudaMemsetAsync(ws.queue, 0, sizeof(unsigned), ws.st);
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
+    // Blocks per SM of the persistent P2P kernels. The P2P kernels run
+    // concurrently with the far field, so they should leave room on each SM.
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * GB_P2P_BLOCKS_PER_SM;
     const bool soft = ws.eps > 0;
     if (ws.mixed) {
         const float eps2 = static_cast<float>(ws.eps * ws.eps);

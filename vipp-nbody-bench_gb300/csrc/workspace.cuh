@@ -36,6 +36,9 @@ struct Workspace {
     bool p2p_newton = false;  // one Newton step after the FP32 rsqrt
     bool m2l_tensor = false;  // tcgen05 M2L (mixed precision only)
     cudaStream_t st = nullptr;
+    cudaStream_t st2 = nullptr;         // near field, concurrent with the far field on st
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool serial = false;                // near field on st after the far field
     int64_t launches = 0;
     int num_sms = 152;
 

@@ -24,6 +24,7 @@ GB_OK, GB_ERR_INVALID, GB_ERR_NONFINITE, GB_ERR_DEPTH, GB_ERR_CUDA, GB_ERR_NO_DE
 PREC = {"fp64": 0, "mixed": 1}
 FLAG_P2P_NEWTON = 1
 FLAG_M2L_CUDA_CORES = 2
+FLAG_SERIAL = 4
 TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
 
 # Every symbol include/vipp_gb300.h declares.

@@ -344,9 +344,26 @@ def main():
                       "ms_per_launch": 1e3 * t, "launches": kt["p2p"][1]}
     if kt["m2l"][1]:
         t = kt["m2l"][0] / kt["m2l"][1] / 1e3
-        ach = 2.0 * K * K * st["m2l_pairs"] / t / 1e12
-        per["m2l"] = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
-                      "ms_per_launch": 1e3 * t, "launches": kt["m2l"][1]}
+        ach = 2.0 * K * K * st["m2l_pairs"] / t / 1e12  # algorithmic: one K x K operator per pair
+        tensor = args.precision == "mixed" and args.p >= 2 and not (args.flags & vipp_gb300.FLAG_M2L_CUDA_CORES)
+        if tensor:
+            # TF32 tcgen05 MMAs run at half the bf16 rate (same cycles per MMA, half
+            # the K), so the bound is half the measured bf16 GEMM rate. Executed
+            # tensor work: 128-row tiles of same-octant targets x 189 slots, K and
+            # N padded (N to 16, K to 8 per MMA), three hi/lo products.
+            tf32_peak = peaks["bf16_tflops"] / 2
+            nt = max(st["ncells"] - 9, 0)
+            tiles = 8 * math.ceil(nt / 8 / 128)
+            N = (K + 15) // 16 * 16
+            ksteps = sum(min(4, math.ceil((K - 32 * kc) / 8)) for kc in range(math.ceil(K / 32)))
+            exe = tiles * 189 * ksteps * 3 * 2.0 * 128 * N * 8 / t / 1e12
+            per["m2l"] = {"bound": "tensor", "achieved": ach, "peak": tf32_peak, "unit": "TFLOP/s",
+                          "frac": ach / tf32_peak, "executed_tflops": exe, "executed_frac": exe / tf32_peak,
+                          "ms_per_launch": 1e3 * t, "launches": kt["m2l"][1],
+                          "peak_source": f"{src} bf16_tflops / 2 (TF32 MMA rate)"}
+        else:
+            per["m2l"] = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                          "ms_per_launch": 1e3 * t, "launches": kt["m2l"][1]}
     if kt["tree"][1]:
         t = kt["tree"][0] / kt["tree"][1] / 1e3
         ncell = st["ncells"]
@@ -356,9 +373,9 @@ def main():
     dom = max(per, key=lambda k: per[k]["ms_per_launch"] * per[k]["launches"]) if per else None
     roof = dict(per[dom]) if dom else {}
     if dom:
-        roof.update({"kernel": dom, "traffic": None,
-                     "peak_source": (f"{src}: FP32 = 2 x 128 lanes x {nsm} SMs x sm_max_mhz {sm_mhz:.0f}"
-                                     if roof["bound"] == "fp32" else f"{src} hbm_gbs")})
+        roof.update({"kernel": dom, "traffic": None})
+        roof.setdefault("peak_source", f"{src}: FP32 = 2 x 128 lanes x {nsm} SMs x sm_max_mhz {sm_mhz:.0f}"
+                        if roof["bound"] == "fp32" else f"{src} hbm_gbs")
 
     cpu = None
     if rank == 0 and not args.no_cpu:

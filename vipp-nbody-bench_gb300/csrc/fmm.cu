@@ -6,6 +6,8 @@
 // (index > 8), L2L into cells at level >= 3, L2P on leaves at level >= 2.
 #include <cstdio>
 
+#include <cooperative_groups.h>
+
 #include "workspace.cuh"
 
 namespace gb {
@@ -314,51 +316,66 @@ __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, 
     }
 }
 
-// M2M for one level L >= 2: tiles of 64 non-leaf cells, 8 octant slots
-// (child o of each cell through M2M_o).
+// M2M for one level L >= 2 on thread-block clusters of 8 CTAs: a cluster
+// takes a tile of 64 non-leaf cells and CTA o of the cluster applies M2M_o to
+// the children in octant o. Each CTA leaves its partial tile in its shared
+// memory; after a cluster barrier, CTA o adds rows 8o .. 8o+7 of the eight
+// partial tiles through distributed shared memory, in octant order 0..7, and
+// writes the parents' multipoles. (One CTA doing the 8 octants in turn made a
+// level cost ~165 us whatever its size.)
 template <int P, typename T>
-__global__ void __launch_bounds__(256) k_m2m(int L, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell,
-                                             const int *__restrict__ c_child, const T *__restrict__ ops, T *M) {
+__global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256)
+    k_m2m(int L, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell, const int *__restrict__ c_child,
+          const T *__restrict__ ops, T *M) {
+    namespace cg = cooperative_groups;
     using C = TileCfg<P, T>;
     extern __shared__ __align__(16) unsigned char smraw[];
-    T *A = reinterpret_cast<T *>(smraw);
+    T *A = reinterpret_cast<T *>(smraw);  // [64][KS]: gathered children, then the partial tile
     T *Op = A + kTile * C::KS;
     __shared__ int par[kTile], srcs[kTile];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int o = static_cast<int>(cluster.block_rank());
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int e0 = info->split_start[L], cnt = info->split_count[L];
     const int tiles = (cnt + kTile - 1) / kTile;
-    if (tiles == 0) return;
+    if (tiles == 0) return;  // uniform over the grid: no cluster barrier reached
     tile_clear<P, T>(A);
-    for (int w = blockIdx.x; w < tiles; w += gridDim.x) {
+    tile_load_op<P, T>(Op, ops, kOpM2M + o);
+    const int nclusters = static_cast<int>(gridDim.x) / 8;
+    for (int w = static_cast<int>(blockIdx.x) / 8; w < tiles; w += nclusters) {  // same w in all 8 CTAs
         if (tid < kTile) {
             const int e = w * kTile + tid;
             par[tid] = e < cnt ? split_cell[e0 + e] : -1;
+            srcs[tid] = par[tid] >= 0 ? c_child[par[tid]] + o : -1;
         }
+        __syncthreads();
+        tile_gather<P, T>(A, srcs, M);
+        __syncthreads();
         T acc[4][C::NJ];
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
             for (int j = 0; j < C::NJ; ++j) acc[a][j] = 0;
-        for (int o = 0; o < 8; ++o) {
-            __syncthreads();
-            if (tid < kTile) srcs[tid] = par[tid] >= 0 ? c_child[par[tid]] + o : -1;
-            __syncthreads();
-            tile_load_op<P, T>(Op, ops, kOpM2M + o);
-            tile_gather<P, T>(A, srcs, M);
-            __syncthreads();
-            tile_gemm<P, T>(A, Op, acc, ty, tx);
-        }
+        tile_gemm<P, T>(A, Op, acc, ty, tx);
+        __syncthreads();
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int pc = par[ty * 4 + a];
-            if (pc < 0) continue;
+        for (int a = 0; a < 4; ++a)
 #pragma unroll
             for (int j = 0; j < C::NJ; ++j) {
                 const int r = tx + 16 * j;
-                if (r < C::K) M[static_cast<size_t>(pc) * C::K + r] = acc[a][j];
+                if (r < C::K) A[(ty * 4 + a) * C::KS + r] = acc[a][j];
             }
+        cluster.sync();  // all eight partial tiles written
+        for (int i = tid; i < 8 * C::K; i += blockDim.x) {
+            const int row = 8 * o + i / C::K, r = i % C::K;
+            const int pc = par[row];
+            if (pc < 0) continue;
+            T sum = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) sum += cluster.map_shared_rank(A, q)[row * C::KS + r];
+            M[static_cast<size_t>(pc) * C::K + r] = sum;
         }
-        __syncthreads();
+        cluster.sync();  // no CTA overwrites its partial tile while others read it
     }
 }
 
@@ -521,7 +538,7 @@ template <int P, typename T>
 void launch_m2m_levels(Workspace &ws) {
     const size_t smem = TileCfg<P, T>::smem;
     cudaFuncSetAttribute(k_m2m<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 2;
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) / 8 * 16;  // clusters of 8 CTAs
     for (int L = kMaxLevel - 1; L >= 2; --L) {
         k_m2m<P, T><<<gs, 256, smem, ws.st>>>(L, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws), static_cast<T *>(ws.Mexp));
         ws.launches += 1;

@@ -63,12 +63,31 @@ __global__ void k_bbox_partial(const double *__restrict__ x, unsigned n, double 
     }
 }
 
-__global__ void k_bbox_final(const double *__restrict__ part, int nb, TreeInfo *info) {
+// One block of kTB threads; min and max do not depend on the order of the
+// partials, so the parallel reduction gives the same box as a serial one.
+__global__ void __launch_bounds__(kTB) k_bbox_final(const double *__restrict__ part, int nb, TreeInfo *info) {
+    __shared__ double red[6][kTB / 32];
+    double v[6];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) v[a] = DBL_MAX, v[3 + a] = -DBL_MAX;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) v[a] = fmin(v[a], part[a * nb + b]), v[3 + a] = fmax(v[3 + a], part[(3 + a) * nb + b]);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        for (int o = 16; o; o >>= 1) {
+            const double u = __shfl_xor_sync(0xffffffffu, v[q], o);
+            v[q] = q < 3 ? fmin(v[q], u) : fmax(v[q], u);
+        }
+        if (lane == 0) red[q][w] = v[q];
+    }
+    __syncthreads();
     if (threadIdx.x != 0) return;
     double mn[3], mx[3];
     for (int a = 0; a < 3; ++a) {
         mn[a] = DBL_MAX, mx[a] = -DBL_MAX;
-        for (int b = 0; b < nb; ++b) mn[a] = fmin(mn[a], part[a * nb + b]), mx[a] = fmax(mx[a], part[(3 + a) * nb + b]);
+        for (int k = 0; k < static_cast<int>(blockDim.x >> 5); ++k) mn[a] = fmin(mn[a], red[a][k]), mx[a] = fmax(mx[a], red[3 + a][k]);
     }
     const double pad = 1e-5;  // Problem::OCTREE_WIDTH_PADDING (problem.hpp:167)
     double S = 0, margin = 0;
@@ -612,7 +631,7 @@ void build_tree(Workspace &ws) {
     const int nb = 2 * ws.num_sms;
     double *part = ws.bbox_part;
     k_bbox_partial<<<nb, kTB, 0, st>>>(ws.x, n, part, ws.info);
-    k_bbox_final<<<1, 32, 0, st>>>(part, nb, ws.info);
+    k_bbox_final<<<1, kTB, 0, st>>>(part, nb, ws.info);
     k_keys<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.keys0, ws.perm0);
     ws.launches += 3;
     const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, 0, 3 * kMaxLevel, ws.sort, st,

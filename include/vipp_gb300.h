@@ -118,11 +118,26 @@ GB_API int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos);
 GB_API int gb_rk4_step(gb_ctx *ctx, double dt);
 
 /* One FMM force evaluation (SolverRef::acceleration, solver_ref.hpp:164-177)
- * at the current positions; a_aos receives n accelerations (AoS doubles).
- * phi may be NULL; when given it receives the potential sum_j -G m / r_j over
- * the same interactions (near field softened; far field from the local
- * expansion, which like the reference's far field carries no G). */
+ * at the current positions; a_aos (may be NULL) receives n accelerations (AoS
+ * doubles). phi may be NULL; when given it receives n potentials per unit mass
+ * in the accelerations' convention a = -grad phi: the softened near-field sum
+ * -G m sum_{j != i} (r^2 + eps^2)^-1/2 (FP64) plus the far field from the local
+ * expansions, which like the reference's far field carries no G. The reference
+ * has no potential; this output has no counterpart there. */
 GB_API int gb_accel(gb_ctx *ctx, double *a_aos, double *phi);
+
+/* Conserved quantities of the current state, for energy-drift checks (no
+ * counterpart in the reference, which computes no potential). The potential
+ * comes from one FMM evaluation of the current positions (gb_accel's phi);
+ * sums in FP64 with a fixed reduction order (deterministic). */
+typedef struct gb_conserved {
+    double kinetic;             /* 1/2 m sum |v|^2 */
+    double potential;           /* 1/2 m sum phi_i */
+    double total;               /* kinetic + potential */
+    double momentum[3];         /* m sum v */
+    double angular_momentum[3]; /* m sum x cross v */
+} gb_conserved;
+GB_API int gb_get_conserved(gb_ctx *ctx, gb_conserved *out);
 
 /* FP64 direct softened sum on the GPU for the listed targets of the current
  * positions (the accuracy oracle; SolverRefNaive::acceleration,

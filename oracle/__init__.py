@@ -208,6 +208,17 @@ def direct_accel(x, G, m, eps, targets=None):
     return a
 
 
+def direct_phi(x, G, m, eps, targets=None):
+    """FP64 direct softened potential -G m sum_{j != i} (r^2 + eps^2)^-1/2 (OpenMP)."""
+    x = _aos(x)
+    n = x.shape[0]
+    t = None if targets is None else np.ascontiguousarray(targets, dtype=np.int64)
+    phi = np.zeros(n if t is None else len(t))
+    lib().orc_direct_phi(_dp(x), _size(n), ctypes.c_double(G), ctypes.c_double(m), ctypes.c_double(eps),
+                         None if t is None else _lp(t), _size(0 if t is None else len(t)), _dp(phi))
+    return phi
+
+
 def plummer_reference(n, eps, seed):
     """Problem::initialize (problem.hpp:188-211) restated: (x, v) AoS."""
     x = np.zeros((n, 3))

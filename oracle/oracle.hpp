@@ -545,6 +545,19 @@ inline V3 direct_one(const std::vector<V3> &x, std::size_t i, double G, double m
     return acc;
 }
 
+// Softened potential of the direct sum at target i, phi_i = -G m sum_{j != i}
+// (|x_j - x_i|^2 + eps^2)^(-1/2). The reference computes no potential; this is
+// the FP64 checker of the GPU potentials (same softening and self exclusion as
+// direct_one, solver_ref_naive.hpp:103-119).
+inline double direct_phi_one(const std::vector<V3> &x, std::size_t i, double G, double mass, double eps) {
+    double s = 0;
+    for (std::size_t j = 0; j < x.size(); ++j) {
+        if (i == j) continue;
+        s += 1.0 / std::sqrt(norm2(sub(x[j], x[i])) + eps * eps);
+    }
+    return -G * mass * s;
+}
+
 // Classical RK4 step (solver_ref.hpp:36-104): stage weights dt/6, dt/3, dt/3,
 // dt/6; stage states x0 + c dt v_stage, v0 + c dt a with c = 1/2, 1/2, 1.
 template <class AccelFn>

@@ -155,6 +155,14 @@ void orc_direct_accel(const double *x_aos, std::size_t n, double G, double m, do
     }
 }
 
+void orc_direct_phi(const double *x_aos, std::size_t n, double G, double m, double eps, const long long *targets,
+                    std::size_t nt, double *phi) {
+    auto x = to_v3(x_aos, n);
+    const std::size_t cnt = targets ? nt : n;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (std::size_t k = 0; k < cnt; ++k) phi[k] = direct_phi_one(x, targets ? static_cast<std::size_t>(targets[k]) : k, G, m, eps);
+}
+
 void orc_direct_rk4(double *x_aos, double *v_aos, std::size_t n, double G, double m, double eps, double dt, int steps) {
     auto x = to_v3(x_aos, n), v = to_v3(v_aos, n);
     for (int k = 0; k < steps; ++k)

@@ -176,3 +176,13 @@ def test_fmm_accel_and_rk4_match_reference(orc, name):
     x1, v1 = orc.rk4(d["x"], d["v"], d["s"], d["G"], d["m"], d["eps"], d["dt"], d["p"], 1)
     assert np.max(np.abs(x1 - d["x1"])) <= 1e-14 * max(1.0, np.max(np.abs(d["x"])))
     assert np.max(np.abs(v1 - d["v1"])) <= 1e-12 * max(1e-3, np.max(np.abs(d["v1"])))
+
+
+def test_direct_potential_known_answer():
+    """The oracle's FP64 potential (checker of the GPU potentials; the
+    reference computes none): three particles, G = 2, m = 0.5, eps = 0.1."""
+    x = np.array([[0.0, 0.0, 0.0], [3.0, 4.0, 0.0], [0.0, 0.0, 1.0]])
+    phi = O.direct_phi(x, 2.0, 0.5, 0.1)
+    d = lambda r2: 1.0 / math.sqrt(r2 + 0.01)
+    want = [-(d(25) + d(1)), -(d(25) + d(26)), -(d(1) + d(26))]
+    np.testing.assert_allclose(phi, want, rtol=1e-15)

@@ -32,6 +32,7 @@ struct gb_ctx {
     std::string err;
     bool have_state = false;
     long long retries = 0;  // evaluations repeated after a capacity overflow
+    size_t phi_cap = 0;     // particles ws.phi / ws.phis are sized for
     std::vector<gb::PendingTimer> pending;
     std::vector<cudaEvent_t> free_events;
     long long *d_targets = nullptr;
@@ -444,7 +445,7 @@ void gb_destroy(gb_ctx *ctx) {
                     ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
-                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.ms_tc, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
+                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.ms_tc, ws.diag, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
                     ctx->d_direct};
     for (void *b : bufs) dfree(b);
     gb::sort_temp_free(ws.sort);
@@ -553,20 +554,64 @@ int gb_rk4_step(gb_ctx *ctx, double dt) {
     return rc;
 }
 
+// Potential buffers (allocated on the first request): ws.phi [N] in the
+// caller's order, ws.phis [2][N] near and far parts in tree order, ws.diag.
+int ensure_potential(gb_ctx *ctx) {
+    gb::Workspace &ws = ctx->ws;
+    if (ws.n <= ctx->phi_cap && ws.phi) return GB_OK;
+    GB_TRY(dalloc(ws.phi, ws.n));
+    GB_TRY(dalloc(ws.phis, 2 * static_cast<size_t>(ws.n)));
+    if (!ws.diag) GB_TRY(dalloc(ws.diag, gb::diag_scratch_doubles()));
+    ctx->phi_cap = ws.n;
+    return GB_OK;
+}
+
 int gb_accel(gb_ctx *ctx, double *a_aos, double *phi) {
     if (!ctx) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
     GB_TRY(cudaSetDevice(ctx->cfg.device));
     gb::Workspace &ws = ctx->ws;
     if (ws.n == 0) return GB_OK;
-    if (phi) return ctx->err = "potential output is not available in this build", GB_ERR_INVALID;
+    if (phi) {
+        const int r = ensure_potential(ctx);
+        if (r) return r;
+    }
     const int rc = run_with_capacity(ctx, [&]() { evaluate(ctx); });
     if (rc) return rc;
     if (a_aos) {
         gb::soa_to_aos(ws, ws.acc, ws.staging, ws.n);
         GB_TRY(cudaMemcpyAsync(a_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
-        GB_TRY(cudaStreamSynchronize(ws.st));
     }
+    if (phi) {
+        gb::potential_orig(ws, ws.phi);
+        GB_TRY(cudaMemcpyAsync(phi, ws.phi, sizeof(double) * ws.n, cudaMemcpyDeviceToHost, ws.st));
+    }
+    GB_TRY(cudaStreamSynchronize(ws.st));
+    return GB_OK;
+}
+
+int gb_get_conserved(gb_ctx *ctx, gb_conserved *out) {
+    if (!ctx || !out) return GB_ERR_INVALID;
+    if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    gb::Workspace &ws = ctx->ws;
+    std::memset(out, 0, sizeof(*out));
+    if (ws.n == 0) return GB_OK;
+    int rc = ensure_potential(ctx);
+    if (rc) return rc;
+    rc = run_with_capacity(ctx, [&]() { evaluate(ctx); });
+    if (rc) return rc;
+    gb::potential_orig(ws, ws.phi);
+    double *sums = ws.diag + gb::diag_scratch_doubles() - 8;
+    gb::conserved_sums(ws, ws.phi, sums);
+    double h[8];
+    GB_TRY(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, ws.st));
+    GB_TRY(cudaStreamSynchronize(ws.st));
+    const double m = ws.m;
+    out->kinetic = 0.5 * m * h[0];
+    out->potential = 0.5 * m * h[1];
+    out->total = out->kinetic + out->potential;
+    for (int a = 0; a < 3; ++a) out->momentum[a] = m * h[2 + a], out->angular_momentum[a] = m * h[5 + a];
     return GB_OK;
 }
 

@@ -505,6 +505,53 @@ __global__ void k_finalize(const unsigned *__restrict__ perm, unsigned n, const 
             static_cast<double>(nearv[static_cast<size_t>(a) * n + j]) + static_cast<double>(farv[static_cast<size_t>(a) * n + j]);
 }
 
+// Far-field potential (diagnostic, after an evaluation): the potential of
+// the local expansion at each particle of a leaf at level >= 2,
+// Phi = (1/s) sum_j [L~_j^0 R_j^0(u) + 2 Re sum_k L~_j^k R_j^k(u)], u = (x - c)/s,
+// whose gradient is the far-field acceleration of k_l2p (no G, as there).
+template <int P, typename T>
+__global__ void __launch_bounds__(128) k_l2p_phi(const int *__restrict__ leaves, const unsigned *counts,
+                                                 const int *__restrict__ c_begin, const int *__restrict__ c_end,
+                                                 const int *__restrict__ c_level, const double *__restrict__ c_ctr,
+                                                 const double *__restrict__ xs, unsigned n, const TreeInfo *__restrict__ info,
+                                                 const T *__restrict__ Lx, double *__restrict__ farphi) {
+    constexpr int K = (P + 1) * (P + 1);
+    __shared__ T Ls[4][K];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned NL = counts[3];
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    for (unsigned li = blockIdx.x * (blockDim.x >> 5) + w; li < NL; li += warps) {
+        const int c = leaves[li];
+        const int L = c_level[c];
+        if (L < 2) continue;  // warp-uniform
+        for (int r = lane; r < K; r += 32) Ls[w][r] = Lx[static_cast<size_t>(c) * K + r];
+        __syncwarp();
+        const double s = level_scale(info, L), inv_s = 1.0 / s;
+        const double cx = c_ctr[3 * c], cy = c_ctr[3 * c + 1], cz = c_ctr[3 * c + 2];
+        const T *Lc = Ls[w];
+        for (int j = c_begin[c] + lane; j < c_end[c]; j += 32) {
+            const T ux = static_cast<T>((xs[j] - cx) * inv_s);
+            const T uy = static_cast<T>((xs[n + j] - cy) * inv_s);
+            const T uz = static_cast<T>((xs[2 * static_cast<size_t>(n) + j] - cz) * inv_s);
+            T phi = 0;
+            for_each_regular<P, T>(ux, uy, uz, [&](int nn, int q, T rr, T ri) {
+                const T lr = Lc[ridx(nn, q, 0)], li2 = q ? Lc[ridx(nn, q, 1)] : T(0);
+                phi += (q ? T(2) : T(1)) * (lr * rr - li2 * ri);
+            });
+            farphi[j] = static_cast<double>(phi) * inv_s;
+        }
+        __syncwarp();
+    }
+}
+
+template <int P, typename T>
+void launch_l2p_phi(Workspace &ws, double *farphi) {
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
+    k_l2p_phi<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.n,
+                                           ws.info, static_cast<const T *>(ws.Lexp), farphi);
+    ws.launches += 1;
+}
+
 template <int P, typename T>
 void launch_p2m(Workspace &ws) {
     const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
@@ -557,10 +604,11 @@ void launch_l2l_levels(Workspace &ws) {
 }
 
 template <typename T>
-void dispatch_p(Workspace &ws, int which) {
+void dispatch_p(Workspace &ws, int which, double *farphi = nullptr) {
     switch (ws.p) {
 #define GB_CASE(PP)                      \
     case PP:                             \
+        if (which == 5) launch_l2p_phi<PP, T>(ws, farphi); \
         if (which == 0) launch_p2m<PP, T>(ws); \
         if (which == 1) launch_m2l<PP, T>(ws); \
         if (which == 2) launch_l2p<PP, T>(ws); \
@@ -628,6 +676,14 @@ void downward_pass(Workspace &ws) {
     }
     ws.launches += 1;
     timer_end(ws, kTDown);
+}
+
+void far_potential(Workspace &ws, double *farphi) {
+    cudaMemsetAsync(farphi, 0, sizeof(double) * ws.n, ws.st);  // particles of leaves above level 2
+    if (ws.mixed)
+        dispatch_p<float>(ws, 5, farphi);
+    else
+        dispatch_p<double>(ws, 5, farphi);
 }
 
 void finalize_accel(Workspace &ws, double *acc_orig) {

@@ -290,7 +290,95 @@ __global__ void k_p2p_combine(const int4 *__restrict__ chunks, const unsigned *c
     }
 }
 
+// Near-field potential (diagnostic, FP64, after an evaluation): for every
+// target i of a work item, sum over its near-field sources j != i (tree
+// indices) of (|x_j - x_i|^2 + eps^2)^(-1/2). Split items leave per-slice
+// partial sums in part[slot][0..31]; k_p2p_phi_combine adds them in slice order.
+__global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_phi(const int4 *__restrict__ chunks, const unsigned *counts,
+                                                            unsigned *queue, const unsigned *__restrict__ rng_off,
+                                                            const unsigned *__restrict__ rng_len, const uint2 *__restrict__ ranges,
+                                                            const double *__restrict__ xs, const unsigned *__restrict__ src_total,
+                                                            double *__restrict__ part, double Gm, double eps2,
+                                                            double *__restrict__ phiv, unsigned n) {
+    __shared__ double src[kP2PWarps][3][32];
+    __shared__ double red[kP2PWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned nch = counts[5];
+    while (true) {
+        unsigned ci = 0;
+        if (lane == 0) ci = atomicAdd(queue, 1u);
+        ci = __shfl_sync(0xffffffffu, ci, 0);
+        if (ci >= nch) break;
+        const Item it(chunks[ci], src_total);
+        const int nt = it.nt;
+        const int g = 32 / nt;
+        const int grp = lane / nt;
+        const int t = lane - grp * nt;
+        const bool tact = grp < g;
+        const unsigned i = static_cast<unsigned>(it.t0 + t);
+        const double tx = tact ? xs[i] : 0.0, ty = tact ? xs[n + i] : 0.0, tz = tact ? xs[2 * static_cast<size_t>(n) + i] : 0.0;
+        double pot = 0;
+        Cursor cur;
+        cur.start(ranges + rng_off[it.li], rng_len[it.li], it.v0, it.len);
+        while (cur.valid()) {
+            const unsigned cnt = cur.count(), jb = cur.b;
+            if (static_cast<unsigned>(lane) < cnt) {
+                const unsigned j = jb + lane;
+                src[w][0][lane] = xs[j];
+                src[w][1][lane] = xs[n + j];
+                src[w][2][lane] = xs[2 * static_cast<size_t>(n) + j];
+            }
+            __syncwarp();
+            if (tact)
+                for (unsigned k = grp; k < cnt; k += g) {
+                    if (jb + k == i) continue;
+                    const double dx = src[w][0][k] - tx, dy = src[w][1][k] - ty, dz = src[w][2][k] - tz;
+                    pot += 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+                }
+            __syncwarp();
+            cur.advance();
+        }
+        if (g > 1) {
+            red[w][lane] = pot;
+            __syncwarp();
+            if (grp == 0)
+                for (int q = 1; q < g; ++q) pot += red[w][t + q * nt];
+            __syncwarp();
+        }
+        if (grp == 0) {
+            if (it.ns == 1)
+                phiv[i] = Gm * pot;
+            else
+                part[static_cast<size_t>(it.pslot) * 96 + t] = pot;
+        }
+    }
+}
+
+__global__ void k_p2p_phi_combine(const int4 *__restrict__ chunks, const unsigned *counts, const double *__restrict__ part,
+                                  double Gm, double *__restrict__ phiv) {
+    const unsigned nit = counts[5];
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < nit * 32u; q += gridDim.x * blockDim.x) {
+        const int4 w = chunks[q >> 5];
+        const int t = static_cast<int>(q & 31u);
+        const int ns = item_nslices(w.z);
+        if (ns <= 1 || item_slice(w.z) != 0 || t >= item_nt(w.z)) continue;
+        double s = 0;
+        for (int k = 0; k < ns; ++k) s += part[static_cast<size_t>(w.w + k) * 96 + t];
+        phiv[w.y + t] = Gm * s;
+    }
+}
+
 }  // namespace
+
+void near_potential(Workspace &ws, double *phiv) {
+    cudaMemsetAsync(ws.queue, 0, sizeof(unsigned), ws.st);
+    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
+    k_p2p_phi<<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.rng_off, ws.rng_len, ws.ranges, ws.xs,
+                                                ws.src_total, static_cast<double *>(ws.part), ws.G * ws.m, ws.eps * ws.eps,
+                                                phiv, ws.n);
+    k_p2p_phi_combine<<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, static_cast<const double *>(ws.part), ws.G * ws.m, phiv);
+    ws.launches += 2;
+}
 
 void p2p_pass(Workspace &ws) {
     timer_begin(ws, kTP2P);

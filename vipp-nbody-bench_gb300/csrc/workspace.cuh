@@ -65,7 +65,8 @@ struct Workspace {
     double *xs = nullptr;                   // [3][N]
     float4 *ph = nullptr, *pl = nullptr;    // hi/lo positions, w = mass (hi) / 0
     void *nearf = nullptr, *farf = nullptr; // [3][N] of FP32 or FP64
-    double *phis = nullptr;                 // potential, tree order [N] (optional)
+    double *phis = nullptr;                 // potential parts, tree order [2][N]: near, far (optional)
+    double *diag = nullptr;                 // reduction partials of the conserved sums
     unsigned *cnt = nullptr, *off = nullptr;  // [N+1]
 
     // split entries
@@ -141,6 +142,14 @@ const char *m2l_tc_encode(Workspace &ws);     // (re)build tmap_ms; nullptr or a
 void downward_pass(Workspace &ws);            // L2L + L2P into far
 void p2p_pass(Workspace &ws);                 // near field into near
 void finalize_accel(Workspace &ws, double *acc_orig);  // acc[perm] = near + far
+// diagnostics after an evaluation (tree order, FP64): far-field potential of the
+// local expansions (no G, like the far-field acceleration) and the near-field
+// softened potential sum (times G m, i == j excluded)
+void far_potential(Workspace &ws, double *farphi);
+void near_potential(Workspace &ws, double *nearphi);
+void potential_orig(Workspace &ws, double *phi_orig);    // phi[perm] = -(near + far), needs ws.phis [2N]
+void conserved_sums(Workspace &ws, const double *phi_orig, double *sums8);  // see diag.cu
+size_t diag_scratch_doubles();
 void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, unsigned nt, double *out_soa,
                 double *part, unsigned nsplit);  // part: [nsplit][3][nt] scratch
 

@@ -30,12 +30,18 @@ TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
 # Every symbol include/vipp_gb300.h declares.
 EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_upload", "gb_download", "gb_rk4_step",
            "gb_accel", "gb_direct_accel", "gb_sync", "gb_get_stats", "gb_tree_dump", "gb_enable_timing",
-           "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream", "gb_direct_accel_noalloc")
+           "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream", "gb_direct_accel_noalloc",
+           "gb_get_conserved")
 
 
 class GbConfig(ctypes.Structure):
     _fields_ = [("p", ctypes.c_int), ("s", ctypes.c_int), ("eps", ctypes.c_double), ("G", ctypes.c_double),
                 ("m", ctypes.c_double), ("precision", ctypes.c_int), ("device", ctypes.c_int), ("flags", ctypes.c_int)]
+
+
+class GbConserved(ctypes.Structure):
+    _fields_ = [("kinetic", ctypes.c_double), ("potential", ctypes.c_double), ("total", ctypes.c_double),
+                ("momentum", ctypes.c_double * 3), ("angular_momentum", ctypes.c_double * 3)]
 
 
 class GbStats(ctypes.Structure):
@@ -70,6 +76,7 @@ def load(path: str | None = None):
     lib.gb_direct_accel.argtypes = [vp, vp, ctypes.c_size_t, vp]
     lib.gb_sync.argtypes = [vp]
     lib.gb_get_stats.argtypes = [vp, ctypes.POINTER(GbStats)]
+    lib.gb_get_conserved.argtypes = [vp, ctypes.POINTER(GbConserved)]
     lib.gb_tree_dump.argtypes = [vp] + [vp] * 17
     lib.gb_enable_timing.argtypes = [vp, ctypes.c_int]
     lib.gb_kernel_times.argtypes = [vp, vp, vp, ctypes.c_int]
@@ -164,10 +171,24 @@ class Solver:
     def download_ptr(self, x_ptr: int, v_ptr: int):
         self._check(self.lib.gb_download(self.h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(v_ptr)))
 
-    def accel(self):
+    def accel(self, potential=False):
+        """Accelerations (n, 3); with potential=True also the potentials (n,),
+        a = -grad phi (the near field FP64, softened, i == j excluded)."""
         a = np.zeros((self.n, 3))
-        self._check(self.lib.gb_accel(self.h, _ptr(a), None))
-        return a
+        if not potential:
+            self._check(self.lib.gb_accel(self.h, _ptr(a), None))
+            return a
+        phi = np.zeros(self.n)
+        self._check(self.lib.gb_accel(self.h, _ptr(a), _ptr(phi)))
+        return a, phi
+
+    def conserved(self) -> dict:
+        """Kinetic, potential and total energy, momentum and angular momentum
+        of the current state (one FMM evaluation for the potential)."""
+        c = GbConserved()
+        self._check(self.lib.gb_get_conserved(self.h, ctypes.byref(c)))
+        return {"kinetic": c.kinetic, "potential": c.potential, "total": c.total,
+                "momentum": np.array(c.momentum[:]), "angular_momentum": np.array(c.angular_momentum[:])}
 
     def direct_accel(self, targets=None):
         if targets is None:

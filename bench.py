@@ -225,6 +225,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--flags", type=int, default=0, help="gb_config flags (vipp_gb300.FLAG_*)")
+    ap.add_argument("--no-energy", action="store_true", help="skip the total-energy drift (two extra evaluations)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
@@ -251,6 +252,9 @@ def main():
     for _ in range(args.warmup):
         sol.solve(args.dt)
     sol.sync()
+    # total energy before and after the timed steps (untimed; one extra FMM
+    # evaluation with potentials each)
+    cons0 = sol.conserved() if not args.no_energy else None
 
     # --- timed region: state resident in HBM -------------------------------------
     sol.enable_timing(True)
@@ -279,6 +283,12 @@ def main():
     kt = sol.kernel_times()
     sol.enable_timing(False)
     st = sol.stats()
+    energy = None
+    if cons0 is not None:
+        cons1 = sol.conserved()
+        energy = {"e_before": cons0["total"], "e_after": cons1["total"], "steps": args.steps, "dt": args.dt,
+                  "rel_drift": abs(cons1["total"] - cons0["total"]) / abs(cons0["total"]),
+                  "potential_from": "FMM far field + FP64 near field of the same method"}
     elapsed = max_over_ranks(elapsed, ws)
     value = n * ws * args.steps / elapsed
 
@@ -386,7 +396,7 @@ def main():
            "s": args.s, "eps": args.eps, "dt": args.dt, "precision": args.precision, "seed": 2,
            "l2": "inputs larger than L2 (state 192 MB, per-step working set > 1 GB)",
            "tree": {k: st[k] for k in ("ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges")},
-           "kernel_ms_per_step": kt_ms, **acc_info, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
+           "kernel_ms_per_step": kt_ms, **acc_info, "energy": energy, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * elapsed / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
             "higher_is_better": True, "scaling": "weak",

@@ -106,6 +106,14 @@ GB_API const char *gb_last_error(const gb_ctx *ctx);
  * read by SolverRef::solve, solver_ref.hpp:21-25). */
 GB_API int gb_set_config(gb_ctx *ctx, const gb_config *cfg);
 
+/* Initial state generated on the device: the reference's Plummer sphere
+ * (Problem::initialize, problem.hpp:188-211, 245-292; G = M = a = 1) with one
+ * counter-based random stream per particle. r_max = 0 keeps the reference's
+ * radius cap (mass fraction below 1 - eps, eps from the config); r_max > 0
+ * caps radii at r_max instead. Same distribution as the reference, not the
+ * same numbers. Replaces the state like gb_upload; gb_download reads it. */
+GB_API int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max);
+
 /* preprocess: copy n particles (AoS doubles) to the device. n may be 0. */
 GB_API int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n);
 /* postprocess: copy the current state back (AoS doubles, n entries each). */

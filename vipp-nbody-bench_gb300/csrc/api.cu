@@ -511,6 +511,33 @@ int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
     return GB_OK;
 }
 
+int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max) {
+    if (!ctx) return GB_ERR_INVALID;
+    if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
+    if (!(r_max >= 0) || !std::isfinite(r_max)) return ctx->err = "r_max must be finite and >= 0", GB_ERR_INVALID;
+    if (r_max == 0 && !(ctx->cfg.eps > 0 && ctx->cfg.eps < 1))
+        return ctx->err = "the reference's radius cap needs 0 < eps < 1 (or give r_max)", GB_ERR_INVALID;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    gb::Workspace &ws = ctx->ws;
+    const unsigned nn = static_cast<unsigned>(n);
+    int rc = ensure_particles(ctx, nn);
+    if (rc) return rc;
+    ws.n = nn;
+    if (nn) {
+        gb::generate_plummer(ws, nn, seed, 1.0 - ctx->cfg.eps, r_max);
+        GB_TRY(cudaGetLastError());
+        int err = 0;
+        GB_TRY(cudaMemcpyAsync(&err, &ws.info->err, sizeof(int), cudaMemcpyDeviceToHost, ws.st));
+        GB_TRY(cudaStreamSynchronize(ws.st));
+        if (err) return ctx->err = "initial-condition sampling did not converge", GB_ERR_CUDA;
+        rc = initial_capacity(ctx);
+        if (rc) return rc;
+    }
+    GB_TRY(cudaStreamSynchronize(ws.st));
+    ctx->have_state = true;
+    return GB_OK;
+}
+
 int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos) {
     if (!ctx) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;

@@ -31,7 +31,7 @@ TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
 EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_upload", "gb_download", "gb_rk4_step",
            "gb_accel", "gb_direct_accel", "gb_sync", "gb_get_stats", "gb_tree_dump", "gb_enable_timing",
            "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream", "gb_direct_accel_noalloc",
-           "gb_get_conserved")
+           "gb_get_conserved", "gb_init_plummer")
 
 
 class GbConfig(ctypes.Structure):
@@ -77,6 +77,7 @@ def load(path: str | None = None):
     lib.gb_sync.argtypes = [vp]
     lib.gb_get_stats.argtypes = [vp, ctypes.POINTER(GbStats)]
     lib.gb_get_conserved.argtypes = [vp, ctypes.POINTER(GbConserved)]
+    lib.gb_init_plummer.argtypes = [vp, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_double]
     lib.gb_tree_dump.argtypes = [vp] + [vp] * 17
     lib.gb_enable_timing.argtypes = [vp, ctypes.c_int]
     lib.gb_kernel_times.argtypes = [vp, vp, vp, ctypes.c_int]
@@ -181,6 +182,12 @@ class Solver:
         phi = np.zeros(self.n)
         self._check(self.lib.gb_accel(self.h, _ptr(a), _ptr(phi)))
         return a, phi
+
+    def init_plummer(self, n, seed=0, r_max=0.0):
+        """Generate the reference's Plummer sphere on the device (r_max = 0: the
+        reference's radius cap from eps; r_max > 0: radii <= r_max)."""
+        self._check(self.lib.gb_init_plummer(self.h, int(n), int(seed), float(r_max)))
+        self.n = int(n)
 
     def conserved(self) -> dict:
         """Kinetic, potential and total energy, momentum and angular momentum

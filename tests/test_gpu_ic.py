@@ -45,7 +45,7 @@ def q_cdf():
 
 def generate(n, seed, eps=0.01, r_max=0.0):
     import vipp_gb300
-    with vipp_gb300.Solver(p=4, s=32, eps=eps, m=1.0 / n) as s:
+    with vipp_gb300.Solver(p=4, s=32, eps=eps, m=1.0 / max(n, 1)) as s:
         s.init_plummer(n, seed, r_max)
         return s.postprocess()
 

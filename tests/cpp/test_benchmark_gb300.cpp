@@ -15,15 +15,18 @@
 
 namespace {
 
-struct Vec {
-    double x_ = 0, y_ = 0, z_ = 0;
-    double x() const { return x_; }
-    double y() const { return y_; }
-    double z() const { return z_; }
-    double &x() { return x_; }
-    double &y() { return y_; }
-    double &z() { return z_; }
+template <class U>
+struct VecT {
+    U x_ = 0, y_ = 0, z_ = 0;
+    U x() const { return x_; }
+    U y() const { return y_; }
+    U z() const { return z_; }
+    U &x() { return x_; }
+    U &y() { return y_; }
+    U &z() { return z_; }
 };
+using Vec = VecT<double>;
+using VecF = VecT<float>;  // the reference's GRAVITY_FLOAT vectors
 
 // Problem stand-in: the reference's accessors plus initialize() from the
 // oracle's bit-identical restatement of Problem::initialize (Plummer sphere).
@@ -40,13 +43,15 @@ struct PlummerProblem {
     unsigned p() const { return p_; }
     std::size_t s() const { return s_; }
     double delta_t() const { return eps / std::sqrt(2.0); }  // problem.hpp:235-243
-    void initialize(std::vector<Vec> &x, std::vector<Vec> &v) const {
+    template <class W>
+    void initialize(std::vector<W> &x, std::vector<W> &v) const {
         std::vector<vipp_oracle::V3> x3, v3;
         vipp_oracle::plummer_reference(n, eps, seed, x3, v3);
         x.resize(n), v.resize(n);
+        using U = decltype(x[0].x_);
         for (std::size_t i = 0; i < n; ++i) {
-            x[i].x_ = x3[i].x, x[i].y_ = x3[i].y, x[i].z_ = x3[i].z;
-            v[i].x_ = v3[i].x, v[i].y_ = v3[i].y, v[i].z_ = v3[i].z;
+            x[i].x_ = static_cast<U>(x3[i].x), x[i].y_ = static_cast<U>(x3[i].y), x[i].z_ = static_cast<U>(x3[i].z);
+            v[i].x_ = static_cast<U>(v3[i].x), v[i].y_ = static_cast<U>(v3[i].y), v[i].z_ = static_cast<U>(v3[i].z);
         }
     }
 };
@@ -114,6 +119,15 @@ int main() {
         const auto r = BenchmarkGB300::run(eval, ref, pr, pr, xe, ve, xr, vr);
         show("1% short step", r);
         expect(!r.passed && r.c > -1.5, "a solver with a wrong step fails (E ~ T^-1)");
+    }
+    {  // benchmark_different_precision (benchmark.hpp:33-87): float state, mixed GPU solver, FP64 comparator
+        using MixedF = gravity::SolverGB300<float, float, float, float, float, float, GB_PREC_MIXED>;
+        MixedF eval;
+        Fp64 ref;
+        std::vector<VecF> xf, vf;
+        const auto r = BenchmarkGB300::run(eval, ref, pr, pr, xf, vf, xr, vr);
+        show("float mixed vs FP64", r);
+        expect(r.passed, "float-typed mixed solver passes against the FP64 pipeline");
     }
     std::printf(failures ? "%d FAILED\n" : "ALL PASSED\n", failures);
     return failures ? 1 : 0;

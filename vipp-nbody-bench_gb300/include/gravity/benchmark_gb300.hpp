@@ -76,10 +76,12 @@ struct BenchmarkGB300 {
         return {num / den, c};
     }
 
-    template <class EvalSolver, class RefSolver, class ProblemEval, class ProblemRef, class VecX, class VecV>
+    // The evaluated and comparator states may use different vector types
+    // (the reference's benchmark_different_precision, benchmark.hpp:33-87).
+    template <class EvalSolver, class RefSolver, class ProblemEval, class ProblemRef, class XE, class VE, class XR, class VR>
     static BenchmarkResultGB300 run(EvalSolver &eval, RefSolver &ref, const ProblemEval &problem, const ProblemRef &problem_ref,
-                                    std::vector<VecX> &x_eval, std::vector<VecV> &v_eval, std::vector<VecX> &x_ref,
-                                    std::vector<VecV> &v_ref, std::vector<double> t_set = geometric_sequence(1, 2, 5),
+                                    std::vector<XE> &x_eval, std::vector<VE> &v_eval, std::vector<XR> &x_ref,
+                                    std::vector<VR> &v_ref, std::vector<double> t_set = geometric_sequence(1, 2, 5),
                                     std::size_t subdivide = 1) {
         BenchmarkResultGB300 r;
         r.t_set = t_set;

@@ -121,9 +121,13 @@ __global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f32(const int4 *__restri
                                                             const unsigned *__restrict__ src_total, float *__restrict__ part,
                                                             float Gm, float eps2, float *__restrict__ nearv, unsigned n) {
     __shared__ float4 src[kP2PWarps][32];
+    __shared__ float4 srcxy[kP2PWarps][16];  // sources 2m, 2m+1 as {x, x', y, y'}
+    __shared__ float2 srcz[kP2PWarps][16];   // and {z, z'}
     __shared__ float red[kP2PWarps][3][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned nch = counts[5];
+    float *pxy = reinterpret_cast<float *>(srcxy[w]);
+    float *pz = reinterpret_cast<float *>(srcz[w]);
     while (true) {
         unsigned ci = 0;
         if (lane == 0) ci = atomicAdd(queue, 1u);
@@ -153,10 +157,17 @@ __global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f32(const int4 *__restri
             cnt = cur.count();
             if (static_cast<unsigned>(lane) < cnt) h = ph[cur.b + lane], l = pl[cur.b + lane];
         }
+        const float2 ntx = make_float2(-tx, -tx), nty = make_float2(-ty, -ty), ntz = make_float2(-tz, -tz);
+        const float2 e2 = make_float2(eps2, eps2);
         while (cnt) {
-            if (static_cast<unsigned>(lane) < cnt)
-                src[w][lane] = make_float4((h.x - cc.hx) + (l.x - cc.lx), (h.y - cc.hy) + (l.y - cc.ly),
-                                           (h.z - cc.hz) + (l.z - cc.lz), 0.f);
+            if (static_cast<unsigned>(lane) < cnt) {
+                const float qx = (h.x - cc.hx) + (l.x - cc.lx), qy = (h.y - cc.hy) + (l.y - cc.ly),
+                            qz = (h.z - cc.hz) + (l.z - cc.lz);
+                src[w][lane] = make_float4(qx, qy, qz, 0.f);
+                pxy[(lane >> 1) * 4 + (lane & 1)] = qx;
+                pxy[(lane >> 1) * 4 + 2 + (lane & 1)] = qy;
+                pz[(lane >> 1) * 2 + (lane & 1)] = qz;
+            }
             __syncwarp();
             const unsigned now = cnt;
             cur.advance();
@@ -167,8 +178,28 @@ __global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f32(const int4 *__restri
             }
             float bx = 0, by = 0, bz = 0;
             if (g == 1 && now == 32) {
+                // two sources per step on paired FP32 instructions (.f32x2);
+                // each component rounds exactly like the scalar operation
+                float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
 #pragma unroll
-                for (int k = 0; k < 32; ++k) pair_f32<kNewton, kSoft>(src[w][k], tx, ty, tz, eps2, bx, by, bz);
+                for (int m = 0; m < 16; ++m) {
+                    const float4 q = srcxy[w][m];
+                    const float2 dx = __fadd2_rn(make_float2(q.x, q.y), ntx);
+                    const float2 dy = __fadd2_rn(make_float2(q.z, q.w), nty);
+                    const float2 dz = __fadd2_rn(srcz[w][m], ntz);
+                    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+                    float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+                    if (kNewton) {
+                        ri.x = ri.x * fmaf(-0.5f * r2.x * ri.x, ri.x, 1.5f);
+                        ri.y = ri.y * fmaf(-0.5f * r2.y * ri.y, ri.y, 1.5f);
+                    }
+                    if (!kSoft) ri.x = r2.x > 0.f ? ri.x : 0.f, ri.y = r2.y > 0.f ? ri.y : 0.f;
+                    const float2 f = __fmul2_rn(ri, __fmul2_rn(ri, ri));
+                    ax = __ffma2_rn(dx, f, ax);
+                    ay = __ffma2_rn(dy, f, ay);
+                    az = __ffma2_rn(dz, f, az);
+                }
+                bx = ax.x + ax.y, by = ay.x + ay.y, bz = az.x + az.y;
             } else if (tact) {
                 for (unsigned k = grp; k < now; k += g) pair_f32<kNewton, kSoft>(src[w][k], tx, ty, tz, eps2, bx, by, bz);
             }

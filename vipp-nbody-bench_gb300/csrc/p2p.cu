@@ -111,8 +111,12 @@ __device__ __forceinline__ void pair_f32(const float4 s, float tx, float ty, flo
     bz = fmaf(dz, f, bz);
 }
 
+#ifndef GB_P2P_MIN_BLOCKS
+#define GB_P2P_MIN_BLOCKS 1
+#endif
+
 template <bool kNewton, bool kSoft>
-__global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_f32(const int4 *__restrict__ chunks, const unsigned *counts,
+__global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(const int4 *__restrict__ chunks, const unsigned *counts,
                                                             unsigned *queue, const int *__restrict__ leaves,
                                                             const double *__restrict__ c_ctr,
                                                             const TreeInfo *__restrict__ info, const unsigned *__restrict__ rng_off,

@@ -112,7 +112,7 @@ __device__ __forceinline__ void pair_f32(const float4 s, float tx, float ty, flo
 }
 
 #ifndef GB_P2P_MIN_BLOCKS
-#define GB_P2P_MIN_BLOCKS 1
+#define GB_P2P_MIN_BLOCKS 8  // 8 resident blocks per SM (62 registers, no spills): measured 7% faster than 6
 #endif
 
 template <bool kNewton, bool kSoft>

@@ -205,29 +205,7 @@ __global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(c
                 }
                 bx = ax.x + ax.y, by = ay.x + ay.y, bz = az.x + az.y;
             } else if (tact) {
-                // lane groups / partial batches: sources k and k + g of this lane's
-                // group paired the same way, an odd last one alone
-                float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
-                unsigned k = grp;
-                for (; k + g < now; k += 2 * g) {
-                    const float4 s0 = src[w][k], s1 = src[w][k + g];
-                    const float2 dx = __fadd2_rn(make_float2(s0.x, s1.x), ntx);
-                    const float2 dy = __fadd2_rn(make_float2(s0.y, s1.y), nty);
-                    const float2 dz = __fadd2_rn(make_float2(s0.z, s1.z), ntz);
-                    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-                    float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
-                    if (kNewton) {
-                        ri.x = ri.x * fmaf(-0.5f * r2.x * ri.x, ri.x, 1.5f);
-                        ri.y = ri.y * fmaf(-0.5f * r2.y * ri.y, ri.y, 1.5f);
-                    }
-                    if (!kSoft) ri.x = r2.x > 0.f ? ri.x : 0.f, ri.y = r2.y > 0.f ? ri.y : 0.f;
-                    const float2 f = __fmul2_rn(ri, __fmul2_rn(ri, ri));
-                    ax = __ffma2_rn(dx, f, ax);
-                    ay = __ffma2_rn(dy, f, ay);
-                    az = __ffma2_rn(dz, f, az);
-                }
-                bx = ax.x + ax.y, by = ay.x + ay.y, bz = az.x + az.y;
-                if (k < now) pair_f32<kNewton, kSoft>(src[w][k], tx, ty, tz, eps2, bx, by, bz);
+                for (unsigned k = grp; k < now; k += g) pair_f32<kNewton, kSoft>(src[w][k], tx, ty, tz, eps2, bx, by, bz);
             }
             __syncwarp();
             float y = bx - kx, tt = sx + y;

@@ -338,6 +338,8 @@ void evaluate(gb_ctx *ctx) {
 int grow(gb_ctx *ctx, const unsigned *counts) {
     gb::Workspace &ws = ctx->ws;
     const unsigned need_s = counts[6], need_r = counts[4], need_items = counts[7], need_part = counts[8];
+    if (counts[9] > static_cast<unsigned>(ws.sort_levels))
+        ws.sort_levels = std::min(gb::kMaxLevel, static_cast<int>(counts[9]));
     const unsigned s = need_s > ws.s_cap ? need_s + need_s / 2 + 64 : ws.s_cap;
     const unsigned r = need_r > ws.r_cap ? need_r + need_r / 2 + 1024 : ws.r_cap;
     const int rc = ensure_cells(ctx, s, r);

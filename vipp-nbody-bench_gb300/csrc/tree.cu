@@ -167,15 +167,22 @@ __global__ void k_keys(const double *__restrict__ x, unsigned n, const TreeInfo 
     perm[i] = i;
 }
 
-__global__ void k_split_count(const uint64_t *__restrict__ keys, unsigned n, int T, unsigned *__restrict__ cnt,
-                              TreeInfo *info) {
+// Keys are sorted on their top `sorted` levels only (particles inside a leaf
+// are put in index order afterwards, so deeper key bits never matter while no
+// cell of level `sorted` has to split). A run whose level-`sorted` prefix
+// still holds more than T particles asks for a deeper sort through counts[9].
+__global__ void k_split_count(const uint64_t *__restrict__ keys, unsigned n, int T, int sorted, unsigned *__restrict__ cnt,
+                              unsigned *counts, TreeInfo *info) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int Ls = i == 0 ? 0 : first_diff_level(keys[i - 1], keys[i]);
     int Lm = -1;
     if (static_cast<unsigned long long>(i) + T < n) {
         Lm = first_diff_level(keys[i], keys[i + T]) - 1;
-        if (Lm >= kMaxLevel) {  // a deepest-level cell would still split
+        if (Lm >= sorted && sorted < kMaxLevel) {
+            atomicMax(&counts[9], static_cast<unsigned>(min(sorted + 6, kMaxLevel)));
+            Lm = sorted - 1;
+        } else if (Lm >= kMaxLevel) {  // a deepest-level cell would still split
             atomicOr(&info->err, kDevDepth);
             Lm = kMaxLevel - 1;
         }
@@ -183,9 +190,11 @@ __global__ void k_split_count(const uint64_t *__restrict__ keys, unsigned n, int
     cnt[i] = Lm >= Ls ? static_cast<unsigned>(Lm - Ls + 1) : 0u;
 }
 
+// Overflow of the split buffer or a too shallow key sort: the attempt builds
+// a root-only tree (nothing addresses past a buffer) and the host repeats it.
 __global__ void k_check_split_total(unsigned *counts, unsigned s_cap, TreeInfo *info) {
     counts[6] = counts[1];  // requested size, kept for the host when it overflows
-    if (counts[1] > s_cap) {
+    if (counts[1] > s_cap || counts[9] != 0) {
         atomicOr(&info->err, kDevCapacity);
         counts[1] = 0;
     }
@@ -634,12 +643,12 @@ void build_tree(Workspace &ws) {
     k_bbox_final<<<1, kTB, 0, st>>>(part, nb, ws.info);
     k_keys<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.keys0, ws.perm0);
     ws.launches += 3;
-    const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, 0, 3 * kMaxLevel, ws.sort, st,
-                                   &ws.launches);
+    const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, 3 * (kMaxLevel - ws.sort_levels),
+                                   3 * kMaxLevel, ws.sort, st, &ws.launches);
     ws.keys = res ? ws.keys1 : ws.keys0;
     ws.perm = res ? ws.perm1 : ws.perm0;
     // split cells of every level
-    k_split_count<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.cnt, ws.info);
+    k_split_count<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.sort_levels, ws.cnt, ws.d_counts, ws.info);
     scan_exclusive_u32(ws.cnt, ws.off, n, nullptr, ws.d_counts + 1, ws.scan, st, &ws.launches);
     k_check_split_total<<<1, 1, 0, st>>>(ws.d_counts, ws.s_cap, ws.info);
     k_split_emit<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.off, ws.d_counts, ws.s_cap, ws.ent0);

@@ -39,6 +39,7 @@ struct Workspace {
     cudaStream_t st2 = nullptr;         // near field, concurrent with the far field on st
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool serial = false;                // near field on st after the far field
+    int sort_levels = 10;               // key levels the radix sort orders (grown on demand, up to 21)
     int64_t launches = 0;
     int num_sms = 152;
 
@@ -111,7 +112,8 @@ struct Workspace {
     // device-side info and device-resident counters
     TreeInfo *info = nullptr;
     unsigned *d_counts = nullptr;  // [kNumCounts]: 0 n, 1 S, 2 C, 3 leaves, 4 ranges, 5 items,
-                                   // 6 S requested, 7 items requested, 8 partial slots
+                                   // 6 S requested, 7 items requested, 8 partial slots,
+                                   // 9 key levels a deeper sort needs (0: enough)
     TreeInfo *h_info = nullptr;    // pinned mirror
 
     SortTemp sort;

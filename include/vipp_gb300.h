@@ -77,9 +77,13 @@ enum gb_flags {
     GB_FLAG_M2L_CUDA_CORES = 2, /* mixed M2L on CUDA cores in FP32 instead of the
                                    default tensor-core M2L (tcgen05, TF32 with a
                                    three-term hi/lo split) */
-    GB_FLAG_SERIAL = 4          /* run the near field (P2P) after the far field on
+    GB_FLAG_SERIAL = 4,         /* run the near field (P2P) after the far field on
                                    one stream instead of concurrently on a second
                                    stream of the context (same results) */
+    GB_FLAG_NO_GRAPH = 8        /* launch every kernel of an RK4 step instead of
+                                   replaying the step's captured CUDA graph (same
+                                   results; graphs are also off while kernel
+                                   timing is enabled) */
 };
 
 typedef struct gb_ctx gb_ctx;

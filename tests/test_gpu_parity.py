@@ -232,3 +232,27 @@ def test_edge_cases_and_errors():
         with pytest.raises(vipp_gb300.GB300Error) as ei:
             s.solve(1e-3)
         assert ei.value.code == vipp_gb300.GB_ERR_STATE
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_replayed_steps_equal_direct_launches(plummer16k, precision):
+    """RK4 steps replayed from the captured CUDA graph give exactly the
+    results of launching every kernel (GB_FLAG_NO_GRAPH), across a change of
+    dt (re-capture) and a new upload of a different size."""
+    import vipp_gb300
+    x, v = plummer16k
+    out = []
+    for flags in (0, vipp_gb300.FLAG_NO_GRAPH):
+        with vipp_gb300.Solver(p=4, s=32, eps=0.01, m=1.0 / len(x), precision=precision, flags=flags) as s:
+            s.preprocess(x, v)
+            for dt in (1e-3, 1e-3, 2e-3, 2e-3):
+                s.solve(dt)
+            a = s.postprocess()
+            s.preprocess(x[:5000], v[:5000])
+            s.solve(1e-3)
+            s.solve(1e-3)
+            out.append((a, s.postprocess(), s.launch_count()))
+    (a0, b0, l0), (a1, b1, l1) = out
+    assert np.array_equal(a0[0], a1[0]) and np.array_equal(a0[1], a1[1])
+    assert np.array_equal(b0[0], b1[0]) and np.array_equal(b0[1], b1[1])
+    assert l0 == l1

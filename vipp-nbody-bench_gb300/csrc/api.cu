@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../../include/vipp_gb300.h"
@@ -33,6 +34,14 @@ struct gb_ctx {
     bool have_state = false;
     long long retries = 0;  // evaluations repeated after a capacity overflow
     size_t phi_cap = 0;     // particles ws.phi / ws.phis are sized for
+    // CUDA graph of one RK4 step, valid for (n, dt, buffer epoch)
+    uint64_t epoch = 0;     // bumped whenever buffers or the configuration change
+    cudaGraphExec_t step_exec = nullptr;
+    unsigned step_n = 0;
+    double step_dt = 0;
+    uint64_t step_epoch = 0;
+    int64_t step_launches = 0;
+    bool graph_failed = false;
     std::vector<gb::PendingTimer> pending;
     std::vector<cudaEvent_t> free_events;
     long long *d_targets = nullptr;
@@ -337,6 +346,7 @@ void evaluate(gb_ctx *ctx) {
 // the sizes the evaluation asked for).
 int grow(gb_ctx *ctx, const unsigned *counts) {
     gb::Workspace &ws = ctx->ws;
+    ++ctx->epoch;
     const unsigned need_s = counts[6], need_r = counts[4], need_items = counts[7], need_part = counts[8];
     if (counts[9] > static_cast<unsigned>(ws.sort_levels))
         ws.sort_levels = std::min(gb::kMaxLevel, static_cast<int>(counts[9]));
@@ -453,6 +463,7 @@ void gb_destroy(gb_ctx *ctx) {
     gb::sort_temp_free(ws.sort);
     gb::scan_temp_free(ws.scan);
     if (ws.h_info) cudaFreeHost(ws.h_info);
+    if (ctx->step_exec) cudaGraphExecDestroy(ctx->step_exec);
     if (ws.ev_fork) cudaEventDestroy(ws.ev_fork);
     if (ws.ev_join) cudaEventDestroy(ws.ev_join);
     if (ws.st2) cudaStreamDestroy(ws.st2);
@@ -465,6 +476,7 @@ const char *gb_last_error(const gb_ctx *ctx) { return ctx ? ctx->err.c_str() : g
 
 int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
     if (!ctx) return GB_ERR_INVALID;
+    ++ctx->epoch;  // buffers, sizes or configuration may change: the step graph is rebuilt
     std::string msg;
     int rc = validate(cfg, msg);
     if (rc) return ctx->err = msg, rc;
@@ -492,6 +504,7 @@ int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
 
 int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
     if (!ctx) return GB_ERR_INVALID;
+    ++ctx->epoch;  // buffers, sizes or configuration may change: the step graph is rebuilt
     if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
     if (n && (!x_aos || !v_aos)) return ctx->err = "null input", GB_ERR_INVALID;
     GB_TRY(cudaSetDevice(ctx->cfg.device));
@@ -515,6 +528,7 @@ int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
 
 int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max) {
     if (!ctx) return GB_ERR_INVALID;
+    ++ctx->epoch;  // buffers, sizes or configuration may change: the step graph is rebuilt
     if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
     if (!(r_max >= 0) || !std::isfinite(r_max)) return ctx->err = "r_max must be finite and >= 0", GB_ERR_INVALID;
     if (r_max == 0 && !(ctx->cfg.eps > 0 && ctx->cfg.eps < 1))
@@ -560,6 +574,36 @@ int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos) {
     return GB_OK;
 }
 
+// Captures one RK4 step (restore, 4 x evaluate + stage) into a CUDA graph.
+// Kernel sizes come from the device, so the graph holds while n, dt and the
+// buffers stay the same. On any capture failure the context stops using
+// graphs and launches the kernels directly.
+void capture_step(gb_ctx *ctx, double dt, const std::function<void()> &body) {
+    gb::Workspace &ws = ctx->ws;
+    if (ctx->step_exec) cudaGraphExecDestroy(ctx->step_exec);
+    ctx->step_exec = nullptr;
+    const int64_t l0 = ws.launches;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(ws.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        ctx->graph_failed = true;
+        return;
+    }
+    body();
+    cudaError_t e = cudaStreamEndCapture(ws.st, &g);
+    ctx->step_launches = ws.launches - l0;
+    ws.launches = l0;  // counted when the graph runs
+    if (e == cudaSuccess && g) e = cudaGraphInstantiate(&ctx->step_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess || !ctx->step_exec) {
+        cudaGetLastError();
+        ctx->step_exec = nullptr;
+        ctx->graph_failed = true;
+        return;
+    }
+    ctx->step_n = ws.n, ctx->step_dt = dt, ctx->step_epoch = ctx->epoch;
+}
+
 int gb_rk4_step(gb_ctx *ctx, double dt) {
     if (!ctx) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
@@ -568,12 +612,25 @@ int gb_rk4_step(gb_ctx *ctx, double dt) {
     gb::Workspace &ws = ctx->ws;
     if (ws.n == 0) return GB_OK;
     gb::rk4_begin(ws);
-    const int rc = run_with_capacity(ctx, [&]() {
+    const std::function<void()> body = [&]() {
         gb::rk4_restore(ws);
         for (int stage = 0; stage < 4; ++stage) {
             evaluate(ctx);
             gb::rk4_stage(ws, stage, dt);
         }
+    };
+    const bool graphs = !ws.timing && (ctx->cfg.flags & GB_FLAG_NO_GRAPH) == 0 && !ctx->graph_failed;
+    const int rc = run_with_capacity(ctx, [&]() {
+        if (graphs) {
+            if (!ctx->step_exec || ctx->step_n != ws.n || ctx->step_dt != dt || ctx->step_epoch != ctx->epoch)
+                capture_step(ctx, dt, body);
+            if (ctx->step_exec && cudaGraphLaunch(ctx->step_exec, ws.st) == cudaSuccess) {
+                ws.launches += ctx->step_launches;
+                return;
+            }
+            cudaGetLastError();
+        }
+        body();
     });
     if (rc != GB_OK) {
         // leave the state as it was before the step

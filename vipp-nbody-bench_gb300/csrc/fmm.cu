@@ -10,6 +10,13 @@
 
 #include "workspace.cuh"
 
+// Far-field kernels that run beside the P2P blocks of the concurrent near
+// field: GB_FAR_MIN_BLOCKS > 1 caps their registers (65536 / (threads x
+// min blocks) per thread) so that they fit on an SM next to P2P.
+#ifndef GB_FAR_MIN_BLOCKS
+#define GB_FAR_MIN_BLOCKS 1
+#endif
+
 namespace gb {
 
 __constant__ HTab<double> c_htd;
@@ -127,7 +134,7 @@ __global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, double *__
 // --------------------------------------------------------------------- P2M
 // One warp per leaf at level >= 2: M~_n^m = sum_i m conj(R_n^m((x_i - c)/s)).
 template <int P, typename T>
-__global__ void __launch_bounds__(128) k_p2m(const int *__restrict__ leaves, const unsigned *counts,
+__global__ void __launch_bounds__(128, GB_FAR_MIN_BLOCKS) k_p2m(const int *__restrict__ leaves, const unsigned *counts,
                                              const int *__restrict__ c_begin, const int *__restrict__ c_end,
                                              const int *__restrict__ c_level, const double *__restrict__ c_ctr,
                                              const double *__restrict__ xs, unsigned n, const TreeInfo *__restrict__ info,
@@ -324,7 +331,7 @@ __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, 
 // writes the parents' multipoles. (One CTA doing the 8 octants in turn made a
 // level cost ~165 us whatever its size.)
 template <int P, typename T>
-__global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256)
+__global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256, GB_FAR_MIN_BLOCKS)
     k_m2m(int L, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell, const int *__restrict__ c_child,
           const T *__restrict__ ops, T *M) {
     namespace cg = cooperative_groups;
@@ -382,7 +389,7 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256)
 // L2L into level Lp+1 (Lp >= 2): for each octant o, tiles of 64 non-leaf cells
 // of level Lp; child o of each gets L~ += L2L_o L~_parent.
 template <int P, typename T>
-__global__ void __launch_bounds__(256) k_l2l(int Lp, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell,
+__global__ void __launch_bounds__(256, GB_FAR_MIN_BLOCKS) k_l2l(int Lp, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell,
                                              const int *__restrict__ c_child, const T *__restrict__ ops, T *Lx) {
     using C = TileCfg<P, T>;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -434,7 +441,7 @@ __global__ void __launch_bounds__(256) k_l2l(int Lp, const TreeInfo *__restrict_
 //   a_z        = s^-2 sum_j [ L~_j^0 j R_{j-1}^0 + 2 Re sum_{k>=1} L~_j^k sqrt((j-k)(j+k)) R_{j-1}^k ]
 // so every R_n^q (n <= p-1) meets L~ of degree n+1 and orders q-1, q, q+1.
 template <int P, typename T>
-__global__ void __launch_bounds__(128) k_l2p(const int *__restrict__ leaves, const unsigned *counts,
+__global__ void __launch_bounds__(128, GB_FAR_MIN_BLOCKS) k_l2p(const int *__restrict__ leaves, const unsigned *counts,
                                              const int *__restrict__ c_begin, const int *__restrict__ c_end,
                                              const int *__restrict__ c_level, const double *__restrict__ c_ctr,
                                              const double *__restrict__ xs, unsigned n, const TreeInfo *__restrict__ info,

@@ -56,6 +56,9 @@ constexpr int kDrainThreads = 128;  // warps 0-3
 #ifndef M2L_MAX_STAGES
 #define M2L_MAX_STAGES 4  // 3 leaves shared memory for concurrent P2P blocks
 #endif
+#ifndef M2L_MIN_BLOCKS
+#define M2L_MIN_BLOCKS 1  // > 1 caps registers so the kernel fits beside P2P blocks
+#endif
 #ifndef M2L_WIDE_B
 #define M2L_WIDE_B 1
 #endif
@@ -219,7 +222,7 @@ __device__ __forceinline__ int next_slot(int cls, int s) {
 }
 
 template <int P>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
     k_m2l_tc(const __grid_constant__ CUtensorMap tmap, const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
              const float *__restrict__ bimg, int rows_cap, float *__restrict__ Lx, TreeInfo *info_rw) {
     using C = TcCfg<P>;

@@ -22,6 +22,9 @@
 #include "direct.cuh"
 #include "workspace.cuh"
 
+#ifndef GB_P2P_CARVEOUT_MAX
+#define GB_P2P_CARVEOUT_MAX 0
+#endif
 #ifndef GB_P2P_BLOCKS_PER_SM
 #define GB_P2P_BLOCKS_PER_SM 8
 #endif
@@ -417,6 +420,14 @@ void near_potential(Workspace &ws, double *phiv) {
 
 void p2p_pass(Workspace &ws) {
     timer_begin(ws, kTP2P);
+#if GB_P2P_CARVEOUT_MAX
+    // keep the SMs that run P2P configured for full shared memory, so far-field
+    // kernels (M2L: 173 KB) can start beside the P2P blocks
+    cudaFuncSetAttribute(k_p2p_f32<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_p2p_f32<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_p2p_f32<true, true>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_p2p_f32<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+#endif
     cudaMemsetAsync(ws.queue, 0, sizeof(unsigned), ws.st);
     // Blocks per SM of the persistent P2P kernels. The P2P kernels run
     // concurrently with the far field, so they should leave room on each SM.

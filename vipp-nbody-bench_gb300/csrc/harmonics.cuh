@@ -47,6 +47,8 @@ struct HTab {
 // A_n^m = (-1)^n / sqrt((n-m)! (n+m)!)  (fmm.hpp:201-221), m = |m|.
 struct ATab {
     double a[kTabN][kTabN];
+    double ainv[kTabN][kTabN];  // 1 / a (0 where a is 0): operator entries multiply instead of
+                                // divide, FP64 division being costly on this GPU
 };
 
 inline void fill_tables(HTab<double> &t, ATab &at) {
@@ -67,8 +69,10 @@ inline void fill_tables(HTab<double> &t, ATab &at) {
                 for (int i = 2; i <= n - m; ++i) f1 *= i;
                 for (int i = 2; i <= n + m; ++i) f2 *= i;
                 at.a[n][m] = (n % 2 ? -1.0 : 1.0) / std::sqrt(f1 * f2);
+                at.ainv[n][m] = 1.0 / at.a[n][m];
             } else {
                 at.a[n][m] = 0.0;
+                at.ainv[n][m] = 0.0;
             }
         }
 }
@@ -146,6 +150,7 @@ GB_HD void ydir(const double *yt, int n, int m, double &re, double &im) {
 }
 
 GB_HD double aco(const ATab &at, int n, int m) { return at.a[n][m < 0 ? -m : m]; }
+GB_HD double aco_inv(const ATab &at, int n, int m) { return at.ainv[n][m < 0 ? -m : m]; }
 GB_HD double phase_even(int e) { return ((e / 2) % 2 == 0) ? 1.0 : -1.0; }  // i^e, e even
 GB_HD int iabs(int v) { return v < 0 ? -v : v; }
 
@@ -156,8 +161,8 @@ GB_HD void m2l_coef(const ATab &at, const double *yt, const double *rinv_pow, in
                     double &im) {
     double yr, yi;
     ydir(yt, j + n, m - k, yr, yi);
-    const double c = phase_even(iabs(k - m) - iabs(k) - iabs(m)) * aco(at, n, m) * aco(at, j, k) /
-                     ((n % 2 ? -1.0 : 1.0) * aco(at, j + n, m - k)) * rinv_pow[j + n + 1];
+    const double c = phase_even(iabs(k - m) - iabs(k) - iabs(m)) * aco(at, n, m) * aco(at, j, k) *
+                     ((n % 2 ? -1.0 : 1.0) * aco_inv(at, j + n, m - k)) * rinv_pow[j + n + 1];
     re = c * yr;
     im = c * yi;
 }
@@ -174,8 +179,8 @@ GB_HD bool m2m_coef(const ATab &at, const double *yt, const double *rpow, int j,
     }
     double yr, yi;
     ydir(yt, n, -m, yr, yi);
-    const double c = phase_even(iabs(k) - iabs(m) - iabs(mp)) * aco(at, n, m) * aco(at, np, mp) * rpow[n] /
-                     aco(at, j, k) * ldexp(1.0, -np);
+    const double c = phase_even(iabs(k) - iabs(m) - iabs(mp)) * aco(at, n, m) * aco(at, np, mp) * rpow[n] *
+                     aco_inv(at, j, k) * ldexp(1.0, -np);
     re = c * yr;
     im = c * yi;
     return true;
@@ -192,8 +197,8 @@ GB_HD bool l2l_coef(const ATab &at, const double *yt, const double *rpow, int j,
     }
     double yr, yi;
     ydir(yt, n - j, m - k, yr, yi);
-    const double c = phase_even(iabs(m) - iabs(m - k) - iabs(k)) * aco(at, n - j, m - k) * aco(at, j, k) * rpow[n - j] /
-                     (((n + j) % 2 ? -1.0 : 1.0) * aco(at, n, m)) * ldexp(1.0, -(j + 1));
+    const double c = phase_even(iabs(m) - iabs(m - k) - iabs(k)) * aco(at, n - j, m - k) * aco(at, j, k) * rpow[n - j] *
+                     (((n + j) % 2 ? -1.0 : 1.0) * aco_inv(at, n, m)) * ldexp(1.0, -(j + 1));
     re = c * yr;
     im = c * yi;
     return true;

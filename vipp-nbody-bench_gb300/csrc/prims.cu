@@ -132,12 +132,19 @@ __global__ void k_radix_hist(const uint64_t *__restrict__ keys, unsigned n_cap, 
     hist[threadIdx.x * ntiles_cap + blockIdx.x] = cnt[threadIdx.x];
 }
 
+constexpr size_t kScatterSmem = sizeof(uint64_t) * kSortTile + sizeof(unsigned) * kSortTile;  // 48 KB
+
 __global__ void __launch_bounds__(256) k_radix_scatter(const uint64_t *__restrict__ kin, const unsigned *__restrict__ vin,
                                                        uint64_t *__restrict__ kout, unsigned *__restrict__ vout,
                                                        unsigned n_cap, const unsigned *d_n, int bit,
                                                        const unsigned *__restrict__ hist, unsigned ntiles_cap) {
     constexpr int kRounds = kSortTile / 256;  // 16
     __shared__ unsigned wcnt[8][256];
+    __shared__ unsigned dstart[256];  // first tile-local position of each digit
+    __shared__ unsigned wsum[8];
+    extern __shared__ __align__(16) unsigned char stage_raw[];  // the tile in digit order
+    uint64_t *skey = reinterpret_cast<uint64_t *>(stage_raw);
+    unsigned *sval = reinterpret_cast<unsigned *>(skey + kSortTile);
     const unsigned n = d_n ? *d_n : n_cap;
     const unsigned base = blockIdx.x * kSortTile;
     if (base >= n) return;  // uniform
@@ -172,16 +179,40 @@ __global__ void __launch_bounds__(256) k_radix_scatter(const uint64_t *__restric
             wcnt[ww][d] = run;
             run += c;
         }
+        // exclusive scan of the tile's digit totals (thread d holds digit d)
+        unsigned incl = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned u = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        unsigned wofs = 0;
+        for (int ww = 0; ww < w; ++ww) wofs += wsum[ww];
+        dstart[d] = wofs + incl - run;
     }
     __syncthreads();
+    // tile-local sorted order in shared memory ...
 #pragma unroll
     for (int k = 0; k < kRounds; ++k) {
         const unsigned d = dig[k];
         if (d < 256u) {
-            const unsigned pos = hist[d * ntiles_cap + blockIdx.x] + wcnt[w][d] + rank[k];
-            kout[pos] = key[k];
-            if (vout) vout[pos] = val[k];
+            const unsigned lp = dstart[d] + wcnt[w][d] + rank[k];
+            skey[lp] = key[k];
+            sval[lp] = val[k];
         }
+    }
+    __syncthreads();
+    // ... then written out in that order: consecutive threads write
+    // consecutive positions of each digit's run
+    const unsigned cnt = min(n - base, static_cast<unsigned>(kSortTile));
+    for (unsigned lp = threadIdx.x; lp < cnt; lp += blockDim.x) {
+        const uint64_t kk = skey[lp];
+        const unsigned d = static_cast<unsigned>((kk >> bit) & 0xffu);
+        const unsigned pos = hist[d * ntiles_cap + blockIdx.x] + (lp - dstart[d]);
+        kout[pos] = kk;
+        if (vout) vout[pos] = sval[lp];
     }
 }
 
@@ -242,13 +273,14 @@ int radix_sort_u64(uint64_t *k0, unsigned *v0, uint64_t *k1, unsigned *v1, unsig
                    int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches) {
     const unsigned tiles = (n_cap + kSortTile - 1) / kSortTile;
     if (tiles == 0) return 0;
+    cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kScatterSmem));
     int cur = 0;
     for (int bit = bit_lo; bit < bit_hi; bit += 8) {
         uint64_t *ki = cur ? k1 : k0, *ko = cur ? k0 : k1;
         unsigned *vi = cur ? v1 : v0, *vo = cur ? v0 : v1;
         k_radix_hist<<<tiles, 256, 0, st>>>(ki, n_cap, d_n, bit, tmp.hist, tiles);
         scan_exclusive_u32(tmp.hist, tmp.hist, 256u * tiles, nullptr, nullptr, tmp.scan, st, launches);
-        k_radix_scatter<<<tiles, 256, 0, st>>>(ki, vi, ko, vo, n_cap, d_n, bit, tmp.hist, tiles);
+        k_radix_scatter<<<tiles, 256, kScatterSmem, st>>>(ki, vi, ko, vo, n_cap, d_n, bit, tmp.hist, tiles);
         if (launches) *launches += 2;
         cur ^= 1;
     }

@@ -110,6 +110,26 @@ GB_API const char *gb_last_error(const gb_ctx *ctx);
  * read by SolverRef::solve, solver_ref.hpp:21-25). */
 GB_API int gb_set_config(gb_ctx *ctx, const gb_config *cfg);
 
+/* Batches of independent systems (the batching form of the benchmark: many
+ * Plummer systems of uneven N concatenated with segment offsets). No
+ * counterpart in the reference, which runs one Problem per Solver. System k
+ * holds particles [seg_offsets[k], seg_offsets[k+1]) of the concatenated AoS
+ * arrays, particle mass m_per_system[k] (cfg->m when NULL) and the rest of
+ * cfg. A batch step advances every system by one RK4 step; all systems' steps
+ * are queued before any is waited for, so they run concurrently on the GPU.
+ * gb_batch_system gives system k's context (for gb_accel, gb_get_conserved,
+ * gb_get_stats; the batch owns it). */
+typedef struct gb_batch gb_batch;
+GB_API int gb_batch_create(const gb_config *cfg, size_t nsys, const uint64_t *seg_offsets, const double *m_per_system,
+                           gb_batch **out);
+GB_API void gb_batch_destroy(gb_batch *b);
+GB_API const char *gb_batch_last_error(const gb_batch *b);
+GB_API int gb_batch_upload(gb_batch *b, const double *x_aos, const double *v_aos);
+GB_API int gb_batch_download(gb_batch *b, double *x_aos, double *v_aos);
+GB_API int gb_batch_rk4_step(gb_batch *b, double dt);
+GB_API int gb_batch_size(const gb_batch *b, size_t *nsys, uint64_t *n_total);
+GB_API gb_ctx *gb_batch_system(gb_batch *b, size_t k);
+
 /* Initial state generated on the device: the reference's Plummer sphere
  * (Problem::initialize, problem.hpp:188-211, 245-292; G = M = a = 1) with one
  * counter-based random stream per particle. r_max = 0 keeps the reference's

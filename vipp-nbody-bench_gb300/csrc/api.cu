@@ -440,7 +440,7 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     const size_t kk = static_cast<size_t>(ws.K) * ws.K * gb::kNumOps;
     if ((e = cudaMalloc(&ws.ops_d, sizeof(double) * kk)) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.ops_f, sizeof(float) * kk)) != cudaSuccess) return fail("ops", e);
-    if ((e = cudaMalloc(&ws.bimg, sizeof(float) * gb::m2l_tc_image_floats(gb::kMaxP))) != cudaSuccess) return fail("ops", e);
+    if ((e = cudaMalloc(&ws.bimg, sizeof(float) * gb::m2l_tc_image_floats(ws.p))) != cudaSuccess) return fail("ops", e);
     *out = ctx;
     return GB_OK;
 }
@@ -490,6 +490,7 @@ int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
         const size_t kk = static_cast<size_t>(ctx->ws.K) * ctx->ws.K * gb::kNumOps;
         GB_TRY(dalloc(ctx->ws.ops_d, kk));
         GB_TRY(dalloc(ctx->ws.ops_f, kk));
+        GB_TRY(dalloc(ctx->ws.bimg, gb::m2l_tc_image_floats(ctx->ws.p)));
     }
     if (ctx->ws.T != oldT && ctx->have_state) {
         const int r = initial_capacity(ctx);
@@ -578,7 +579,7 @@ int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos) {
 // Kernel sizes come from the device, so the graph holds while n, dt and the
 // buffers stay the same. On any capture failure the context stops using
 // graphs and launches the kernels directly.
-void capture_step(gb_ctx *ctx, double dt, const std::function<void()> &body) {
+static void capture_step(gb_ctx *ctx, double dt, const std::function<void()> &body) {
     gb::Workspace &ws = ctx->ws;
     if (ctx->step_exec) cudaGraphExecDestroy(ctx->step_exec);
     ctx->step_exec = nullptr;
@@ -604,6 +605,31 @@ void capture_step(gb_ctx *ctx, double dt, const std::function<void()> &body) {
     ctx->step_n = ws.n, ctx->step_dt = dt, ctx->step_epoch = ctx->epoch;
 }
 
+// Queue one RK4 step from the saved step start (rk4_begin): the captured
+// graph when graphs are on, else every kernel. Asynchronous.
+static void step_enqueue(gb_ctx *ctx, double dt) {
+    gb::Workspace &ws = ctx->ws;
+    const std::function<void()> body = [ctx, dt]() {
+        gb::Workspace &w = ctx->ws;
+        gb::rk4_restore(w);
+        for (int stage = 0; stage < 4; ++stage) {
+            evaluate(ctx);
+            gb::rk4_stage(w, stage, dt);
+        }
+    };
+    const bool graphs = !ws.timing && (ctx->cfg.flags & GB_FLAG_NO_GRAPH) == 0 && !ctx->graph_failed;
+    if (graphs) {
+        if (!ctx->step_exec || ctx->step_n != ws.n || ctx->step_dt != dt || ctx->step_epoch != ctx->epoch)
+            capture_step(ctx, dt, body);
+        if (ctx->step_exec && cudaGraphLaunch(ctx->step_exec, ws.st) == cudaSuccess) {
+            ws.launches += ctx->step_launches;
+            return;
+        }
+        cudaGetLastError();
+    }
+    body();
+}
+
 int gb_rk4_step(gb_ctx *ctx, double dt) {
     if (!ctx) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
@@ -612,26 +638,7 @@ int gb_rk4_step(gb_ctx *ctx, double dt) {
     gb::Workspace &ws = ctx->ws;
     if (ws.n == 0) return GB_OK;
     gb::rk4_begin(ws);
-    const std::function<void()> body = [&]() {
-        gb::rk4_restore(ws);
-        for (int stage = 0; stage < 4; ++stage) {
-            evaluate(ctx);
-            gb::rk4_stage(ws, stage, dt);
-        }
-    };
-    const bool graphs = !ws.timing && (ctx->cfg.flags & GB_FLAG_NO_GRAPH) == 0 && !ctx->graph_failed;
-    const int rc = run_with_capacity(ctx, [&]() {
-        if (graphs) {
-            if (!ctx->step_exec || ctx->step_n != ws.n || ctx->step_dt != dt || ctx->step_epoch != ctx->epoch)
-                capture_step(ctx, dt, body);
-            if (ctx->step_exec && cudaGraphLaunch(ctx->step_exec, ws.st) == cudaSuccess) {
-                ws.launches += ctx->step_launches;
-                return;
-            }
-            cudaGetLastError();
-        }
-        body();
-    });
+    const int rc = run_with_capacity(ctx, [&]() { step_enqueue(ctx, dt); });
     if (rc != GB_OK) {
         // leave the state as it was before the step
         gb::rk4_restore(ws);
@@ -639,6 +646,133 @@ int gb_rk4_step(gb_ctx *ctx, double dt) {
     }
     return rc;
 }
+
+// ------------------------------------------------------------------- batches
+// Many independent systems of uneven size (the batching form of the
+// benchmark: systems concatenated with segment offsets). Every system has its
+// own context, tree, operators and step graph on its own stream; a batch step
+// queues all systems' steps before waiting for any, so the GPU runs the small,
+// launch-latency-bound systems concurrently. A system whose buffers overflow is
+// grown and stepped again on its own.
+}  // extern "C"
+
+struct gb_batch {
+    std::vector<gb_ctx *> ctx;
+    std::vector<uint64_t> off;  // nsys + 1 particle offsets
+    std::string err;
+};
+
+extern "C" {
+
+int gb_batch_create(const gb_config *cfg, size_t nsys, const uint64_t *seg_offsets, const double *m_per_system,
+                    gb_batch **out) {
+    if (!out) return GB_ERR_INVALID;
+    *out = nullptr;
+    if (!cfg || !seg_offsets || nsys == 0) {
+        g_create_error = "batch needs a config, segment offsets and at least one system";
+        return GB_ERR_INVALID;
+    }
+    for (size_t k = 0; k < nsys; ++k)
+        if (seg_offsets[k + 1] < seg_offsets[k]) {
+            g_create_error = "segment offsets must not decrease";
+            return GB_ERR_INVALID;
+        }
+    auto *b = new gb_batch;
+    b->off.assign(seg_offsets, seg_offsets + nsys + 1);
+    for (size_t k = 0; k < nsys; ++k) {
+        gb_config c = *cfg;
+        if (m_per_system) c.m = m_per_system[k];
+        gb_ctx *h = nullptr;
+        const int rc = gb_create(&c, &h);
+        if (rc != GB_OK) {
+            for (gb_ctx *x : b->ctx) gb_destroy(x);
+            delete b;
+            return rc;
+        }
+        b->ctx.push_back(h);
+    }
+    *out = b;
+    return GB_OK;
+}
+
+void gb_batch_destroy(gb_batch *b) {
+    if (!b) return;
+    for (gb_ctx *x : b->ctx) gb_destroy(x);
+    delete b;
+}
+
+const char *gb_batch_last_error(const gb_batch *b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+static int batch_fail(gb_batch *b, size_t k, int rc) {
+    b->err = "system " + std::to_string(k) + ": " + b->ctx[k]->err;
+    return rc;
+}
+
+int gb_batch_upload(gb_batch *b, const double *x_aos, const double *v_aos) {
+    if (!b || !x_aos || !v_aos) return GB_ERR_INVALID;
+    for (size_t k = 0; k < b->ctx.size(); ++k) {
+        const uint64_t o = b->off[k], n = b->off[k + 1] - o;
+        const int rc = gb_upload(b->ctx[k], x_aos + 3 * o, v_aos + 3 * o, n);
+        if (rc != GB_OK) return batch_fail(b, k, rc);
+    }
+    return GB_OK;
+}
+
+int gb_batch_download(gb_batch *b, double *x_aos, double *v_aos) {
+    if (!b || !x_aos || !v_aos) return GB_ERR_INVALID;
+    for (size_t k = 0; k < b->ctx.size(); ++k) {
+        const uint64_t o = b->off[k];
+        const int rc = gb_download(b->ctx[k], x_aos + 3 * o, v_aos + 3 * o);
+        if (rc != GB_OK) return batch_fail(b, k, rc);
+    }
+    return GB_OK;
+}
+
+int gb_batch_rk4_step(gb_batch *b, double dt) {
+    if (!b) return GB_ERR_INVALID;
+    if (!std::isfinite(dt)) return b->err = "dt must be finite", GB_ERR_INVALID;
+    const size_t ns = b->ctx.size();
+    std::vector<char> live(ns, 0);
+    for (size_t k = 0; k < ns; ++k) {  // queue every system's step
+        gb_ctx *c = b->ctx[k];
+        if (!c->have_state) return b->err = "system " + std::to_string(k) + ": no state uploaded", GB_ERR_STATE;
+        if (c->ws.n == 0) continue;
+        if (cudaSetDevice(c->cfg.device) != cudaSuccess) return b->err = "cudaSetDevice failed", GB_ERR_CUDA;
+        gb::rk4_begin(c->ws);
+        step_enqueue(c, dt);
+        live[k] = 1;
+    }
+    int first_rc = GB_OK;
+    for (size_t k = 0; k < ns; ++k) {  // then check them
+        if (!live[k]) continue;
+        gb_ctx *c = b->ctx[k];
+        cudaSetDevice(c->cfg.device);
+        unsigned counts[gb::kNumCounts];
+        int rc = check_device_errors(c, counts);
+        if (rc == GB_ERR_CAPACITY) {
+            rc = grow(c, counts);
+            if (rc == GB_OK) {
+                ++c->retries;
+                rc = run_with_capacity(c, [&]() { step_enqueue(c, dt); });
+            }
+        }
+        if (rc != GB_OK) {
+            gb::rk4_restore(c->ws);
+            cudaStreamSynchronize(c->ws.st);
+            if (first_rc == GB_OK) first_rc = batch_fail(b, k, rc);
+        }
+    }
+    return first_rc;
+}
+
+int gb_batch_size(const gb_batch *b, size_t *nsys, uint64_t *n_total) {
+    if (!b) return GB_ERR_INVALID;
+    if (nsys) *nsys = b->ctx.size();
+    if (n_total) *n_total = b->off.back();
+    return GB_OK;
+}
+
+gb_ctx *gb_batch_system(gb_batch *b, size_t k) { return b && k < b->ctx.size() ? b->ctx[k] : nullptr; }
 
 // Potential buffers (allocated on the first request): ws.phi [N] in the
 // caller's order, ws.phis [2][N] near and far parts in tree order, ws.diag.

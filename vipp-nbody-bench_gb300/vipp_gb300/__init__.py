@@ -32,7 +32,8 @@ TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
 EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_upload", "gb_download", "gb_rk4_step",
            "gb_accel", "gb_direct_accel", "gb_sync", "gb_get_stats", "gb_tree_dump", "gb_enable_timing",
            "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream", "gb_direct_accel_noalloc",
-           "gb_get_conserved", "gb_init_plummer")
+           "gb_get_conserved", "gb_init_plummer", "gb_batch_create", "gb_batch_destroy", "gb_batch_last_error",
+           "gb_batch_upload", "gb_batch_download", "gb_batch_rk4_step", "gb_batch_size", "gb_batch_system")
 
 
 class GbConfig(ctypes.Structure):
@@ -85,6 +86,16 @@ def load(path: str | None = None):
     lib.gb_launch_count.argtypes = [vp]
     lib.gb_launch_count.restype = ctypes.c_int64
     lib.gb_version.restype = ctypes.c_char_p
+    lib.gb_batch_create.argtypes = [ctypes.POINTER(GbConfig), ctypes.c_size_t, vp, vp, ctypes.POINTER(vp)]
+    lib.gb_batch_destroy.argtypes = [vp]
+    lib.gb_batch_destroy.restype = None
+    lib.gb_batch_last_error.argtypes = [vp]
+    lib.gb_batch_last_error.restype = ctypes.c_char_p
+    lib.gb_batch_upload.argtypes = [vp, vp, vp]
+    lib.gb_batch_download.argtypes = [vp, vp, vp]
+    lib.gb_batch_rk4_step.argtypes = [vp, ctypes.c_double]
+    lib.gb_batch_system.argtypes = [vp, ctypes.c_size_t]
+    lib.gb_batch_system.restype = vp
     lib.gb_stream.argtypes = [vp]
     lib.gb_stream.restype = vp
     lib.gb_direct_accel_noalloc.argtypes = [vp, ctypes.c_size_t, vp, ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
@@ -268,3 +279,67 @@ class Solver:
 
 def version() -> str:
     return load().gb_version().decode()
+
+
+class Batch:
+    """Independent systems of uneven N advanced together (gb_batch_*):
+    sizes[k] particles of system k, concatenated in x and v; masses[k] is the
+    particle mass of system k."""
+
+    def __init__(self, sizes, p=4, s=32, eps=0.01, G=1.0, masses=None, precision="mixed", device=0, flags=0):
+        self.lib = load()
+        sizes = np.asarray(sizes, dtype=np.uint64)
+        self.off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+        self.cfg = GbConfig(p, s, eps, G, 1.0, PREC[precision], device, flags)
+        m = None if masses is None else np.ascontiguousarray(masses, dtype=np.float64)
+        h = ctypes.c_void_p()
+        rc = self.lib.gb_batch_create(ctypes.byref(self.cfg), len(sizes), _ptr(self.off), _ptr(m), ctypes.byref(h))
+        if rc != GB_OK:
+            raise GB300Error(rc, self.lib.gb_batch_last_error(None).decode())
+        self.h = h
+        self.n = int(self.off[-1])
+
+    def _check(self, rc):
+        if rc != GB_OK:
+            raise GB300Error(rc, self.lib.gb_batch_last_error(self.h).decode())
+
+    def upload(self, x, v):
+        x, v = _aos(x), _aos(v)
+        assert x.shape[0] == self.n and v.shape[0] == self.n
+        self._check(self.lib.gb_batch_upload(self.h, _ptr(x), _ptr(v)))
+
+    def step(self, dt):
+        self._check(self.lib.gb_batch_rk4_step(self.h, float(dt)))
+
+    def download(self):
+        x = np.zeros((self.n, 3))
+        v = np.zeros((self.n, 3))
+        self._check(self.lib.gb_batch_download(self.h, _ptr(x), _ptr(v)))
+        return x, v
+
+    def system_accel(self, k):
+        """Accelerations of system k at its current positions."""
+        c = self.lib.gb_batch_system(self.h, k)
+        n = int(self.off[k + 1] - self.off[k])
+        a = np.zeros((n, 3))
+        rc = self.lib.gb_accel(c, _ptr(a), None)
+        if rc != GB_OK:
+            raise GB300Error(rc, self.lib.gb_last_error(c).decode())
+        return a
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -32,6 +32,9 @@ import time
 
 import numpy as np
 
+# many concurrent streams in the batching form: one hardware queue each (set before CUDA starts)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "vipp-nbody-bench_gb300")
 for _p in (ROOT, PKG):
@@ -73,6 +76,52 @@ def plummer(n: int, seed: int, rmax: float = 10.0):
     x = iso(r, rng.random(n), rng.random(n))
     v = iso(q * ve, rng.random(n), rng.random(n))
     return np.ascontiguousarray(x), np.ascontiguousarray(v)
+
+
+def batch_measure(steps=4, warmup=2, nsys=512, seed=3, sample=8):
+    """Batching form: nsys Plummer systems, N log-uniform in [1024, 65536],
+    scale radius uniform in [0.5, 2] (positions x R, velocities x R^-1/2), total
+    mass 1 each, eps = 0.01, p = 6, s = 32, mixed precision, dt = 1e-3, all
+    advanced together (gb_batch_rk4_step). Wall clock per step (a batch step
+    returns after every system's step has finished); error vs the FP64 direct
+    sum on `sample` systems."""
+    import vipp_gb300
+    rng = np.random.default_rng(seed)
+    sizes = np.rint(np.exp(rng.uniform(math.log(1024), math.log(65536), nsys))).astype(np.int64)
+    radii = rng.uniform(0.5, 2.0, nsys)
+    xs, vs = [], []
+    for k in range(nsys):
+        x, v = plummer(int(sizes[k]), 1000 + k)
+        xs.append(x * radii[k])
+        vs.append(v / math.sqrt(radii[k]))
+    X, V = np.concatenate(xs), np.concatenate(vs)
+    t0 = time.perf_counter()
+    b = vipp_gb300.Batch(sizes, p=6, s=32, eps=0.01, masses=1.0 / sizes, precision="mixed")
+    b.upload(X, V)
+    setup = time.perf_counter() - t0
+    for _ in range(warmup):
+        b.step(1e-3)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b.step(1e-3)
+    dt_wall = time.perf_counter() - t0
+    errs = []
+    xb, _ = b.download()
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for k in np.linspace(0, nsys - 1, sample).astype(int):
+        a = b.system_accel(int(k))
+        with vipp_gb300.Solver(p=6, s=32, eps=0.01, m=1.0 / sizes[k], precision="fp64") as sd:
+            sd.preprocess(xb[off[k]:off[k + 1]], np.zeros((sizes[k], 3)))
+            ad = sd.direct_accel()
+        e = np.linalg.norm(a - ad, axis=1) / np.linalg.norm(ad, axis=1)
+        errs.append(float(math.sqrt(np.mean(e * e))))
+    b.close()
+    n = int(sizes.sum())
+    return {"workload": f"{nsys} Plummer systems, N log-uniform in [1024, 65536] (seed {seed}), R in [0.5, 2], p=6 s=32 "
+                        "eps=0.01 mixed, dt=1e-3", "value": n * steps / dt_wall, "unit": UNIT, "n_total": n,
+            "systems": nsys, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * dt_wall / steps,
+            "setup_s": setup, "rms_rel_err_vs_fp64_direct_per_system": errs,
+            "timing": "host wall clock per gb_batch_rk4_step (it returns after all systems' steps)"}
 
 
 class ClockSampler:
@@ -226,6 +275,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--flags", type=int, default=0, help="gb_config flags (vipp_gb300.FLAG_*)")
     ap.add_argument("--no-energy", action="store_true", help="skip the total-energy drift (two extra evaluations)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batching form (512 independent systems)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
@@ -394,6 +444,10 @@ def main():
         roof.setdefault("peak_source", f"{src}: FP32 = 2 x 128 lanes x {nsm} SMs x sm_max_mhz {sm_mhz:.0f}"
                         if roof["bound"] == "fp32" else f"{src} hbm_gbs")
 
+    batched = None
+    if rank == 0 and not args.no_batch:
+        batched = batch_measure()
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline_sample(x, args.s, args.p, args.eps)
@@ -409,7 +463,7 @@ def main():
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
             "config": cfg, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
-            "roofline_kernels": per, "plain_fp64": plain, "cpu_baseline": cpu}
+            "roofline_kernels": per, "plain_fp64": plain, "batched": batched, "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

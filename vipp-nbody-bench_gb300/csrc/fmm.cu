@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(128) k_l2p_phi(const int *__restrict__ leaves,
 
 template <int P, typename T>
 void launch_l2p_phi(Workspace &ws, double *farphi) {
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));  // a warp per leaf
     k_l2p_phi<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.n,
                                            ws.info, static_cast<const T *>(ws.Lexp), farphi);
     ws.launches += 1;
@@ -561,14 +561,14 @@ void launch_l2p_phi(Workspace &ws, double *farphi) {
 
 template <int P, typename T>
 void launch_p2m(Workspace &ws) {
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));
     k_p2m<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.n,
                                        ws.info, ws.m, static_cast<T *>(ws.Mexp));
 }
 
 template <int P, typename T>
 void launch_l2p(Workspace &ws) {
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));
     k_l2p<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.n,
                                        ws.info, static_cast<const T *>(ws.Lexp), static_cast<T *>(ws.farf));
 }
@@ -582,7 +582,7 @@ template <int P, typename T>
 void launch_m2l(Workspace &ws) {
     const size_t smem = TileCfg<P, T>::smem;
     cudaFuncSetAttribute(k_m2l<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 2;
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 2, 8 * ceil_div(ceil_div(ws.c_cap, 8), kTile));
     k_m2l<P, T><<<gs, 256, smem, ws.st>>>(ws.info, ws.m2l_src, ops_of<P, T>(ws), static_cast<const T *>(ws.Mexp),
                                           static_cast<T *>(ws.Lexp));
     ws.launches += 1;
@@ -592,7 +592,7 @@ template <int P, typename T>
 void launch_m2m_levels(Workspace &ws) {
     const size_t smem = TileCfg<P, T>::smem;
     cudaFuncSetAttribute(k_m2m<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) / 8 * 16;  // clusters of 8 CTAs
+    const unsigned gs = 8 * capped_grid(static_cast<unsigned>(ws.num_sms) / 8 * 2, ceil_div(ws.s_cap, kTile));  // clusters of 8 CTAs
     for (int L = kMaxLevel - 1; L >= 2; --L) {
         k_m2m<P, T><<<gs, 256, smem, ws.st>>>(L, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws), static_cast<T *>(ws.Mexp));
         ws.launches += 1;
@@ -603,7 +603,7 @@ template <int P, typename T>
 void launch_l2l_levels(Workspace &ws) {
     const size_t smem = TileCfg<P, T>::smem;
     cudaFuncSetAttribute(k_l2l<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 2;
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 2, 8 * ceil_div(ws.s_cap, kTile));
     for (int Lp = 2; Lp <= kMaxLevel - 1; ++Lp) {
         k_l2l<P, T><<<gs, 256, smem, ws.st>>>(Lp, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws), static_cast<T *>(ws.Lexp));
         ws.launches += 1;

@@ -492,7 +492,8 @@ void launch(Workspace &ws) {
     k_split_m<P><<<4 * ws.num_sms, 256, 0, ws.st>>>(ws.info, static_cast<const float *>(ws.Mexp), ws.ms_tc,
                                                    static_cast<int>(ws.ms_rows));
     cudaFuncSetAttribute(k_m2l_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(C::SMEM));
-    k_m2l_tc<P><<<ws.num_sms, kThreads, C::SMEM, ws.st>>>(ws.tmap_ms, ws.info, ws.m2l_src, ws.bimg,
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms), 8 * ceil_div(ceil_div(ws.c_cap, 8), kRows));  // tiles
+    k_m2l_tc<P><<<gs, kThreads, C::SMEM, ws.st>>>(ws.tmap_ms, ws.info, ws.m2l_src, ws.bimg,
                                                          static_cast<int>(ws.ms_rows), static_cast<float *>(ws.Lexp), ws.info);
     ws.launches += 3;
 }

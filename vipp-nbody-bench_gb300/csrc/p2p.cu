@@ -431,7 +431,7 @@ void p2p_pass(Workspace &ws) {
     cudaMemsetAsync(ws.queue, 0, sizeof(unsigned), ws.st);
     // Blocks per SM of the persistent P2P kernels. The P2P kernels run
     // concurrently with the far field, so they should leave room on each SM.
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * GB_P2P_BLOCKS_PER_SM;
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * GB_P2P_BLOCKS_PER_SM, ceil_div(ws.n, 128));
     const bool soft = ws.eps > 0;
     if (ws.mixed) {
         const float eps2 = static_cast<float>(ws.eps * ws.eps);

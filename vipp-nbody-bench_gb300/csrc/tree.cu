@@ -661,7 +661,7 @@ void build_tree(Workspace &ws) {
     k_level_table<<<1, 32, 0, st>>>(ws.ent, ws.d_counts, ws.info, n);
     k_root<<<1, 32, 0, st>>>(n, ws.T, ws.info, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path,
                              ws.c_coord, ws.c_box, ws.c_ctr, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt);
-    const unsigned gs = static_cast<unsigned>(ws.num_sms) * 4;
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 4, ceil_div(ws.c_cap, 32));
     k_cells<<<gs, 128, 0, st>>>(ws.ent, ws.d_counts, ws.keys, n, ws.T, ws.info, ws.split_cell, ws.c_begin, ws.c_end,
                                 ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr);
     k_leaf_flags<<<gs, kTB, 0, st>>>(ws.c_child, ws.d_counts, ws.flag);

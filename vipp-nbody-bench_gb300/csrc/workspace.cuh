@@ -127,6 +127,15 @@ struct Workspace {
 };
 
 constexpr int kNumCounts = 16;
+
+// Grid of a grid-stride kernel: the full-GPU size, capped by an upper bound of
+// the work (from the buffer capacities) so that small systems launch small
+// grids and several systems' kernels can share the GPU.
+inline unsigned capped_grid(unsigned full, size_t work_bound) {
+    const size_t b = work_bound < 1 ? 1 : work_bound;
+    return b < full ? static_cast<unsigned>(b) : full;
+}
+inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
 constexpr int kOpM2M = 343;  // op index of M2M octant 0
 constexpr int kOpL2L = 351;  // op index of L2L octant 0
 constexpr int kNumOps = 359;

@@ -98,6 +98,8 @@ typedef struct gb_stats {
     int64_t p2p_pairs;    /* near-field (target, source) particle pairs */
     int64_t p2p_ranges;   /* source ranges over all leaves after merging */
     int64_t retries;      /* evaluations of this context repeated after growing its buffers */
+    int64_t graph_steps;  /* RK4 steps run by replaying the captured step graph */
+    int64_t direct_steps; /* RK4 steps run by launching every kernel */
 } gb_stats;
 
 /* Create a context on cfg->device. Validates cfg (p in 1..10, s >= 1). */

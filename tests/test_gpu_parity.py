@@ -251,8 +251,10 @@ def test_graph_replayed_steps_equal_direct_launches(plummer16k, precision):
             s.preprocess(x[:5000], v[:5000])
             s.solve(1e-3)
             s.solve(1e-3)
-            out.append((a, s.postprocess(), s.launch_count()))
-    (a0, b0, l0), (a1, b1, l1) = out
+            out.append((a, s.postprocess(), s.launch_count(), s.stats()))
+    (a0, b0, l0, st0), (a1, b1, l1, st1) = out
+    assert st0["graph_steps"] == 6 and st0["direct_steps"] == 0  # the graph path really ran
+    assert st1["graph_steps"] == 0 and st1["direct_steps"] == 6
     assert np.array_equal(a0[0], a1[0]) and np.array_equal(a0[1], a1[1])
     assert np.array_equal(b0[0], b1[0]) and np.array_equal(b0[1], b1[1])
     assert l0 == l1

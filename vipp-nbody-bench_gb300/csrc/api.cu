@@ -42,6 +42,7 @@ struct gb_ctx {
     uint64_t step_epoch = 0;
     int64_t step_launches = 0;
     bool graph_failed = false;
+    long long graph_steps = 0, direct_steps = 0;
     std::vector<gb::PendingTimer> pending;
     std::vector<cudaEvent_t> free_events;
     long long *d_targets = nullptr;
@@ -623,11 +624,13 @@ static void step_enqueue(gb_ctx *ctx, double dt) {
             capture_step(ctx, dt, body);
         if (ctx->step_exec && cudaGraphLaunch(ctx->step_exec, ws.st) == cudaSuccess) {
             ws.launches += ctx->step_launches;
+            ++ctx->graph_steps;
             return;
         }
         cudaGetLastError();
     }
     body();
+    ++ctx->direct_steps;
 }
 
 int gb_rk4_step(gb_ctx *ctx, double dt) {
@@ -888,6 +891,8 @@ int gb_get_stats(gb_ctx *ctx, gb_stats *out) {
     out->p2p_pairs = h.p2p_pairs;
     out->p2p_ranges = h.p2p_ranges;
     out->retries = ctx->retries;
+    out->graph_steps = ctx->graph_steps;
+    out->direct_steps = ctx->direct_steps;
     return GB_OK;
 }
 

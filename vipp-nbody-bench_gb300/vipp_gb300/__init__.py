@@ -47,7 +47,8 @@ class GbConserved(ctypes.Structure):
 
 
 class GbStats(ctypes.Structure):
-    _fields_ = [(k, ctypes.c_int64) for k in ("n", "ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges", "retries")]
+    _fields_ = [(k, ctypes.c_int64) for k in ("n", "ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges", "retries",
+                                                        "graph_steps", "direct_steps")]
 
 
 _LIB = None
@@ -316,6 +317,14 @@ class Batch:
         v = np.zeros((self.n, 3))
         self._check(self.lib.gb_batch_download(self.h, _ptr(x), _ptr(v)))
         return x, v
+
+    def system_stats(self, k) -> dict:
+        c = self.lib.gb_batch_system(self.h, k)
+        st = GbStats()
+        rc = self.lib.gb_get_stats(c, ctypes.byref(st))
+        if rc != GB_OK:
+            raise GB300Error(rc, self.lib.gb_last_error(c).decode())
+        return {f: int(getattr(st, f)) for f, _ in GbStats._fields_}
 
     def system_accel(self, k):
         """Accelerations of system k at its current positions."""

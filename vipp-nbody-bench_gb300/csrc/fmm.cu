@@ -593,7 +593,9 @@ void launch_m2m_levels(Workspace &ws) {
     const size_t smem = TileCfg<P, T>::smem;
     cudaFuncSetAttribute(k_m2m<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     const unsigned gs = 8 * capped_grid(static_cast<unsigned>(ws.num_sms) / 8 * 2, ceil_div(ws.s_cap, kTile));  // clusters of 8 CTAs
-    for (int L = kMaxLevel - 1; L >= 2; --L) {
+    // no cell is deeper than the key levels the sort ordered (tree.cu), so
+    // parents lie at levels < ws.sort_levels
+    for (int L = ws.sort_levels - 1; L >= 2; --L) {
         k_m2m<P, T><<<gs, 256, smem, ws.st>>>(L, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws), static_cast<T *>(ws.Mexp));
         ws.launches += 1;
     }
@@ -604,7 +606,7 @@ void launch_l2l_levels(Workspace &ws) {
     const size_t smem = TileCfg<P, T>::smem;
     cudaFuncSetAttribute(k_l2l<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 2, 8 * ceil_div(ws.s_cap, kTile));
-    for (int Lp = 2; Lp <= kMaxLevel - 1; ++Lp) {
+    for (int Lp = 2; Lp <= ws.sort_levels - 1; ++Lp) {
         k_l2l<P, T><<<gs, 256, smem, ws.st>>>(Lp, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws), static_cast<T *>(ws.Lexp));
         ws.launches += 1;
     }

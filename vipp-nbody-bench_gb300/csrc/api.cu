@@ -6,6 +6,7 @@
 #include <cstring>
 #include <string>
 #include <functional>
+#include <thread>
 #include <vector>
 
 #include "../../include/vipp_gb300.h"
@@ -50,6 +51,10 @@ struct gb_ctx {
     double *d_direct = nullptr;
     size_t direct_cap = 0;
 };
+
+#ifndef GB_BATCH_THREADS
+#define GB_BATCH_THREADS 8
+#endif
 
 namespace {
 
@@ -736,14 +741,28 @@ int gb_batch_rk4_step(gb_batch *b, double dt) {
     if (!std::isfinite(dt)) return b->err = "dt must be finite", GB_ERR_INVALID;
     const size_t ns = b->ctx.size();
     std::vector<char> live(ns, 0);
-    for (size_t k = 0; k < ns; ++k) {  // queue every system's step
-        gb_ctx *c = b->ctx[k];
-        if (!c->have_state) return b->err = "system " + std::to_string(k) + ": no state uploaded", GB_ERR_STATE;
-        if (c->ws.n == 0) continue;
-        if (cudaSetDevice(c->cfg.device) != cudaSuccess) return b->err = "cudaSetDevice failed", GB_ERR_CUDA;
-        gb::rk4_begin(c->ws);
-        step_enqueue(c, dt);
-        live[k] = 1;
+    for (size_t k = 0; k < ns; ++k) {
+        if (!b->ctx[k]->have_state) return b->err = "system " + std::to_string(k) + ": no state uploaded", GB_ERR_STATE;
+        live[k] = b->ctx[k]->ws.n > 0;
+    }
+    // queue every system's step; the host cost of a graph launch grows with its
+    // node count, so several host threads queue disjoint sets of systems
+    auto enqueue = [&](size_t k0, size_t k1) {
+        for (size_t k = k0; k < k1; ++k) {
+            if (!live[k]) continue;
+            gb_ctx *c = b->ctx[k];
+            cudaSetDevice(c->cfg.device);
+            gb::rk4_begin(c->ws);
+            step_enqueue(c, dt);
+        }
+    };
+    const size_t nt = std::min<size_t>(GB_BATCH_THREADS, ns);
+    if (nt <= 1) {
+        enqueue(0, ns);
+    } else {
+        std::vector<std::thread> th;
+        for (size_t t = 0; t < nt; ++t) th.emplace_back(enqueue, ns * t / nt, ns * (t + 1) / nt);
+        for (auto &x : th) x.join();
     }
     int first_rc = GB_OK;
     for (size_t k = 0; k < ns; ++k) {  // then check them

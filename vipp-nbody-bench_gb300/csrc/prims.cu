@@ -47,6 +47,34 @@ __device__ unsigned block_exclusive_scan(unsigned v, unsigned *warp_buf /*[32]*/
     return before + x - v;
 }
 
+// Whole scan in one block (small inputs): chunks of 4 elements per thread,
+// carried from chunk to chunk; in == out is allowed.
+constexpr unsigned kSmallScanMax = 1u << 16;
+__global__ void __launch_bounds__(1024) k_scan_small(const unsigned *in, unsigned *out, unsigned n_cap, const unsigned *d_n,
+                                                     unsigned *d_total) {
+    __shared__ unsigned wb[32];
+    const unsigned n = d_n ? *d_n : n_cap;
+    unsigned carry = 0;
+    for (unsigned base = 0; base < n; base += 4 * blockDim.x) {
+        const unsigned i0 = base + 4 * threadIdx.x;
+        unsigned v[4], s = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            v[j] = i0 + j < n ? in[i0 + j] : 0u;
+            s += v[j];
+        }
+        unsigned tot;
+        unsigned ex = carry + block_exclusive_scan(s, wb, &tot);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (i0 + j < n) out[i0 + j] = ex;
+            ex += v[j];
+        }
+        carry += tot;
+    }
+    if (d_total && threadIdx.x == 0) *d_total = carry;
+}
+
 __global__ void k_scan_reduce(const unsigned *__restrict__ in, unsigned n_cap, const unsigned *d_n,
                               unsigned *__restrict__ tile_sums) {
     __shared__ unsigned wb[32];
@@ -261,6 +289,11 @@ void scan_exclusive_u32(const unsigned *in, unsigned *out, unsigned n_cap, const
     const unsigned tiles = (n_cap + kScanTile - 1) / kScanTile;
     if (tiles == 0) {
         if (d_total) cudaMemsetAsync(d_total, 0, sizeof(unsigned), st);
+        return;
+    }
+    if (n_cap <= kSmallScanMax) {  // one launch instead of three
+        k_scan_small<<<1, 1024, 0, st>>>(in, out, n_cap, d_n, d_total);
+        if (launches) *launches += 1;
         return;
     }
     k_scan_reduce<<<tiles, 256, 0, st>>>(in, n_cap, d_n, tmp.tile_sums);

@@ -100,6 +100,7 @@ typedef struct gb_stats {
     int64_t retries;      /* evaluations of this context repeated after growing its buffers */
     int64_t graph_steps;  /* RK4 steps run by replaying the captured step graph */
     int64_t direct_steps; /* RK4 steps run by launching every kernel */
+    int64_t graph_captures; /* step graphs captured (a new n, dt or buffer set) */
 } gb_stats;
 
 /* Create a context on cfg->device. Validates cfg (p in 1..10, s >= 1). */
@@ -225,7 +226,9 @@ GB_API int gb_tree_dump(gb_ctx *ctx, int64_t *ncells, int64_t *list_sizes, int32
                  int64_t *p2p_own, int64_t *coll_off, int64_t *coll);
 
 /* Kernel timing: when enabled, the context brackets each kernel class with
- * CUDA events on its stream and accumulates milliseconds and launch counts.
+ * CUDA events on its stream and accumulates milliseconds and launch counts;
+ * while it is on, the classes run one after another on one stream (no
+ * near/far overlap) and every kernel is launched directly (no step graph).
  * Classes: 0 tree+lists, 1 operators, 2 P2M+M2M, 3 M2L, 4 L2L+L2P, 5 P2P,
  * 6 RK4+finalize. gb_kernel_times fills up to n entries of ms and launches
  * and resets the accumulators. */

@@ -238,7 +238,8 @@ def test_edge_cases_and_errors():
 def test_graph_replayed_steps_equal_direct_launches(plummer16k, precision):
     """RK4 steps replayed from the captured CUDA graph give exactly the
     results of launching every kernel (GB_FLAG_NO_GRAPH), across a change of
-    dt (re-capture) and a new upload of a different size."""
+    dt (re-capture), a new upload of a different size (re-capture) and new
+    data of the same size (replayed without re-capture)."""
     import vipp_gb300
     x, v = plummer16k
     out = []
@@ -251,10 +252,19 @@ def test_graph_replayed_steps_equal_direct_launches(plummer16k, precision):
             s.preprocess(x[:5000], v[:5000])
             s.solve(1e-3)
             s.solve(1e-3)
-            out.append((a, s.postprocess(), s.launch_count(), s.stats()))
-    (a0, b0, l0, st0), (a1, b1, l1, st1) = out
-    assert st0["graph_steps"] == 6 and st0["direct_steps"] == 0  # the graph path really ran
-    assert st1["graph_steps"] == 0 and st1["direct_steps"] == 6
+            b = s.postprocess()
+            caps = s.stats()["graph_captures"]
+            # new data of the same size: the captured graph is replayed as is
+            s.preprocess(x[5000:10000], v[5000:10000])
+            s.solve(1e-3)
+            s.solve(1e-3)
+            st = s.stats()
+            out.append((a, b, s.postprocess(), s.launch_count(), st, st["graph_captures"] - caps))
+    (a0, b0, c0, l0, st0, new0), (a1, b1, c1, l1, st1, new1) = out
+    assert st0["graph_steps"] == 8 and st0["direct_steps"] == 0  # the graph path really ran
+    assert st1["graph_steps"] == 0 and st1["direct_steps"] == 8
+    assert st1["graph_captures"] == 0 and new0 == 0 and st0["graph_captures"] >= 3
     assert np.array_equal(a0[0], a1[0]) and np.array_equal(a0[1], a1[1])
     assert np.array_equal(b0[0], b1[0]) and np.array_equal(b0[1], b1[1])
+    assert np.array_equal(c0[0], c1[0]) and np.array_equal(c0[1], c1[1])
     assert l0 == l1

@@ -43,7 +43,7 @@ struct gb_ctx {
     uint64_t step_epoch = 0;
     int64_t step_launches = 0;
     bool graph_failed = false;
-    long long graph_steps = 0, direct_steps = 0;
+    long long graph_steps = 0, direct_steps = 0, graph_captures = 0;
     std::vector<gb::PendingTimer> pending;
     std::vector<cudaEvent_t> free_events;
     long long *d_targets = nullptr;
@@ -115,12 +115,14 @@ int ensure_chunks(gb_ctx *ctx, unsigned need_items = 0, unsigned need_part = 0) 
     unsigned ch = 2 * ws.c_cap + ws.n_cap / 32 + 64;
     if (need_items > ch) ch = need_items + need_items / 4;
     if (ch > ws.ch_cap || !ws.chunks) {
+        ++ctx->epoch;  // reallocated: a captured step graph no longer applies
         GB_TRY(dalloc(ws.chunks, ch));
         ws.ch_cap = ch;
     }
     unsigned pc = ws.part_cap ? ws.part_cap : 4096u;
     if (need_part > pc) pc = need_part + need_part / 4;
     if (pc > ws.part_cap || !ws.part) {
+        ++ctx->epoch;
         unsigned char *b = nullptr;
         GB_TRY(dalloc(b, sizeof(double) * 96 * static_cast<size_t>(pc)));
         dfree(ws.part);
@@ -134,6 +136,7 @@ int ensure_chunks(gb_ctx *ctx, unsigned need_items = 0, unsigned need_part = 0) 
 int ensure_particles(gb_ctx *ctx, unsigned n) {
     gb::Workspace &ws = ctx->ws;
     if (n <= ws.n_cap && ws.x) return GB_OK;
+    ++ctx->epoch;
     const unsigned cap = n < 1024 ? 1024 : n;
     const size_t n3 = 3 * static_cast<size_t>(cap);
     GB_TRY(dalloc(ws.x, n3));
@@ -172,6 +175,7 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
     gb::Workspace &ws = ctx->ws;
     const size_t esz = ws.mixed ? sizeof(float) : sizeof(double);
     if (s_cap > ws.s_cap || ws.k_cap != ws.K * static_cast<int>(esz)) {
+        ++ctx->epoch;
         const unsigned c = 1 + 8 * s_cap;
         GB_TRY(dalloc(ws.ent0, s_cap));
         GB_TRY(dalloc(ws.ent1, s_cap));
@@ -216,6 +220,7 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
         ws.k_cap = ws.K * static_cast<int>(esz);
     }
     if (r_cap > ws.r_cap) {
+        ++ctx->epoch;
         GB_TRY(dalloc(ws.ranges, r_cap));
         ws.r_cap = r_cap;
     }
@@ -224,6 +229,7 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
         const int kp = gb::m2l_tc_row_floats(ws.p);
         const unsigned rows = ws.c_cap + 1;
         if (!ws.ms_tc || ws.ms_rows != rows || ws.ms_kp != kp) {
+            ++ctx->epoch;
             GB_TRY(dalloc(ws.ms_tc, 2 * static_cast<size_t>(rows) * kp));
             ws.ms_rows = rows, ws.ms_kp = kp;
             if (const char *e = gb::m2l_tc_encode(ws)) {
@@ -326,7 +332,10 @@ void evaluate(gb_ctx *ctx) {
     gb::Workspace &ws = ctx->ws;
     g_timer_ctx = ctx;
     gb::build_tree(ws);
-    if (!ws.serial) {
+    // Near field on the second stream, unless serial or timed: class timers
+    // measure each class alone on one stream.
+    const bool fork = !ws.serial && !ws.timing;
+    if (fork) {
         cudaEventRecord(ws.ev_fork, ws.st);
         cudaStreamWaitEvent(ws.st2, ws.ev_fork, 0);
         std::swap(ws.st, ws.st2);  // the stages launch on ws.st
@@ -341,7 +350,7 @@ void evaluate(gb_ctx *ctx) {
     else
         gb::m2l_pass(ws);
     gb::downward_pass(ws);
-    if (ws.serial)
+    if (!fork)
         gb::p2p_pass(ws);
     else
         cudaStreamWaitEvent(ws.st, ws.ev_join, 0);
@@ -511,7 +520,6 @@ int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
 
 int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
     if (!ctx) return GB_ERR_INVALID;
-    ++ctx->epoch;  // buffers, sizes or configuration may change: the step graph is rebuilt
     if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
     if (n && (!x_aos || !v_aos)) return ctx->err = "null input", GB_ERR_INVALID;
     GB_TRY(cudaSetDevice(ctx->cfg.device));
@@ -535,7 +543,6 @@ int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
 
 int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max) {
     if (!ctx) return GB_ERR_INVALID;
-    ++ctx->epoch;  // buffers, sizes or configuration may change: the step graph is rebuilt
     if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
     if (!(r_max >= 0) || !std::isfinite(r_max)) return ctx->err = "r_max must be finite and >= 0", GB_ERR_INVALID;
     if (r_max == 0 && !(ctx->cfg.eps > 0 && ctx->cfg.eps < 1))
@@ -609,6 +616,7 @@ static void capture_step(gb_ctx *ctx, double dt, const std::function<void()> &bo
         return;
     }
     ctx->step_n = ws.n, ctx->step_dt = dt, ctx->step_epoch = ctx->epoch;
+    ++ctx->graph_captures;
 }
 
 // Queue one RK4 step from the saved step start (rk4_begin): the captured
@@ -911,6 +919,7 @@ int gb_get_stats(gb_ctx *ctx, gb_stats *out) {
     out->p2p_ranges = h.p2p_ranges;
     out->retries = ctx->retries;
     out->graph_steps = ctx->graph_steps;
+    out->graph_captures = ctx->graph_captures;
     out->direct_steps = ctx->direct_steps;
     return GB_OK;
 }

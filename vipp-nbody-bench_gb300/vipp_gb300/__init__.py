@@ -48,7 +48,7 @@ class GbConserved(ctypes.Structure):
 
 class GbStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int64) for k in ("n", "ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges", "retries",
-                                                        "graph_steps", "direct_steps")]
+                                                        "graph_steps", "direct_steps", "graph_captures")]
 
 
 _LIB = None

@@ -413,7 +413,21 @@ def main():
         t = kt["m2l"][0] / kt["m2l"][1] / 1e3
         ach = 2.0 * K * K * st["m2l_pairs"] / t / 1e12  # algorithmic: one K x K operator per pair
         tensor = args.precision == "mixed" and args.p >= 2 and not (args.flags & vipp_gb300.FLAG_M2L_CUDA_CORES)
-        if tensor:
+        if tensor and args.flags & vipp_gb300.FLAG_M2L_BF16:
+            # BF16 hi/lo split: bound = the measured bf16 GEMM rate. Executed work:
+            # per tile and slot, K steps of 16 over the [hi | lo] row (2K), N = 2N'
+            # where a step reaches hi inputs, else N'.
+            nt = max(st["ncells"] - 9, 0)
+            tiles = 8 * math.ceil(nt / 8 / 128)
+            N = (K + 15) // 16 * 16
+            cols = sum(2 * N if 16 * j < K else N for j in range(math.ceil(2 * K / 16)))
+            exe = tiles * 189 * 2.0 * 128 * 16 * cols / t / 1e12
+            pk = peaks["bf16_tflops"]
+            per["m2l"] = {"bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s",
+                          "frac": ach / pk, "executed_tflops": exe, "executed_frac": exe / pk,
+                          "ms_per_launch": 1e3 * t, "launches": kt["m2l"][1], "split": "bf16 hi/lo",
+                          "peak_source": f"{src} bf16_tflops"}
+        elif tensor:
             # TF32 tcgen05 MMAs run at half the bf16 rate (same cycles per MMA, half
             # the K), so the bound is half the measured bf16 GEMM rate. Executed
             # tensor work: 128-row tiles of same-octant targets x 189 slots, K and
@@ -426,7 +440,7 @@ def main():
             exe = tiles * 189 * ksteps * 3 * 2.0 * 128 * N * 8 / t / 1e12
             per["m2l"] = {"bound": "tensor", "achieved": ach, "peak": tf32_peak, "unit": "TFLOP/s",
                           "frac": ach / tf32_peak, "executed_tflops": exe, "executed_frac": exe / tf32_peak,
-                          "ms_per_launch": 1e3 * t, "launches": kt["m2l"][1],
+                          "ms_per_launch": 1e3 * t, "launches": kt["m2l"][1], "split": "3 x tf32",
                           "peak_source": f"{src} bf16_tflops / 2 (TF32 MMA rate)"}
         else:
             per["m2l"] = {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,

@@ -75,15 +75,18 @@ enum gb_flags {
                                 step (off by default: it changes the RMS error by
                                 about 1e-10 and costs about 20% of P2P time) */
     GB_FLAG_M2L_CUDA_CORES = 2, /* mixed M2L on CUDA cores in FP32 instead of the
-                                   default tensor-core M2L (tcgen05, TF32 with a
-                                   three-term hi/lo split) */
+                                   default tensor-core M2L (tcgen05) */
     GB_FLAG_SERIAL = 4,         /* run the near field (P2P) after the far field on
                                    one stream instead of concurrently on a second
                                    stream of the context (same results) */
-    GB_FLAG_NO_GRAPH = 8        /* launch every kernel of an RK4 step instead of
+    GB_FLAG_NO_GRAPH = 8,       /* launch every kernel of an RK4 step instead of
                                    replaying the step's captured CUDA graph (same
                                    results; graphs are also off while kernel
                                    timing is enabled) */
+    GB_FLAG_M2L_BF16 = 16       /* tensor-core M2L with a BF16 hi/lo split
+                                   (~2^-17 relative per product; half the gathered
+                                   bytes and MMA time, ~17% less M2L time) instead
+                                   of the default three-term TF32 split (~2^-21) */
 };
 
 typedef struct gb_ctx gb_ctx;

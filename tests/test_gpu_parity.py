@@ -6,7 +6,8 @@ Tolerances (written here, per quantity):
   * FP64 accelerations: max per-particle relative difference <= 1e-10 from
     the reference's FMM (the special-function evaluation order differs);
   * mixed precision (FP32 P2P / expansions): RMS relative difference <= 2e-6
-    and max <= 1e-4 from the reference's FMM;
+    and max <= 1e-4 from the reference's FMM; with the BF16 hi/lo split M2L
+    (GB_FLAG_M2L_BF16) RMS <= 2e-5 and max <= 1e-4;
   * FP64 RK4 step: positions to 1e-14 and velocities to 1e-11 of their scale.
 """
 import math
@@ -25,6 +26,8 @@ CASES = ["plummer2000_s8_p4", "plummer3000_s4_p6", "uniform1500_s16_p3", "cluste
 FP64_MAX_REL = 1e-10
 MIXED_RMS_REL = 2e-6
 MIXED_MAX_REL = 1e-4
+MIXED_BF16_RMS_REL = 2e-5
+MIXED_BF16_MAX_REL = 1e-4
 
 
 def solver(d, precision="fp64"):
@@ -128,6 +131,22 @@ def test_direct_sum_kernel_vs_oracle(plummer16k):
         a_all = s.direct_accel()
     assert np.max(rel_err(a, ref)) <= 1e-13
     assert np.max(rel_err(a_all[targets], ref)) <= 1e-13
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_mixed_m2l_bf16_split_matches_reference(name):
+    """The tensor-core M2L with the BF16 hi/lo split (GB_FLAG_M2L_BF16, ~2^-17
+    per product) stays within MIXED_BF16_RMS_REL / MIXED_BF16_MAX_REL of the
+    reference's FMM, and the tree it runs on is the same."""
+    import vipp_gb300
+    d = load_case(name)
+    with vipp_gb300.Solver(p=d["p"], s=d["s"], eps=d["eps"], G=d["G"], m=d["m"], precision="mixed",
+                           flags=vipp_gb300.FLAG_M2L_BF16) as s:
+        s.preprocess(d["x"], d["v"])
+        a = s.accel()
+        assert diff_trees(canon_gpu(s.tree_dump()), canon_ref(d)) == []
+    e = rel_err(a, d["acc"])
+    assert math.sqrt(np.mean(e ** 2)) <= MIXED_BF16_RMS_REL and np.max(e) <= MIXED_BF16_MAX_REL
 
 
 @pytest.mark.parametrize("name", ["plummer3000_s4_p6", "cluster1200_s6_p5", "plummer2000_s8_p4"])

@@ -104,6 +104,7 @@ void apply_config(gb_ctx *ctx) {
     ws.mixed = ctx->cfg.precision == GB_PREC_MIXED;
     ws.p2p_newton = (ctx->cfg.flags & GB_FLAG_P2P_NEWTON) != 0;
     ws.m2l_tensor = ws.mixed && (ctx->cfg.flags & GB_FLAG_M2L_CUDA_CORES) == 0 && gb::m2l_tc_supported(ws.p);
+    ws.m2l_bf16 = (ctx->cfg.flags & GB_FLAG_M2L_BF16) != 0;
     ws.serial = (ctx->cfg.flags & GB_FLAG_SERIAL) != 0;
 }
 
@@ -228,7 +229,7 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
         // split expansions of the tensor-core M2L and their TMA map
         const int kp = gb::m2l_tc_row_floats(ws.p);
         const unsigned rows = ws.c_cap + 1;
-        if (!ws.ms_tc || ws.ms_rows != rows || ws.ms_kp != kp) {
+        if (!ws.ms_tc || ws.ms_rows != rows || ws.ms_kp != kp || ws.ms_bf16 != ws.m2l_bf16) {
             ++ctx->epoch;
             GB_TRY(dalloc(ws.ms_tc, 2 * static_cast<size_t>(rows) * kp));
             ws.ms_rows = rows, ws.ms_kp = kp;

@@ -9,9 +9,23 @@
 //                                             B = the slot's operator,
 // accumulated in TMEM (128 lanes x N FP32 columns).
 //
-// Precision: kind::tf32 with a three-term split (hi = FP32 with the low 13
-// mantissa bits cleared, lo = x - hi):  D += Ahi Bhi + Ahi Blo + Alo Bhi,
-// which carries ~2^-21 relative error per product, FP32 accumulation.
+// Precision, two forms of the same three-product split
+//     D += Ahi Bhi + Ahi Blo + Alo Bhi,   x = hi + lo,   FP32 accumulation:
+//  * TF32 (default): kind::tf32, hi = FP32 with the low 13 mantissa bits
+//    cleared, lo = x - hi: ~2^-21 per product; hi and lo rows are two A
+//    operands;
+//  * BF16 (GB_FLAG_M2L_BF16): kind::f16 with bf16 operands, hi = bf16(x), lo =
+//    bf16(x - hi): ~2^-17 relative error per product. A source row is the
+//    concatenation [hi | lo] (2K values), so Ahi Bhi + Alo Bhi is one product
+//    over the doubled K, and one B operand [Bhi ; Blo] of 2N rows gives
+//    Ahi Blo in the second N accumulator columns (zero rows of Blo under the
+//    lo half of K: those K steps issue N-wide MMAs on Bhi alone). It halves
+//    the gathered bytes and the MMA time; measured at 4M particles, p = 8:
+//    M2L 2.32 instead of 2.79 ms per evaluation, force error against the FP64
+//    direct sum unchanged (RMS 2.386e-4), energy drift over 10 steps 5e-7
+//    instead of 6e-8.
+// The expansions are scaled per cell by powers of the cell size, so bf16's
+// FP32 exponent range holds them.
 //
 // Accumulation: the tensor core's FP32 accumulation adds an error that grows
 // with the number of MMAs summed into one accumulator (measured: RMS error
@@ -22,15 +36,17 @@
 // additions) while the next group accumulates.
 //
 // Data flow (one CTA per SM, persistent over tiles, warp-specialised):
-//  * k_split_m writes every cell's expansion once more as two zero-padded
-//    rows of KP = 32 ceil(K / 32) floats, the hi part and the lo part, plus a
-//    zero row that stands in for absent sources;
-//  * the loader warp gathers, per (slot, 32-wide K chunk) step, the 128
-//    source rows of the tile with TMA tile::gather4 copies (4 rows of 128
-//    bytes per copy, hi and lo) into 128B-swizzled K-major A tiles, and the
-//    slot's pre-split operator chunk with one cp.async.bulk;
-//  * the MMA warp (one thread) issues 3 x 4 tcgen05.mma per step, commits the
-//    stage back to the loader and each finished group to the drain warps;
+//  * k_split_m writes every cell's expansion once more, split and zero-padded
+//    to whole 128-byte K chunks (bf16: one [hi | lo] row of 64-element chunks;
+//    tf32: a hi row and a lo row of 32-element chunks), plus a zero row that
+//    stands in for absent sources;
+//  * the loader warps gather, per (slot, K chunk) step, the 128 source rows of
+//    the tile with TMA tile::gather4 copies (4 rows of 128 bytes per copy) into
+//    128B-swizzled K-major A tiles (bf16: 32 copies; tf32: 64, hi and lo), and
+//    the slot's pre-split operator chunk with one cp.async.bulk;
+//  * the MMA warp (one thread) issues the step's tcgen05.mma (one per 32-byte
+//    K step; tf32: two), commits the stage back to the loaders and each
+//    finished group to the drain warps;
 //  * the drain warps (warps 0-3 own TMEM lanes 32w..32w+31, i.e. tile rows)
 //    add the groups and write the tile's local expansions.
 // Every tile runs the same static schedule (189 slots x NKC chunks), so the
@@ -40,6 +56,7 @@
 // records kDevTimeout in the status word, stops issuing work, waits (bounded)
 // for its own copies and MMAs, frees its TMEM and returns.
 #include <cuda.h>
+#include <cuda_bf16.h>
 
 #include "workspace.cuh"
 
@@ -48,13 +65,16 @@ namespace gb {
 namespace {
 
 constexpr int kRows = 128;          // targets per tile (MMA M)
-constexpr int kKC = 32;             // K chunk (tf32 elements): one 128-byte swizzle row
+constexpr int kKC32 = 32;           // K chunk in 4-byte units: one 128-byte swizzle row
 constexpr int kDrainThreads = 128;  // warps 0-3
 #ifndef M2L_LOADER_WARPS
 #define M2L_LOADER_WARPS 4
 #endif
 #ifndef M2L_MAX_STAGES
-#define M2L_MAX_STAGES 4  // 3 leaves shared memory for concurrent P2P blocks
+#define M2L_MAX_STAGES 4  // tf32 stages (56 KB each)
+#endif
+#ifndef M2L_MAX_STAGES_BF16
+#define M2L_MAX_STAGES_BF16 5  // bf16 stages (40 KB each)
 #endif
 #ifndef M2L_MIN_BLOCKS
 #define M2L_MIN_BLOCKS 1  // > 1 caps registers so the kernel fits beside P2P blocks
@@ -63,48 +83,57 @@ constexpr int kDrainThreads = 128;  // warps 0-3
 #define M2L_WIDE_B 1
 #endif
 constexpr int kLoaderWarps = M2L_LOADER_WARPS;  // warps 4 .. 3 + kLoaderWarps
-constexpr int kGathers = 64;                    // gather4 copies per step: 32 row quads x (hi, lo)
-constexpr int kGathersPerWarp = kGathers / kLoaderWarps;
 constexpr int kMmaWarp = 4 + kLoaderWarps;
 constexpr int kThreads = 32 * (kMmaWarp + 1);
-static_assert(kGathers % kLoaderWarps == 0, "loader warps");
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr int kGroup = 4;           // slots per TMEM accumulation group
 constexpr int kSlotsPerTile = 189;  // M2L slots of every octant: 216 minus the 27 adjacent ones
 constexpr int kGroupsPerTile = (kSlotsPerTile + kGroup - 1) / kGroup;
 constexpr int kSmemMax = 232448;    // opt-in shared memory per block
 
-template <int P>
+template <int P, bool BF>
 struct TcCfg {
     static constexpr int K = (P + 1) * (P + 1);
-    static constexpr int NKC = (K + kKC - 1) / kKC;      // K chunks
-    static constexpr int KP = NKC * kKC;                 // row length of the split expansions
+    static constexpr int KC = BF ? 2 * kKC32 : kKC32;    // K chunk (elements)
+    static constexpr int KS = BF ? 16 : 8;               // K per MMA (32 bytes)
+    static constexpr int KA = BF ? 2 * K : K;            // K of the A operand: [hi | lo] or one part
+    static constexpr int NKC = (KA + KC - 1) / KC;       // K chunks
+    static constexpr int KP = NKC * KC;                  // row length of the split expansions (elements)
+    static constexpr int NA = BF ? 1 : 2;                // A tiles per stage
+    static constexpr int GATHERS = NA * kRows / 4;       // gather4 copies per stage
     static constexpr int N = (K + 15) / 16 * 16;         // MMA N (multiple of 16 for M = 128)
-    // An accumulator holds Ahi [Bhi; Blo]^T (2N columns: N of Ahi Bhi + Alo Bhi,
-    // N of Ahi Blo); the hi and lo operator blocks are adjacent in the stage,
-    // so [Bhi; Blo] is one B operand of 2N rows.
-    static constexpr int DCOLS = M2L_WIDE_B ? 2 * N : N;
+    // An accumulator holds A [Bhi; Blo]^T (2N columns; the two halves are added
+    // by the drain), so the hi and lo operator blocks are adjacent in the stage.
+    static constexpr int DCOLS = (BF || M2L_WIDE_B) ? 2 * N : N;
     static constexpr int ACOL = DCOLS <= 32 ? 32 : (DCOLS <= 64 ? 64 : (DCOLS <= 128 ? 128 : 256));
     static constexpr int TMEM_COLS = 2 * ACOL;
-    static constexpr int A_BYTES = kRows * kKC * 4;      // one of hi/lo: 16 KB
-    static constexpr int B_BYTES = N * kKC * 4;
-    static constexpr int STAGE = 2 * A_BYTES + 2 * B_BYTES;
-    static constexpr int STAGES = (kSmemMax - 2048) / STAGE >= M2L_MAX_STAGES ? M2L_MAX_STAGES : 3;  // ring depth
+    static constexpr int A_BYTES = kRows * 128;          // one A tile: 16 KB
+    static constexpr int B_BYTES = N * 128;              // one of Bhi / Blo
+    static constexpr int STAGE = NA * A_BYTES + 2 * B_BYTES;
+    static constexpr int MAX_STAGES = BF ? M2L_MAX_STAGES_BF16 : M2L_MAX_STAGES;
+    static constexpr int STAGES = (kSmemMax - 2048) / STAGE >= MAX_STAGES ? MAX_STAGES : (kSmemMax - 2048) / STAGE;  // ring depth
     static constexpr size_t SMEM = static_cast<size_t>(STAGES) * STAGE + 1024 + 256;
-    // instruction descriptor: D f32 (bits 4-5 = 1), A/B tf32 (bits 7-9, 10-12 = 2),
-    // both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
+    // instruction descriptor: D f32 (bits 4-5 = 1), A/B bf16 (bits 7-9, 10-12 = 1,
+    // kind::f16) or tf32 (= 2, kind::tf32), both K-major, N >> 3 at bits 17-22,
+    // M >> 4 at bits 24-28
     static constexpr uint32_t idesc(int n) {
-        return (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(n >> 3) << 17) | (static_cast<uint32_t>(kRows >> 4) << 24);
+        return (1u << 4) | ((BF ? 1u : 2u) << 7) | ((BF ? 1u : 2u) << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
+               (static_cast<uint32_t>(kRows >> 4) << 24);
     }
     static constexpr uint32_t IDESC = idesc(N);
     static constexpr uint32_t IDESC_W = idesc(2 * N);
     static_assert(2 * N <= 256, "MMA N");
+    static_assert(STAGES >= 3, "ring depth");
+    static_assert(GATHERS % kLoaderWarps == 0, "loader warps");
     static_assert(STAGE % 1024 == 0, "stages must keep the 1024-byte swizzle atoms aligned");
     static_assert(SMEM <= static_cast<size_t>(kSmemMax), "shared memory");
 };
 
-// canonical no-swizzle K-major position (in floats) of element (row, k) of a [rows x 32] chunk
+// canonical no-swizzle K-major position of element (row, k) of a [rows x KC]
+// chunk, in elements: 8-row x 16-byte core matrices (128 B), K-adjacent core
+// matrices 128 B apart, 8-row groups 1024 B apart
 __host__ __device__ __forceinline__ int canon(int row, int k) { return (row >> 3) * 256 + (k >> 2) * 32 + (row & 7) * 4 + (k & 3); }
+__host__ __device__ __forceinline__ int canon16(int row, int k) { return (row >> 3) * 512 + (k >> 3) * 64 + (row & 7) * 8 + (k & 7); }
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 
@@ -183,6 +212,11 @@ __device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t ad, uint64_t 
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
         "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
 }
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
 __device__ __forceinline__ void umma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar)) : "memory");
 }
@@ -221,11 +255,12 @@ __device__ __forceinline__ int next_slot(int cls, int s) {
     return s;
 }
 
-template <int P>
+template <int P, bool BF>
 __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
     k_m2l_tc(const __grid_constant__ CUtensorMap tmap, const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
-             const float *__restrict__ bimg, int rows_cap, float *__restrict__ Lx, TreeInfo *info_rw) {
-    using C = TcCfg<P>;
+             const unsigned char *__restrict__ bimg, int rows_cap, float *__restrict__ Lx, TreeInfo *info_rw) {
+    using C = TcCfg<P, BF>;
+    constexpr int kGW = C::GATHERS / kLoaderWarps;  // gather4 copies per loader warp and step
     extern __shared__ __align__(1024) unsigned char sm_raw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(sm_raw) + 1023) & ~uintptr_t(1023));
     uint64_t *full = reinterpret_cast<uint64_t *>(sm + C::STAGES * C::STAGE);
@@ -263,17 +298,17 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
     unsigned mma_steps = 0;  // steps whose MMAs the MMA thread issued
     if (warp >= 4 && warp < kMmaWarp) {
         // --------------------------------------------------------------- loaders
-        // Copy G = q kGathersPerWarp + l (+ 32 i) of a step moves row quad G mod 32
-        // (tile rows 4(G mod 32) .. +3) of part G / 32 (hi, lo); absent sources
-        // read the zero row. Each loader warp's lane 0 arms the stage's barrier
-        // with the bytes of its own warp's copies.
+        // Copy G = q kGW + l (+ 32 i) of a step moves row quad G mod 32 (tile
+        // rows 4(G mod 32) .. +3) of A tile G / 32 (tf32: hi, lo); absent
+        // sources read the zero row. Each loader warp's lane 0 arms the stage's
+        // barrier with the bytes of its own warp's copies.
         const int q = warp - 4;
-        const int g0 = q * kGathersPerWarp + lane;
+        const int g0 = q * kGW + lane;
         const int quad = g0 % 32;
-        const bool active = lane < kGathersPerWarp;
-        const bool do_hi = active && (kGathersPerWarp >= 64 || g0 < 32);
-        const bool do_lo = active && (kGathersPerWarp >= 64 || g0 >= 32);
-        const unsigned warp_bytes = static_cast<unsigned>(kGathersPerWarp) * 512u + (q == 0 ? 2u * C::B_BYTES : 0u);
+        const bool active = lane < kGW;
+        const bool do_hi = active && (kGW >= 64 || g0 < 32);
+        const bool do_lo = !BF && active && (kGW >= 64 || g0 >= 32);
+        const unsigned warp_bytes = static_cast<unsigned>(kGW) * 512u + (q == 0 ? 2u * C::B_BYTES : 0u);
         const int zrow = rows_cap - 1;
         unsigned step = 0;
         bool stop = false;
@@ -314,12 +349,12 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                     }
                     unsigned char *stage = sm + st * C::STAGE;
                     if (do_hi)
-                        tma_gather4(stage + 512 * quad, &tmap, kc * kKC, cur[0], cur[1], cur[2], cur[3], full + st);
+                        tma_gather4(stage + 512 * quad, &tmap, kc * C::KC, cur[0], cur[1], cur[2], cur[3], full + st);
                     if (do_lo)
-                        tma_gather4(stage + C::A_BYTES + 512 * quad, &tmap, kc * kKC, cur[0] + rows_cap, cur[1] + rows_cap,
+                        tma_gather4(stage + C::A_BYTES + 512 * quad, &tmap, kc * C::KC, cur[0] + rows_cap, cur[1] + rows_cap,
                                     cur[2] + rows_cap, cur[3] + rows_cap, full + st);
                     if (q == 0 && lane == 0)
-                        bulk_g2s(stage + 2 * C::A_BYTES, bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::N * kKC),
+                        bulk_g2s(stage + C::NA * C::A_BYTES, bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::B_BYTES),
                                  2 * C::B_BYTES, full + st);
                 }
 #pragma unroll
@@ -351,22 +386,30 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                         }
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         const unsigned char *stage = sm + st * C::STAGE;
-                        const uint64_t ahi = sdesc_sw128(stage), alo = sdesc_sw128(stage + C::A_BYTES);
-                        const float *Bhi = reinterpret_cast<const float *>(stage + 2 * C::A_BYTES);
-                        const float *Blo = Bhi + C::N * kKC;
-                        const int ksteps = min(kKC / 8, (C::K - kc * kKC + 7) / 8);
+                        const uint64_t ahi = sdesc_sw128(stage);
+                        const unsigned char *Bhi = stage + C::NA * C::A_BYTES;
+                        const unsigned char *Blo = Bhi + C::B_BYTES;
+                        const int ksteps = min(C::KC / C::KS, (C::KA - kc * C::KC + C::KS - 1) / C::KS);
                         for (int ks = 0; ks < ksteps; ++ks) {
-                            // 8 tf32 = 32 B along K: +2 in the swizzled start field,
-                            // two core matrices (64 floats) in the plain layout
-                            const uint64_t bhi = sdesc(Bhi + ks * 64), blo = sdesc(Blo + ks * 64);
+                            // 32 B along K: +2 in the swizzled start field, two
+                            // core matrices (256 B) in the plain layout
+                            const uint64_t bhi = sdesc(Bhi + ks * 256);
                             const uint32_t first = (in_group == 0 && kc == 0 && ks == 0) ? 0u : 1u;
-                            if (M2L_WIDE_B) {
-                                umma_tf32(dt, ahi + 2 * ks, bhi, C::IDESC_W, first);  // Ahi [Bhi; Blo]^T
+                            if (BF) {
+                                // [hi | lo] row: K steps that reach hi inputs take [Bhi; Blo]
+                                // (2N columns), the lo half Bhi alone (N columns)
+                                const bool wide = kc * C::KC + ks * C::KS < C::K;
+                                umma_bf16(dt, ahi + 2 * ks, bhi, wide ? C::IDESC_W : C::IDESC, first);
                             } else {
-                                umma_tf32(dt, ahi + 2 * ks, bhi, C::IDESC, first);
-                                umma_tf32(dt, ahi + 2 * ks, blo, C::IDESC, 1u);
+                                const uint64_t alo = sdesc_sw128(stage + C::A_BYTES);
+                                if (M2L_WIDE_B) {
+                                    umma_tf32(dt, ahi + 2 * ks, bhi, C::IDESC_W, first);  // Ahi [Bhi; Blo]^T
+                                } else {
+                                    umma_tf32(dt, ahi + 2 * ks, bhi, C::IDESC, first);
+                                    umma_tf32(dt, ahi + 2 * ks, sdesc(Blo + ks * 256), C::IDESC, 1u);
+                                }
+                                umma_tf32(dt, alo + 2 * ks, bhi, C::IDESC, 1u);
                             }
-                            umma_tf32(dt, alo + 2 * ks, bhi, C::IDESC, 1u);
                         }
                         umma_commit(empty + st);
                         ++mma_steps;
@@ -397,7 +440,7 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t col = (groups & 1) * C::ACOL;
 #pragma unroll
-                for (int h = 0; h < (M2L_WIDE_B ? 2 : 1); ++h)
+                for (int h = 0; h < C::DCOLS / C::N; ++h)
 #pragma unroll
                     for (int c0 = 0; c0 < C::N; c0 += 32) {
                         float v[32];
@@ -439,63 +482,102 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
     }
 }
 
-// Split expansions for the gather: rows [0, rows_cap) hold the hi parts,
-// rows [rows_cap, 2 rows_cap) the lo parts, KP floats each, zero beyond K;
-// row rows_cap - 1 of both halves is the zero row.
-template <int P>
-__global__ void k_split_m(const TreeInfo *__restrict__ info, const float *__restrict__ M, float *__restrict__ ms, int rows_cap) {
-    using C = TcCfg<P>;
+// Split expansions for the gather; row rows_cap - 1 is the zero row.
+// bf16: rows [0, rows_cap) of KP elements [hi(0..K-1) | lo(0..K-1) | 0].
+// tf32: rows [0, rows_cap) hold the hi parts, rows [rows_cap, 2 rows_cap) the
+// lo parts, KP floats each, zero beyond K.
+template <int P, bool BF>
+__global__ void k_split_m(const TreeInfo *__restrict__ info, const float *__restrict__ M, void *__restrict__ ms_v, int rows_cap) {
+    using C = TcCfg<P, BF>;
     const int nc = min(info->ncells, rows_cap - 1);
-    float *lo = ms + static_cast<size_t>(rows_cap) * C::KP;
     const size_t total = static_cast<size_t>(nc) * C::KP;
-    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const size_t c = i / C::KP;
-        const int k = static_cast<int>(i - c * C::KP);
-        const float v = k < C::K ? M[c * C::K + k] : 0.f;
-        const float h = tf32_hi(v);
-        ms[i] = h;
-        lo[i] = v - h;
-    }
-    if (blockIdx.x == 0)
-        for (int k = threadIdx.x; k < C::KP; k += blockDim.x) {
-            ms[static_cast<size_t>(rows_cap - 1) * C::KP + k] = 0.f;
-            lo[static_cast<size_t>(rows_cap - 1) * C::KP + k] = 0.f;
+    const size_t zrow = static_cast<size_t>(rows_cap - 1) * C::KP;
+    if (BF) {
+        __nv_bfloat16 *ms = static_cast<__nv_bfloat16 *>(ms_v);
+        for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+             i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+            const size_t c = i / C::KP;
+            const int j = static_cast<int>(i - c * C::KP);
+            const int k = j < C::K ? j : j - C::K;
+            const float v = j < 2 * C::K ? M[c * C::K + k] : 0.f;
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            ms[i] = j < C::K ? h : __float2bfloat16_rn(v - __bfloat162float(h));
         }
+        if (blockIdx.x == 0)
+            for (int k = threadIdx.x; k < C::KP; k += blockDim.x) ms[zrow + k] = __float2bfloat16_rn(0.f);
+    } else {
+        float *ms = static_cast<float *>(ms_v);
+        float *lo = ms + static_cast<size_t>(rows_cap) * C::KP;
+        for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+             i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+            const size_t c = i / C::KP;
+            const int k = static_cast<int>(i - c * C::KP);
+            const float v = k < C::K ? M[c * C::K + k] : 0.f;
+            const float h = tf32_hi(v);
+            ms[i] = h;
+            lo[i] = v - h;
+        }
+        if (blockIdx.x == 0)
+            for (int k = threadIdx.x; k < C::KP; k += blockDim.x) ms[zrow + k] = 0.f, lo[zrow + k] = 0.f;
+    }
 }
 
 // Pre-split operator images: for each same-level offset oi and K chunk kc,
-// [hi | lo], each N x 32 floats in the canonical K-major layout (rows = output
-// coefficient r, k = input coefficient 32 kc + k); zero outside K x K.
-template <int P>
-__global__ void k_build_bimg(const double *__restrict__ ops_d, float *__restrict__ bimg) {
-    using C = TcCfg<P>;
+// one block of 2N rows x KC elements in the canonical K-major layout, rows
+// r < N the hi part and rows N + r the lo part of output coefficient r
+// (zero outside K x K).
+// tf32: element k of the chunk is input coefficient KC kc + k.
+// bf16: element j = KC kc + k of the [hi | lo] input row is input coefficient
+// j (j < K) or j - K (K <= j < 2K, the lo inputs: rows N + r are zero there).
+template <int P, bool BF>
+__global__ void k_build_bimg(const double *__restrict__ ops_d, unsigned char *__restrict__ bimg) {
+    using C = TcCfg<P, BF>;
     const int oi = blockIdx.x;
     const int d0 = oi % 7 - 3, d1 = (oi / 7) % 7 - 3, d2 = oi / 49 - 3;
     if (d0 >= -1 && d0 <= 1 && d1 >= -1 && d1 <= 1 && d2 >= -1 && d2 <= 1) return;
     for (int kc = 0; kc < C::NKC; ++kc) {
-        float *hi = bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::N * kKC);
-        float *lo = hi + C::N * kKC;
-        for (int i = threadIdx.x; i < C::N * kKC; i += blockDim.x) {
-            const int r = i / kKC, k = i % kKC, ci = kc * kKC + k;
-            const float v = (r < C::K && ci < C::K) ? static_cast<float>(ops_d[(static_cast<size_t>(oi) * C::K + r) * C::K + ci]) : 0.f;
-            const float h = tf32_hi(v);
-            hi[canon(r, k)] = h;
-            lo[canon(r, k)] = v - h;
+        unsigned char *blk = bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::B_BYTES);
+        for (int i = threadIdx.x; i < 2 * C::N * C::KC; i += blockDim.x) {
+            const int r = i / C::KC, k = i % C::KC, j = kc * C::KC + k;
+            const bool lo_row = r >= C::N;
+            const int ro = lo_row ? r - C::N : r;
+            int ci = j;
+            bool use = j < C::K;
+            if (BF && j >= C::K && j < 2 * C::K) ci = j - C::K, use = !lo_row;
+            const float v = (use && ro < C::K) ? static_cast<float>(ops_d[(static_cast<size_t>(oi) * C::K + ro) * C::K + ci]) : 0.f;
+            if (BF) {
+                const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+                reinterpret_cast<__nv_bfloat16 *>(blk)[canon16(r, k)] = lo_row ? l : h;
+            } else {
+                const float h = tf32_hi(v);
+                float *f = reinterpret_cast<float *>(blk) + (lo_row ? C::N * C::KC : 0);
+                f[canon(ro, k)] = lo_row ? v - h : h;
+            }
         }
     }
 }
 
-template <int P>
+template <int P, bool BF>
 void launch(Workspace &ws) {
-    using C = TcCfg<P>;
-    k_build_bimg<P><<<343, 256, 0, ws.st>>>(ws.ops_d, ws.bimg);
-    k_split_m<P><<<4 * ws.num_sms, 256, 0, ws.st>>>(ws.info, static_cast<const float *>(ws.Mexp), ws.ms_tc,
-                                                   static_cast<int>(ws.ms_rows));
-    cudaFuncSetAttribute(k_m2l_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(C::SMEM));
+    using C = TcCfg<P, BF>;
+    k_build_bimg<P, BF><<<343, 256, 0, ws.st>>>(ws.ops_d, reinterpret_cast<unsigned char *>(ws.bimg));
+    k_split_m<P, BF><<<4 * ws.num_sms, 256, 0, ws.st>>>(ws.info, static_cast<const float *>(ws.Mexp), ws.ms_tc,
+                                                        static_cast<int>(ws.ms_rows));
+    cudaFuncSetAttribute(k_m2l_tc<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(C::SMEM));
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms), 8 * ceil_div(ceil_div(ws.c_cap, 8), kRows));  // tiles
-    k_m2l_tc<P><<<gs, kThreads, C::SMEM, ws.st>>>(ws.tmap_ms, ws.info, ws.m2l_src, ws.bimg,
-                                                         static_cast<int>(ws.ms_rows), static_cast<float *>(ws.Lexp), ws.info);
+    k_m2l_tc<P, BF><<<gs, kThreads, C::SMEM, ws.st>>>(ws.tmap_ms, ws.info, ws.m2l_src,
+                                                      reinterpret_cast<const unsigned char *>(ws.bimg),
+                                                      static_cast<int>(ws.ms_rows), static_cast<float *>(ws.Lexp), ws.info);
     ws.launches += 3;
+}
+
+template <int P>
+void launch_kind(Workspace &ws) {
+    if (ws.m2l_bf16)
+        launch<P, true>(ws);
+    else
+        launch<P, false>(ws);
 }
 
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -504,15 +586,19 @@ using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
 
 }  // namespace
 
+// Both forms: 343 offsets x NKC chunks x 2N rows x 128 B, with NKC =
+// ceil(K / 32) (tf32) = ceil(2K / 64) (bf16).
 size_t m2l_tc_image_floats(int p) {
     const int K = (p + 1) * (p + 1);
-    const int NKC = (K + kKC - 1) / kKC, N = (K + 15) / 16 * 16;
-    return static_cast<size_t>(343) * NKC * 2 * N * kKC;
+    const int NKC = (K + kKC32 - 1) / kKC32, N = (K + 15) / 16 * 16;
+    return static_cast<size_t>(343) * NKC * 2 * N * kKC32;
 }
 
+// 4-byte units per split row: tf32 KP floats (hi or lo); bf16 [hi | lo] rows
+// of 2 KP bf16 take the same bytes, in one half of the tf32 allocation.
 int m2l_tc_row_floats(int p) {
     const int K = (p + 1) * (p + 1);
-    return (K + kKC - 1) / kKC * kKC;
+    return (K + kKC32 - 1) / kKC32 * kKC32;
 }
 
 bool m2l_tc_supported(int p) { return p >= 2 && p <= kMaxP; }
@@ -527,28 +613,34 @@ const char *m2l_tc_encode(Workspace &ws) {
             return "cuTensorMapEncodeTiled is not available";
         encode = reinterpret_cast<EncodeTiled>(fn);
     }
-    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(ws.ms_kp), 2ull * ws.ms_rows};
+    // bf16: ms_rows rows of 2 ms_kp elements; tf32: 2 ms_rows rows (hi, lo) of
+    // ms_kp floats. Rows are ms_kp * 4 bytes either way; boxes are one row
+    // (gather4) of 128 bytes.
+    const bool bf = ws.m2l_bf16;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(bf ? 2 * ws.ms_kp : ws.ms_kp), (bf ? 1ull : 2ull) * ws.ms_rows};
     const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ws.ms_kp) * sizeof(float)};
-    const cuuint32_t box[2] = {static_cast<cuuint32_t>(kKC), 1u};  // gather4 boxes are one row high
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(bf ? 2 * kKC32 : kKC32), 1u};
     const cuuint32_t estr[2] = {1u, 1u};
-    const CUresult r = encode(&ws.tmap_ms, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, ws.ms_tc, dims, strides, box, estr,
-                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS ? nullptr : "cuTensorMapEncodeTiled rejected the split-expansion tensor";
+    const CUresult r = encode(&ws.tmap_ms, bf ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, ws.ms_tc,
+                              dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return "cuTensorMapEncodeTiled rejected the split-expansion tensor";
+    ws.ms_bf16 = bf;
+    return nullptr;
 }
 
 void m2l_pass_tc(Workspace &ws) {
     timer_begin(ws, kTM2L);
     switch (ws.p) {
-        case 2: launch<2>(ws); break;
-        case 3: launch<3>(ws); break;
-        case 4: launch<4>(ws); break;
-        case 5: launch<5>(ws); break;
-        case 6: launch<6>(ws); break;
-        case 7: launch<7>(ws); break;
-        case 8: launch<8>(ws); break;
-        case 9: launch<9>(ws); break;
-        case 10: launch<10>(ws); break;
+        case 2: launch_kind<2>(ws); break;
+        case 3: launch_kind<3>(ws); break;
+        case 4: launch_kind<4>(ws); break;
+        case 5: launch_kind<5>(ws); break;
+        case 6: launch_kind<6>(ws); break;
+        case 7: launch_kind<7>(ws); break;
+        case 8: launch_kind<8>(ws); break;
+        case 9: launch_kind<9>(ws); break;
+        case 10: launch_kind<10>(ws); break;
         default: break;
     }
     timer_end(ws, kTM2L);

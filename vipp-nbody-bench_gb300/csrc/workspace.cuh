@@ -35,6 +35,7 @@ struct Workspace {
     bool mixed = false;
     bool p2p_newton = false;  // one Newton step after the FP32 rsqrt
     bool m2l_tensor = false;  // tcgen05 M2L (mixed precision only)
+    bool m2l_bf16 = false;    // its split: bf16 hi/lo (kind::f16), else 3 x tf32
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;         // near field, concurrent with the far field on st
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -104,10 +105,11 @@ struct Workspace {
     double *ops_d = nullptr;  // [(343+16) K K]
     float *ops_f = nullptr;
     float *bimg = nullptr;    // tensor-core M2L operator images (m2l_tc.cu)
-    float *ms_tc = nullptr;   // tensor-core M2L split expansions [2][ms_rows][ms_kp] (hi, lo)
-    unsigned ms_rows = 0;     // c_cap + 1: the last row of each half is zero
+    float *ms_tc = nullptr;   // tensor-core M2L split expansions, 2 ms_rows ms_kp floats (m2l_tc.cu)
+    unsigned ms_rows = 0;     // c_cap + 1: the last row is zero
     int ms_kp = 0;
-    CUtensorMap tmap_ms{};    // TMA map of ms_tc: 2 ms_rows rows of ms_kp floats
+    bool ms_bf16 = false;     // the split form tmap_ms was encoded for
+    CUtensorMap tmap_ms{};    // TMA map of ms_tc
 
     // device-side info and device-resident counters
     TreeInfo *info = nullptr;

@@ -26,6 +26,7 @@ FLAG_P2P_NEWTON = 1
 FLAG_M2L_CUDA_CORES = 2
 FLAG_SERIAL = 4
 FLAG_NO_GRAPH = 8
+FLAG_M2L_BF16 = 16
 TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
 
 # Every symbol include/vipp_gb300.h declares.

@@ -56,6 +56,10 @@ struct TreeInfo {
     double key_scale[3];  // 2^21 / H: root box -> [0, 2^21) key coordinates
     double key_margin;    // distance (key units) from an integer below which
                           // a key is recomputed by exact midpoint bisection
+    double key_scale32[3];  // key_scale 2^32 and -root_min key_scale 2^32:
+    double key_off32[3];    // fma(x, scale32, off32) = key coordinate 2^32
+    unsigned long long key_mfrac;  // ceil(key_margin 2^32) + 1
+    double root_c[3];     // (root_min + root_max) / 2
     int nsplit_total;     // non-leaf cells
     int ncells;
     int nleaves;

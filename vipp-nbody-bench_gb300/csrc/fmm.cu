@@ -16,6 +16,15 @@
 #ifndef GB_FAR_MIN_BLOCKS
 #define GB_FAR_MIN_BLOCKS 1
 #endif
+// P2M and L2P: 4 resident 128-thread blocks per SM (128 registers, no FP32
+// spills); uncapped they took ~200-240 registers and 2 blocks per SM, 15%
+// slower.
+#ifndef GB_P2M_MIN_BLOCKS
+#define GB_P2M_MIN_BLOCKS 4
+#endif
+#ifndef GB_L2P_MIN_BLOCKS
+#define GB_L2P_MIN_BLOCKS 4
+#endif
 
 namespace gb {
 
@@ -131,13 +140,41 @@ __global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, double *__
     }
 }
 
+// Particle position relative to cell centre c in units of s: FP64 from xs,
+// or (FP32 forms) from the hi/lo pairs re-centred on the cell, which keeps the
+// FP64 pipe out of the per-particle work.
+template <typename T>
+struct CellFrame {
+    double cx, cy, cz, inv_s;
+    RootC cc;
+    float is;
+    __device__ __forceinline__ CellFrame(const double *c_ctr, int c, const TreeInfo *info, double inv_s_) {
+        cx = c_ctr[3 * c], cy = c_ctr[3 * c + 1], cz = c_ctr[3 * c + 2], inv_s = inv_s_;
+        if (sizeof(T) == 4) cc = leaf_centre(c_ctr, c, info), is = static_cast<float>(inv_s_);
+    }
+    __device__ __forceinline__ void at(int j, const double *xs, unsigned n, const float4 *ph, const float4 *pl, T &ux, T &uy,
+                                       T &uz) const {
+        if (sizeof(T) == 4) {
+            const float4 h = ph[j], l = pl[j];
+            ux = static_cast<T>(((h.x - cc.hx) + (l.x - cc.lx)) * is);
+            uy = static_cast<T>(((h.y - cc.hy) + (l.y - cc.ly)) * is);
+            uz = static_cast<T>(((h.z - cc.hz) + (l.z - cc.lz)) * is);
+        } else {
+            ux = static_cast<T>((xs[j] - cx) * inv_s);
+            uy = static_cast<T>((xs[n + j] - cy) * inv_s);
+            uz = static_cast<T>((xs[2 * static_cast<size_t>(n) + j] - cz) * inv_s);
+        }
+    }
+};
+
 // --------------------------------------------------------------------- P2M
 // One warp per leaf at level >= 2: M~_n^m = sum_i m conj(R_n^m((x_i - c)/s)).
 template <int P, typename T>
-__global__ void __launch_bounds__(128, GB_FAR_MIN_BLOCKS) k_p2m(const int *__restrict__ leaves, const unsigned *counts,
+__global__ void __launch_bounds__(128, GB_P2M_MIN_BLOCKS) k_p2m(const int *__restrict__ leaves, const unsigned *counts,
                                              const int *__restrict__ c_begin, const int *__restrict__ c_end,
                                              const int *__restrict__ c_level, const double *__restrict__ c_ctr,
-                                             const double *__restrict__ xs, unsigned n, const TreeInfo *__restrict__ info,
+                                             const double *__restrict__ xs, const float4 *__restrict__ ph,
+                                             const float4 *__restrict__ pl, unsigned n, const TreeInfo *__restrict__ info,
                                              double mass, T *__restrict__ M) {
     constexpr int K = (P + 1) * (P + 1);
     const int lane = threadIdx.x & 31;
@@ -147,16 +184,14 @@ __global__ void __launch_bounds__(128, GB_FAR_MIN_BLOCKS) k_p2m(const int *__res
         const int c = leaves[li];
         const int L = c_level[c];
         if (L < 2) continue;
-        const double inv_s = 1.0 / level_scale(info, L);
-        const double cx = c_ctr[3 * c], cy = c_ctr[3 * c + 1], cz = c_ctr[3 * c + 2];
+        const CellFrame<T> fr(c_ctr, c, info, 1.0 / level_scale(info, L));
         T acc[K];
 #pragma unroll
         for (int r = 0; r < K; ++r) acc[r] = 0;
         const T q = static_cast<T>(mass);
         for (int j = c_begin[c] + lane; j < c_end[c]; j += 32) {
-            const T ux = static_cast<T>((xs[j] - cx) * inv_s);
-            const T uy = static_cast<T>((xs[n + j] - cy) * inv_s);
-            const T uz = static_cast<T>((xs[2 * static_cast<size_t>(n) + j] - cz) * inv_s);
+            T ux, uy, uz;
+            fr.at(j, xs, n, ph, pl, ux, uy, uz);
             for_each_regular<P, T>(ux, uy, uz, [&](int nn, int mm, T re, T im) {
                 acc[ridx(nn, mm, 0)] += q * re;
                 if (mm > 0) acc[ridx(nn, mm, 1)] -= q * im;
@@ -441,10 +476,11 @@ __global__ void __launch_bounds__(256, GB_FAR_MIN_BLOCKS) k_l2l(int Lp, const Tr
 //   a_z        = s^-2 sum_j [ L~_j^0 j R_{j-1}^0 + 2 Re sum_{k>=1} L~_j^k sqrt((j-k)(j+k)) R_{j-1}^k ]
 // so every R_n^q (n <= p-1) meets L~ of degree n+1 and orders q-1, q, q+1.
 template <int P, typename T>
-__global__ void __launch_bounds__(128, GB_FAR_MIN_BLOCKS) k_l2p(const int *__restrict__ leaves, const unsigned *counts,
+__global__ void __launch_bounds__(128, GB_L2P_MIN_BLOCKS) k_l2p(const int *__restrict__ leaves, const unsigned *counts,
                                              const int *__restrict__ c_begin, const int *__restrict__ c_end,
                                              const int *__restrict__ c_level, const double *__restrict__ c_ctr,
-                                             const double *__restrict__ xs, unsigned n, const TreeInfo *__restrict__ info,
+                                             const double *__restrict__ xs, const float4 *__restrict__ ph,
+                                             const float4 *__restrict__ pl, unsigned n, const TreeInfo *__restrict__ info,
                                              const T *__restrict__ Lx, T *__restrict__ far) {
     constexpr int K = (P + 1) * (P + 1);
     __shared__ T Ls[4][K];
@@ -459,13 +495,12 @@ __global__ void __launch_bounds__(128, GB_FAR_MIN_BLOCKS) k_l2p(const int *__res
         for (int r = lane; r < K; r += 32) Ls[w][r] = Lx[static_cast<size_t>(c) * K + r];
         __syncwarp();
         const double s = level_scale(info, L), inv_s = 1.0 / s;
-        const double cx = c_ctr[3 * c], cy = c_ctr[3 * c + 1], cz = c_ctr[3 * c + 2];
+        const CellFrame<T> fr(c_ctr, c, info, inv_s);
         const T sc = static_cast<T>(inv_s * inv_s);
         const T *Lc = Ls[w];
         for (int j = c_begin[c] + lane; j < c_end[c]; j += 32) {
-            const T ux = static_cast<T>((xs[j] - cx) * inv_s);
-            const T uy = static_cast<T>((xs[n + j] - cy) * inv_s);
-            const T uz = static_cast<T>((xs[2 * static_cast<size_t>(n) + j] - cz) * inv_s);
+            T ux, uy, uz;
+            fr.at(j, xs, n, ph, pl, ux, uy, uz);
             T gre = 0, gim = 0, gz = 0;
             for_each_regular<P - 1, T>(ux, uy, uz, [&](int nn, int q, T rr, T ri) {
                 const int jj = nn + 1;
@@ -562,15 +597,15 @@ void launch_l2p_phi(Workspace &ws, double *farphi) {
 template <int P, typename T>
 void launch_p2m(Workspace &ws) {
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));
-    k_p2m<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.n,
-                                       ws.info, ws.m, static_cast<T *>(ws.Mexp));
+    k_p2m<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.ph,
+                                       ws.pl, ws.n, ws.info, ws.m, static_cast<T *>(ws.Mexp));
 }
 
 template <int P, typename T>
 void launch_l2p(Workspace &ws) {
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));
-    k_l2p<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.n,
-                                       ws.info, static_cast<const T *>(ws.Lexp), static_cast<T *>(ws.farf));
+    k_l2p<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.ph,
+                                       ws.pl, ws.n, ws.info, static_cast<const T *>(ws.Lexp), static_cast<T *>(ws.farf));
 }
 
 template <int P, typename T>

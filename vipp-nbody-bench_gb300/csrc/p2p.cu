@@ -35,20 +35,6 @@ namespace {
 
 constexpr int kP2PWarps = 4;
 
-struct RootC {
-    float hx, hy, hz, lx, ly, lz;
-};
-
-__device__ __forceinline__ RootC leaf_centre(const double *c_ctr, int c, const TreeInfo *info) {
-    RootC r;
-    const double d0 = c_ctr[3 * c] - (info->root_min[0] + info->root_max[0]) / 2;
-    const double d1 = c_ctr[3 * c + 1] - (info->root_min[1] + info->root_max[1]) / 2;
-    const double d2 = c_ctr[3 * c + 2] - (info->root_min[2] + info->root_max[2]) / 2;
-    r.hx = static_cast<float>(d0), r.hy = static_cast<float>(d1), r.hz = static_cast<float>(d2);
-    r.lx = static_cast<float>(d0 - r.hx), r.ly = static_cast<float>(d1 - r.hy), r.lz = static_cast<float>(d2 - r.hz);
-    return r;
-}
-
 __device__ __forceinline__ float rsqrt_ftz(float x) {
     float r;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));

@@ -31,19 +31,34 @@ namespace {
 
 constexpr int kTB = 256;
 
+// Order-preserving map of finite doubles to signed integers (an involution):
+// negative values get their magnitude bits flipped, so integer order is the
+// order of the values (-0 just below +0). Min and max then run on the integer
+// pipe instead of GB300's narrow FP64 pipe.
+__device__ __forceinline__ long long ord_key(long long b) { return b ^ ((b >> 63) & 0x7fffffffffffffffLL); }
+
 __global__ void k_bbox_partial(const double *__restrict__ x, unsigned n, double *__restrict__ part, TreeInfo *info) {
-    double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    const long long kmax = ord_key(__double_as_longlong(DBL_MAX)), kmin = ord_key(__double_as_longlong(-DBL_MAX));
+    long long kn[3] = {kmax, kmax, kmax}, kx[3] = {kmin, kmin, kmin};
     bool bad = false;
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const double v = x[static_cast<size_t>(a) * n + i];
-            bad |= !isfinite(v);
-            mn[a] = fmin(mn[a], v);
-            mx[a] = fmax(mx[a], v);
+            const long long b = __double_as_longlong(x[static_cast<size_t>(a) * n + i]);
+            const bool fin = ((b >> 52) & 0x7ff) != 0x7ff;  // non-finite values are skipped, as fmin / fmax do NaN
+            bad |= !fin;
+            const long long k = ord_key(b);
+            if (fin) kn[a] = min(kn[a], k), kx[a] = max(kx[a], k);
         }
     }
     if (bad) atomicOr(&info->err, kDevNonFinite);
+    double mn[3], mx[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        // +-0 compare equal as doubles: either is the box's bound (the padding makes them the same)
+        mn[a] = __longlong_as_double(ord_key(kn[a]));
+        mx[a] = __longlong_as_double(ord_key(kx[a]));
+    }
     __shared__ double red[6][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -105,6 +120,12 @@ __global__ void __launch_bounds__(kTB) k_bbox_final(const double *__restrict__ p
     }
     info->S = S;
     info->key_margin = margin;
+    for (int a = 0; a < 3; ++a) {
+        info->key_scale32[a] = ldexp(info->key_scale[a], 32);
+        info->key_off32[a] = -info->root_min[a] * info->key_scale32[a];
+        info->root_c[a] = (info->root_min[a] + info->root_max[a]) / 2;
+    }
+    info->key_mfrac = static_cast<unsigned long long>(ceil(ldexp(margin, 32))) + 1;
 }
 
 // Spread the 21 low bits of v to every third bit.
@@ -127,18 +148,21 @@ __global__ void k_keys(const double *__restrict__ x, unsigned n, const TreeInfo 
     // Fast path: every split decision of the 21 levels compares x with a
     // midpoint that sits at an integer of u = (x - lo) 2^21 / H up to the
     // rounding bounded by key_margin, so away from integers the child offsets
-    // are the complemented bits of floor(u).
+    // are the complemented bits of floor(u). u is taken in 32.32 fixed point,
+    // q = trunc(fma(x, 2^32 scale, -lo 2^32 scale)): one FMA and one
+    // conversion on the FP64 pipe, the rest integer. The FMA's error (about one
+    // ulp of max|bound| in key units, plus 2^-33) lies well inside key_margin,
+    // which allows 64 such ulps.
     {
-        const double margin = info->key_margin;
-        bool ok = margin < 0.25;
+        const unsigned long long mf = info->key_mfrac;
+        bool ok = info->key_margin < 0.25;
         uint64_t k[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const double u = (p[a] - info->root_min[a]) * info->key_scale[a];
-            const double f = floor(u);
-            const double fr = u - f;
-            ok &= u >= 0.0 && u < 2097152.0 && fr > margin && fr < 1.0 - margin;
-            k[a] = ok ? (~static_cast<uint64_t>(f)) & 0x1fffffull : 0;
+            const long long q = __double2ll_rz(fma(p[a], info->key_scale32[a], info->key_off32[a]));
+            const unsigned long long fr = static_cast<unsigned long long>(q) & 0xffffffffull;
+            ok &= q >= 0 && q < (1LL << 53) && fr > mf && fr < (1ull << 32) - mf;
+            k[a] = ok ? (~static_cast<uint64_t>(q >> 32)) & 0x1fffffull : 0;
         }
         if (ok) {
             keys[i] = spread3(k[0]) | (spread3(k[1]) << 1) | (spread3(k[2]) << 2);
@@ -403,7 +427,7 @@ __global__ void k_gather(const double *__restrict__ x, unsigned n, const unsigne
     for (int a = 0; a < 3; ++a) {
         const double v = x[static_cast<size_t>(a) * n + i];
         xs[static_cast<size_t>(a) * n + j] = v;
-        d[a] = v - (info->root_min[a] + info->root_max[a]) / 2;
+        d[a] = v - info->root_c[a];
     }
     const float hx = static_cast<float>(d[0]), hy = static_cast<float>(d[1]), hz = static_cast<float>(d[2]);
     ph[j] = make_float4(hx, hy, hz, mass_f);

@@ -171,4 +171,23 @@ void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, u
 void timer_begin(Workspace &ws, int cls);
 void timer_end(Workspace &ws, int cls);
 
+#ifdef __CUDACC__
+// Cell centre relative to the root-box centre as an FP32 hi/lo pair, to
+// re-centre the FP32 hi/lo particle positions ph/pl on a cell:
+// (ph - c.h) + (pl - c.l) keeps ~1e-7 of the cell's neighbourhood.
+struct RootC {
+    float hx, hy, hz, lx, ly, lz;
+};
+
+__device__ __forceinline__ RootC leaf_centre(const double *c_ctr, int c, const TreeInfo *info) {
+    RootC r;
+    const double d0 = c_ctr[3 * c] - info->root_c[0];
+    const double d1 = c_ctr[3 * c + 1] - info->root_c[1];
+    const double d2 = c_ctr[3 * c + 2] - info->root_c[2];
+    r.hx = static_cast<float>(d0), r.hy = static_cast<float>(d1), r.hz = static_cast<float>(d2);
+    r.lx = static_cast<float>(d0 - r.hx), r.ly = static_cast<float>(d1 - r.hy), r.lz = static_cast<float>(d2 - r.hz);
+    return r;
+}
+#endif
+
 }  // namespace gb

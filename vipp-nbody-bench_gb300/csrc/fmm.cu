@@ -16,9 +16,9 @@
 #ifndef GB_FAR_MIN_BLOCKS
 #define GB_FAR_MIN_BLOCKS 1
 #endif
-// P2M and L2P: 4 resident 128-thread blocks per SM (128 registers, no FP32
+// FP32 P2M and L2P: 4 resident 128-thread blocks per SM (128 registers, no
 // spills); uncapped they took ~200-240 registers and 2 blocks per SM, 15%
-// slower.
+// slower. The FP64 forms stay uncapped (a cap of 128 spills ~1 KB).
 #ifndef GB_P2M_MIN_BLOCKS
 #define GB_P2M_MIN_BLOCKS 4
 #endif
@@ -170,7 +170,7 @@ struct CellFrame {
 // --------------------------------------------------------------------- P2M
 // One warp per leaf at level >= 2: M~_n^m = sum_i m conj(R_n^m((x_i - c)/s)).
 template <int P, typename T>
-__global__ void __launch_bounds__(128, GB_P2M_MIN_BLOCKS) k_p2m(const int *__restrict__ leaves, const unsigned *counts,
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_P2M_MIN_BLOCKS : GB_FAR_MIN_BLOCKS) k_p2m(const int *__restrict__ leaves, const unsigned *counts,
                                              const int *__restrict__ c_begin, const int *__restrict__ c_end,
                                              const int *__restrict__ c_level, const double *__restrict__ c_ctr,
                                              const double *__restrict__ xs, const float4 *__restrict__ ph,
@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(256, GB_FAR_MIN_BLOCKS) k_l2l(int Lp, const Tr
 //   a_z        = s^-2 sum_j [ L~_j^0 j R_{j-1}^0 + 2 Re sum_{k>=1} L~_j^k sqrt((j-k)(j+k)) R_{j-1}^k ]
 // so every R_n^q (n <= p-1) meets L~ of degree n+1 and orders q-1, q, q+1.
 template <int P, typename T>
-__global__ void __launch_bounds__(128, GB_L2P_MIN_BLOCKS) k_l2p(const int *__restrict__ leaves, const unsigned *counts,
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_L2P_MIN_BLOCKS : GB_FAR_MIN_BLOCKS) k_l2p(const int *__restrict__ leaves, const unsigned *counts,
                                              const int *__restrict__ c_begin, const int *__restrict__ c_end,
                                              const int *__restrict__ c_level, const double *__restrict__ c_ctr,
                                              const double *__restrict__ xs, const float4 *__restrict__ ph,

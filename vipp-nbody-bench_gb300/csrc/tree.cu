@@ -259,30 +259,45 @@ __device__ unsigned lower_bound_pre(const uint64_t *keys, unsigned lo, unsigned 
     return lo;
 }
 
+// One warp: lane L finds level L's split entries (ent is sorted by level),
+// then the cell counts and starts of every level follow by a warp scan.
 __global__ void k_level_table(const uint64_t *__restrict__ ent, unsigned *counts, TreeInfo *info, unsigned n) {
-    if (threadIdx.x != 0) return;
+    static_assert(kMaxLevel + 2 <= 32, "one lane per level");
+    const int L = static_cast<int>(threadIdx.x);
+    if (L >= 32) return;
     const unsigned S = counts[1];
-    int start = 0, depth = 0;
-    info->level_count[0] = 1;
-    for (int L = 0; L <= kMaxLevel; ++L) {
+    unsigned split = 0;
+    if (L <= kMaxLevel) {
         const unsigned a = lower_bound_ent(ent, 0, S, static_cast<uint64_t>(L) << 32);
         const unsigned b = lower_bound_ent(ent, 0, S, static_cast<uint64_t>(L + 1) << 32);
         info->split_start[L] = static_cast<int>(a);
         info->split_count[L] = static_cast<int>(b - a);
-        if (L + 1 <= kMaxLevel + 1) info->level_count[L + 1] = 8 * static_cast<int>(b - a);
+        split = b - a;
     }
-    for (int L = 0; L <= kMaxLevel + 1; ++L) {
-        info->level_start[L] = start;
-        start += info->level_count[L];
-        if (info->level_count[L] > 0) depth = L;
+    // cells of level L: 1 at the root, 8 per split cell of level L - 1
+    const unsigned below = __shfl_up_sync(0xffffffffu, split, 1);
+    const bool lv = L <= kMaxLevel + 1;
+    const int cnt = !lv ? 0 : (L == 0 ? 1 : 8 * static_cast<int>(below));
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (L >= o) incl += y;
     }
-    info->ncells = start;
-    info->nsplit_total = static_cast<int>(S);
-    info->nleaves = start - static_cast<int>(S);
-    info->depth = depth;
-    info->n_targets_m2l = depth >= 2 ? start - info->level_start[2] : 0;
-    counts[2] = static_cast<unsigned>(start);
-    counts[3] = static_cast<unsigned>(start) - S;
+    if (lv) info->level_count[L] = cnt, info->level_start[L] = incl - cnt;
+    const int start = __shfl_sync(0xffffffffu, incl, kMaxLevel + 1);  // all cells
+    const int start2 = __shfl_sync(0xffffffffu, incl - cnt, 2);
+    const unsigned nonempty = __ballot_sync(0xffffffffu, lv && cnt > 0);
+    if (L == 0) {
+        const int depth = 31 - __clz(static_cast<int>(nonempty));
+        info->ncells = start;
+        info->nsplit_total = static_cast<int>(S);
+        info->nleaves = start - static_cast<int>(S);
+        info->depth = depth;
+        info->n_targets_m2l = depth >= 2 ? start - start2 : 0;
+        counts[2] = static_cast<unsigned>(start);
+        counts[3] = static_cast<unsigned>(start) - S;
+    }
     (void)n;
 }
 
@@ -332,12 +347,17 @@ __global__ void k_root(unsigned n, int T, const TreeInfo *__restrict__ info, int
     }
 }
 
+// One thread per (split cell, child octant): the 8 threads of a split cell
+// find its number and particle range (the same searches, in one warp), then
+// each its child's range, links and geometry.
 __global__ void k_cells(const uint64_t *__restrict__ ent, const unsigned *counts, const uint64_t *__restrict__ keys,
                         unsigned n, int T, const TreeInfo *__restrict__ info, int *split_cell, int *c_begin, int *c_end,
                         int *c_parent, int *c_child, int *c_level, uint64_t *c_path, int *c_coord, double *c_box,
                         double *c_ctr) {
     const unsigned S = counts[1];
-    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < S; e += gridDim.x * blockDim.x) {
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < 8u * S; t += gridDim.x * blockDim.x) {
+        const unsigned e = t >> 3;
+        const int o = static_cast<int>(t & 7u);
         const int L = static_cast<int>(ent[e] >> 32);
         const unsigned i = static_cast<unsigned>(ent[e] & 0xffffffffu);
         const unsigned r = e - static_cast<unsigned>(info->split_start[L]);
@@ -352,15 +372,17 @@ __global__ void k_cells(const uint64_t *__restrict__ ent, const unsigned *counts
             const unsigned rp = lower_bound_ent(ent, a, b, (static_cast<uint64_t>(L - 1) << 32) | ip) - a;
             own = info->level_start[L] + 8 * static_cast<int>(rp) + static_cast<int>(pre & 7u);
         }
-        split_cell[e] = own;
+        if (o == 0) split_cell[e] = own;
         const unsigned pe = L == 0 ? n : lower_bound_pre(keys, i + 1, n, sh, pre + 1);
         const int shc = path_shift(L + 1);
         const unsigned a1 = static_cast<unsigned>(info->split_start[L + 1]);
         const unsigned b1 = a1 + static_cast<unsigned>(info->split_count[L + 1]);
-        unsigned cb = i;
-        for (int o = 0; o < 8; ++o) {
+        {
+            // [i, pe) is sorted on the child prefix, so each child's bounds are
+            // lower bounds over the whole range
             const uint64_t cpath = (pre << 3) | static_cast<uint64_t>(o);
-            const unsigned ce = o == 7 ? pe : lower_bound_pre(keys, cb, pe, shc, cpath + 1);
+            const unsigned cb = o == 0 ? i : lower_bound_pre(keys, i, pe, shc, cpath);
+            const unsigned ce = o == 7 ? pe : lower_bound_pre(keys, i, pe, shc, cpath + 1);
             const int c = info->level_start[L + 1] + 8 * static_cast<int>(r) + o;
             c_begin[c] = static_cast<int>(cb);
             c_end[c] = static_cast<int>(ce);
@@ -375,7 +397,6 @@ __global__ void k_cells(const uint64_t *__restrict__ ent, const unsigned *counts
             c_child[c] = fc;
             path_geometry(cpath, L + 1, info, c_box + 6 * static_cast<size_t>(c), c_ctr + 3 * static_cast<size_t>(c),
                           c_coord + 3 * static_cast<size_t>(c));
-            cb = ce;
         }
     }
 }
@@ -396,23 +417,25 @@ __global__ void k_leaf_compact(const unsigned *__restrict__ flag, const unsigned
 // index (octree.hpp:143-145). Rank sort of each leaf's permutation slice.
 __global__ void k_leaf_sort(const int *__restrict__ leaves, const unsigned *counts, const int *__restrict__ c_begin,
                             const int *__restrict__ c_end, int T, unsigned *perm) {
-    extern __shared__ unsigned sh[];
+    extern __shared__ unsigned sh[];  // per warp: 2 (T + 1)
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned *in = sh + static_cast<size_t>(w) * 2 * (T + 1), *out = in + (T + 1);
     const unsigned NL = counts[3];
-    for (unsigned li = blockIdx.x; li < NL; li += gridDim.x) {
+    for (unsigned li = blockIdx.x * nw + w; li < NL; li += gridDim.x * nw) {  // a warp per leaf
         const int c = leaves[li];
         const int b = c_begin[c], e = c_end[c], len = e - b;
-        if (len < 2 || len > T) continue;  // uniform per block
-        for (int k = threadIdx.x; k < len; k += blockDim.x) sh[k] = perm[b + k];
-        __syncthreads();
-        for (int k = threadIdx.x; k < len; k += blockDim.x) {
-            const unsigned v = sh[k];
+        if (len < 2 || len > T) continue;  // uniform per warp
+        for (int k = lane; k < len; k += 32) in[k] = perm[b + k];
+        __syncwarp();
+        for (int k = lane; k < len; k += 32) {
+            const unsigned v = in[k];
             int rank = 0;
-            for (int q = 0; q < len; ++q) rank += sh[q] < v;
-            sh[T + 1 + rank] = v;
+            for (int q = 0; q < len; ++q) rank += in[q] < v;
+            out[rank] = v;
         }
-        __syncthreads();
-        for (int k = threadIdx.x; k < len; k += blockDim.x) perm[b + k] = sh[T + 1 + k];
-        __syncthreads();
+        __syncwarp();
+        for (int k = lane; k < len; k += 32) perm[b + k] = out[k];
+        __syncwarp();
     }
 }
 
@@ -686,13 +709,20 @@ void build_tree(Workspace &ws) {
     k_root<<<1, 32, 0, st>>>(n, ws.T, ws.info, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path,
                              ws.c_coord, ws.c_box, ws.c_ctr, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt);
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 4, ceil_div(ws.c_cap, 32));
-    k_cells<<<gs, 128, 0, st>>>(ws.ent, ws.d_counts, ws.keys, n, ws.T, ws.info, ws.split_cell, ws.c_begin, ws.c_end,
+    k_cells<<<capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 128)), 128, 0, st>>>(ws.ent, ws.d_counts, ws.keys, n, ws.T, ws.info, ws.split_cell, ws.c_begin, ws.c_end,
                                 ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr);
     k_leaf_flags<<<gs, kTB, 0, st>>>(ws.c_child, ws.d_counts, ws.flag);
     scan_exclusive_u32(ws.flag, ws.flag_off, ws.c_cap, ws.d_counts + 2, nullptr, ws.scan, st, &ws.launches);
     k_leaf_compact<<<gs, kTB, 0, st>>>(ws.flag, ws.flag_off, ws.d_counts, ws.leaves);
-    const size_t smem = sizeof(unsigned) * (2 * static_cast<size_t>(ws.T) + 2);
-    k_leaf_sort<<<gs * 2, 128, smem, st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.T, ws.perm);
+    {
+        // a warp per leaf, up to 4 warps per block within 48 KB of shared memory
+        const size_t per_warp = sizeof(unsigned) * 2 * (static_cast<size_t>(ws.T) + 1);
+        const int nw = static_cast<int>(std::max<size_t>(1, std::min<size_t>(4, 49152 / per_warp)));
+        const size_t smem = per_warp * nw;
+        if (smem > 49152) cudaFuncSetAttribute(k_leaf_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        k_leaf_sort<<<capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4)), 32 * nw, smem, st>>>(
+            ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.T, ws.perm);
+    }
     k_gather<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.perm, ws.info, static_cast<float>(ws.m), ws.xs, ws.ph, ws.pl);
     k_lists<<<gs, 256, 0, st>>>(ws.ent, ws.d_counts, ws.split_cell, ws.info, ws.c_child, ws.c_path, ws.c_coord,
                                 ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,

@@ -336,11 +336,13 @@ void evaluate(gb_ctx *ctx) {
     // Near field on the second stream, unless serial or timed: class timers
     // measure each class alone on one stream.
     const bool fork = !ws.serial && !ws.timing;
+    gb::p2p_reset(ws);
+    const unsigned conc = gb::p2p_blocks_per_sm(true), full = gb::p2p_blocks_per_sm(false);
     if (fork) {
         cudaEventRecord(ws.ev_fork, ws.st);
         cudaStreamWaitEvent(ws.st2, ws.ev_fork, 0);
         std::swap(ws.st, ws.st2);  // the stages launch on ws.st
-        gb::p2p_pass(ws);
+        gb::p2p_pass(ws, conc);
         std::swap(ws.st, ws.st2);
         cudaEventRecord(ws.ev_join, ws.st2);
     }
@@ -351,10 +353,14 @@ void evaluate(gb_ctx *ctx) {
     else
         gb::m2l_pass(ws);
     gb::downward_pass(ws);
-    if (!fork)
-        gb::p2p_pass(ws);
-    else
+    if (!fork) {
+        gb::p2p_pass(ws, full);
+    } else {
+        // more P2P blocks on the SMs the far field leaves, draining the same queue
+        gb::p2p_pass(ws, full > conc ? full - conc : 0u);
         cudaStreamWaitEvent(ws.st, ws.ev_join, 0);
+    }
+    gb::p2p_finish(ws);
     gb::finalize_accel(ws, ws.acc);
 }
 

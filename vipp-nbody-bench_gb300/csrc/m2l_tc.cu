@@ -82,6 +82,9 @@ constexpr int kDrainThreads = 128;  // warps 0-3
 #ifndef M2L_WIDE_B
 #define M2L_WIDE_B 1
 #endif
+#ifndef M2L_TMEM_TOTAL
+#define M2L_TMEM_TOTAL 1  // drain keeps a tile's running sums in free TMEM columns, not registers
+#endif
 constexpr int kLoaderWarps = M2L_LOADER_WARPS;  // warps 4 .. 3 + kLoaderWarps
 constexpr int kMmaWarp = 4 + kLoaderWarps;
 constexpr int kThreads = 32 * (kMmaWarp + 1);
@@ -106,7 +109,16 @@ struct TcCfg {
     // by the drain), so the hi and lo operator blocks are adjacent in the stage.
     static constexpr int DCOLS = (BF || M2L_WIDE_B) ? 2 * N : N;
     static constexpr int ACOL = DCOLS <= 32 ? 32 : (DCOLS <= 64 ? 64 : (DCOLS <= 128 ? 128 : 256));
-    static constexpr int TMEM_COLS = 2 * ACOL;
+    // The tile's running sums (NCH chunks of 32 columns) stay in TMEM when
+    // columns are free: after both accumulators, or in the gaps behind them.
+    static constexpr int NCH = (N + 31) / 32;
+    static constexpr bool TOT_AFTER = 2 * ACOL + 32 * NCH <= 512;
+    static constexpr int GAPCH = (ACOL - DCOLS) / 32;
+    static constexpr bool TOTAL_TMEM = M2L_TMEM_TOTAL && (TOT_AFTER || 2 * GAPCH >= NCH);
+    static constexpr int TMEM_COLS = TOTAL_TMEM ? 512 : 2 * ACOL;
+    static constexpr uint32_t tcol(int k) {
+        return static_cast<uint32_t>(TOT_AFTER ? 2 * ACOL + 32 * k : (k < GAPCH ? DCOLS + 32 * k : ACOL + DCOLS + 32 * (k - GAPCH)));
+    }
     static constexpr int A_BYTES = kRows * 128;          // one A tile: 16 KB
     static constexpr int B_BYTES = N * 128;              // one of Bhi / Blo
     static constexpr int STAGE = NA * A_BYTES + 2 * B_BYTES;
@@ -236,6 +248,21 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float *v) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
+        "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+        "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+        "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15])),
+        "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])), "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])),
+        "r"(__float_as_uint(v[20])), "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
+        "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])), "r"(__float_as_uint(v[27])),
+        "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])), "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+        : "memory");
 }
 
 // Slot s of a target with octant cls maps to same-level offset 2d + u(o') - u(cls);
@@ -427,6 +454,53 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
         // ----------------------------------------------------------------- drain
         unsigned groups = 0;
         bool stop = false;
+        const uint32_t lanes = tmem + (static_cast<uint32_t>(32 * warp) << 16);  // TMEM lanes 32 warp .. + 31
+        if (C::TOTAL_TMEM) {
+            // running sums in TMEM (columns tcol(k)), added in the same order as
+            // the register form below: total, then each half of the group
+            for (int w = blockIdx.x; w < ntiles && !stop; w += gridDim.x) {
+                const int cls = w % 8, t0 = (w / 8) * kRows;
+                for (int gi = 0; gi < kGroupsPerTile; ++gi, ++groups) {
+                    if (!__all_sync(0xffffffffu, mbar_wait(accum + (groups & 1), (groups >> 1) & 1, abort_flag))) {
+                        stop = true;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t col = (groups & 1) * C::ACOL;
+#pragma unroll 1
+                    for (int k = 0; k < C::NCH; ++k) {
+                        float sum[32], v[32];
+                        if (gi > 0) {
+                            tmem_ld32(lanes + C::tcol(k), sum);
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < 32; ++i) sum[i] = 0.f;
+                        }
+#pragma unroll
+                        for (int h = 0; h < C::DCOLS / C::N; ++h) {
+                            tmem_ld32(lanes + col + static_cast<uint32_t>(h * C::N + 32 * k), v);
+#pragma unroll
+                            for (int i = 0; i < 32; ++i) sum[i] += v[i];
+                        }
+                        tmem_st32(lanes + C::tcol(k), sum);
+                    }
+                    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    mbar_arrive(tfree + (groups & 1));
+                }
+                if (stop) break;
+                const int t = t0 + tid;
+                float *out = Lx + static_cast<size_t>(base + cls + 8 * t) * C::K;
+#pragma unroll 1
+                for (int k = 0; k < C::NCH; ++k) {
+                    float sum[32];
+                    tmem_ld32(lanes + C::tcol(k), sum);  // all lanes: the load is warp-collective
+#pragma unroll
+                    for (int i = 0; i < 32; ++i)
+                        if (t < per_class && 32 * k + i < C::K) out[32 * k + i] = sum[i];
+                }
+            }
+        } else {
         float acc[C::N];
         for (int w = blockIdx.x; w < ntiles && !stop; w += gridDim.x) {
             const int cls = w % 8, t0 = (w / 8) * kRows;
@@ -458,6 +532,7 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                 float *out = Lx + static_cast<size_t>(base + cls + 8 * t) * C::K;
                 for (int r = 0; r < C::K; ++r) out[r] = acc[r];
             }
+        }
         }
     }
     // Orderly exit: every wait above is bounded, so all threads get here.

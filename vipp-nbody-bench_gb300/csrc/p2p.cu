@@ -28,6 +28,9 @@
 #ifndef GB_P2P_BLOCKS_PER_SM
 #define GB_P2P_BLOCKS_PER_SM 8
 #endif
+#ifndef GB_P2P_CONCURRENT_PER_SM
+#define GB_P2P_CONCURRENT_PER_SM 8  // blocks per SM of the P2P launch beside the far field
+#endif
 
 namespace gb {
 
@@ -404,7 +407,16 @@ void near_potential(Workspace &ws, double *phiv) {
     ws.launches += 2;
 }
 
-void p2p_pass(Workspace &ws) {
+// Near-field kernel over the work queue, `per_sm` blocks per SM. The queue
+// counter is reset by p2p_reset; several launches (on any streams) may drain
+// the same queue, each item is taken once. p2p_finish adds the slices of
+// split items after all of them.
+void p2p_reset(Workspace &ws) { cudaMemsetAsync(ws.queue, 0, sizeof(unsigned), ws.st); }
+
+unsigned p2p_blocks_per_sm(bool concurrent) { return concurrent ? GB_P2P_CONCURRENT_PER_SM : GB_P2P_BLOCKS_PER_SM; }
+
+void p2p_pass(Workspace &ws, unsigned per_sm) {
+    if (per_sm == 0) return;
     timer_begin(ws, kTP2P);
 #if GB_P2P_CARVEOUT_MAX
     // keep the SMs that run P2P configured for full shared memory, so far-field
@@ -414,10 +426,7 @@ void p2p_pass(Workspace &ws) {
     cudaFuncSetAttribute(k_p2p_f32<true, true>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(k_p2p_f32<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
 #endif
-    cudaMemsetAsync(ws.queue, 0, sizeof(unsigned), ws.st);
-    // Blocks per SM of the persistent P2P kernels. The P2P kernels run
-    // concurrently with the far field, so they should leave room on each SM.
-    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * GB_P2P_BLOCKS_PER_SM, ceil_div(ws.n, 128));
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * per_sm, ceil_div(ws.n, 128));
     const bool soft = ws.eps > 0;
     if (ws.mixed) {
         const float eps2 = static_cast<float>(ws.eps * ws.eps);
@@ -440,7 +449,6 @@ void p2p_pass(Workspace &ws) {
                 GB_P2P32(false, false);
         }
 #undef GB_P2P32
-        k_p2p_combine<float><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, pf, Gm, o, ws.n);
     } else {
         const double Gm = ws.G * ws.m, eps2 = ws.eps * ws.eps;
         auto *o = static_cast<double *>(ws.nearf);
@@ -451,10 +459,20 @@ void p2p_pass(Workspace &ws) {
         else
             k_p2p_f64<false><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.rng_off, ws.rng_len,
                                                                ws.ranges, ws.xs, ws.src_total, pd, Gm, eps2, o, ws.n);
-        k_p2p_combine<double><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, pd, Gm, o, ws.n);
     }
-    ws.launches += 2;
+    ws.launches += 1;
     timer_end(ws, kTP2P);
+}
+
+void p2p_finish(Workspace &ws) {
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * GB_P2P_BLOCKS_PER_SM, ceil_div(ws.n, 128));
+    if (ws.mixed)
+        k_p2p_combine<float><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, static_cast<const float *>(ws.part),
+                                                    static_cast<float>(ws.G * ws.m), static_cast<float *>(ws.nearf), ws.n);
+    else
+        k_p2p_combine<double><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, static_cast<const double *>(ws.part), ws.G * ws.m,
+                                                     static_cast<double *>(ws.nearf), ws.n);
+    ws.launches += 1;
 }
 
 void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, unsigned nt, double *out_soa,

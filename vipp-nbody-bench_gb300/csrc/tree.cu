@@ -464,6 +464,7 @@ __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts
                         const uint64_t *__restrict__ c_path, const int *__restrict__ c_coord, int *m2l_src, int *p2p_own,
                         int *p2p_cnt, int *coll, int *coll_cnt, unsigned long long *m2l_pairs) {
     __shared__ int nb[8][32], ord[8][32], nord[8];
+    __shared__ int uch[8][27 * 8];  // per neighbour (in order) and octant: child u, or ~u if u is a leaf
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned S = counts[1];
     const unsigned warps = gridDim.x * (blockDim.x >> 5);
@@ -517,6 +518,12 @@ __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts
         // every child's 216 M2L slots start empty
         for (int k = lane; k < 8 * kM2LSlots; k += 32) m2l_src[static_cast<size_t>(fcP + k / kM2LSlots) * kM2LSlots + k % kM2LSlots] = -1;
         __syncwarp();
+        // the neighbours' children, loaded once by the whole warp
+        for (int idx = lane; idx < 8 * nord[w]; idx += 32) {
+            const int u = c_child[nb[w][ord[w][idx >> 3]]] + (idx & 7);
+            uch[w][idx] = c_child[u] >= 0 ? u : ~u;
+        }
+        __syncwarp();
         if (lane < 8) {
             const int c = fcP + lane;
             const int uc[3] = {1 - (lane & 1), 1 - ((lane >> 1) & 1), 1 - ((lane >> 2) & 1)};
@@ -525,11 +532,11 @@ __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts
             unsigned nm2l = 0;
             for (int k = 0; k < nord[w]; ++k) {
                 const int dd = ord[w][k];
-                const int Q = nb[w][dd];
-                const int fq = c_child[Q];
                 const int d[3] = {dd % 3 - 1, (dd / 3) % 3 - 1, dd / 9 - 1};
                 for (int o = 0; o < 8; ++o) {
-                    const int u = fq + o;
+                    const int code = uch[w][8 * k + o];
+                    const int u = code >= 0 ? code : ~code;
+                    const bool usplit = code >= 0;
                     const int uo[3] = {1 - (o & 1), 1 - ((o >> 1) & 1), 1 - ((o >> 2) & 1)};
                     bool adj = true;
 #pragma unroll
@@ -538,7 +545,7 @@ __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts
                         adj &= off >= -1 && off <= 1;
                     }
                     if (adj) {
-                        if (!cleaf && c_child[u] >= 0)
+                        if (!cleaf && usplit)
                             coll[static_cast<size_t>(c) * kNbrCap + ncoll++] = u;
                         else
                             p2p_own[static_cast<size_t>(c) * kNbrCap + np2p++] = u;

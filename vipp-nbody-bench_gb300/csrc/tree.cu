@@ -468,6 +468,7 @@ __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned S = counts[1];
     const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    unsigned long long pairs = 0;  // M2L pairs of this lane's cells, added once per warp below
     for (unsigned e = blockIdx.x * (blockDim.x >> 5) + w; e < S; e += warps) {
         const int L = static_cast<int>(ent[e] >> 32);
         const int P = split_cell[e];
@@ -557,10 +558,14 @@ __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts
             }
             coll_cnt[c] = ncoll;
             p2p_cnt[c] = np2p;
-            if (L + 1 >= 2 && nm2l) atomicAdd(m2l_pairs, static_cast<unsigned long long>(nm2l));
+            if (L + 1 >= 2) pairs += nm2l;
         }
         __syncwarp();
     }
+    // one atomic per warp: the same counter from every cell serialised the kernel
+#pragma unroll
+    for (int o = 16; o; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    if (lane == 0 && pairs) atomicAdd(m2l_pairs, pairs);
 }
 
 // Near-field source ranges of every leaf: the own-p2p entries of its
@@ -600,6 +605,7 @@ __global__ void k_rng_fill(const int *__restrict__ leaves, const unsigned *count
                            const unsigned *__restrict__ chunk_off, int4 *chunks, const unsigned *__restrict__ src_total,
                            const unsigned *__restrict__ part_off, unsigned part_cap, TreeInfo *info) {
     const unsigned NL = counts[3];
+    unsigned long long pairs = 0, nranges = 0;  // this thread's totals, added once per warp below
     for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < NL; li += gridDim.x * blockDim.x) {
         const int c = leaves[li];
         const int b = c_begin[c], e = c_end[c];
@@ -663,8 +669,18 @@ __global__ void k_rng_fill(const int *__restrict__ leaves, const unsigned *count
             }
         }
         if (overflow) atomicOr(&info->err, kDevCapacity);
-        atomicAdd(reinterpret_cast<unsigned long long *>(&info->p2p_pairs), static_cast<unsigned long long>(e - b) * srcs);
-        atomicAdd(reinterpret_cast<unsigned long long *>(&info->p2p_ranges), static_cast<unsigned long long>(k));
+        pairs += static_cast<unsigned long long>(e - b) * srcs;
+        nranges += k;
+    }
+    // one atomic per warp and counter (per-leaf atomics on two addresses serialised the kernel)
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+        nranges += __shfl_xor_sync(0xffffffffu, nranges, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (pairs) atomicAdd(reinterpret_cast<unsigned long long *>(&info->p2p_pairs), pairs);
+        if (nranges) atomicAdd(reinterpret_cast<unsigned long long *>(&info->p2p_ranges), nranges);
     }
 }
 

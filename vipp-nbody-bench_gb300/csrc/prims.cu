@@ -1,10 +1,17 @@
 // Exclusive scan and stable LSD radix sort (8-bit digits).
 //
-// Radix pass = histogram per 4096-key tile, one exclusive scan of the
-// digit-major histogram (giving every (digit, tile) its output base), then a
-// scatter in which each warp ranks its keys with __match_any_sync so equal
-// digits keep their input order (stability is what preserves the reference's
-// ascending-index order among particles with equal keys).
+// Radix sort, one launch per pass after one histogram launch for all passes
+// (single-sweep LSD sort with decoupled look-back): every block takes the next
+// 4096-key tile from an atomic ticket, ranks its keys by digit (each warp with
+// __match_any_sync, so equal digits keep their input order: stability is what
+// preserves the reference's ascending-index order among particles with equal
+// keys), publishes its per-digit counts, and finds the keys of its digits in
+// all earlier tiles by looking back over their published counts. A tile waits
+// only on tiles whose blocks have already started (tickets are taken in
+// order) and that publish their counts before they look back themselves, so
+// every wait ends; it is bounded all the same (kSpinMax polls, then an error
+// bit and an orderly finish). The tile is then staged in shared memory in
+// digit order and written out in coalesced runs.
 #include "prims.cuh"
 
 namespace gb {
@@ -142,43 +149,58 @@ __global__ void k_scan_apply(const unsigned *__restrict__ in, unsigned *__restri
     }
 }
 
-__global__ void k_radix_hist(const uint64_t *__restrict__ keys, unsigned n_cap, const unsigned *d_n, int bit,
-                             unsigned *__restrict__ hist, unsigned ntiles_cap) {
-    __shared__ unsigned cnt[256];
+constexpr unsigned long long kAggregate = 1ull << 32;  // status word: count of the tile's own keys
+constexpr unsigned long long kInclusive = 2ull << 32;  // count of keys in this and all earlier tiles
+constexpr unsigned kSpinMax = 1u << 24;
+
+// Digit counts of all passes in one read of the keys: ghist[p][d].
+__global__ void k_sweep_hist(const uint64_t *__restrict__ keys, unsigned n_cap, const unsigned *d_n, int bit_lo, int npasses,
+                             unsigned *__restrict__ ghist) {
+    __shared__ unsigned cnt[kMaxPasses][256];
     const unsigned n = d_n ? *d_n : n_cap;
-    cnt[threadIdx.x] = 0;
+    for (int k = threadIdx.x; k < kMaxPasses * 256; k += blockDim.x) (&cnt[0][0])[k] = 0;
     __syncthreads();
-    const unsigned base = blockIdx.x * kSortTile;
     const int lane = threadIdx.x & 31;
-    for (int k = 0; k < kSortTile / 256; ++k) {
-        const unsigned i = base + k * 256 + threadIdx.x;
-        const unsigned d = i < n ? static_cast<unsigned>((keys[i] >> bit) & 0xffu) : 256u;
-        const unsigned peers = __match_any_sync(kFull, d);
-        if (d < 256u && lane == __ffs(peers) - 1) atomicAdd(&cnt[d], __popc(peers));
+    // whole warps step together so that every lane takes part in __match_any_sync
+    for (unsigned i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const unsigned i = i0 + threadIdx.x;
+        const uint64_t key = i < n ? keys[i] : 0ull;
+        for (int p = 0; p < npasses; ++p) {
+            const unsigned d = i < n ? static_cast<unsigned>((key >> (bit_lo + 8 * p)) & 0xffu) : 256u;
+            const unsigned peers = __match_any_sync(kFull, d);
+            if (d < 256u && lane == __ffs(peers) - 1) atomicAdd(&cnt[p][d], __popc(peers));
+        }
     }
     __syncthreads();
-    hist[threadIdx.x * ntiles_cap + blockIdx.x] = cnt[threadIdx.x];
+    for (int k = threadIdx.x; k < npasses * 256; k += blockDim.x)
+        if ((&cnt[0][0])[k]) atomicAdd(&ghist[k], (&cnt[0][0])[k]);
 }
 
 constexpr size_t kScatterSmem = sizeof(uint64_t) * kSortTile + sizeof(unsigned) * kSortTile;  // 48 KB
 
-__global__ void __launch_bounds__(256) k_radix_scatter(const uint64_t *__restrict__ kin, const unsigned *__restrict__ vin,
-                                                       uint64_t *__restrict__ kout, unsigned *__restrict__ vout,
-                                                       unsigned n_cap, const unsigned *d_n, int bit,
-                                                       const unsigned *__restrict__ hist, unsigned ntiles_cap) {
+// One pass over bits [bit, bit + 8): ghist = this pass's digit counts, status
+// = tiles x 256 zeroed look-back words, ticket = zeroed tile counter.
+__global__ void __launch_bounds__(256) k_sweep(const uint64_t *__restrict__ kin, const unsigned *__restrict__ vin,
+                                               uint64_t *__restrict__ kout, unsigned *__restrict__ vout, unsigned n_cap,
+                                               const unsigned *d_n, int bit, const unsigned *__restrict__ ghist,
+                                               unsigned long long *status, unsigned *ticket, int *d_err, int err_bit) {
     constexpr int kRounds = kSortTile / 256;  // 16
     __shared__ unsigned wcnt[8][256];
     __shared__ unsigned dstart[256];  // first tile-local position of each digit
+    __shared__ unsigned dbase[256];   // first output position of the tile's keys of each digit
     __shared__ unsigned wsum[8];
+    __shared__ unsigned s_tile;
     extern __shared__ __align__(16) unsigned char stage_raw[];  // the tile in digit order
     uint64_t *skey = reinterpret_cast<uint64_t *>(stage_raw);
     unsigned *sval = reinterpret_cast<unsigned *>(skey + kSortTile);
     const unsigned n = d_n ? *d_n : n_cap;
-    const unsigned base = blockIdx.x * kSortTile;
-    if (base >= n) return;  // uniform
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int d = threadIdx.x; d < 8 * 256; d += 256) (&wcnt[0][0])[d] = 0;
     __syncthreads();
+    const unsigned tile = s_tile;
+    const unsigned base = tile * kSortTile;
+    if (base >= n) return;  // uniform; no later tile looks back at it
     uint64_t key[kRounds];
     unsigned val[kRounds], rank[kRounds], dig[kRounds];
     const unsigned lt = lanemask_lt();
@@ -207,18 +229,45 @@ __global__ void __launch_bounds__(256) k_radix_scatter(const uint64_t *__restric
             wcnt[ww][d] = run;
             run += c;
         }
-        // exclusive scan of the tile's digit totals (thread d holds digit d)
-        unsigned incl = run;
+        // publish this tile's count of digit d, then add up the earlier tiles'
+        volatile unsigned long long *sw = status + static_cast<size_t>(tile) * 256 + d;
+        *sw = (tile == 0 ? kInclusive : kAggregate) | run;
+        __threadfence();
+        unsigned long long before = 0;
+        if (tile > 0) {
+            unsigned spins = 0;
+            for (long long tt = static_cast<long long>(tile) - 1; tt >= 0;) {
+                const unsigned long long v = *(volatile unsigned long long *)(status + static_cast<size_t>(tt) * 256 + d);
+                if ((v >> 32) == 0) {
+                    if (++spins > kSpinMax) {
+                        if (d_err) atomicOr(d_err, err_bit);
+                        break;
+                    }
+                    continue;
+                }
+                before += v & 0xffffffffull;
+                if ((v >> 32) == (kInclusive >> 32)) break;
+                --tt;
+            }
+            *sw = kInclusive | (before + run);
+            __threadfence();
+        }
+        // exclusive scan of the digit totals: the pass's global digit bases
+        // (ghist) and the tile's local digit starts (run)
+        const unsigned g = ghist[d];
+        unsigned gi = g, incl = run;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const unsigned u = __shfl_up_sync(kFull, incl, o);
-            if (lane >= o) incl += u;
+            const unsigned u = __shfl_up_sync(kFull, incl, o), ug = __shfl_up_sync(kFull, gi, o);
+            if (lane >= o) incl += u, gi += ug;
         }
-        if (lane == 31) wsum[w] = incl;
+        if (lane == 31) wsum[w] = incl, dbase[w] = gi;  // dbase[0..7] as scratch for the warps' ghist totals
         __syncthreads();
-        unsigned wofs = 0;
-        for (int ww = 0; ww < w; ++ww) wofs += wsum[ww];
+        unsigned wofs = 0, gofs = 0;
+        for (int ww = 0; ww < w; ++ww) wofs += wsum[ww], gofs += dbase[ww];
+        __syncthreads();
         dstart[d] = wofs + incl - run;
+        dbase[d] = gofs + gi - g + static_cast<unsigned>(before);
     }
     __syncthreads();
     // tile-local sorted order in shared memory ...
@@ -238,7 +287,7 @@ __global__ void __launch_bounds__(256) k_radix_scatter(const uint64_t *__restric
     for (unsigned lp = threadIdx.x; lp < cnt; lp += blockDim.x) {
         const uint64_t kk = skey[lp];
         const unsigned d = static_cast<unsigned>((kk >> bit) & 0xffu);
-        const unsigned pos = hist[d * ntiles_cap + blockIdx.x] + (lp - dstart[d]);
+        const unsigned pos = dbase[d] + (lp - dstart[d]);
         kout[pos] = kk;
         if (vout) vout[pos] = sval[lp];
     }
@@ -265,23 +314,24 @@ void scan_temp_free(ScanTemp &t) {
 cudaError_t sort_temp_alloc(SortTemp &t, unsigned n_cap) {
     const int tiles = static_cast<int>((static_cast<uint64_t>(n_cap) + kSortTile - 1) / kSortTile) + 1;
     if (tiles > t.max_tiles) {
-        if (t.hist) cudaFree(t.hist);
-        t.hist = nullptr;
-        cudaError_t e = cudaMalloc(&t.hist, sizeof(unsigned) * 256 * static_cast<size_t>(tiles));
+        sort_temp_free(t);
+        cudaError_t e = cudaMalloc(&t.status, sizeof(unsigned long long) * 256 * kMaxPasses * static_cast<size_t>(tiles));
+        if (e == cudaSuccess) e = cudaMalloc(&t.ghist, sizeof(unsigned) * (256 + 1) * kMaxPasses);
         if (e != cudaSuccess) {
-            t.max_tiles = 0;
+            sort_temp_free(t);
             return e;
         }
+        t.ticket = t.ghist + 256 * kMaxPasses;
         t.max_tiles = tiles;
     }
-    return scan_temp_alloc(t.scan, 256u * static_cast<unsigned>(t.max_tiles));
+    return cudaSuccess;
 }
 
 void sort_temp_free(SortTemp &t) {
-    if (t.hist) cudaFree(t.hist);
-    t.hist = nullptr;
+    if (t.status) cudaFree(t.status);
+    if (t.ghist) cudaFree(t.ghist);
+    t.status = nullptr, t.ghist = nullptr, t.ticket = nullptr;
     t.max_tiles = 0;
-    scan_temp_free(t.scan);
 }
 
 void scan_exclusive_u32(const unsigned *in, unsigned *out, unsigned n_cap, const unsigned *d_n, unsigned *d_total,
@@ -303,20 +353,28 @@ void scan_exclusive_u32(const unsigned *in, unsigned *out, unsigned n_cap, const
 }
 
 int radix_sort_u64(uint64_t *k0, unsigned *v0, uint64_t *k1, unsigned *v1, unsigned n_cap, const unsigned *d_n,
-                   int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches) {
+                   int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches, int *d_err, int err_bit) {
     const unsigned tiles = (n_cap + kSortTile - 1) / kSortTile;
-    if (tiles == 0) return 0;
-    cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kScatterSmem));
+    const int npasses = (bit_hi - bit_lo + 7) / 8;
+    if (tiles == 0 || npasses <= 0) return 0;
+    if (npasses > kMaxPasses || static_cast<int>(tiles) > tmp.max_tiles) {
+        if (d_err) cudaMemsetAsync(d_err, 0xff, sizeof(int), st);  // cannot happen with the allocation helpers
+        return 0;
+    }
+    cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kScatterSmem));
+    cudaMemsetAsync(tmp.ghist, 0, sizeof(unsigned) * (256 + 1) * kMaxPasses, st);  // histograms and tickets
+    cudaMemsetAsync(tmp.status, 0, sizeof(unsigned long long) * 256 * static_cast<size_t>(npasses) * tiles, st);
+    k_sweep_hist<<<tiles < 1024u ? tiles : 1024u, 256, 0, st>>>(k0, n_cap, d_n, bit_lo, npasses, tmp.ghist);
     int cur = 0;
-    for (int bit = bit_lo; bit < bit_hi; bit += 8) {
+    for (int p = 0; p < npasses; ++p) {
         uint64_t *ki = cur ? k1 : k0, *ko = cur ? k0 : k1;
         unsigned *vi = cur ? v1 : v0, *vo = cur ? v0 : v1;
-        k_radix_hist<<<tiles, 256, 0, st>>>(ki, n_cap, d_n, bit, tmp.hist, tiles);
-        scan_exclusive_u32(tmp.hist, tmp.hist, 256u * tiles, nullptr, nullptr, tmp.scan, st, launches);
-        k_radix_scatter<<<tiles, 256, kScatterSmem, st>>>(ki, vi, ko, vo, n_cap, d_n, bit, tmp.hist, tiles);
-        if (launches) *launches += 2;
+        k_sweep<<<tiles, 256, kScatterSmem, st>>>(ki, vi, ko, vo, n_cap, d_n, bit_lo + 8 * p, tmp.ghist + 256 * p,
+                                                  tmp.status + static_cast<size_t>(p) * 256 * tiles, tmp.ticket + p, d_err,
+                                                  err_bit);
         cur ^= 1;
     }
+    if (launches) *launches += 1 + npasses;
     return cur;
 }
 

@@ -24,18 +24,22 @@ void scan_exclusive_u32(const unsigned *in, unsigned *out, unsigned n_cap, const
                         ScanTemp &tmp, cudaStream_t st, int64_t *launches);
 
 constexpr int kSortTile = 4096;  // 256 threads x 16 keys
+constexpr int kMaxPasses = 8;    // 8-bit digits: up to 64 key bits
 
 struct SortTemp {
-    unsigned *hist = nullptr;  // 256 * max_tiles
+    unsigned long long *status = nullptr;  // [kMaxPasses][max_tiles][256] look-back words
+    unsigned *ghist = nullptr;             // [kMaxPasses][256] digit counts, then [kMaxPasses] tile tickets
+    unsigned *ticket = nullptr;
     int max_tiles = 0;
-    ScanTemp scan;
 };
 
 // Stable sort of (key, val) pairs by bits [bit_lo, bit_hi) of the key.
 // Ping-pongs between (k0, v0) and (k1, v1); returns 0 if the result is in
-// (k0, v0), 1 if in (k1, v1). vals may be nullptr (keys only).
+// (k0, v0), 1 if in (k1, v1). vals may be nullptr (keys only). A look-back
+// wait that gives up sets err_bit in *d_err (if d_err is not null).
 int radix_sort_u64(uint64_t *k0, unsigned *v0, uint64_t *k1, unsigned *v1, unsigned n_cap, const unsigned *d_n,
-                   int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches);
+                   int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches, int *d_err = nullptr,
+                   int err_bit = 0);
 
 // Allocation helpers for the temporaries (sized for n_cap elements).
 cudaError_t scan_temp_alloc(ScanTemp &t, unsigned n_cap);

@@ -716,7 +716,7 @@ void build_tree(Workspace &ws) {
     k_keys<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.keys0, ws.perm0);
     ws.launches += 3;
     const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, 3 * (kMaxLevel - ws.sort_levels),
-                                   3 * kMaxLevel, ws.sort, st, &ws.launches);
+                                   3 * kMaxLevel, ws.sort, st, &ws.launches, &ws.info->err, kDevTimeout);
     ws.keys = res ? ws.keys1 : ws.keys0;
     ws.perm = res ? ws.perm1 : ws.perm0;
     // split cells of every level
@@ -726,7 +726,7 @@ void build_tree(Workspace &ws) {
     k_split_emit<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.off, ws.d_counts, ws.s_cap, ws.ent0);
     ws.launches += 3;
     const int re = radix_sort_u64(ws.ent0, nullptr, ws.ent1, nullptr, ws.s_cap, ws.d_counts + 1, 32, 40, ws.sort, st,
-                                  &ws.launches);
+                                  &ws.launches, &ws.info->err, kDevTimeout);
     ws.ent = re ? ws.ent1 : ws.ent0;
     k_level_table<<<1, 32, 0, st>>>(ws.ent, ws.d_counts, ws.info, n);
     k_root<<<1, 32, 0, st>>>(n, ws.T, ws.info, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path,

@@ -454,7 +454,15 @@ def main():
     dom = max(per, key=lambda k: per[k]["ms_per_launch"] * per[k]["launches"]) if per else None
     roof = dict(per[dom]) if dom else {}
     if dom:
-        roof.update({"kernel": dom, "traffic": None})
+        # DRAM bytes (read + write) per launch from one ncu capture of this exact
+        # default workload (profiles/dram_plummer4M_p8_mixed.md); other
+        # workloads have no capture, so null
+        default_cfg = (n == 1 << 22 and args.p == 8 and args.s == 64 and args.eps == 0.005 and args.precision == "mixed"
+                       and args.flags == 0)
+        traffic = {"p2p": 293120768 + 40724736, "m2l": 188582656 + 19934464} if default_cfg else {}
+        for k in per:
+            per[k]["traffic"] = traffic.get(k)
+        roof.update({"kernel": dom, "traffic": traffic.get(dom), "traffic_unit": "B per launch"})
         roof.setdefault("peak_source", f"{src}: FP32 = 2 x 128 lanes x {nsm} SMs x sm_max_mhz {sm_mhz:.0f}"
                         if roof["bound"] == "fp32" else f"{src} hbm_gbs")
 

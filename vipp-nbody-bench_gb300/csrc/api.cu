@@ -463,6 +463,9 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     if ((e = cudaMalloc(&ws.ops_d, sizeof(double) * kk)) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.ops_f, sizeof(float) * kk)) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.bimg, sizeof(float) * gb::m2l_tc_image_floats(ws.p))) != cudaSuccess) return fail("ops", e);
+    if ((e = cudaMalloc(&ws.m2l_tab, gb::m2l_table_bytes(ws.p))) != cudaSuccess) return fail("ops", e);
+    gb::build_m2l_table(ws);
+    if ((e = cudaStreamSynchronize(ws.st)) != cudaSuccess) return fail("ops table", e);
     *out = ctx;
     return GB_OK;
 }
@@ -479,7 +482,7 @@ void gb_destroy(gb_ctx *ctx) {
                     ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
-                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.ms_tc, ws.diag, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
+                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.m2l_tab, ws.ms_tc, ws.diag, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
                     ctx->d_direct};
     for (void *b : bufs) dfree(b);
     gb::sort_temp_free(ws.sort);
@@ -513,6 +516,11 @@ int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
         GB_TRY(dalloc(ctx->ws.ops_d, kk));
         GB_TRY(dalloc(ctx->ws.ops_f, kk));
         GB_TRY(dalloc(ctx->ws.bimg, gb::m2l_tc_image_floats(ctx->ws.p)));
+        unsigned char *t = nullptr;
+        GB_TRY(dalloc(t, gb::m2l_table_bytes(ctx->ws.p)));
+        dfree(ctx->ws.m2l_tab);
+        ctx->ws.m2l_tab = t;
+        gb::build_m2l_table(ctx->ws);
     }
     if (ctx->ws.T != oldT && ctx->have_state) {
         const int r = initial_capacity(ctx);
@@ -835,10 +843,8 @@ int gb_accel(gb_ctx *ctx, double *a_aos, double *phi) {
     }
     const int rc = run_with_capacity(ctx, [&]() { evaluate(ctx); });
     if (rc) return rc;
-    if (a_aos) {
-        gb::soa_to_aos(ws, ws.acc, ws.staging, ws.n);
-        GB_TRY(cudaMemcpyAsync(a_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
-    }
+    if (a_aos)  // acc is [N][3] already
+        GB_TRY(cudaMemcpyAsync(a_aos, ws.acc, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
     if (phi) {
         gb::potential_orig(ws, ws.phi);
         GB_TRY(cudaMemcpyAsync(phi, ws.phi, sizeof(double) * ws.n, cudaMemcpyDeviceToHost, ws.st));

@@ -91,13 +91,60 @@ __device__ __forceinline__ void for_each_regular(T x, T y, T z, F &&f) {
 __device__ __forceinline__ double level_scale(const TreeInfo *info, int L) { return ldexp(info->S, -L); }
 
 // ---------------------------------------------------------------- operators
+// The same-level M2L entry (j,k,po | n,m,pi) is c(m') (Y or conj Y) with
+//   c(m') = [phase(m') a(n,m') a(j,k) ((-1)^n ainv(j+n, m'-k))] rho^-(j+n+1)
+// for m' = m and m' = -m. The bracket does not depend on the offset, so it is
+// tabulated once per p (in FP64, multiplied in the same order as m2l_coef, so
+// every entry keeps its bits) and an evaluation only multiplies by the
+// offset's power of rho and harmonics.
+struct M2LEnt {
+    double t[2];        // bracket of the m' = m and m' = -m terms
+    short y[2];         // index of Re Y_{j+n}^{|m'-k|} in yt (Im follows)
+    signed char sg[2];  // Y order m' - k: 0 (real), +1, -1 (conjugate)
+    unsigned char q;    // j + n
+    unsigned char f;    // bit 0: m > 0 (second term), bit 1: input Im part, bit 2: output Im part
+};
+
+__global__ void k_m2l_table(int p, M2LEnt *__restrict__ tab) {
+    const int K = (p + 1) * (p + 1);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < K * K; idx += gridDim.x * blockDim.x) {
+        const int ro = idx / K, ri = idx % K;
+        int j, k, po, n, m, pi;
+        rdecode(ro, j, k, po);
+        rdecode(ri, n, m, pi);
+        M2LEnt e;
+        for (int s = 0; s < 2; ++s) {
+            const int mm = s == 0 ? m : -m;
+            const int o = mm - k;
+            e.t[s] = (s == 1 && m == 0) ? 0.0
+                                        : phase_even(iabs(k - mm) - iabs(k) - iabs(mm)) * aco(c_at, n, mm) * aco(c_at, j, k) *
+                                              ((n % 2 ? -1.0 : 1.0) * aco_inv(c_at, j + n, o));
+            e.y[s] = static_cast<short>(ridx(j + n, iabs(o), 0));
+            e.sg[s] = static_cast<signed char>(o == 0 ? 0 : (o > 0 ? 1 : -1));
+        }
+        e.q = static_cast<unsigned char>(j + n);
+        e.f = static_cast<unsigned char>((m > 0 ? 1 : 0) | (pi ? 2 : 0) | (po ? 4 : 0));
+        tab[idx] = e;
+    }
+}
+
+// ydir + m2l_coef's last factors from a table entry (same operations, same order)
+__device__ __forceinline__ void m2l_term(const M2LEnt &e, int s, const double *yt, const double *rinv_pow, double &re, double &im) {
+    const double yr = yt[e.y[s]];
+    double yi = e.sg[s] == 0 ? 0.0 : yt[e.y[s] + 1];
+    if (e.sg[s] < 0) yi = -yi;
+    const double c = e.t[s] * rinv_pow[e.q + 1];
+    re = c * yr;
+    im = c * yi;
+}
 // One block per operator: 343 same-level M2L offsets (adjacent ones unused),
 // 8 M2M octants, 8 L2L octants. Shifts are the ideal cell-centre offsets of
 // the current root box in units of the level's length s:
 //   M2L  t = (dx Hx, dy Hy, dz Hz) / S,
 //   M2M  t = child - parent = (+-Hx, +-Hy, +-Hz) / (4 S) (minus for a lower half),
 //   L2L  t = parent - child.
-__global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, double *__restrict__ ops_d, float *__restrict__ ops_f) {
+__global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, const M2LEnt *__restrict__ m2l_tab,
+                            double *__restrict__ ops_d, float *__restrict__ ops_f) {
     extern __shared__ double sm[];
     const int K = (p + 1) * (p + 1);
     const int b = blockIdx.x;
@@ -129,6 +176,27 @@ __global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, double *__
     __syncthreads();
     double *od = ops_d + static_cast<size_t>(b) * K * K;
     float *of = ops_f + static_cast<size_t>(b) * K * K;
+    if (kind == 0) {
+        // real_entry's combination of the two terms, from the table
+        for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
+            const M2LEnt e = m2l_tab[idx];
+            double ar, ai, br = 0, bi = 0;
+            m2l_term(e, 0, yt, pw, ar, ai);
+            if (e.f & 1) m2l_term(e, 1, yt, pw, br, bi);
+            double vr, vi;
+            if ((e.f & 2) == 0) {
+                vr = ar + br;
+                vi = ai + bi;
+            } else {
+                vr = -(ai - bi);
+                vi = ar - br;
+            }
+            const double v = (e.f & 4) ? vi : vr;
+            od[idx] = v;
+            of[idx] = static_cast<float>(v);
+        }
+        return;
+    }
     for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
         const int ro = idx / K, ri = idx % K;  // output-major storage: [ro][ri]
         int j, k, po, n, m, pi;
@@ -536,17 +604,18 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_L2P_MIN_BLOCKS : GB_F
 }
 
 // acc[perm[j]] = near[j] + far[j], added in T (FP32 forms: one rounding of
-// 2^-24 of the sum, below the error of either part, and no FP64 add).
+// 2^-24 of the sum, below the error of either part, and no FP64 add). acc is
+// [N][3] (AoS): a particle's three components share one scattered 24-byte
+// write instead of three 8-byte ones.
 template <typename T>
 __global__ void k_finalize(const unsigned *__restrict__ perm, unsigned n, const T *__restrict__ nearv,
                            const T *__restrict__ farv, double *__restrict__ acc) {
     const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    const unsigned i = perm[j];
+    const size_t i = perm[j];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-        acc[static_cast<size_t>(a) * n + i] =
-            static_cast<double>(nearv[static_cast<size_t>(a) * n + j] + farv[static_cast<size_t>(a) * n + j]);
+        acc[3 * i + a] = static_cast<double>(nearv[static_cast<size_t>(a) * n + j] + farv[static_cast<size_t>(a) * n + j]);
 }
 
 // Far-field potential (diagnostic, after an evaluation): the potential of
@@ -679,10 +748,20 @@ void dispatch_p(Workspace &ws, int which, double *farphi = nullptr) {
 
 }  // namespace
 
+size_t m2l_table_bytes(int p) {
+    const size_t K = static_cast<size_t>(p + 1) * (p + 1);
+    return sizeof(M2LEnt) * K * K;
+}
+
+void build_m2l_table(Workspace &ws) {
+    k_m2l_table<<<64, 256, 0, ws.st>>>(ws.p, static_cast<M2LEnt *>(ws.m2l_tab));
+    ws.launches += 1;
+}
+
 void build_operators(Workspace &ws) {
     timer_begin(ws, kTOps);
     const size_t smem = sizeof(double) * ((2 * ws.p + 1) * (2 * ws.p + 1) + 2 * ws.p + 3);
-    k_build_ops<<<kNumOps, 256, smem, ws.st>>>(ws.info, ws.p, ws.ops_d, ws.ops_f);
+    k_build_ops<<<kNumOps, 256, smem, ws.st>>>(ws.info, ws.p, static_cast<const M2LEnt *>(ws.m2l_tab), ws.ops_d, ws.ops_f);
     ws.launches += 1;
     timer_end(ws, kTOps);
 }

@@ -23,20 +23,25 @@ __global__ void k_rk4_begin(const double *__restrict__ x, const double *__restri
     }
 }
 
+// a is [N][3] (AoS, as the force evaluation leaves it); the state is SoA.
 __global__ void k_rk4_stage(int stage, double w, double c, double *__restrict__ x, double *__restrict__ v,
                             const double *__restrict__ x0, const double *__restrict__ v0, double *__restrict__ xo,
-                            double *__restrict__ vo, const double *__restrict__ a, size_t n3) {
-    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n3; e += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const double ve = v[e], ae = a[e];
-        const double xoe = __dadd_rn(xo[e], __dmul_rn(w, ve));
-        const double voe = __dadd_rn(vo[e], __dmul_rn(w, ae));
-        xo[e] = xoe, vo[e] = voe;
-        if (stage < 3) {
-            x[e] = __dadd_rn(x0[e], __dmul_rn(ve, c));
-            v[e] = __dadd_rn(v0[e], __dmul_rn(ae, c));
-        } else {
-            x[e] = xoe;
-            v[e] = voe;
+                            double *__restrict__ vo, const double *__restrict__ a, size_t n) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const size_t e = k * n + i;
+            const double ve = v[e], ae = a[3 * i + k];
+            const double xoe = __dadd_rn(xo[e], __dmul_rn(w, ve));
+            const double voe = __dadd_rn(vo[e], __dmul_rn(w, ae));
+            xo[e] = xoe, vo[e] = voe;
+            if (stage < 3) {
+                x[e] = __dadd_rn(x0[e], __dmul_rn(ve, c));
+                v[e] = __dadd_rn(v0[e], __dmul_rn(ae, c));
+            } else {
+                x[e] = xoe;
+                v[e] = voe;
+            }
         }
     }
 }
@@ -76,7 +81,7 @@ void rk4_stage(Workspace &ws, int stage, double dt) {
     const double w = (stage == 0 || stage == 3) ? dt / 6 : dt / 3;
     const double c = stage < 2 ? dt / 2 : dt;
     k_rk4_stage<<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.acc,
-                                                          3 * static_cast<size_t>(ws.n));
+                                                          static_cast<size_t>(ws.n));
     ws.launches += 1;
     timer_end(ws, kTRK4);
 }

@@ -2,7 +2,8 @@
 //
 // HBM layout (N particles, C cells, S non-leaf cells, K = (p+1)^2):
 //   state, original particle order, FP64 SoA planes [3][N]:
-//     x, v (current), x0, v0 (step start), xo, vo (RK4 accumulators), acc
+//     x, v (current), x0, v0 (step start), xo, vo (RK4 accumulators) [3][N];
+//     acc [N][3] (as returned to the caller)
 //   per evaluation, tree (Morton) order:
 //     keys/perm (u64/u32 ping-pong pairs), xs [3][N] FP64 positions,
 //     ph/pl float4 hi/lo split of the positions (mixed P2P),
@@ -104,6 +105,7 @@ struct Workspace {
     // operators
     double *ops_d = nullptr;  // [(343+16) K K]
     float *ops_f = nullptr;
+    void *m2l_tab = nullptr;  // offset-independent factors of the M2L operator entries (fmm.cu)
     float *bimg = nullptr;    // tensor-core M2L operator images (m2l_tc.cu)
     float *ms_tc = nullptr;   // tensor-core M2L split expansions, 2 ms_rows ms_kp floats (m2l_tc.cu)
     unsigned ms_rows = 0;     // c_cap + 1: the last row is zero
@@ -145,6 +147,8 @@ constexpr int kNumOps = 359;
 // stages (all asynchronous on ws.st)
 void build_tree(Workspace &ws);               // bbox, keys, sort, cells, leaves, lists, near-field ranges
 void build_operators(Workspace &ws);          // 359 translation matrices for the current root box
+size_t m2l_table_bytes(int p);
+void build_m2l_table(Workspace &ws);          // fill m2l_tab for ws.p (once per p, outside step graphs)
 void upward_pass(Workspace &ws);              // P2M + M2M
 void m2l_pass(Workspace &ws);                 // M2L into L (CUDA cores)
 void m2l_pass_tc(Workspace &ws);              // M2L into L (tensor cores, mixed)

@@ -167,13 +167,44 @@ __global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, const M2LE
     double *yt = sm;                   // (D+1)^2
     double *pw = sm + (2 * p + 1) * (2 * p + 1);  // 2p+3
     const double rho = sqrt(tv[0] * tv[0] + tv[1] * tv[1] + tv[2] * tv[2]);
-    if (threadIdx.x == 0) {
-        solid_regular_rt<double>(D, tv[0] / rho, tv[1] / rho, tv[2] / rho, c_htd, yt);
-        double a = 1;
-        const double f = kind == 0 ? 1.0 / rho : rho;
-        for (int i = 0; i < 2 * p + 3; ++i) pw[i] = a, a *= f;
+    // solid_regular_rt's recurrences spread over threads, each value by the
+    // same operations: thread 0 walks the diagonal (m, m), then thread m the
+    // degrees of order m; thread 32 the powers of rho
+    {
+        const double x = tv[0] / rho, y = tv[1] / rho, z = tv[2] / rho;
+        const HTab<double> &t = c_htd;
+        if (threadIdx.x == 0) {
+            double cre = 1, cim = 0;
+            for (int m = 0; m <= D; ++m) {
+                if (m > 0) {
+                    const double nre = t.mm[m] * (x * cre - y * cim);
+                    const double nim = t.mm[m] * (x * cim + y * cre);
+                    cre = nre, cim = nim;
+                }
+                yt[ridx(m, m, 0)] = cre;
+                if (m > 0) yt[ridx(m, m, 1)] = cim;
+            }
+        } else if (threadIdx.x == 32) {
+            double a = 1;
+            const double f = kind == 0 ? 1.0 / rho : rho;
+            for (int i = 0; i < 2 * p + 3; ++i) pw[i] = a, a *= f;
+        }
+        __syncthreads();
+        const int m = threadIdx.x;
+        if (m <= D) {
+            const double r2 = x * x + y * y + z * z;
+            const double cre = yt[ridx(m, m, 0)], cim = m > 0 ? yt[ridx(m, m, 1)] : 0.0;
+            if (m + 1 <= D) {
+                yt[ridx(m + 1, m, 0)] = t.m1[m] * z * cre;
+                if (m > 0) yt[ridx(m + 1, m, 1)] = t.m1[m] * z * cim;
+            }
+            for (int n = m + 2; n <= D; ++n) {
+                yt[ridx(n, m, 0)] = t.ra[n][m] * z * yt[ridx(n - 1, m, 0)] - t.rb[n][m] * r2 * yt[ridx(n - 2, m, 0)];
+                if (m > 0) yt[ridx(n, m, 1)] = t.ra[n][m] * z * yt[ridx(n - 1, m, 1)] - t.rb[n][m] * r2 * yt[ridx(n - 2, m, 1)];
+            }
+        }
+        __syncthreads();
     }
-    __syncthreads();
     double *od = ops_d + static_cast<size_t>(b) * K * K;
     float *of = ops_f + static_cast<size_t>(b) * K * K;
     if (kind == 0) {

@@ -43,6 +43,7 @@ struct gb_ctx {
     uint64_t step_epoch = 0;
     int64_t step_launches = 0;
     bool graph_failed = false;
+    bool levels_fitted = false;  // sort_levels fitted to the tree since the last upload
     long long graph_steps = 0, direct_steps = 0, graph_captures = 0;
     std::vector<gb::PendingTimer> pending;
     std::vector<cudaEvent_t> free_events;
@@ -322,6 +323,15 @@ int check_device_errors(gb_ctx *ctx, unsigned *need) {
         ctx->err = "capacity";
         return GB_ERR_CAPACITY;
     }
+    // After the first good evaluation of an upload, sort only the key levels
+    // the tree uses plus two (never more than now): shallow trees get fewer
+    // sort passes and M2M/L2L level launches. A tree that deepens later asks
+    // for more through counts[9].
+    if (!ctx->levels_fitted) {
+        ctx->levels_fitted = true;
+        const int want = std::max(3, ws.h_info->depth + 2);
+        if (want < ws.sort_levels) ws.sort_levels = want, ++ctx->epoch;
+    }
     return GB_OK;
 }
 
@@ -500,6 +510,7 @@ void gb_destroy(gb_ctx *ctx) {
 const char *gb_last_error(const gb_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
 
 int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
+    if (ctx) ctx->levels_fitted = false;
     if (!ctx) return GB_ERR_INVALID;
     ++ctx->epoch;  // buffers, sizes or configuration may change: the step graph is rebuilt
     std::string msg;
@@ -534,6 +545,7 @@ int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
 }
 
 int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
+    if (ctx) ctx->levels_fitted = false;
     if (!ctx) return GB_ERR_INVALID;
     if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
     if (n && (!x_aos || !v_aos)) return ctx->err = "null input", GB_ERR_INVALID;
@@ -557,6 +569,7 @@ int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
 }
 
 int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max) {
+    if (ctx) ctx->levels_fitted = false;
     if (!ctx) return GB_ERR_INVALID;
     if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
     if (!(r_max >= 0) || !std::isfinite(r_max)) return ctx->err = "r_max must be finite and >= 0", GB_ERR_INVALID;

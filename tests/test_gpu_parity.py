@@ -103,6 +103,25 @@ def test_plummer16k_tree_and_accel_vs_oracle(plummer16k):
     assert math.sqrt(np.mean(e ** 2)) <= MIXED_RMS_REL and np.max(e) <= MIXED_MAX_REL
 
 
+def test_plummer1m_tree_bit_exact_vs_oracle():
+    """A million-particle Plummer sphere (reference generator, seed 1, s = 64):
+    256 radix tiles per key pass and a 7-8 level tree; the tree, lists and cell
+    numbering equal the oracle's, on the first evaluation and on a later one
+    (after the sorted key levels have been fitted to the tree)."""
+    import vipp_gb300
+    x, v = O.plummer_reference(1 << 20, 0.01, 1)
+    n = x.shape[0]
+    ref = canon_ref(O.oracle().tree(x, 64))
+    with vipp_gb300.Solver(p=4, s=64, eps=0.01, m=1.0 / n, precision="mixed") as s:
+        s.preprocess(x, v)
+        s.accel()
+        assert diff_trees(canon_gpu(s.tree_dump()), ref) == []
+        r1 = s.stats()["retries"]
+        s.accel()
+        assert diff_trees(canon_gpu(s.tree_dump()), ref) == []
+        assert s.stats()["retries"] == r1  # the fitted levels need no repeat
+
+
 def test_plummer16k_rk4_trajectory_vs_oracle(plummer16k):
     import vipp_gb300
     x, v = plummer16k

@@ -183,6 +183,25 @@ def test_mixed_m2l_tensor_and_cuda_cores_agree(name):
     assert np.max(rel_err(res["tensor"], res["cuda"])) <= 2 * MIXED_MAX_REL
 
 
+@pytest.mark.parametrize("p", [2, 3, 7, 9, 10])
+def test_mixed_tensor_m2l_every_order(plummer16k, p):
+    """The tensor-core M2L over the expansion orders whose drains differ: the
+    running sums in TMEM after both accumulators (p <= 7), in the gaps behind
+    them (p = 8, covered above), or in registers (p = 9, 10, no free columns).
+    Mixed against FP64 on the same tree: RMS <= MIXED_RMS_REL, max <= MIXED_MAX_REL."""
+    import vipp_gb300
+    x, v = plummer16k
+    x, v = x[:8192].copy(), v[:8192].copy()
+    n = x.shape[0]
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with vipp_gb300.Solver(p=p, s=32, eps=0.01, m=1.0 / n, precision=prec) as s:
+            s.preprocess(x, v)
+            out[prec] = s.accel()
+    e = rel_err(out["mixed"], out["fp64"])
+    assert math.sqrt(np.mean(e ** 2)) <= MIXED_RMS_REL and np.max(e) <= MIXED_MAX_REL
+
+
 def test_results_are_deterministic():
     import vipp_gb300
     d = load_case("cluster1200_s6_p5")

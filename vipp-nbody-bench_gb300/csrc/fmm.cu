@@ -267,7 +267,23 @@ struct CellFrame {
 };
 
 // --------------------------------------------------------------------- P2M
+// One step of a warp reduce-scatter: each lane keeps one half of its S values
+// (the upper half if lane & o) and adds its partner's copy of that half.
+template <int S, typename T>
+__device__ __forceinline__ void rs_step(T *a, int lane, int o) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < S / 2; ++i) {
+        const T send = up ? a[i] : a[i + S / 2];
+        const T keep = up ? a[i + S / 2] : a[i];
+        a[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+}
+
 // One warp per leaf at level >= 2: M~_n^m = sum_i m conj(R_n^m((x_i - c)/s)).
+// The lanes' partial sums (KR = K rounded up to 32) are combined by a
+// five-step reduce-scatter, after which lane l holds coefficients
+// [KR/32 l, KR/32 (l+1)): 2 KR shuffles instead of 5 K.
 template <int P, typename T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_P2M_MIN_BLOCKS : GB_FAR_MIN_BLOCKS) k_p2m(const int *__restrict__ leaves, const unsigned *counts,
                                              const int *__restrict__ c_begin, const int *__restrict__ c_end,
@@ -284,9 +300,10 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_P2M_MIN_BLOCKS : GB_F
         const int L = c_level[c];
         if (L < 2) continue;
         const CellFrame<T> fr(c_ctr, c, info, 1.0 / level_scale(info, L));
-        T acc[K];
+        constexpr int KR = (K + 31) / 32 * 32;
+        T acc[KR];
 #pragma unroll
-        for (int r = 0; r < K; ++r) acc[r] = 0;
+        for (int r = 0; r < KR; ++r) acc[r] = 0;
         const T q = static_cast<T>(mass);
         for (int j = c_begin[c] + lane; j < c_end[c]; j += 32) {
             T ux, uy, uz;
@@ -296,12 +313,15 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_P2M_MIN_BLOCKS : GB_F
                 if (mm > 0) acc[ridx(nn, mm, 1)] -= q * im;
             });
         }
+        rs_step<KR>(acc, lane, 16);
+        rs_step<KR / 2>(acc, lane, 8);
+        rs_step<KR / 4>(acc, lane, 4);
+        rs_step<KR / 8>(acc, lane, 2);
+        rs_step<KR / 16>(acc, lane, 1);
 #pragma unroll
-        for (int r = 0; r < K; ++r) {
-            T v = acc[r];
-#pragma unroll
-            for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == (r & 31)) M[static_cast<size_t>(c) * K + r] = v;
+        for (int i = 0; i < KR / 32; ++i) {
+            const int r = (KR / 32) * lane + i;
+            if (r < K) M[static_cast<size_t>(c) * K + r] = acc[i];
         }
     }
 }

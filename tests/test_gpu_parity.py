@@ -258,6 +258,23 @@ def test_uniform_cube_mixed_vs_fp64_at_scale():
     assert st["nleaves"] == int(leaf.sum()) and st["p2p_pairs"] > 0
 
 
+@pytest.mark.parametrize("n,s", [(3000, 1200), (20000, 1000)])
+def test_large_leaf_capacity_vs_oracle(n, s):
+    """Leaf capacity T = floor(sqrt(8) s) in the thousands: a root-only tree
+    (n <= T) and a shallow tree whose leaves hold up to T particles, so the
+    within-leaf index sort runs on long leaves with fewer warps per block.
+    Tree bit-exact, FP64 accelerations within FP64_MAX_REL of the oracle."""
+    import vipp_gb300
+    x, v = O.plummer_reference(n, 0.01, 3)
+    orc = O.oracle()
+    ref = orc.accel(x, s, 1.0, 1.0 / n, 0.01, 4)
+    with vipp_gb300.Solver(p=4, s=s, eps=0.01, m=1.0 / n) as sol:
+        sol.preprocess(x, v)
+        a = sol.accel()
+        assert diff_trees(canon_gpu(sol.tree_dump()), canon_ref(orc.tree(x, s))) == []
+    assert np.max(rel_err(a, ref)) <= FP64_MAX_REL
+
+
 def test_edge_cases_and_errors():
     import vipp_gb300
     with vipp_gb300.Solver(p=4, s=4, eps=0.01, m=1.0) as s:

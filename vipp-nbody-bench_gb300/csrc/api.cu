@@ -153,6 +153,7 @@ int ensure_particles(gb_ctx *ctx, unsigned n) {
     GB_TRY(dalloc(ws.keys1, cap));
     GB_TRY(dalloc(ws.perm0, cap));
     GB_TRY(dalloc(ws.perm1, cap));
+    GB_TRY(dalloc(ws.inv, cap));
     GB_TRY(dalloc(ws.xs, n3));
     GB_TRY(dalloc(ws.ph, cap));
     GB_TRY(dalloc(ws.pl, cap));
@@ -339,7 +340,10 @@ int check_device_errors(gb_ctx *ctx, unsigned *need) {
 // cores) and the far field (operators, P2M/M2M, M2L on the tensor cores,
 // L2L/L2P) read only tree data and write separate buffers, so the near field
 // runs on a second stream concurrently with the far field; finalize joins them.
-void evaluate(gb_ctx *ctx) {
+// One force evaluation; with to_acc the accelerations are also written out
+// in particle order (acc), which RK4 stages do not need (they read the tree-
+// order parts directly).
+void evaluate(gb_ctx *ctx, bool to_acc = true) {
     gb::Workspace &ws = ctx->ws;
     g_timer_ctx = ctx;
     gb::build_tree(ws);
@@ -371,7 +375,7 @@ void evaluate(gb_ctx *ctx) {
         cudaStreamWaitEvent(ws.st, ws.ev_join, 0);
     }
     gb::p2p_finish(ws);
-    gb::finalize_accel(ws, ws.acc);
+    if (to_acc) gb::finalize_accel(ws, ws.acc);
 }
 
 // Grow capacities after an overflow reported by the device (counts holds
@@ -655,7 +659,7 @@ static void step_enqueue(gb_ctx *ctx, double dt) {
         gb::Workspace &w = ctx->ws;
         gb::rk4_restore(w);
         for (int stage = 0; stage < 4; ++stage) {
-            evaluate(ctx);
+            evaluate(ctx, false);
             gb::rk4_stage(w, stage, dt);
         }
     };

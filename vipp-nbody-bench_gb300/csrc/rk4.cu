@@ -23,15 +23,21 @@ __global__ void k_rk4_begin(const double *__restrict__ x, const double *__restri
     }
 }
 
-// a is [N][3] (AoS, as the force evaluation leaves it); the state is SoA.
+// The stage's acceleration is read where the force evaluation left it, in
+// tree order: a = near[inv[i]] + far[inv[i]], added in T exactly as the
+// accelerations returned to the caller are (finalize), so no separate pass
+// writes them out in particle order; the state is SoA in particle order.
+template <typename T>
 __global__ void k_rk4_stage(int stage, double w, double c, double *__restrict__ x, double *__restrict__ v,
                             const double *__restrict__ x0, const double *__restrict__ v0, double *__restrict__ xo,
-                            double *__restrict__ vo, const double *__restrict__ a, size_t n) {
+                            double *__restrict__ vo, const unsigned *__restrict__ inv, const T *__restrict__ nearv,
+                            const T *__restrict__ farv, size_t n) {
     for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const size_t j = inv[i];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const size_t e = k * n + i;
-            const double ve = v[e], ae = a[3 * i + k];
+            const double ve = v[e], ae = static_cast<double>(nearv[k * n + j] + farv[k * n + j]);
             const double xoe = __dadd_rn(xo[e], __dmul_rn(w, ve));
             const double voe = __dadd_rn(vo[e], __dmul_rn(w, ae));
             xo[e] = xoe, vo[e] = voe;
@@ -80,8 +86,14 @@ void rk4_stage(Workspace &ws, int stage, double dt) {
     // weights and stage offsets exactly as solver_ref.hpp:58, 64, 71, 77, 84, 90, 97
     const double w = (stage == 0 || stage == 3) ? dt / 6 : dt / 3;
     const double c = stage < 2 ? dt / 2 : dt;
-    k_rk4_stage<<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.acc,
-                                                          static_cast<size_t>(ws.n));
+    if (ws.mixed)
+        k_rk4_stage<float><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.inv,
+                                                                     static_cast<const float *>(ws.nearf),
+                                                                     static_cast<const float *>(ws.farf), static_cast<size_t>(ws.n));
+    else
+        k_rk4_stage<double><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.inv,
+                                                                      static_cast<const double *>(ws.nearf),
+                                                                      static_cast<const double *>(ws.farf), static_cast<size_t>(ws.n));
     ws.launches += 1;
     timer_end(ws, kTRK4);
 }

@@ -441,10 +441,11 @@ __global__ void k_leaf_sort(const int *__restrict__ leaves, const unsigned *coun
 
 __global__ void k_gather(const double *__restrict__ x, unsigned n, const unsigned *__restrict__ perm,
                          const TreeInfo *__restrict__ info, float mass_f, double *__restrict__ xs, float4 *__restrict__ ph,
-                         float4 *__restrict__ pl) {
+                         float4 *__restrict__ pl, unsigned *__restrict__ inv) {
     const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const unsigned i = perm[j];
+    inv[i] = j;
     double d[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -746,7 +747,8 @@ void build_tree(Workspace &ws) {
         k_leaf_sort<<<capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4)), 32 * nw, smem, st>>>(
             ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.T, ws.perm);
     }
-    k_gather<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.perm, ws.info, static_cast<float>(ws.m), ws.xs, ws.ph, ws.pl);
+    k_gather<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.perm, ws.info, static_cast<float>(ws.m), ws.xs, ws.ph, ws.pl,
+                                               ws.inv);
     k_lists<<<gs, 256, 0, st>>>(ws.ent, ws.d_counts, ws.split_cell, ws.info, ws.c_child, ws.c_path, ws.c_coord,
                                 ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                                 reinterpret_cast<unsigned long long *>(&ws.info->m2l_pairs));

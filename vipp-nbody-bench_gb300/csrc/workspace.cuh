@@ -65,6 +65,7 @@ struct Workspace {
     unsigned *perm0 = nullptr, *perm1 = nullptr;
     uint64_t *keys = nullptr;  // points at the sorted buffer
     unsigned *perm = nullptr;
+    unsigned *inv = nullptr;                // [N] tree position of particle i (perm[inv[i]] = i)
     double *xs = nullptr;                   // [3][N]
     float4 *ph = nullptr, *pl = nullptr;    // hi/lo positions, w = mass (hi) / 0
     void *nearf = nullptr, *farf = nullptr; // [3][N] of FP32 or FP64

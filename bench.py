@@ -78,7 +78,12 @@ def plummer(n: int, seed: int, rmax: float = 10.0):
     return np.ascontiguousarray(x), np.ascontiguousarray(v)
 
 
-def batch_measure(steps=4, warmup=2, nsys=512, seed=3, sample=8):
+# DRAM bytes per launch of the BF16-split M2L on the 4M workload
+# (profiles/dram_plummer4M_p8_mixed.md)
+M2L_BF16_TRAFFIC = 139474944 + 19757568
+
+
+def batch_measure(steps=4, warmup=2, nsys=512, seed=3, sample=8, flags=0):
     """Batching form: nsys Plummer systems, N log-uniform in [1024, 65536],
     scale radius uniform in [0.5, 2] (positions x R, velocities x R^-1/2), total
     mass 1 each, eps = 0.01, p = 6, s = 32, mixed precision, dt = 1e-3, all
@@ -96,7 +101,7 @@ def batch_measure(steps=4, warmup=2, nsys=512, seed=3, sample=8):
         vs.append(v / math.sqrt(radii[k]))
     X, V = np.concatenate(xs), np.concatenate(vs)
     t0 = time.perf_counter()
-    b = vipp_gb300.Batch(sizes, p=6, s=32, eps=0.01, masses=1.0 / sizes, precision="mixed")
+    b = vipp_gb300.Batch(sizes, p=6, s=32, eps=0.01, masses=1.0 / sizes, precision="mixed", flags=flags)
     b.upload(X, V)
     setup = time.perf_counter() - t0
     for _ in range(warmup):
@@ -276,6 +281,10 @@ def main():
     ap.add_argument("--flags", type=int, default=0, help="gb_config flags (vipp_gb300.FLAG_*)")
     ap.add_argument("--no-energy", action="store_true", help="skip the total-energy drift (two extra evaluations)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching form (512 independent systems)")
+    ap.add_argument("--m2l", default="bf16", choices=["bf16", "tf32"],
+                    help="mixed form's tensor-core M2L split: bf16 hi/lo (the 4M Plummer and batching configurations' "
+                         "form, GB_FLAG_M2L_BF16) or 3 x tf32 (the library default)")
+    ap.add_argument("--no-alt", action="store_true", help="skip the timing of the other M2L split")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
@@ -293,6 +302,9 @@ def main():
         dist.init_process_group("nccl")
     import vipp_gb300
 
+    base_flags = args.flags
+    if args.precision == "mixed" and args.m2l == "bf16":
+        args.flags |= vipp_gb300.FLAG_M2L_BF16
     n = args.n
     x, v = plummer(n, 2 + rank)
     m = 1.0 / n
@@ -458,8 +470,9 @@ def main():
         # default workload (profiles/dram_plummer4M_p8_mixed.md); other
         # workloads have no capture, so null
         default_cfg = (n == 1 << 22 and args.p == 8 and args.s == 64 and args.eps == 0.005 and args.precision == "mixed"
-                       and args.flags == 0)
-        traffic = {"p2p": 293120768 + 40724736, "m2l": 188582656 + 19934464} if default_cfg else {}
+                       and args.flags & ~vipp_gb300.FLAG_M2L_BF16 == 0)
+        bf = bool(args.flags & vipp_gb300.FLAG_M2L_BF16)
+        traffic = {"p2p": 293120768 + 40724736, "m2l": (M2L_BF16_TRAFFIC if bf else 188582656 + 19934464)} if default_cfg else {}
         for k in per:
             per[k]["traffic"] = traffic.get(k)
         roof.update({"kernel": dom, "traffic": traffic.get(dom), "traffic_unit": "B per launch"})
@@ -468,15 +481,47 @@ def main():
 
     batched = None
     if rank == 0 and not args.no_batch:
-        batched = batch_measure()
+        batched = batch_measure(flags=args.flags & vipp_gb300.FLAG_M2L_BF16)
+        batched["m2l_split"] = "bf16 hi/lo" if args.flags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32"
+
+    # --- the other M2L split on the same workload (value and energy drift) -------
+    alt = None
+    if rank == 0 and args.precision == "mixed" and not args.no_alt:
+        aflags = base_flags if args.flags & vipp_gb300.FLAG_M2L_BF16 else base_flags | vipp_gb300.FLAG_M2L_BF16
+        with vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision="mixed", device=local,
+                               flags=aflags) as sa:
+            sa.preprocess(x, v)
+            for _ in range(args.warmup):
+                sa.solve(args.dt)
+            sa.sync()
+            ca0 = sa.conserved() if not args.no_energy else None
+            sta = torch.cuda.ExternalStream(sa.stream_ptr(), device=local)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            sa.sync()
+            e0.record(sta)
+            for _ in range(args.steps):
+                sa.solve(args.dt)
+            e1.record(sta)
+            e1.synchronize()
+            sa.sync()
+            ta = e0.elapsed_time(e1) / 1e3
+            drift = None
+            if ca0 is not None:
+                ca1 = sa.conserved()
+                drift = abs(ca1["total"] - ca0["total"]) / abs(ca0["total"])
+        alt = {"m2l_split": "bf16 hi/lo" if aflags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32", "value": n * args.steps / ta,
+               "unit": UNIT, "steps": args.steps, "ms_per_step": 1e3 * ta / args.steps, "energy_rel_drift": drift}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline_sample(x, args.s, args.p, args.eps)
 
     kt_ms = {k: round(v[0] / class_steps, 4) for k, v in kt.items()}
+    m2l_split = (None if args.precision != "mixed" else "cuda cores fp32" if args.flags & vipp_gb300.FLAG_M2L_CUDA_CORES
+                 else "bf16 hi/lo" if args.flags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32")
     cfg = {"workload": f"plummer-{n} p={args.p} s={args.s} eps={args.eps} {args.precision}", "N": n, "p": args.p,
-           "s": args.s, "eps": args.eps, "dt": args.dt, "precision": args.precision, "seed": 2,
+           "s": args.s, "eps": args.eps, "dt": args.dt, "precision": args.precision, "m2l_split": m2l_split, "seed": 2,
            "l2": "inputs larger than L2 (state 192 MB, per-step working set > 1 GB)",
            "tree": {k: st[k] for k in ("ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges")},
            "kernel_ms_per_step": kt_ms, **acc_info, "energy": energy, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
@@ -485,7 +530,7 @@ def main():
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
             "config": cfg, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
-            "roofline_kernels": per, "plain_fp64": plain, "batched": batched, "cpu_baseline": cpu}
+            "roofline_kernels": per, "plain_fp64": plain, "batched": batched, "m2l_other_split": alt, "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -335,7 +335,9 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
         const bool active = lane < kGW;
         const bool do_hi = active && (kGW >= 64 || g0 < 32);
         const bool do_lo = !BF && active && (kGW >= 64 || g0 >= 32);
-        const unsigned warp_bytes = static_cast<unsigned>(kGW) * 512u + (q == 0 ? 2u * C::B_BYTES : 0u);
+        // operator bytes of chunk kc: [Bhi; Blo], or (bf16) Bhi alone for a chunk
+        // of lo inputs only, whose MMAs read only the first N rows
+        auto b_bytes = [](int kc) { return (BF && kc * C::KC >= C::K) ? 1u * C::B_BYTES : 2u * C::B_BYTES; };
         const int zrow = rows_cap - 1;
         unsigned step = 0;
         bool stop = false;
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                     int ok = 1;
                     if (lane == 0) {
                         if (use > 0 && !mbar_wait(empty + st, (use - 1) & 1, abort_flag)) ok = 0;
-                        if (ok) mbar_expect_tx(full + st, warp_bytes);
+                        if (ok) mbar_expect_tx(full + st, static_cast<unsigned>(kGW) * 512u + (q == 0 ? b_bytes(kc) : 0u));
                     }
                     if (!__shfl_sync(0xffffffffu, ok, 0)) {
                         stop = true;
@@ -382,7 +384,7 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                                     cur[2] + rows_cap, cur[3] + rows_cap, full + st);
                     if (q == 0 && lane == 0)
                         bulk_g2s(stage + C::NA * C::A_BYTES, bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::B_BYTES),
-                                 2 * C::B_BYTES, full + st);
+                                 b_bytes(kc), full + st);
                 }
 #pragma unroll
                 for (int i = 0; i < 4; ++i) cur[i] = nxt[i];

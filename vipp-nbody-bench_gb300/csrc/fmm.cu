@@ -499,7 +499,9 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256, GB_FAR_MIN_BLOC
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int e0 = info->split_start[L], cnt = info->split_count[L];
     const int tiles = (cnt + kTile - 1) / kTile;
-    if (tiles == 0) return;  // uniform over the grid: no cluster barrier reached
+    // uniform over each cluster (it shares blockIdx.x / 8): a cluster without a
+    // tile reaches no cluster barrier and skips loading its operator
+    if (static_cast<int>(blockIdx.x) / 8 >= tiles) return;
     tile_clear<P, T>(A);
     tile_load_op<P, T>(Op, ops, kOpM2M + o);
     const int nclusters = static_cast<int>(gridDim.x) / 8;
@@ -553,7 +555,7 @@ __global__ void __launch_bounds__(256, GB_FAR_MIN_BLOCKS) k_l2l(int Lp, const Tr
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int e0 = info->split_start[Lp], cnt = info->split_count[Lp];
     const int tiles = (cnt + kTile - 1) / kTile;
-    if (tiles == 0) return;
+    if (static_cast<int>(blockIdx.x) >= 8 * tiles) return;  // no (tile, octant) for this block
     tile_clear<P, T>(A);
     for (int w = blockIdx.x; w < 8 * tiles; w += gridDim.x) {
         const int o = w % 8, tile = w / 8;

@@ -350,7 +350,6 @@ void evaluate(gb_ctx *ctx, bool to_acc = true) {
     // Near field on the second stream, unless serial or timed: class timers
     // measure each class alone on one stream.
     const bool fork = !ws.serial && !ws.timing;
-    gb::p2p_reset(ws);
     const unsigned conc = gb::p2p_blocks_per_sm(true), full = gb::p2p_blocks_per_sm(false);
     if (fork) {
         cudaEventRecord(ws.ev_fork, ws.st);

@@ -612,7 +612,11 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_L2P_MIN_BLOCKS : GB_F
     for (unsigned li = blockIdx.x * (blockDim.x >> 5) + w; li < NL; li += warps) {
         const int c = leaves[li];
         const int L = c_level[c];
-        if (L < 2) continue;
+        if (L < 2) {  // no local expansion: these particles' far field is zero
+            for (int j = c_begin[c] + lane; j < c_end[c]; j += 32)
+                far[j] = T(0), far[n + j] = T(0), far[2 * static_cast<size_t>(n) + j] = T(0);
+            continue;
+        }
         for (int r = lane; r < K; r += 32) Ls[w][r] = Lx[static_cast<size_t>(c) * K + r];
         __syncwarp();
         const double s = level_scale(info, L), inv_s = 1.0 / s;
@@ -843,9 +847,7 @@ void m2l_pass(Workspace &ws) {
 
 void downward_pass(Workspace &ws) {
     timer_begin(ws, kTDown);
-    const size_t esz = ws.mixed ? sizeof(float) : sizeof(double);
-    cudaMemsetAsync(ws.farf, 0, esz * 3 * ws.n, ws.st);
-    if (ws.mixed) {
+    if (ws.mixed) {  // L2P writes every particle's far field (zero above level 2)
         dispatch_p<float>(ws, 4);
         dispatch_p<float>(ws, 2);
     } else {

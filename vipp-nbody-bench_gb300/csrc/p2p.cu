@@ -408,10 +408,9 @@ void near_potential(Workspace &ws, double *phiv) {
 }
 
 // Near-field kernel over the work queue, `per_sm` blocks per SM. The queue
-// counter is reset by p2p_reset; several launches (on any streams) may drain
-// the same queue, each item is taken once. p2p_finish adds the slices of
-// split items after all of them.
-void p2p_reset(Workspace &ws) { cudaMemsetAsync(ws.queue, 0, sizeof(unsigned), ws.st); }
+// counter is zeroed at the start of every evaluation (build_tree); several
+// launches (on any streams) may drain the same queue, each item is taken once.
+// p2p_finish adds the slices of split items after all of them.
 
 unsigned p2p_blocks_per_sm(bool concurrent) { return concurrent ? GB_P2P_CONCURRENT_PER_SM : GB_P2P_BLOCKS_PER_SM; }
 

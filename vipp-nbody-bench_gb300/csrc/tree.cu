@@ -259,9 +259,14 @@ __device__ unsigned lower_bound_pre(const uint64_t *keys, unsigned lo, unsigned 
     return lo;
 }
 
+__device__ void path_geometry(uint64_t path, int L, const TreeInfo *info, double *box, double *ctr, int *coord);
+
 // One warp: lane L finds level L's split entries (ent is sorted by level),
 // then the cell counts and starts of every level follow by a warp scan.
-__global__ void k_level_table(const uint64_t *__restrict__ ent, unsigned *counts, TreeInfo *info, unsigned n) {
+__global__ void k_level_table(const uint64_t *__restrict__ ent, unsigned *counts, TreeInfo *info, unsigned n, int T,
+                              int *c_begin, int *c_end, int *c_parent, int *c_child, int *c_level, uint64_t *c_path,
+                              int *c_coord, double *c_box, double *c_ctr, int *p2p_own, int *p2p_cnt, int *coll,
+                              int *coll_cnt) {
     static_assert(kMaxLevel + 2 <= 32, "one lane per level");
     const int L = static_cast<int>(threadIdx.x);
     if (L >= 32) return;
@@ -297,8 +302,22 @@ __global__ void k_level_table(const uint64_t *__restrict__ ent, unsigned *counts
         info->n_targets_m2l = depth >= 2 ? start - start2 : 0;
         counts[2] = static_cast<unsigned>(start);
         counts[3] = static_cast<unsigned>(start) - S;
+        // the root cell
+        c_begin[0] = 0;
+        c_end[0] = static_cast<int>(n);
+        c_parent[0] = -1;
+        c_level[0] = 0;
+        c_path[0] = 0;
+        const bool split = static_cast<long long>(n) > T;
+        c_child[0] = split ? 1 : -1;
+        path_geometry(0, 0, info, c_box, c_ctr, c_coord);
+        // calc_link at the root (solver_ref.hpp:148-154)
+        if (split) {
+            coll[0] = 0, coll_cnt[0] = 1, p2p_cnt[0] = 0;
+        } else {
+            p2p_own[0] = 0, p2p_cnt[0] = 1, coll_cnt[0] = 0;
+        }
     }
-    (void)n;
 }
 
 __device__ void path_geometry(uint64_t path, int L, const TreeInfo *info, double *box, double *ctr, int *coord) {
@@ -327,25 +346,6 @@ __device__ void path_geometry(uint64_t path, int L, const TreeInfo *info, double
     }
 }
 
-__global__ void k_root(unsigned n, int T, const TreeInfo *__restrict__ info, int *c_begin, int *c_end, int *c_parent,
-                       int *c_child, int *c_level, uint64_t *c_path, int *c_coord, double *c_box, double *c_ctr,
-                       int *p2p_own, int *p2p_cnt, int *coll, int *coll_cnt) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    c_begin[0] = 0;
-    c_end[0] = static_cast<int>(n);
-    c_parent[0] = -1;
-    c_level[0] = 0;
-    c_path[0] = 0;
-    const bool split = static_cast<long long>(n) > T;
-    c_child[0] = split ? 1 : -1;
-    path_geometry(0, 0, info, c_box, c_ctr, c_coord);
-    // calc_link at the root (solver_ref.hpp:148-154)
-    if (split) {
-        coll[0] = 0, coll_cnt[0] = 1, p2p_cnt[0] = 0;
-    } else {
-        p2p_own[0] = 0, p2p_cnt[0] = 1, coll_cnt[0] = 0;
-    }
-}
 
 // One thread per (split cell, child octant): the 8 threads of a split cell
 // find its number and particle range (the same searches, in one warp), then
@@ -697,7 +697,16 @@ __global__ void k_check_totals(unsigned *counts, unsigned r_cap, unsigned ch_cap
     info->n_p2p_chunks = static_cast<int>(counts[5]);
 }
 
-__global__ void k_set_count(unsigned *counts, unsigned n) { counts[0] = n; }
+// Start of an evaluation (one block): TreeInfo and the device counters zeroed,
+// counts[0] = n, the near-field work queue emptied; a kernel rather than host
+// copies or memsets, so the whole evaluation is one short graph section.
+__global__ void k_eval_begin(TreeInfo *info, unsigned *counts, unsigned n, unsigned *queue) {
+    static_assert(sizeof(TreeInfo) % sizeof(unsigned) == 0, "TreeInfo in words");
+    unsigned *iw = reinterpret_cast<unsigned *>(info);
+    for (unsigned k = threadIdx.x; k < sizeof(TreeInfo) / sizeof(unsigned); k += blockDim.x) iw[k] = 0;
+    for (unsigned k = threadIdx.x; k < static_cast<unsigned>(kNumCounts); k += blockDim.x) counts[k] = k == 0 ? n : 0u;
+    if (threadIdx.x == 0) *queue = 0;
+}
 
 inline unsigned grid_for(unsigned n, int tb) { return (n + tb - 1) / tb; }
 
@@ -707,15 +716,13 @@ void build_tree(Workspace &ws) {
     const unsigned n = ws.n;
     cudaStream_t st = ws.st;
     timer_begin(ws, kTTree);
-    cudaMemsetAsync(ws.info, 0, sizeof(TreeInfo), st);
-    cudaMemsetAsync(ws.d_counts, 0, kNumCounts * sizeof(unsigned), st);
-    k_set_count<<<1, 1, 0, st>>>(ws.d_counts, n);  // a kernel, not a host copy: the step is captured in a graph
+    k_eval_begin<<<1, 128, 0, st>>>(ws.info, ws.d_counts, n, ws.queue);
     const int nb = 2 * ws.num_sms;
     double *part = ws.bbox_part;
     k_bbox_partial<<<nb, kTB, 0, st>>>(ws.x, n, part, ws.info);
     k_bbox_final<<<1, kTB, 0, st>>>(part, nb, ws.info);
     k_keys<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.keys0, ws.perm0);
-    ws.launches += 3;
+    ws.launches += 4;
     const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, 3 * (kMaxLevel - ws.sort_levels),
                                    3 * kMaxLevel, ws.sort, st, &ws.launches, &ws.info->err, kDevTimeout);
     ws.keys = res ? ws.keys1 : ws.keys0;
@@ -729,9 +736,9 @@ void build_tree(Workspace &ws) {
     const int re = radix_sort_u64(ws.ent0, nullptr, ws.ent1, nullptr, ws.s_cap, ws.d_counts + 1, 32, 40, ws.sort, st,
                                   &ws.launches, &ws.info->err, kDevTimeout);
     ws.ent = re ? ws.ent1 : ws.ent0;
-    k_level_table<<<1, 32, 0, st>>>(ws.ent, ws.d_counts, ws.info, n);
-    k_root<<<1, 32, 0, st>>>(n, ws.T, ws.info, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path,
-                             ws.c_coord, ws.c_box, ws.c_ctr, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt);
+    k_level_table<<<1, 32, 0, st>>>(ws.ent, ws.d_counts, ws.info, n, ws.T, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child,
+                                    ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr, ws.p2p_own, ws.p2p_cnt, ws.coll,
+                                    ws.coll_cnt);
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 4, ceil_div(ws.c_cap, 32));
     k_cells<<<capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 128)), 128, 0, st>>>(ws.ent, ws.d_counts, ws.keys, n, ws.T, ws.info, ws.split_cell, ws.c_begin, ws.c_end,
                                 ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr);
@@ -761,7 +768,7 @@ void build_tree(Workspace &ws) {
     k_rng_fill<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.r_cap, ws.ch_cap, ws.c_parent, ws.c_begin, ws.c_end,
                                    ws.p2p_own, ws.p2p_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_off, ws.chunks,
                                    ws.src_total, ws.part_off, ws.part_cap, ws.info);
-    ws.launches += 13;
+    ws.launches += 10;
     timer_end(ws, kTTree);
 }
 

@@ -158,7 +158,6 @@ size_t m2l_tc_image_floats(int p);
 int m2l_tc_row_floats(int p);
 const char *m2l_tc_encode(Workspace &ws);     // (re)build tmap_ms; nullptr or an error message
 void downward_pass(Workspace &ws);            // L2L + L2P into far
-void p2p_reset(Workspace &ws);                // empty the near-field work queue
 void p2p_pass(Workspace &ws, unsigned per_sm); // near-field kernel over the queue, per_sm blocks per SM
 void p2p_finish(Workspace &ws);               // add the slices of split items: near complete
 unsigned p2p_blocks_per_sm(bool concurrent);   // P2P blocks per SM alone / beside the far field

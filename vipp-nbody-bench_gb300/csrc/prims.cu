@@ -352,8 +352,15 @@ void scan_exclusive_u32(const unsigned *in, unsigned *out, unsigned n_cap, const
     if (launches) *launches += 3;
 }
 
+SortZero sort_zero_plan(const SortTemp &t, unsigned n_cap, int bit_lo, int bit_hi) {
+    const unsigned tiles = (n_cap + kSortTile - 1) / kSortTile;
+    const int npasses = (bit_hi - bit_lo + 7) / 8;
+    return SortZero{t.ghist, t.status, static_cast<size_t>(256) * static_cast<size_t>(npasses > 0 ? npasses : 0) * tiles};
+}
+
 int radix_sort_u64(uint64_t *k0, unsigned *v0, uint64_t *k1, unsigned *v1, unsigned n_cap, const unsigned *d_n,
-                   int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches, int *d_err, int err_bit) {
+                   int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches, int *d_err, int err_bit,
+                   bool prezeroed) {
     const unsigned tiles = (n_cap + kSortTile - 1) / kSortTile;
     const int npasses = (bit_hi - bit_lo + 7) / 8;
     if (tiles == 0 || npasses <= 0) return 0;
@@ -362,8 +369,10 @@ int radix_sort_u64(uint64_t *k0, unsigned *v0, uint64_t *k1, unsigned *v1, unsig
         return 0;
     }
     cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kScatterSmem));
-    cudaMemsetAsync(tmp.ghist, 0, sizeof(unsigned) * (256 + 1) * kMaxPasses, st);  // histograms and tickets
-    cudaMemsetAsync(tmp.status, 0, sizeof(unsigned long long) * 256 * static_cast<size_t>(npasses) * tiles, st);
+    if (!prezeroed) {
+        cudaMemsetAsync(tmp.ghist, 0, sizeof(unsigned) * (256 + 1) * kMaxPasses, st);  // histograms and tickets
+        cudaMemsetAsync(tmp.status, 0, sizeof(unsigned long long) * 256 * static_cast<size_t>(npasses) * tiles, st);
+    }
     k_sweep_hist<<<tiles < 1024u ? tiles : 1024u, 256, 0, st>>>(k0, n_cap, d_n, bit_lo, npasses, tmp.ghist);
     int cur = 0;
     for (int p = 0; p < npasses; ++p) {

@@ -37,9 +37,30 @@ struct SortTemp {
 // Ping-pongs between (k0, v0) and (k1, v1); returns 0 if the result is in
 // (k0, v0), 1 if in (k1, v1). vals may be nullptr (keys only). A look-back
 // wait that gives up sets err_bit in *d_err (if d_err is not null).
+// prezeroed: a kernel queued before the sort has run sort_temp_zero over
+// the sort's temporaries (saves two memset nodes per sort).
 int radix_sort_u64(uint64_t *k0, unsigned *v0, uint64_t *k1, unsigned *v1, unsigned n_cap, const unsigned *d_n,
                    int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches, int *d_err = nullptr,
-                   int err_bit = 0);
+                   int err_bit = 0, bool prezeroed = false);
+
+// What a sort of n_cap keys over bits [bit_lo, bit_hi) needs zeroed: the
+// histogram and ticket words, and npasses x tiles x 256 look-back words.
+struct SortZero {
+    unsigned *ghist;
+    unsigned long long *status;
+    size_t status_words;
+};
+SortZero sort_zero_plan(const SortTemp &t, unsigned n_cap, int bit_lo, int bit_hi);
+
+#ifdef __CUDACC__
+// Zero the sort temporaries from every thread of a grid (any grid shape).
+__device__ __forceinline__ void sort_temp_zero(const SortZero &z) {
+    const size_t tid = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+    const size_t nt = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t k = tid; k < static_cast<size_t>(256 + 1) * kMaxPasses; k += nt) z.ghist[k] = 0u;
+    for (size_t k = tid; k < z.status_words; k += nt) z.status[k] = 0ull;
+}
+#endif
 
 // Allocation helpers for the temporaries (sized for n_cap elements).
 cudaError_t scan_temp_alloc(ScanTemp &t, unsigned n_cap);

@@ -141,7 +141,8 @@ __device__ __forceinline__ uint64_t spread3(uint64_t v) {
 
 // Child offsets of 21 levels of recursive midpoints (see file comment).
 __global__ void k_keys(const double *__restrict__ x, unsigned n, const TreeInfo *__restrict__ info,
-                       uint64_t *__restrict__ keys, unsigned *__restrict__ perm) {
+                       uint64_t *__restrict__ keys, unsigned *__restrict__ perm, SortZero z) {
+    sort_temp_zero(z);  // for the key sort that follows
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double p[3] = {x[i], x[static_cast<size_t>(n) + i], x[2 * static_cast<size_t>(n) + i]};
@@ -214,20 +215,22 @@ __global__ void k_split_count(const uint64_t *__restrict__ keys, unsigned n, int
     cnt[i] = Lm >= Ls ? static_cast<unsigned>(Lm - Ls + 1) : 0u;
 }
 
-// Overflow of the split buffer or a too shallow key sort: the attempt builds
-// a root-only tree (nothing addresses past a buffer) and the host repeats it.
-__global__ void k_check_split_total(unsigned *counts, unsigned s_cap, TreeInfo *info) {
-    counts[6] = counts[1];  // requested size, kept for the host when it overflows
-    if (counts[1] > s_cap || counts[9] != 0) {
-        atomicOr(&info->err, kDevCapacity);
-        counts[1] = 0;
-    }
-}
-
+// Split entries (level << 32 | first particle) at their scanned offsets. On
+// an overflow of the split buffer or a too shallow key sort (seen by thread
+// 0, which zeroes the count) the attempt builds a root-only tree (nothing
+// addresses past a buffer) and the host repeats it.
 __global__ void k_split_emit(const uint64_t *__restrict__ keys, unsigned n, int T, const unsigned *__restrict__ off,
-                             const unsigned *counts, unsigned s_cap, uint64_t *__restrict__ ent) {
+                             unsigned *counts, unsigned s_cap, uint64_t *__restrict__ ent, TreeInfo *info, SortZero z) {
+    sort_temp_zero(z);  // for the entry sort that follows (the key sort is done with them)
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || counts[1] == 0) return;
+    const unsigned total = counts[1];
+    const bool over = total > s_cap || counts[9] != 0;
+    if (i == 0) {
+        counts[6] = total;  // requested size, kept for the host when it overflows
+        if (over) atomicOr(&info->err, kDevCapacity), counts[1] = 0;
+    }
+    // a block that reads counts[1] after thread 0 zeroed it sees 0 and also writes nothing
+    if (i >= n || over || total == 0) return;
     const int Ls = i == 0 ? 0 : first_diff_level(keys[i - 1], keys[i]);
     int Lm = -1;
     if (static_cast<unsigned long long>(i) + T < n) Lm = min(first_diff_level(keys[i], keys[i + T]) - 1, kMaxLevel - 1);
@@ -599,12 +602,24 @@ __global__ void k_rng_count(const int *__restrict__ leaves, const unsigned *coun
     }
 }
 
-__global__ void k_rng_fill(const int *__restrict__ leaves, const unsigned *counts, unsigned r_cap, unsigned ch_cap,
+// Thread 0 first checks the near-field totals against the buffers: on any
+// overflow the evaluation queues no P2P work item at all (this kernel may still
+// address items whose partial-sum slot lies past part_cap, and the P2P kernels
+// run before the host sees the flag, grows the buffers and repeats the
+// evaluation).
+__global__ void k_rng_fill(const int *__restrict__ leaves, unsigned *counts, unsigned r_cap, unsigned ch_cap,
                            const int *__restrict__ c_parent, const int *__restrict__ c_begin, const int *__restrict__ c_end,
                            const int *__restrict__ p2p_own, const int *__restrict__ p2p_cnt,
                            const unsigned *__restrict__ rng_off, unsigned *rng_len, uint2 *ranges,
                            const unsigned *__restrict__ chunk_off, int4 *chunks, const unsigned *__restrict__ src_total,
                            const unsigned *__restrict__ part_off, unsigned part_cap, TreeInfo *info) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counts[7] = counts[5];  // requested sizes, kept for the host when they overflow
+        const bool over = counts[4] > r_cap || counts[5] > ch_cap || counts[8] > part_cap;
+        if (over) atomicOr(&info->err, kDevCapacity);
+        counts[5] = over ? 0u : counts[5];
+        info->n_p2p_chunks = static_cast<int>(counts[5]);
+    }
     const unsigned NL = counts[3];
     unsigned long long pairs = 0, nranges = 0;  // this thread's totals, added once per warp below
     for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < NL; li += gridDim.x * blockDim.x) {
@@ -685,18 +700,6 @@ __global__ void k_rng_fill(const int *__restrict__ leaves, const unsigned *count
     }
 }
 
-// On any overflow of the near-field buffers the evaluation queues no P2P work
-// item at all: k_rng_fill may still address items whose partial-sum slot lies
-// past part_cap, and the P2P kernels run before the host sees the flag, grows
-// the buffers and repeats the evaluation.
-__global__ void k_check_totals(unsigned *counts, unsigned r_cap, unsigned ch_cap, unsigned part_cap, TreeInfo *info) {
-    counts[7] = counts[5];  // requested sizes, kept for the host when they overflow
-    const bool over = counts[4] > r_cap || counts[5] > ch_cap || counts[8] > part_cap;
-    if (over) atomicOr(&info->err, kDevCapacity);
-    counts[5] = over ? 0u : counts[5];
-    info->n_p2p_chunks = static_cast<int>(counts[5]);
-}
-
 // Start of an evaluation (one block): TreeInfo and the device counters zeroed,
 // counts[0] = n, the near-field work queue emptied; a kernel rather than host
 // copies or memsets, so the whole evaluation is one short graph section.
@@ -721,20 +724,22 @@ void build_tree(Workspace &ws) {
     double *part = ws.bbox_part;
     k_bbox_partial<<<nb, kTB, 0, st>>>(ws.x, n, part, ws.info);
     k_bbox_final<<<1, kTB, 0, st>>>(part, nb, ws.info);
-    k_keys<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.keys0, ws.perm0);
+    const int kbit = 3 * (kMaxLevel - ws.sort_levels);
+    k_keys<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.keys0, ws.perm0,
+                                             sort_zero_plan(ws.sort, n, kbit, 3 * kMaxLevel));
     ws.launches += 4;
-    const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, 3 * (kMaxLevel - ws.sort_levels),
-                                   3 * kMaxLevel, ws.sort, st, &ws.launches, &ws.info->err, kDevTimeout);
+    const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, kbit, 3 * kMaxLevel, ws.sort, st,
+                                   &ws.launches, &ws.info->err, kDevTimeout, true);
     ws.keys = res ? ws.keys1 : ws.keys0;
     ws.perm = res ? ws.perm1 : ws.perm0;
     // split cells of every level
     k_split_count<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.sort_levels, ws.cnt, ws.d_counts, ws.info);
     scan_exclusive_u32(ws.cnt, ws.off, n, nullptr, ws.d_counts + 1, ws.scan, st, &ws.launches);
-    k_check_split_total<<<1, 1, 0, st>>>(ws.d_counts, ws.s_cap, ws.info);
-    k_split_emit<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.off, ws.d_counts, ws.s_cap, ws.ent0);
-    ws.launches += 3;
+    k_split_emit<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.off, ws.d_counts, ws.s_cap, ws.ent0, ws.info,
+                                                   sort_zero_plan(ws.sort, ws.s_cap, 32, 40));
+    ws.launches += 2;
     const int re = radix_sort_u64(ws.ent0, nullptr, ws.ent1, nullptr, ws.s_cap, ws.d_counts + 1, 32, 40, ws.sort, st,
-                                  &ws.launches, &ws.info->err, kDevTimeout);
+                                  &ws.launches, &ws.info->err, kDevTimeout, true);
     ws.ent = re ? ws.ent1 : ws.ent0;
     k_level_table<<<1, 32, 0, st>>>(ws.ent, ws.d_counts, ws.info, n, ws.T, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child,
                                     ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr, ws.p2p_own, ws.p2p_cnt, ws.coll,
@@ -764,11 +769,10 @@ void build_tree(Workspace &ws) {
     scan_exclusive_u32(ws.rng_cnt, ws.rng_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 4, ws.scan, st, &ws.launches);
     scan_exclusive_u32(ws.chunk_cnt, ws.chunk_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 5, ws.scan, st, &ws.launches);
     scan_exclusive_u32(ws.part_cnt, ws.part_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 8, ws.scan, st, &ws.launches);
-    k_check_totals<<<1, 1, 0, st>>>(ws.d_counts, ws.r_cap, ws.ch_cap, ws.part_cap, ws.info);
     k_rng_fill<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.r_cap, ws.ch_cap, ws.c_parent, ws.c_begin, ws.c_end,
                                    ws.p2p_own, ws.p2p_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_off, ws.chunks,
                                    ws.src_total, ws.part_off, ws.part_cap, ws.info);
-    ws.launches += 10;
+    ws.launches += 9;
     timer_end(ws, kTTree);
 }
 

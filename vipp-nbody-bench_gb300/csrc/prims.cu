@@ -55,11 +55,13 @@ __device__ unsigned block_exclusive_scan(unsigned v, unsigned *warp_buf /*[32]*/
 }
 
 // Whole scan in one block (small inputs): chunks of 4 elements per thread,
-// carried from chunk to chunk; in == out is allowed.
+// carried from chunk to chunk; in == out is allowed. Block a scans array a.
 constexpr unsigned kSmallScanMax = 1u << 16;
-__global__ void __launch_bounds__(1024) k_scan_small(const unsigned *in, unsigned *out, unsigned n_cap, const unsigned *d_n,
-                                                     unsigned *d_total) {
+__global__ void __launch_bounds__(1024) k_scan_small(ScanSet ss, unsigned n_cap, const unsigned *d_n) {
     __shared__ unsigned wb[32];
+    const int a = blockIdx.x;
+    const unsigned *in = ss.in[a];
+    unsigned *out = ss.out[a];
     const unsigned n = d_n ? *d_n : n_cap;
     unsigned carry = 0;
     for (unsigned base = 0; base < n; base += 4 * blockDim.x) {
@@ -79,12 +81,15 @@ __global__ void __launch_bounds__(1024) k_scan_small(const unsigned *in, unsigne
         }
         carry += tot;
     }
-    if (d_total && threadIdx.x == 0) *d_total = carry;
+    if (ss.total[a] && threadIdx.x == 0) *ss.total[a] = carry;
 }
 
-__global__ void k_scan_reduce(const unsigned *__restrict__ in, unsigned n_cap, const unsigned *d_n,
-                              unsigned *__restrict__ tile_sums) {
+// Three-launch scan of larger inputs: tile sums (grid y = array), their scan
+// (block a = array a), then the tiles with their offsets.
+__global__ void k_scan_reduce(ScanSet ss, unsigned n_cap, const unsigned *d_n, unsigned *__restrict__ tile_sums,
+                              unsigned tstride) {
     __shared__ unsigned wb[32];
+    const unsigned *in = ss.in[blockIdx.y];
     const unsigned n = d_n ? *d_n : n_cap;
     const unsigned base = blockIdx.x * kScanTile;
     unsigned s = 0;
@@ -96,29 +101,34 @@ __global__ void k_scan_reduce(const unsigned *__restrict__ in, unsigned n_cap, c
     }
     unsigned tot;
     block_exclusive_scan(s, wb, &tot);
-    if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+    if (threadIdx.x == 0) tile_sums[blockIdx.y * tstride + blockIdx.x] = tot;
 }
 
-__global__ void k_scan_tiles(unsigned *__restrict__ tile_sums, unsigned n_cap, const unsigned *d_n, unsigned *d_total) {
+__global__ void k_scan_tiles(ScanSet ss, unsigned *__restrict__ tile_sums, unsigned tstride, unsigned n_cap,
+                             const unsigned *d_n) {
     __shared__ unsigned wb[32];
+    const int a = blockIdx.x;
+    unsigned *ts = tile_sums + a * tstride;
     const unsigned n = d_n ? *d_n : n_cap;
     const unsigned ntiles = (n + kScanTile - 1) / kScanTile;
     unsigned carry = 0;
     for (unsigned b = 0; b < ntiles; b += blockDim.x) {
         const unsigned i = b + threadIdx.x;
-        const unsigned v = i < ntiles ? tile_sums[i] : 0u;
+        const unsigned v = i < ntiles ? ts[i] : 0u;
         unsigned tot;
         const unsigned ex = block_exclusive_scan(v, wb, &tot);
-        if (i < ntiles) tile_sums[i] = carry + ex;
+        if (i < ntiles) ts[i] = carry + ex;
         carry += tot;
     }
-    if (d_total && threadIdx.x == 0) *d_total = carry;
+    if (ss.total[a] && threadIdx.x == 0) *ss.total[a] = carry;
 }
 
-__global__ void k_scan_apply(const unsigned *__restrict__ in, unsigned *__restrict__ out, unsigned n_cap,
-                             const unsigned *d_n, const unsigned *__restrict__ tile_sums) {
+__global__ void k_scan_apply(ScanSet ss, unsigned n_cap, const unsigned *d_n, const unsigned *__restrict__ tile_sums,
+                             unsigned tstride) {
     __shared__ unsigned buf[kScanTile];
     __shared__ unsigned wb[32];
+    const unsigned *in = ss.in[blockIdx.y];
+    unsigned *out = ss.out[blockIdx.y];
     const unsigned n = d_n ? *d_n : n_cap;
     const unsigned base = blockIdx.x * kScanTile;
     if (base >= n) return;  // uniform per block
@@ -136,7 +146,7 @@ __global__ void k_scan_apply(const unsigned *__restrict__ in, unsigned *__restri
         s += loc[k];
     }
     unsigned tot;
-    unsigned ex = block_exclusive_scan(s, wb, &tot) + tile_sums[blockIdx.x];
+    unsigned ex = block_exclusive_scan(s, wb, &tot) + tile_sums[blockIdx.y * tstride + blockIdx.x];
 #pragma unroll
     for (int k = 0; k < kPer; ++k) {
         buf[threadIdx.x * kPer + k] = ex;
@@ -300,7 +310,7 @@ cudaError_t scan_temp_alloc(ScanTemp &t, unsigned n_cap) {
     if (tiles <= t.max_tiles) return cudaSuccess;
     if (t.tile_sums) cudaFree(t.tile_sums);
     t.tile_sums = nullptr;
-    cudaError_t e = cudaMalloc(&t.tile_sums, sizeof(unsigned) * tiles);
+    cudaError_t e = cudaMalloc(&t.tile_sums, sizeof(unsigned) * kMaxScanArrays * static_cast<size_t>(tiles));
     t.max_tiles = e == cudaSuccess ? tiles : 0;
     return e;
 }
@@ -334,22 +344,32 @@ void sort_temp_free(SortTemp &t) {
     t.max_tiles = 0;
 }
 
-void scan_exclusive_u32(const unsigned *in, unsigned *out, unsigned n_cap, const unsigned *d_n, unsigned *d_total,
-                        ScanTemp &tmp, cudaStream_t st, int64_t *launches) {
+void scan_exclusive_multi(const ScanSet &s, int count, unsigned n_cap, const unsigned *d_n, ScanTemp &tmp, cudaStream_t st,
+                          int64_t *launches) {
     const unsigned tiles = (n_cap + kScanTile - 1) / kScanTile;
+    if (count <= 0) return;
     if (tiles == 0) {
-        if (d_total) cudaMemsetAsync(d_total, 0, sizeof(unsigned), st);
+        for (int a = 0; a < count; ++a)
+            if (s.total[a]) cudaMemsetAsync(s.total[a], 0, sizeof(unsigned), st);
         return;
     }
     if (n_cap <= kSmallScanMax) {  // one launch instead of three
-        k_scan_small<<<1, 1024, 0, st>>>(in, out, n_cap, d_n, d_total);
+        k_scan_small<<<count, 1024, 0, st>>>(s, n_cap, d_n);
         if (launches) *launches += 1;
         return;
     }
-    k_scan_reduce<<<tiles, 256, 0, st>>>(in, n_cap, d_n, tmp.tile_sums);
-    k_scan_tiles<<<1, 1024, 0, st>>>(tmp.tile_sums, n_cap, d_n, d_total);
-    k_scan_apply<<<tiles, 256, 0, st>>>(in, out, n_cap, d_n, tmp.tile_sums);
+    const unsigned tstride = static_cast<unsigned>(tmp.max_tiles);
+    k_scan_reduce<<<dim3(tiles, count), 256, 0, st>>>(s, n_cap, d_n, tmp.tile_sums, tstride);
+    k_scan_tiles<<<count, 1024, 0, st>>>(s, tmp.tile_sums, tstride, n_cap, d_n);
+    k_scan_apply<<<dim3(tiles, count), 256, 0, st>>>(s, n_cap, d_n, tmp.tile_sums, tstride);
     if (launches) *launches += 3;
+}
+
+void scan_exclusive_u32(const unsigned *in, unsigned *out, unsigned n_cap, const unsigned *d_n, unsigned *d_total,
+                        ScanTemp &tmp, cudaStream_t st, int64_t *launches) {
+    ScanSet s{};
+    s.in[0] = in, s.out[0] = out, s.total[0] = d_total;
+    scan_exclusive_multi(s, 1, n_cap, d_n, tmp, st, launches);
 }
 
 SortZero sort_zero_plan(const SortTemp &t, unsigned n_cap, int bit_lo, int bit_hi) {

@@ -11,9 +11,11 @@
 
 namespace gb {
 
+constexpr int kMaxScanArrays = 3;  // arrays one scan launch sequence can take
+
 struct ScanTemp {
-    unsigned *tile_sums = nullptr;  // capacity: max tiles
-    int max_tiles = 0;
+    unsigned *tile_sums = nullptr;  // [kMaxScanArrays][max_tiles]
+    int max_tiles = 0;              // per array
 };
 
 constexpr int kScanTile = 2048;  // 256 threads x 8
@@ -22,6 +24,16 @@ constexpr int kScanTile = 2048;  // 256 threads x 8
 // If d_total != nullptr, *d_total = sum of all n inputs. in == out allowed.
 void scan_exclusive_u32(const unsigned *in, unsigned *out, unsigned n_cap, const unsigned *d_n, unsigned *d_total,
                         ScanTemp &tmp, cudaStream_t st, int64_t *launches);
+
+// The same for up to kMaxScanArrays arrays of one length, in one launch
+// sequence: out[a] = exclusive scan of in[a], *total[a] (if non-null) = sum.
+struct ScanSet {
+    const unsigned *in[kMaxScanArrays];
+    unsigned *out[kMaxScanArrays];
+    unsigned *total[kMaxScanArrays];
+};
+void scan_exclusive_multi(const ScanSet &s, int count, unsigned n_cap, const unsigned *d_n, ScanTemp &tmp, cudaStream_t st,
+                          int64_t *launches);
 
 constexpr int kSortTile = 4096;  // 256 threads x 16 keys
 constexpr int kMaxPasses = 8;    // 8-bit digits: up to 64 key bits

@@ -766,9 +766,13 @@ void build_tree(Workspace &ws) {
                                 reinterpret_cast<unsigned long long *>(&ws.info->m2l_pairs));
     k_rng_count<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.c_parent, ws.c_begin, ws.c_end, ws.p2p_own, ws.p2p_cnt,
                                     ws.rng_cnt, ws.chunk_cnt, ws.src_total, ws.part_cnt);
-    scan_exclusive_u32(ws.rng_cnt, ws.rng_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 4, ws.scan, st, &ws.launches);
-    scan_exclusive_u32(ws.chunk_cnt, ws.chunk_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 5, ws.scan, st, &ws.launches);
-    scan_exclusive_u32(ws.part_cnt, ws.part_off, ws.c_cap, ws.d_counts + 3, ws.d_counts + 8, ws.scan, st, &ws.launches);
+    {  // range, work-item and partial-slot offsets per leaf, one scan sequence
+        ScanSet sc{};
+        sc.in[0] = ws.rng_cnt, sc.out[0] = ws.rng_off, sc.total[0] = ws.d_counts + 4;
+        sc.in[1] = ws.chunk_cnt, sc.out[1] = ws.chunk_off, sc.total[1] = ws.d_counts + 5;
+        sc.in[2] = ws.part_cnt, sc.out[2] = ws.part_off, sc.total[2] = ws.d_counts + 8;
+        scan_exclusive_multi(sc, 3, ws.c_cap, ws.d_counts + 3, ws.scan, st, &ws.launches);
+    }
     k_rng_fill<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.r_cap, ws.ch_cap, ws.c_parent, ws.c_begin, ws.c_end,
                                    ws.p2p_own, ws.p2p_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_off, ws.chunks,
                                    ws.src_total, ws.part_off, ws.part_cap, ws.info);

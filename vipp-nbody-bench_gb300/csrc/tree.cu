@@ -409,6 +409,48 @@ __global__ void k_leaf_flags(const int *__restrict__ c_child, const unsigned *co
     for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) flag[c] = c_child[c] < 0;
 }
 
+// The leaves in cell order by one block (smaller trees: one launch instead of
+// flags, scan and compaction).
+__global__ void __launch_bounds__(1024) k_leaf_list(const int *__restrict__ c_child, const unsigned *counts, int *leaves) {
+    __shared__ unsigned wsum[32];
+    const unsigned C = counts[2];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned base = 0;
+    for (unsigned start = 0; start < C; start += 4 * blockDim.x) {
+        const unsigned c0 = start + 4 * threadIdx.x;
+        unsigned f[4], s = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            f[j] = (c0 + j < C && c_child[c0 + j] < 0) ? 1u : 0u;
+            s += f[j];
+        }
+        unsigned incl = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            unsigned v = lane < nw ? wsum[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += y;
+            }
+            if (lane < nw) wsum[lane] = v;
+        }
+        __syncthreads();
+        unsigned pos = base + (w ? wsum[w - 1] : 0u) + incl - s;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (f[j]) leaves[pos++] = static_cast<int>(c0 + j);
+        base += wsum[nw - 1];
+        __syncthreads();  // wsum is reused by the next chunk
+    }
+}
+
 __global__ void k_leaf_compact(const unsigned *__restrict__ flag, const unsigned *__restrict__ off, const unsigned *counts,
                                int *leaves) {
     const unsigned C = counts[2];
@@ -747,9 +789,14 @@ void build_tree(Workspace &ws) {
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 4, ceil_div(ws.c_cap, 32));
     k_cells<<<capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 128)), 128, 0, st>>>(ws.ent, ws.d_counts, ws.keys, n, ws.T, ws.info, ws.split_cell, ws.c_begin, ws.c_end,
                                 ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr);
-    k_leaf_flags<<<gs, kTB, 0, st>>>(ws.c_child, ws.d_counts, ws.flag);
-    scan_exclusive_u32(ws.flag, ws.flag_off, ws.c_cap, ws.d_counts + 2, nullptr, ws.scan, st, &ws.launches);
-    k_leaf_compact<<<gs, kTB, 0, st>>>(ws.flag, ws.flag_off, ws.d_counts, ws.leaves);
+    if (ws.c_cap <= 65536u) {
+        k_leaf_list<<<1, 1024, 0, st>>>(ws.c_child, ws.d_counts, ws.leaves);
+        ws.launches -= 1;  // one launch in place of the two counted below
+    } else {
+        k_leaf_flags<<<gs, kTB, 0, st>>>(ws.c_child, ws.d_counts, ws.flag);
+        scan_exclusive_u32(ws.flag, ws.flag_off, ws.c_cap, ws.d_counts + 2, nullptr, ws.scan, st, &ws.launches);
+        k_leaf_compact<<<gs, kTB, 0, st>>>(ws.flag, ws.flag_off, ws.d_counts, ws.leaves);
+    }
     {
         // a warp per leaf, up to 4 warps per block within 48 KB of shared memory
         const size_t per_warp = sizeof(unsigned) * 2 * (static_cast<size_t>(ws.T) + 1);

@@ -1,6 +1,6 @@
 """Batches of independent systems (gb_batch_*): every system of a batch step
 must equal the same system stepped alone in its own context, bit for bit,
-in both precisions; uneven sizes, an empty and a one-particle system, per-system
+in both precisions and with either tensor-core M2L split; uneven sizes, an empty and a one-particle system, per-system
 masses, and a system whose first step overflows its buffers (repeated alone)."""
 import numpy as np
 import pytest
@@ -18,15 +18,16 @@ def systems():
     return out
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_batch_equals_separate_contexts(precision):
+@pytest.mark.parametrize("precision,bf16", [("fp64", False), ("mixed", False), ("mixed", True)])
+def test_batch_equals_separate_contexts(precision, bf16):
     import vipp_gb300
+    flags = vipp_gb300.FLAG_M2L_BF16 if bf16 else 0
     sy = systems()
     sizes = [len(x) for x, _ in sy]
     masses = [1.0 / max(n, 1) for n in sizes]
     X = np.concatenate([x for x, _ in sy]) if sum(sizes) else np.zeros((0, 3))
     V = np.concatenate([v for _, v in sy])
-    with vipp_gb300.Batch(sizes, p=5, s=16, eps=0.01, masses=masses, precision=precision) as b:
+    with vipp_gb300.Batch(sizes, p=5, s=16, eps=0.01, masses=masses, precision=precision, flags=flags) as b:
         b.upload(X, V)
         for dt in (1e-3, 1e-3, 2e-3):
             b.step(dt)
@@ -36,7 +37,7 @@ def test_batch_equals_separate_contexts(precision):
     for k, (x, v) in enumerate(sy):
         if len(x) == 0:
             continue
-        with vipp_gb300.Solver(p=5, s=16, eps=0.01, m=masses[k], precision=precision) as s:
+        with vipp_gb300.Solver(p=5, s=16, eps=0.01, m=masses[k], precision=precision, flags=flags) as s:
             s.preprocess(x, v)
             for dt in (1e-3, 1e-3, 2e-3):
                 s.solve(dt)

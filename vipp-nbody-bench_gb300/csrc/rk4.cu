@@ -24,20 +24,31 @@ __global__ void k_rk4_begin(const double *__restrict__ x, const double *__restri
 }
 
 // The stage's acceleration is read where the force evaluation left it, in
-// tree order: a = near[inv[i]] + far[inv[i]], added in T exactly as the
-// accelerations returned to the caller are (finalize), so no separate pass
-// writes them out in particle order; the state is SoA in particle order.
-template <typename T>
+// tree order, through the inverse permutation: a = near[j] + far[j] with
+// j = inv[i], added in T exactly as the accelerations returned to the caller
+// are (finalize); the state is SoA in particle order. Small systems read the
+// six [3][N] planes directly; large ones read one packed sum per particle
+// (near_far_sum: float4, or three doubles), one sector instead of six.
+template <typename T, bool kPacked>
 __global__ void k_rk4_stage(int stage, double w, double c, double *__restrict__ x, double *__restrict__ v,
                             const double *__restrict__ x0, const double *__restrict__ v0, double *__restrict__ xo,
                             double *__restrict__ vo, const unsigned *__restrict__ inv, const T *__restrict__ nearv,
-                            const T *__restrict__ farv, size_t n) {
+                            const T *__restrict__ farv, const T *__restrict__ packed, size_t n) {
+    constexpr int kStride = sizeof(T) == 4 ? 4 : 3;  // packed layout: float4, or three doubles
     for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<size_t>(gridDim.x) * blockDim.x) {
         const size_t j = inv[i];
+        T av[3];
+        if (kPacked && sizeof(T) == 4) {
+            const float4 q = reinterpret_cast<const float4 *>(packed)[j];
+            av[0] = q.x, av[1] = q.y, av[2] = q.z;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) av[k] = kPacked ? packed[kStride * j + k] : nearv[k * n + j] + farv[k * n + j];
+        }
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const size_t e = k * n + i;
-            const double ve = v[e], ae = static_cast<double>(nearv[k * n + j] + farv[k * n + j]);
+            const double ve = v[e], ae = static_cast<double>(av[k]);
             const double xoe = __dadd_rn(xo[e], __dmul_rn(w, ve));
             const double voe = __dadd_rn(vo[e], __dmul_rn(w, ae));
             xo[e] = xoe, vo[e] = voe;
@@ -49,6 +60,22 @@ __global__ void k_rk4_stage(int stage, double w, double c, double *__restrict__ 
                 v[e] = voe;
             }
         }
+    }
+}
+
+// packed[j] = near[j] + far[j] in tree order (coalesced), for the stage's
+// permuted reads of large systems
+template <typename T>
+__global__ void k_near_far_sum(const T *__restrict__ nearv, const T *__restrict__ farv, T *__restrict__ packed, size_t n) {
+    for (size_t j = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; j < n; j += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        T a[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) a[k] = nearv[k * n + j] + farv[k * n + j];
+        if (sizeof(T) == 4)
+            reinterpret_cast<float4 *>(packed)[j] = make_float4(a[0], a[1], a[2], 0.f);
+        else
+#pragma unroll
+            for (int k = 0; k < 3; ++k) packed[3 * j + k] = a[k];
     }
 }
 
@@ -74,6 +101,10 @@ __global__ void k_soa_to_aos(const double *__restrict__ soa, double *__restrict_
 
 inline unsigned grid_stride_blocks(const Workspace &ws) { return static_cast<unsigned>(ws.num_sms) * 8; }
 
+// From this size on the stage reads packed near + far sums (an extra pass that
+// saves the five other sectors each permuted read would touch).
+constexpr unsigned kPackedStageMin = 1u << 16;
+
 }  // namespace
 
 void rk4_begin(Workspace &ws) {
@@ -86,14 +117,34 @@ void rk4_stage(Workspace &ws, int stage, double dt) {
     // weights and stage offsets exactly as solver_ref.hpp:58, 64, 71, 77, 84, 90, 97
     const double w = (stage == 0 || stage == 3) ? dt / 6 : dt / 3;
     const double c = stage < 2 ? dt / 2 : dt;
-    if (ws.mixed)
-        k_rk4_stage<float><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.inv,
-                                                                     static_cast<const float *>(ws.nearf),
-                                                                     static_cast<const float *>(ws.farf), static_cast<size_t>(ws.n));
-    else
-        k_rk4_stage<double><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.inv,
-                                                                      static_cast<const double *>(ws.nearf),
-                                                                      static_cast<const double *>(ws.farf), static_cast<size_t>(ws.n));
+    // large systems: the near + far sums packed per particle in the acc buffer
+    // (free during steps), then one permuted read per particle
+    const bool packed = ws.n >= kPackedStageMin;
+    const size_t n = ws.n;
+    if (ws.mixed) {
+        const float *nf = static_cast<const float *>(ws.nearf), *ff = static_cast<const float *>(ws.farf);
+        float *pk = reinterpret_cast<float *>(ws.acc);
+        if (packed) {
+            k_near_far_sum<float><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(nf, ff, pk, n);
+            k_rk4_stage<float, true><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo,
+                                                                               ws.inv, nf, ff, pk, n);
+        } else {
+            k_rk4_stage<float, false><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo,
+                                                                                ws.vo, ws.inv, nf, ff, pk, n);
+        }
+    } else {
+        const double *nf = static_cast<const double *>(ws.nearf), *ff = static_cast<const double *>(ws.farf);
+        double *pk = ws.acc;
+        if (packed) {
+            k_near_far_sum<double><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(nf, ff, pk, n);
+            k_rk4_stage<double, true><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo,
+                                                                                ws.vo, ws.inv, nf, ff, pk, n);
+        } else {
+            k_rk4_stage<double, false><<<grid_stride_blocks(ws), 256, 0, ws.st>>>(stage, w, c, ws.x, ws.v, ws.x0, ws.v0, ws.xo,
+                                                                                 ws.vo, ws.inv, nf, ff, pk, n);
+        }
+    }
+    if (packed) ws.launches += 1;
     ws.launches += 1;
     timer_end(ws, kTRK4);
 }

@@ -4,14 +4,17 @@ Workload (headline): Plummer sphere of 4,194,304 equal-mass particles (G = 1,
 M = 1, scale radius 1; radii by inverse CDF r = (u^(-2/3) - 1)^(-1/2) with
 r <= 10, isotropic directions, speeds by von Neumann rejection from the
 Plummer distribution function; seed 2), eps = 0.005, p = 8, s = 64, mixed
-precision, RK4 dt = 5e-4. A step is one RK4 step (four force evaluations,
-tree rebuilt at every stage).
+precision with the workload's BF16 hi/lo tensor-core M2L split (--m2l tf32
+for the library's default 3 x TF32 split), RK4 dt = 5e-4. A step is one RK4
+step (four force evaluations, tree rebuilt at every stage).
 
   value   particle-steps/s with the state resident in HBM (CUDA events on the
           solver's stream around exactly --steps steps)
   e2e     the same through the C-ABI with host buffers: per step, upload of
           x, v from pinned host memory, one RK4 step, download of x, v
   plain_fp64  the same step with every stage in FP64 (the plain form)
+  m2l_other_split  the same step with the other M2L split (value, energy drift)
+  batched  512 independent Plummer systems of uneven N (one batch step)
   cpu_baseline  the reference's algorithm on the host cores (oracle port, or
           the compiled reference where it exists), on a bounded sample of one
           force evaluation, extrapolated to a step

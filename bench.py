@@ -19,6 +19,11 @@ step (four force evaluations, tree rebuilt at every stage).
           the compiled reference where it exists), on a bounded sample of one
           force evaluation, extrapolated to a step
 
+``--workload clustered`` runs the adaptive-depth stress workload instead:
+16,777,216 particles in 8 equal-mass Plummer clusters (scale radii uniform in
+[0.01, 0.1], centres uniform in [0, 1)^3, Gaussian bulk velocities sigma 0.3)
+plus a 5% uniform background, eps = 1e-4, p = 8, s = 64, dt = 1e-4, seed 4.
+
 ``--impl reference`` times the reference's CPU implementation instead
 (same metric and config) and prints its own line.
 """
@@ -44,41 +49,22 @@ for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
+from vipp_gb300.workloads import clustered, plummer  # noqa: E402  (numpy only; the library loads later)
+
 METRIC = "RK4 particle-steps/s at stated FP64-direct force error; mixed/batched vs plain"
 UNIT = "particle-steps/s"
 FP32_LANES_PER_SM = 128
 
 
-def plummer(n: int, seed: int, rmax: float = 10.0):
-    """Plummer sphere (G = M = a = 1) with the inverse-CDF radius capped at rmax."""
-    rng = np.random.default_rng(seed)
-    r = np.empty(n)
-    todo = np.arange(n)
-    while todo.size:
-        u = rng.random(todo.size)
-        u = np.where(u == 0, 0.5, u)
-        rr = 1.0 / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
-        ok = rr <= rmax
-        r[todo[ok]] = rr[ok]
-        todo = todo[~ok]
-    q = np.empty(n)
-    todo = np.arange(n)
-    pmax = math.sqrt(7.0) * 686 / 19683
-    while todo.size:
-        x1, x2 = rng.random(todo.size), rng.random(todo.size)
-        ok = pmax * x1 < x2 * x2 * (1 - x2 * x2) ** 3.5
-        q[todo[ok]] = x2[ok]
-        todo = todo[~ok]
-    ve = math.sqrt(2.0) * (1.0 + r * r) ** -0.25
-
-    def iso(norm, a, b):
-        z = (1 - 2 * a) * norm
-        w = np.sqrt(np.maximum(norm * norm - z * z, 0.0))
-        return np.stack([z, w * np.cos(2 * np.pi * b), w * np.sin(2 * np.pi * b)], axis=1)
-
-    x = iso(r, rng.random(n), rng.random(n))
-    v = iso(q * ve, rng.random(n), rng.random(n))
-    return np.ascontiguousarray(x), np.ascontiguousarray(v)
+def make_workload(args, rank=0):
+    """(x, v, seed, name) of the selected workload; replicas use seed + rank."""
+    if args.workload == "clustered":
+        seed = 4 + rank
+        x, v, _ = clustered(args.n, seed)
+        return x, v, seed, f"clustered-{args.n} (8 Plummer clusters + 5% background)"
+    seed = 2 + rank
+    x, v = plummer(args.n, seed)
+    return x, v, seed, f"plummer-{args.n}"
 
 
 # DRAM bytes per launch of the BF16-split M2L on the 4M workload
@@ -243,7 +229,7 @@ def run_reference_arm(args):
         return
     import oracle
 
-    x, v = plummer(args.n, 2)
+    x, v, _, wname = make_workload(args)
     vals = []
     t_start = time.time()
     # CPU runs need no warm-up beyond the first sample; every step is one
@@ -254,7 +240,7 @@ def run_reference_arm(args):
         if time.time() - t_start > 150:
             break
     value = float(np.median(vals))
-    cfg = {"workload": f"plummer-{args.n} p={args.p} s={args.s} eps={args.eps} (reference algorithm, CPU)",
+    cfg = {"workload": f"{wname} p={args.p} s={args.s} eps={args.eps} (reference algorithm, CPU)",
            "N": args.n, "p": args.p, "s": args.s, "eps": args.eps, "dt": args.dt}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": len(vals),
             "warmup": args.warmup, "ms_per_step": 1e3 * args.n / value, "higher_is_better": True, "scaling": "weak",
@@ -272,11 +258,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=1 << 22)
+    ap.add_argument("--workload", default="plummer", choices=["plummer", "clustered"],
+                    help="plummer: the 4M Plummer sphere (headline); clustered: the 16M adaptive-depth stress "
+                         "workload (8 Plummer clusters + 5%% background, eps=1e-4, dt=1e-4)")
+    ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--p", type=int, default=8)
     ap.add_argument("--s", type=int, default=64)
-    ap.add_argument("--eps", type=float, default=0.005)
-    ap.add_argument("--dt", type=float, default=5e-4)
+    ap.add_argument("--eps", type=float, default=None)
+    ap.add_argument("--dt", type=float, default=None)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--error-sample", type=int, default=65536)
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain-form comparison")
@@ -290,6 +279,10 @@ def main():
     ap.add_argument("--no-alt", action="store_true", help="skip the timing of the other M2L split")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    wdef = {"plummer": (1 << 22, 0.005, 5e-4), "clustered": (1 << 24, 1e-4, 1e-4)}[args.workload]
+    args.n = wdef[0] if args.n is None else args.n
+    args.eps = wdef[1] if args.eps is None else args.eps
+    args.dt = wdef[2] if args.dt is None else args.dt
 
     if args.impl == "reference":
         run_reference_arm(args)
@@ -309,7 +302,7 @@ def main():
     if args.precision == "mixed" and args.m2l == "bf16":
         args.flags |= vipp_gb300.FLAG_M2L_BF16
     n = args.n
-    x, v = plummer(n, 2 + rank)
+    x, v, seed, wname = make_workload(args, rank)
     m = 1.0 / n
     sol = vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision=args.precision, device=local,
                             flags=args.flags)
@@ -472,7 +465,7 @@ def main():
         # DRAM bytes (read + write) per launch from one ncu capture of this exact
         # default workload (profiles/dram_plummer4M_p8_mixed.md); other
         # workloads have no capture, so null
-        default_cfg = (n == 1 << 22 and args.p == 8 and args.s == 64 and args.eps == 0.005 and args.precision == "mixed"
+        default_cfg = (args.workload == "plummer" and n == 1 << 22 and args.p == 8 and args.s == 64 and args.eps == 0.005 and args.precision == "mixed"
                        and args.flags & ~vipp_gb300.FLAG_M2L_BF16 == 0)
         bf = bool(args.flags & vipp_gb300.FLAG_M2L_BF16)
         traffic = {"p2p": 293120768 + 40724736, "m2l": (M2L_BF16_TRAFFIC if bf else 188582656 + 19934464)} if default_cfg else {}
@@ -523,9 +516,9 @@ def main():
     kt_ms = {k: round(v[0] / class_steps, 4) for k, v in kt.items()}
     m2l_split = (None if args.precision != "mixed" else "cuda cores fp32" if args.flags & vipp_gb300.FLAG_M2L_CUDA_CORES
                  else "bf16 hi/lo" if args.flags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32")
-    cfg = {"workload": f"plummer-{n} p={args.p} s={args.s} eps={args.eps} {args.precision}", "N": n, "p": args.p,
-           "s": args.s, "eps": args.eps, "dt": args.dt, "precision": args.precision, "m2l_split": m2l_split, "seed": 2,
-           "l2": "inputs larger than L2 (state 192 MB, per-step working set > 1 GB)",
+    cfg = {"workload": f"{wname} p={args.p} s={args.s} eps={args.eps} {args.precision}", "N": n, "p": args.p,
+           "s": args.s, "eps": args.eps, "dt": args.dt, "precision": args.precision, "m2l_split": m2l_split, "seed": seed,
+           "l2": f"inputs larger than L2 (state {48 * n / 1e6:.0f} MB, per-step working set > 1 GB)",
            "tree": {k: st[k] for k in ("ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges")},
            "kernel_ms_per_step": kt_ms, **acc_info, "energy": energy, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,

@@ -2,8 +2,9 @@
 //
 // Radix sort, one launch per pass after one histogram launch for all passes
 // (single-sweep LSD sort with decoupled look-back): every block takes the next
-// 4096-key tile from an atomic ticket, ranks its keys by digit (each warp with
-// __match_any_sync, so equal digits keep their input order: stability is what
+// 4096-key tile from an atomic ticket, ranks its keys by digit (each warp finds
+// the lanes holding its digit with one ballot per digit bit and ranks a key
+// among them by lane, so equal digits keep their input order: stability is what
 // preserves the reference's ascending-index order among particles with equal
 // keys), publishes its per-digit counts, and finds the keys of its digits in
 // all earlier tiles by looking back over their published counts. A tile waits
@@ -23,6 +24,20 @@ constexpr unsigned kFull = 0xffffffffu;
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Lanes of the (fully active) warp whose v equals this lane's, for v < 512
+// (a digit 0..255, or 256 for a lane without a key): one ballot per bit, each
+// keeping the lanes that agree with this lane on that bit.
+__device__ __forceinline__ unsigned warp_peers9(unsigned v) {
+    unsigned m = kFull;
+#pragma unroll
+    for (int b = 0; b < 9; ++b) {
+        const bool bit = (v >> b) & 1u;
+        const unsigned bal = __ballot_sync(kFull, bit);
+        m &= bit ? bal : ~bal;
+    }
     return m;
 }
 
@@ -171,13 +186,13 @@ __global__ void k_sweep_hist(const uint64_t *__restrict__ keys, unsigned n_cap, 
     for (int k = threadIdx.x; k < kMaxPasses * 256; k += blockDim.x) (&cnt[0][0])[k] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    // whole warps step together so that every lane takes part in __match_any_sync
+    // whole warps step together so that every lane takes part in the ballots
     for (unsigned i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
         const unsigned i = i0 + threadIdx.x;
         const uint64_t key = i < n ? keys[i] : 0ull;
         for (int p = 0; p < npasses; ++p) {
             const unsigned d = i < n ? static_cast<unsigned>((key >> (bit_lo + 8 * p)) & 0xffu) : 256u;
-            const unsigned peers = __match_any_sync(kFull, d);
+            const unsigned peers = warp_peers9(d);
             if (d < 256u && lane == __ffs(peers) - 1) atomicAdd(&cnt[p][d], __popc(peers));
         }
     }
@@ -222,7 +237,7 @@ __global__ void __launch_bounds__(256) k_sweep(const uint64_t *__restrict__ kin,
         val[k] = (ok && vin) ? vin[i] : 0u;
         const unsigned d = ok ? static_cast<unsigned>((key[k] >> bit) & 0xffu) : 256u;
         dig[k] = d;
-        const unsigned peers = __match_any_sync(kFull, d);
+        const unsigned peers = warp_peers9(d);
         const unsigned before = d < 256u ? wcnt[w][d] : 0u;
         __syncwarp();
         rank[k] = before + __popc(peers & lt);

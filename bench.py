@@ -67,8 +67,8 @@ def make_workload(args, rank=0):
     return x, v, seed, f"plummer-{args.n}"
 
 
-# DRAM bytes per launch of the BF16-split M2L on the 4M workload
-# (profiles/dram_plummer4M_p8_mixed.md)
+# DRAM bytes (read + write) per launch of the BF16-split M2L on the 4M
+# workload, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum)
 M2L_BF16_TRAFFIC = 139474944 + 19757568
 
 
@@ -252,7 +252,11 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
-def main():
+def parse_args(argv=None):
+    """Command line, with the selected workload's defaults filled in: plummer
+    N = 4,194,304, eps = 0.005, dt = 5e-4; clustered N = 16,777,216,
+    eps = 1e-4, dt = 1e-4 (explicit --n/--eps/--dt win). At least 3 warm-up
+    steps on the GPU arm."""
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -277,12 +281,17 @@ def main():
                     help="mixed form's tensor-core M2L split: bf16 hi/lo (the 4M Plummer and batching configurations' "
                          "form, GB_FLAG_M2L_BF16) or 3 x tf32 (the library default)")
     ap.add_argument("--no-alt", action="store_true", help="skip the timing of the other M2L split")
-    args = ap.parse_args()
+    args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     wdef = {"plummer": (1 << 22, 0.005, 5e-4), "clustered": (1 << 24, 1e-4, 1e-4)}[args.workload]
     args.n = wdef[0] if args.n is None else args.n
     args.eps = wdef[1] if args.eps is None else args.eps
     args.dt = wdef[2] if args.dt is None else args.dt
+    return args
+
+
+def main():
+    args = parse_args()
 
     if args.impl == "reference":
         run_reference_arm(args)
@@ -463,10 +472,9 @@ def main():
     roof = dict(per[dom]) if dom else {}
     if dom:
         # DRAM bytes (read + write) per launch from one ncu capture of this exact
-        # default workload (profiles/dram_plummer4M_p8_mixed.md); other
-        # workloads have no capture, so null
-        default_cfg = (args.workload == "plummer" and n == 1 << 22 and args.p == 8 and args.s == 64 and args.eps == 0.005 and args.precision == "mixed"
-                       and args.flags & ~vipp_gb300.FLAG_M2L_BF16 == 0)
+        # default workload; other workloads have no capture, so null
+        default_cfg = (args.workload == "plummer" and n == 1 << 22 and args.p == 8 and args.s == 64 and args.eps == 0.005
+                       and args.precision == "mixed" and args.flags & ~vipp_gb300.FLAG_M2L_BF16 == 0)
         bf = bool(args.flags & vipp_gb300.FLAG_M2L_BF16)
         traffic = {"p2p": 293120768 + 40724736, "m2l": (M2L_BF16_TRAFFIC if bf else 188582656 + 19934464)} if default_cfg else {}
         for k in per:

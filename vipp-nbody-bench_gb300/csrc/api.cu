@@ -444,9 +444,11 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     ctx->cfg = *cfg;
     apply_config(ctx);
     gb::Workspace &ws = ctx->ws;
+    // gb_destroy frees whatever was created before the failure (the
+    // workspace's handles and buffers start out null)
     auto fail = [&](const char *what, cudaError_t e) {
         g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
-        delete ctx;
+        gb_destroy(ctx);
         return GB_ERR_CUDA;
     };
     cudaError_t e = cudaSetDevice(cfg->device);
@@ -457,7 +459,7 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     if (prop.major < 10) {
         g_create_error = "this build targets sm_103a (Blackwell Ultra); device is sm_" + std::to_string(prop.major) +
                          std::to_string(prop.minor);
-        delete ctx;
+        gb_destroy(ctx);
         return GB_ERR_NO_DEVICE;
     }
     ws.num_sms = prop.multiProcessorCount;
@@ -491,7 +493,7 @@ void gb_destroy(gb_ctx *ctx) {
     collect_timers(ctx);
     for (auto e : ctx->free_events) cudaEventDestroy(e);
     void *bufs[] = {ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.acc, ws.phi, ws.staging, ws.bbox_part, ws.keys0, ws.keys1,
-                    ws.perm0, ws.perm1, ws.xs, ws.ph, ws.pl, ws.nearf, ws.farf, ws.phis, ws.cnt, ws.off, ws.ent0, ws.ent1,
+                    ws.perm0, ws.perm1, ws.inv, ws.xs, ws.ph, ws.pl, ws.nearf, ws.farf, ws.phis, ws.cnt, ws.off, ws.ent0, ws.ent1,
                     ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,

@@ -126,7 +126,6 @@ struct Workspace {
 
     // timing
     bool timing = false;
-    cudaEvent_t ev[kNumTimers][2] = {};
     double t_ms[kNumTimers] = {};
     int64_t t_launch[kNumTimers] = {};
 };

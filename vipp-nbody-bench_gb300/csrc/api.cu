@@ -903,6 +903,7 @@ int gb_direct_accel(gb_ctx *ctx, const int64_t *targets, size_t ntargets, double
     GB_TRY(cudaSetDevice(ctx->cfg.device));
     gb::Workspace &ws = ctx->ws;
     const size_t nt = targets ? ntargets : ws.n;
+    if (nt > 0x7fffffffu) return ctx->err = "too many targets", GB_ERR_INVALID;
     if (nt == 0 || ws.n == 0) return GB_OK;
     if (targets) {
         for (size_t k = 0; k < nt; ++k)
@@ -959,6 +960,9 @@ int gb_tree_dump(gb_ctx *ctx, int64_t *ncells, int64_t *list_sizes, int32_t *lev
                  uint64_t *path, double *box_min, double *box_max, int64_t *pt_begin, int64_t *pt_end, int64_t *order,
                  int64_t *m2l_off, int64_t *m2l, int64_t *p2p_off, int64_t *p2p_own, int64_t *coll_off, int64_t *coll) {
     if (!ctx || !ncells || !list_sizes) return GB_ERR_INVALID;
+    if (level && !(parent && first_child && path && box_min && box_max && pt_begin && pt_end && order && m2l_off && m2l &&
+                   p2p_off && p2p_own && coll_off && coll))
+        return ctx->err = "tree dump: give every output array or none", GB_ERR_INVALID;
     GB_TRY(cudaSetDevice(ctx->cfg.device));
     gb::Workspace &ws = ctx->ws;
     GB_TRY(cudaStreamSynchronize(ws.st));

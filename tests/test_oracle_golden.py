@@ -186,3 +186,23 @@ def test_direct_potential_known_answer():
     d = lambda r2: 1.0 / math.sqrt(r2 + 0.01)
     want = [-(d(25) + d(1)), -(d(25) + d(26)), -(d(1) + d(26))]
     np.testing.assert_allclose(phi, want, rtol=1e-15)
+
+
+def test_oracle_equals_compiled_reference_on_clustered_workload(orc):
+    """The clustered stress workload's shape (8 Plummer clusters with scale
+    radii in [0.01, 0.1] + 5% uniform background) at 12,000 particles, s = 8:
+    the oracle's tree, numbering and lists equal the compiled reference's, and
+    its p = 4 accelerations agree to 1e-12. Runs where the reference headers
+    were compiled (oracle/_ref)."""
+    ref = O.reference()
+    if ref is None:
+        pytest.skip("compiled reference not available")
+    from vipp_gb300.workloads import clustered
+    x, _, _ = clustered(12000, 4)
+    n = x.shape[0]
+    t, tr = orc.tree(x, 8), ref.tree(x, 8)
+    assert int(t["level"].max()) >= 6
+    assert np.array_equal(t["parent"], tr["parent"]) and np.array_equal(t["first_child"], tr["first_child"])
+    assert not diff_trees(canon_ref(t), canon_ref(tr))
+    a, ar = orc.accel(x, 8, 1.0, 1.0 / n, 1e-4, 4), ref.accel(x, 8, 1.0, 1.0 / n, 1e-4, 4)
+    assert np.max(rel_err(a, ar)) <= 1e-12

@@ -23,6 +23,8 @@ step (four force evaluations, tree rebuilt at every stage).
 16,777,216 particles in 8 equal-mass Plummer clusters (scale radii uniform in
 [0.01, 0.1], centres uniform in [0, 1)^3, Gaussian bulk velocities sigma 0.3)
 plus a 5% uniform background, eps = 1e-4, p = 8, s = 64, dt = 1e-4, seed 4.
+``--workload uniform``: 1,048,576 equal-mass particles uniform in the unit
+cube at rest, eps = 1e-3, p = 6, s = 64, dt = 1e-4, seed 1.
 
 ``--impl reference`` times the reference's CPU implementation instead
 (same metric and config) and prints its own line.
@@ -49,7 +51,7 @@ for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-from vipp_gb300.workloads import clustered, plummer  # noqa: E402  (numpy only; the library loads later)
+from vipp_gb300.workloads import clustered, plummer, uniform  # noqa: E402  (numpy only; the library loads later)
 
 METRIC = "RK4 particle-steps/s at stated FP64-direct force error; mixed/batched vs plain"
 UNIT = "particle-steps/s"
@@ -62,6 +64,10 @@ def make_workload(args, rank=0):
         seed = 4 + rank
         x, v, _ = clustered(args.n, seed)
         return x, v, seed, f"clustered-{args.n} (8 Plummer clusters + 5% background)"
+    if args.workload == "uniform":
+        seed = 1 + rank
+        x, v = uniform(args.n, seed)
+        return x, v, seed, f"uniform-{args.n} (unit cube, at rest)"
     seed = 2 + rank
     x, v = plummer(args.n, seed)
     return x, v, seed, f"plummer-{args.n}"
@@ -254,19 +260,21 @@ def run_reference_arm(args):
 
 def parse_args(argv=None):
     """Command line, with the selected workload's defaults filled in: plummer
-    N = 4,194,304, eps = 0.005, dt = 5e-4; clustered N = 16,777,216,
-    eps = 1e-4, dt = 1e-4 (explicit --n/--eps/--dt win). At least 3 warm-up
-    steps on the GPU arm."""
+    N = 4,194,304, eps = 0.005, dt = 5e-4, p = 8; clustered N = 16,777,216,
+    eps = 1e-4, dt = 1e-4, p = 8; uniform N = 1,048,576, eps = 1e-3,
+    dt = 1e-4, p = 6; s = 64 for all (explicit --n/--eps/--dt/--p win). At
+    least 3 warm-up steps on the GPU arm."""
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plummer", choices=["plummer", "clustered"],
+    ap.add_argument("--workload", default="plummer", choices=["plummer", "clustered", "uniform"],
                     help="plummer: the 4M Plummer sphere (headline); clustered: the 16M adaptive-depth stress "
-                         "workload (8 Plummer clusters + 5%% background, eps=1e-4, dt=1e-4)")
+                         "workload (8 Plummer clusters + 5%% background, eps=1e-4, dt=1e-4); uniform: 1M particles "
+                         "in the unit cube at rest (eps=1e-3, p=6, dt=1e-4)")
     ap.add_argument("--n", type=int, default=None)
-    ap.add_argument("--p", type=int, default=8)
+    ap.add_argument("--p", type=int, default=None)
     ap.add_argument("--s", type=int, default=64)
     ap.add_argument("--eps", type=float, default=None)
     ap.add_argument("--dt", type=float, default=None)
@@ -283,10 +291,12 @@ def parse_args(argv=None):
     ap.add_argument("--no-alt", action="store_true", help="skip the timing of the other M2L split")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
-    wdef = {"plummer": (1 << 22, 0.005, 5e-4), "clustered": (1 << 24, 1e-4, 1e-4)}[args.workload]
+    wdef = {"plummer": (1 << 22, 0.005, 5e-4, 8), "clustered": (1 << 24, 1e-4, 1e-4, 8),
+            "uniform": (1 << 20, 1e-3, 1e-4, 6)}[args.workload]
     args.n = wdef[0] if args.n is None else args.n
     args.eps = wdef[1] if args.eps is None else args.eps
     args.dt = wdef[2] if args.dt is None else args.dt
+    args.p = wdef[3] if args.p is None else args.p
     return args
 
 

@@ -29,8 +29,10 @@ def test_default_workload_is_the_4m_plummer_sphere(bench):
 def test_clustered_defaults_and_explicit_values_win(bench):
     a = bench.parse_args(["--workload", "clustered"])
     assert (a.n, a.eps, a.dt, a.p, a.s) == (1 << 24, 1e-4, 1e-4, 8, 64)
-    b = bench.parse_args(["--workload", "clustered", "--n", "4096", "--eps", "0.01", "--dt", "0.001"])
-    assert (b.n, b.eps, b.dt) == (4096, 0.01, 0.001)
+    b = bench.parse_args(["--workload", "clustered", "--n", "4096", "--eps", "0.01", "--dt", "0.001", "--p", "5"])
+    assert (b.n, b.eps, b.dt, b.p) == (4096, 0.01, 0.001, 5)
+    u = bench.parse_args(["--workload", "uniform"])
+    assert (u.n, u.eps, u.dt, u.p, u.s) == (1 << 20, 1e-3, 1e-4, 6, 64)
 
 
 def test_warmup_floor_applies_to_the_gpu_arm_only(bench):
@@ -47,6 +49,9 @@ def test_workloads_are_seeded_per_replica(bench):
     c = bench.parse_args(["--workload", "clustered", "--n", "2048"])
     xc, _, sc, namec = bench.make_workload(c, 0)
     assert sc == 4 and namec.startswith("clustered-2048") and xc.shape == (2048, 3)
+    u = bench.parse_args(["--workload", "uniform", "--n", "2048"])
+    xu, vu, su, nameu = bench.make_workload(u, 0)
+    assert su == 1 and nameu.startswith("uniform-2048") and np.all((xu >= 0) & (xu < 1)) and not vu.any()
 
 
 def test_reference_arm_prints_one_contract_line(bench):

@@ -9,6 +9,7 @@ G = 1 units:
   plummer    a Plummer sphere (total mass 1, scale radius 1) with the
              inverse-CDF radius capped at r_max and speeds by von Neumann
              rejection from the Plummer distribution function;
+  uniform    particles uniform in the unit cube [0, 1)^3 at rest;
   clustered  the adaptive-depth stress workload: 8 equal-mass Plummer
              clusters (scale radii uniform in [0.01, 0.1], centres uniform in
              [0, 1)^3, bulk velocities Gaussian with sigma 0.3 per component,
@@ -54,6 +55,12 @@ def plummer(n: int, seed, rmax: float = 10.0):
     x = iso(r, rng.random(n), rng.random(n))
     v = iso(q * ve, rng.random(n), rng.random(n))
     return np.ascontiguousarray(x), np.ascontiguousarray(v)
+
+
+def uniform(n: int, seed=1):
+    """Uniform in [0, 1)^3, zero velocities."""
+    rng = np.random.default_rng(seed)
+    return np.ascontiguousarray(rng.random((n, 3))), np.zeros((n, 3))
 
 
 CLUSTERS = 8

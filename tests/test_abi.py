@@ -66,3 +66,44 @@ def test_invalid_config_rejected_before_device(lib):
                 vipp_gb300.GbConfig(11, 10, 0.01, 1, 1, 0, 0, 0), vipp_gb300.GbConfig(4, 10, -1.0, 1, 1, 0, 0, 0),
                 vipp_gb300.GbConfig(4, 10, 0.01, 1, 1, 7, 0, 0)):
         assert lib.gb_create(ctypes.byref(bad), ctypes.byref(h)) == vipp_gb300.GB_ERR_INVALID
+
+
+def test_null_handles_are_rejected(lib):
+    """Every entry point taking a context or batch answers a NULL handle with
+    GB_ERR_INVALID (or a neutral value) instead of touching memory."""
+    import vipp_gb300
+    INV = vipp_gb300.GB_ERR_INVALID
+    buf = (ctypes.c_double * 6)()
+    assert lib.gb_upload(None, buf, buf, 2) == INV
+    assert lib.gb_download(None, buf, buf) == INV
+    assert lib.gb_rk4_step(None, 1e-3) == INV
+    assert lib.gb_accel(None, buf, None) == INV
+    assert lib.gb_direct_accel(None, None, 0, buf) == INV
+    assert lib.gb_sync(None) == INV
+    assert lib.gb_get_stats(None, ctypes.byref(vipp_gb300.GbStats())) == INV
+    assert lib.gb_get_conserved(None, ctypes.byref(vipp_gb300.GbConserved())) == INV
+    assert lib.gb_init_plummer(None, 16, 0, 0.0) == INV
+    assert lib.gb_tree_dump(None, *([None] * 17)) == INV
+    assert lib.gb_enable_timing(None, 1) == INV
+    assert lib.gb_kernel_times(None, None, None, 0) == INV
+    assert lib.gb_set_config(None, ctypes.byref(vipp_gb300.GbConfig(4, 10, 0.01, 1, 1, 0, 0, 0))) == INV
+    assert lib.gb_launch_count(None) == 0
+    assert not lib.gb_stream(None)
+    lib.gb_destroy(None)
+    assert lib.gb_batch_upload(None, buf, buf) == INV
+    assert lib.gb_batch_download(None, buf, buf) == INV
+    assert lib.gb_batch_rk4_step(None, 1e-3) == INV
+    assert not lib.gb_batch_system(None, 0)
+    lib.gb_batch_destroy(None)
+
+
+def test_batch_arguments_checked_before_device(lib):
+    import vipp_gb300
+    cfg = vipp_gb300.GbConfig(4, 10, 0.01, 1, 1, 0, 0, 0)
+    b = ctypes.c_void_p()
+    off = (ctypes.c_uint64 * 3)(0, 10, 5)  # decreasing
+    assert lib.gb_batch_create(ctypes.byref(cfg), 2, off, None, ctypes.byref(b)) == vipp_gb300.GB_ERR_INVALID
+    assert b"must not decrease" in lib.gb_batch_last_error(None)
+    assert lib.gb_batch_create(ctypes.byref(cfg), 0, off, None, ctypes.byref(b)) == vipp_gb300.GB_ERR_INVALID
+    assert lib.gb_batch_create(ctypes.byref(cfg), 2, None, None, ctypes.byref(b)) == vipp_gb300.GB_ERR_INVALID
+    assert not b.value

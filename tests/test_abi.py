@@ -107,3 +107,14 @@ def test_batch_arguments_checked_before_device(lib):
     assert lib.gb_batch_create(ctypes.byref(cfg), 0, off, None, ctypes.byref(b)) == vipp_gb300.GB_ERR_INVALID
     assert lib.gb_batch_create(ctypes.byref(cfg), 2, None, None, ctypes.byref(b)) == vipp_gb300.GB_ERR_INVALID
     assert not b.value
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """No fallback: without the built CUDA library the binding raises (in a
+    fresh interpreter, since this one has the library loaded already)."""
+    import sys
+    code = ("import sys; sys.path.insert(0, sys.argv[1]); import vipp_gb300; "
+            "vipp_gb300.load(sys.argv[2])")
+    r = subprocess.run([sys.executable, "-c", code, os.path.join(ROOT, "vipp-nbody-bench_gb300"),
+                        str(tmp_path / "libvipp_gb300.so")], capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "not built" in r.stderr

@@ -206,3 +206,25 @@ def test_oracle_equals_compiled_reference_on_clustered_workload(orc):
     assert not diff_trees(canon_ref(t), canon_ref(tr))
     a, ar = orc.accel(x, 8, 1.0, 1.0 / n, 1e-4, 4), ref.accel(x, 8, 1.0, 1.0 / n, 1e-4, 4)
     assert np.max(rel_err(a, ar)) <= 1e-12
+
+
+def test_reference_method_accuracy_floor_from_softening(orc):
+    """The reference's FMM (oracle, FP64) against the direct sum on 16,384
+    Plummer particles, s = 64: unsoftened, going from p = 8 to p = 10 cuts the
+    RMS error several-fold (the expansion converges); with eps = 0.005 it
+    barely moves (the unsoftened far field's softening bias is the floor)."""
+    import math
+    from vipp_gb300.workloads import plummer
+    n = 16384
+    x, _ = plummer(n, 2)
+
+    def rms(eps, p):
+        a = orc.accel(x, 64, 1.0, 1.0 / n, eps, p)
+        ad = O.direct_accel(x, 1.0, 1.0 / n, eps)
+        e = rel_err(a, ad)
+        return math.sqrt(np.mean(e * e))
+
+    e0 = (rms(0.0, 8), rms(0.0, 10))
+    e5 = (rms(0.005, 8), rms(0.005, 10))
+    assert e0[0] / e0[1] > 4 and e5[0] / e5[1] < 2.5
+    assert e5[1] > 2e-5

@@ -8,6 +8,18 @@ stores inputs and outputs as .npz files:
                first child, box, member list) and calc_link lists
                (solver_ref.hpp:115-162), FMM accelerations
                (SolverRef::acceleration) and one RK4 step (runge_kutta)
+  tree_plummer16384_s64_p8.npz, tree_uniform16384_s64_p6.npz
+               the same at the headline orders and leaf capacity (Plummer
+               sphere from Problem::initialize with eps = 0.005, p = 8, s = 64;
+               unit cube with eps = 1e-3, p = 6, s = 64); positions are not
+               stored but regenerated (the oracle's bit-identical restatement
+               of Problem::initialize, or numpy's PCG64 stream) and checked
+               against a stored checksum
+  traj_plummer16384_s32_p4.npz
+               the reference's CPU-runnable case run to its end: Plummer
+               N = 16,384 (Problem::initialize, seed 0), s = 32, eps = 0.01,
+               p = 4, ten RK4 steps of dt = 1e-3 (solver_ref.hpp:36-104);
+               final positions and velocities
   kat.npz      special functions P, DP, Y (fmm.hpp:20-194) at the angles the
                reference's own tests use, the P2M/M2M/L known answers of
                test_fmm.cpp, Problem pieces (problem.hpp:250-292), curve fits
@@ -15,7 +27,8 @@ stores inputs and outputs as .npz files:
                (solver_ref_naive.hpp)
 
 Usage (needs the reference sources, i.e. the development container):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [small] [headline] [trajectory]
+(no argument: all groups)
 """
 from __future__ import annotations
 
@@ -66,10 +79,62 @@ def tree_case(name, x, v, s, p, eps, G=1.0, dt=1e-3):
     print(name, "cells", len(t["parent"]), "depth", int(t["level"].max()))
 
 
-def main():
+def checksum(a):
+    """Order-sensitive FP64 checksum of an array (exact for identical arrays)."""
+    a = np.ascontiguousarray(a, np.float64).ravel()
+    return np.array([a.sum(), (a * np.arange(1, a.size + 1)).sum(), a.size], np.float64)
+
+
+def big_case(name, gen, x, s, p, eps, G=1.0):
+    """Tree, lists and FP64 accelerations of the reference; positions replaced
+    by their generator description and checksum; integer arrays as int32."""
+    ref = O.reference()
+    n = x.shape[0]
+    m = 1.0 / n
+    t = ref.tree(x, s)
+    a = ref.accel(x, s, G, m, eps, p)
+    out = dict(gen=np.array(gen, np.float64), x_sum=checksum(x), s=s, p=p, eps=eps, G=G, m=m, dt=0.0,
+               parent=t["parent"].astype(np.int32), level=t["level"].astype(np.int32),
+               first_child=t["first_child"].astype(np.int32), mins=t["mins"], maxs=t["maxs"], acc=a)
+    for k in ("pts", "m2l", "p2p", "coll"):
+        off, data = flat(t[k])
+        out[k + "_off"], out[k] = off.astype(np.int32), data.astype(np.int32)
+    np.savez_compressed(os.path.join(HERE, f"tree_{name}.npz"), **out)
+    print(name, "cells", len(t["parent"]), "depth", int(t["level"].max()))
+
+
+def headline():
+    # gen = [kind, n, eps or seed, seed]: kind 0 = Problem::initialize(n, eps, seed), 1 = PCG64(seed) unit cube
+    x, _, eps, _, _ = ref_problem(16384, 64, 0.005, 8, 2)
+    big_case("plummer16384_s64_p8", [0, 16384, 0.005, 2], x, 64, 8, eps)
+    xu = np.random.default_rng(1).random((16384, 3))
+    big_case("uniform16384_s64_p6", [1, 16384, 0, 1], xu, 64, 6, 1e-3)
+
+
+def trajectory():
+    n, s, p, eps, dt, steps = 16384, 32, 4, 0.01, 1e-3, 10
+    x, v, e, _, m = ref_problem(n, s, eps, p, 0)
+    assert e == eps and m == 1.0 / n
+    x10, v10 = O.reference().rk4(x, v, s, 1.0, m, eps, dt, p, steps)
+    np.savez_compressed(os.path.join(HERE, "traj_plummer16384_s32_p4.npz"), gen=np.array([0, n, eps, 0], np.float64),
+                        x_sum=checksum(x), v_sum=checksum(v), s=s, p=p, eps=eps, G=1.0, m=m, dt=dt, steps=steps,
+                        x10=x10, v10=v10)
+    print("trajectory written")
+
+
+def main(groups):
     if O.ref() is None:
         O.build(ref=True)
     assert O.ref() is not None, "reference build (oracle/_ref) unavailable"
+    if "headline" in groups:
+        headline()
+    if "trajectory" in groups:
+        trajectory()
+    if "small" in groups:
+        small()
+
+
+def small():
     ref = O.reference()
     rng = np.random.default_rng(20260101)
 
@@ -132,4 +197,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or ["small", "headline", "trajectory"])

@@ -183,11 +183,12 @@ def test_mixed_m2l_tensor_and_cuda_cores_agree(name):
     assert np.max(rel_err(res["tensor"], res["cuda"])) <= 2 * MIXED_MAX_REL
 
 
-@pytest.mark.parametrize("p", [2, 3, 7, 9, 10])
+@pytest.mark.parametrize("p", [2, 3, 7, 8, 9, 10])
 def test_mixed_tensor_m2l_every_order(plummer16k, p):
     """The tensor-core M2L over the expansion orders whose drains differ: the
     running sums in TMEM after both accumulators (p <= 7), in the gaps behind
-    them (p = 8, covered above), or in registers (p = 9, 10, no free columns).
+    them (p = 8), or in registers (p = 9, 10, no free columns). p = 8 against
+    the reference itself is in test_gpu_headline.py.
     Mixed against FP64 on the same tree: RMS <= MIXED_RMS_REL, max <= MIXED_MAX_REL."""
     import vipp_gb300
     x, v = plummer16k

@@ -178,6 +178,34 @@ def test_fmm_accel_and_rk4_match_reference(orc, name):
     assert np.max(np.abs(v1 - d["v1"])) <= 1e-12 * max(1e-3, np.max(np.abs(d["v1"])))
 
 
+@pytest.mark.parametrize("name", ["plummer16384_s64_p8", "uniform16384_s64_p6"])
+def test_headline_orders_match_reference(orc, name):
+    """The reference at the benchmark's leaf capacity and orders (s = 64;
+    Plummer p = 8, eps = 0.005; unit cube p = 6, eps = 1e-3) on 16,384
+    particles: the oracle's tree, numbering and lists are the reference's,
+    its accelerations agree to 1e-12."""
+    d = load_case(name)
+    t = orc.tree(d["x"], d["s"])
+    assert not diff_trees(canon_ref(t), canon_ref(d))
+    assert np.array_equal(t["parent"], d["parent"]) and np.array_equal(t["first_child"], d["first_child"])
+    a = orc.accel(d["x"], d["s"], d["G"], d["m"], d["eps"], d["p"])
+    assert np.max(rel_err(a, d["acc"])) <= 1e-12
+
+
+def test_ten_step_trajectory_matches_reference(orc):
+    """The reference's CPU-runnable case to its end: Plummer N = 16,384
+    (Problem::initialize, seed 0), s = 32, eps = 0.01, p = 4, ten RK4 steps of
+    dt = 1e-3 (solver_ref.hpp:36-104). Final state within 1e-15 (positions)
+    and 1e-14 (velocities) of the reference's, absolute."""
+    from treecmp import checksum, regenerate
+    z = np.load(f"{GOLDEN}/traj_plummer16384_s32_p4.npz")
+    x, v = regenerate(z["gen"])
+    assert np.array_equal(checksum(x), z["x_sum"]) and np.array_equal(checksum(v), z["v_sum"])
+    x10, v10 = orc.rk4(x, v, int(z["s"]), float(z["G"]), float(z["m"]), float(z["eps"]), float(z["dt"]),
+                       int(z["p"]), int(z["steps"]))
+    assert np.max(np.abs(x10 - z["x10"])) <= 1e-15 and np.max(np.abs(v10 - z["v10"])) <= 1e-14
+
+
 def test_direct_potential_known_answer():
     """The oracle's FP64 potential (checker of the GPU potentials; the
     reference computes none): three particles, G = 2, m = 0.5, eps = 0.1."""

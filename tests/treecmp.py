@@ -11,9 +11,31 @@ import numpy as np
 GOLDEN = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.abspath(__file__)), "golden")
 
 
+def checksum(a):
+    """Order-sensitive FP64 checksum (the one tests/golden/make_golden.py stores)."""
+    a = np.ascontiguousarray(a, np.float64).ravel()
+    return np.array([a.sum(), (a * np.arange(1, a.size + 1)).sum(), a.size], np.float64)
+
+
+def regenerate(gen):
+    """Positions and velocities of a fixture that stores its generator instead:
+    gen = [0, n, eps, seed] is the reference's Problem::initialize (problem.hpp:188-211)
+    through the oracle's bit-identical restatement; [1, n, 0, seed] is numpy's
+    PCG64 unit cube at rest."""
+    kind, n, eps, seed = int(gen[0]), int(gen[1]), float(gen[2]), int(gen[3])
+    if kind == 0:
+        import oracle
+        return oracle.plummer_reference(n, eps, seed)
+    x = np.random.default_rng(seed).random((n, 3))
+    return x, np.zeros_like(x)
+
+
 def load_case(name):
     z = np.load(f"{GOLDEN}/tree_{name}.npz")
     d = {k: z[k] for k in z.files}
+    if "gen" in d:
+        d["x"], d["v"] = regenerate(d["gen"])
+        assert np.array_equal(checksum(d["x"]), d["x_sum"]), f"{name}: regenerated positions differ"
 
     def unflat(k):
         off, data = d[k + "_off"], d[k]

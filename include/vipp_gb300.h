@@ -57,6 +57,20 @@ enum gb_precision {
                            cores (3xTF32); RK4 combination in FP64 */
 };
 
+/* Method of the force evaluation. */
+enum gb_mode {
+    GB_MODE_REF = 0,      /* the reference's method (solver_ref.hpp:164-232): trees,
+                             lists and results as the reference's; its far field
+                             expands the unsoftened 1/r and carries no G */
+    GB_MODE_ACCURATE = 1  /* no counterpart in the reference: the same tree,
+                             lists and expansions, the far field multiplied by G,
+                             plus the far field of the softening difference
+                             (eps^2 + r^2)^-3/2 - r^-3 expanded to second order
+                             about each far source cell's centre of mass; with
+                             p = 10 it follows the softened direct sum to ~1e-5
+                             RMS, where the reference's method stops at ~eps^2/r^2 */
+};
+
 typedef struct gb_config {
     int p;          /* expansion order, 1..10 (Problem::p, problem.hpp:229) */
     int s;          /* leaf parameter; a cell splits above floor(sqrt(8) s)
@@ -68,6 +82,7 @@ typedef struct gb_config {
     int precision;  /* enum gb_precision */
     int device;     /* CUDA device ordinal */
     int flags;      /* bit set of gb_flags, 0 by default */
+    int mode;       /* enum gb_mode, GB_MODE_REF by default */
 } gb_config;
 
 enum gb_flags {
@@ -233,7 +248,7 @@ GB_API int gb_tree_dump(gb_ctx *ctx, int64_t *ncells, int64_t *list_sizes, int32
  * while it is on, the classes run one after another on one stream (no
  * near/far overlap) and every kernel is launched directly (no step graph).
  * Classes: 0 tree+lists, 1 operators, 2 P2M+M2M, 3 M2L, 4 L2L+L2P, 5 P2P,
- * 6 RK4+finalize. gb_kernel_times fills up to n entries of ms and launches
+ * 6 RK4+finalize, 7 softening correction (accurate mode). gb_kernel_times fills up to n entries of ms and launches
  * and resets the accumulators. */
 GB_API int gb_enable_timing(gb_ctx *ctx, int on);
 GB_API int gb_kernel_times(gb_ctx *ctx, double *ms, int64_t *launches, int n);

@@ -58,7 +58,8 @@ def lib():
         _LIB = ctypes.CDLL(path)
         _LIB.orc_tree_build.restype = _size
         _LIB.orc_threads.restype = ctypes.c_int
-        for f in ("orc_accel", "orc_rk4", "orc_accel_sampled"):
+        for f in ("orc_accel", "orc_accel_mode", "orc_rk4", "orc_rk4_mode", "orc_accel_sampled",
+                  "orc_soft_correction_check"):
             getattr(_LIB, f).restype = ctypes.c_int
     return _LIB
 
@@ -94,27 +95,35 @@ class Impl:
     def _f(self, name):
         return getattr(self.h, self.px + name)
 
-    def accel(self, x, s, G, m, eps, p):
+    def accel(self, x, s, G, m, eps, p, mode=0):
+        """One force evaluation. mode 0 is the reference's method; mode 1 the
+        accurate mode (oracle only: far field times G plus the softening
+        correction, oracle.hpp softening_correction)."""
         x = _aos(x)
         a = np.zeros_like(x)
         n = x.shape[0]
         if self.px == "orc_":
-            rc = self.h.orc_accel(_dp(x), _size(n), _size(s), ctypes.c_double(G), ctypes.c_double(m),
-                                  ctypes.c_double(eps), ctypes.c_uint(p), _dp(a), None)
+            rc = self.h.orc_accel_mode(_dp(x), _size(n), _size(s), ctypes.c_double(G), ctypes.c_double(m),
+                                       ctypes.c_double(eps), ctypes.c_uint(p), ctypes.c_int(mode), _dp(a), None)
             if rc:
                 raise RuntimeError("oracle accel failed")
         else:
+            assert mode == 0, "the reference has only its own method"
             self.h.ref_accel(_dp(x), _size(n), _size(s), ctypes.c_double(G), ctypes.c_double(m),
                              ctypes.c_double(eps), ctypes.c_uint(p), _dp(a))
         return a
 
-    def rk4(self, x, v, s, G, m, eps, dt, p, steps=1):
+    def rk4(self, x, v, s, G, m, eps, dt, p, steps=1, mode=0):
         x = _aos(x).copy()
         v = _aos(v).copy()
         n = x.shape[0]
         args = (_dp(x), _dp(v), _size(n), ctypes.c_double(G), ctypes.c_double(m), ctypes.c_double(eps),
                 ctypes.c_double(dt), _size(s), ctypes.c_uint(p), ctypes.c_int(steps))
-        rc = self._f("rk4")(*args)
+        if mode:
+            assert self.px == "orc_", "the reference has only its own method"
+            rc = self.h.orc_rk4_mode(*args, ctypes.c_int(mode))
+        else:
+            rc = self._f("rk4")(*args)
         if self.px == "orc_" and rc:
             raise RuntimeError("oracle rk4 failed")
         return x, v
@@ -225,6 +234,21 @@ def plummer_reference(n, eps, seed):
     v = np.zeros((n, 3))
     lib().orc_plummer_reference(_size(n), ctypes.c_double(eps), ctypes.c_ulonglong(seed), _dp(x), _dp(v))
     return x, v
+
+
+def soft_correction_check(x, s, G, m, eps, targets):
+    """(exact, expanded) far-field softening correction at the targets: the
+    exact sum over the far source particles and the accurate mode's expansion
+    of it (oracle.hpp softening_correction)."""
+    x = _aos(x)
+    t = np.ascontiguousarray(targets, dtype=np.int64)
+    ex = np.zeros((len(t), 3))
+    ap = np.zeros((len(t), 3))
+    rc = lib().orc_soft_correction_check(_dp(x), _size(x.shape[0]), _size(s), ctypes.c_double(G), ctypes.c_double(m),
+                                         ctypes.c_double(eps), _lp(t), _size(len(t)), _dp(ex), _dp(ap))
+    if rc:
+        raise RuntimeError("oracle correction check failed")
+    return ex, ap
 
 
 def curve_fit(e, t):

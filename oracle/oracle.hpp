@@ -412,8 +412,9 @@ inline void l2l(Tree &t, std::size_t ci, unsigned p) {
 }
 
 // L2P (fmm.hpp:332-374): gradient of sum L_l^m r^l Y_l^m in spherical
-// components, converted to Cartesian and added to a[i]. No G factor.
-inline void l2p(const Cell &c, unsigned p, const std::vector<V3> &x, std::vector<V3> &a) {
+// components, converted to Cartesian and added to a[i]. No G factor (the
+// reference's); the accurate mode passes g = G.
+inline void l2p(const Cell &c, unsigned p, const std::vector<V3> &x, std::vector<V3> &a, double g = 1.0) {
     const V3 ctr = c.center();
     for (long long i : c.pts) {
         double r, th, ph;
@@ -435,9 +436,9 @@ inline void l2p(const Cell &c, unsigned p, const std::vector<V3> &x, std::vector
         }
         const double ct = std::cos(th), st = std::sin(th), cp = std::cos(ph), sp = std::sin(ph);
         V3 &ai = a[static_cast<std::size_t>(i)];
-        ai.x += st * cp * dr + ct * cp / r * dth - sp / (r * st) * dph;
-        ai.y += st * sp * dr + ct * sp / r * dth + cp / (r * st) * dph;
-        ai.z += ct * dr - st / r * dth;
+        ai.x += g * (st * cp * dr + ct * cp / r * dth - sp / (r * st) * dph);
+        ai.y += g * (st * sp * dr + ct * sp / r * dth + cp / (r * st) * dph);
+        ai.z += g * (ct * dr - st / r * dth);
     }
 }
 
@@ -480,6 +481,204 @@ inline void p2p(const Tree &t, std::size_t ci, const std::vector<long long> &nb,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Accurate mode (no counterpart in the reference). The reference's far field
+// expands the unsoftened 1/r (M2L fmm.hpp:277-304, L2P fmm.hpp:332-374) while
+// its near field is softened (fmm.hpp:531-540) and only the near field carries
+// G, so against the softened direct sum its error stops near eps^2/r^2 whatever
+// p is. The accurate mode multiplies the far field by G and adds the far field
+// of the softening difference: for every leaf and every far source cell S of
+// it (the M2L lists of the leaf and of its ancestors at level >= 2),
+//   da(x) = G sum_{j in S} m_j F(|x_j - x|^2) (x_j - x),
+//   F(u) = (u + eps^2)^{-3/2} - u^{-3/2},
+// expanded about S's centre of mass z to second order in the source offsets
+// (y_j = x_j - z, Q = sum_j m_j y_j y_j^T; the first order vanishes about z):
+//   M F(u) d + [2 F''(u) (d.Qd) + F'(u) tr Q] d + 2 F'(u) Qd,   d = z - x, u = |d|^2.
+// Evaluation (the approximations the GPU kernels make too):
+//   * the lists of the leaf (k = 0) and of its parent (k = 1) at every
+//     particle; in the leaf's own list, a source at offset o (cell units) with
+//     exactly one |o_a| = 2 and the others <= 1 (the 54 nearest far cells,
+//     where the expansion converges slowest) is taken as its 8 octants, each
+//     with its own moments (children of a non-leaf source; the leaf's own
+//     particles split at its mid-planes, ties to the upper half, otherwise);
+//   * the lists of the ancestors at k >= 2 once at the leaf centre c: the
+//     value above plus the first-order change J (x - c) of its monopole term,
+//     J = -M (2 F'(u) d d^T + F(u) I).
+
+struct CellMoments {
+    double M = 0;          // mass
+    V3 z{0, 0, 0};         // centre of mass
+    double Q[6] = {};      // central second moments xx, yy, zz, xy, xz, yz
+};
+
+// Moments of a point set (equal masses).
+inline CellMoments moments_of(const std::vector<V3> &x, const std::vector<long long> &pts, double mass) {
+    CellMoments mo;
+    if (pts.empty()) return mo;
+    V3 s{0, 0, 0};
+    for (long long j : pts) {
+        const V3 &p = x[static_cast<std::size_t>(j)];
+        s.x += p.x, s.y += p.y, s.z += p.z;
+    }
+    const double c = static_cast<double>(pts.size());
+    mo.M = mass * c;
+    mo.z = {s.x / c, s.y / c, s.z / c};
+    for (long long j : pts) {
+        const V3 y = sub(x[static_cast<std::size_t>(j)], mo.z);
+        mo.Q[0] += mass * y.x * y.x, mo.Q[1] += mass * y.y * y.y, mo.Q[2] += mass * y.z * y.z;
+        mo.Q[3] += mass * y.x * y.y, mo.Q[4] += mass * y.x * y.z, mo.Q[5] += mass * y.y * y.z;
+    }
+    return mo;
+}
+
+// Members of a cell's subtree (tree order within leaves).
+inline void subtree_points(const Tree &t, std::size_t ci, std::vector<long long> &out) {
+    const Cell &c = t.cells[ci];
+    if (c.leaf()) {
+        out.insert(out.end(), c.pts.begin(), c.pts.end());
+        return;
+    }
+    for (long long u = c.first_child; u < c.first_child + 8; ++u) subtree_points(t, static_cast<std::size_t>(u), out);
+}
+
+// Whole-cell moments of every cell, and the 8 octant moments of every leaf
+// (particles split at the leaf's mid-planes, coordinate < mid -> lower half,
+// octant bit set; the tree's own tie rule).
+struct SoftMoments {
+    std::vector<CellMoments> cell;
+    std::vector<CellMoments> leaf_oct;  // [8 * cell], filled for leaves
+};
+
+inline SoftMoments soft_moments(const Tree &t, const std::vector<V3> &x, double mass) {
+    const std::size_t nc = t.cells.size();
+    SoftMoments sm;
+    sm.cell.resize(nc);
+    sm.leaf_oct.resize(8 * nc);
+#pragma omp parallel for schedule(dynamic, 8)
+    for (std::size_t c = 0; c < nc; ++c) {
+        std::vector<long long> pts;
+        subtree_points(t, c, pts);
+        sm.cell[c] = moments_of(x, pts, mass);
+        if (t.cells[c].leaf()) {
+            const V3 mid = t.cells[c].center();
+            std::vector<long long> part[8];
+            for (long long j : pts) {
+                const V3 &p = x[static_cast<std::size_t>(j)];
+                part[(p.x < mid.x ? 1 : 0) | (p.y < mid.y ? 2 : 0) | (p.z < mid.z ? 4 : 0)].push_back(j);
+            }
+            for (int o = 0; o < 8; ++o) sm.leaf_oct[8 * c + static_cast<std::size_t>(o)] = moments_of(x, part[o], mass);
+        }
+    }
+    return sm;
+}
+
+// F, F', F'' of the softening difference at u = |d|^2 (e = eps^2), written
+// without the cancellation of (u + e)^{-k/2} - u^{-k/2}: with w = sqrt(1 + e/u),
+// (1 + e/u)^{-k/2} - 1 = -(w^k - 1) / w^k and w - 1 = (e/u) / (w + 1).
+inline void soft_diff(double u, double e, double &F, double &F1, double &F2) {
+    const double q = e / u, w = std::sqrt(1.0 + q), wm1 = q / (w + 1.0);
+    const double w2 = w * w, w3 = w2 * w, w5 = w3 * w2, w7 = w5 * w2;
+    const double s3 = wm1 * (w2 + w + 1.0);                                    // w^3 - 1
+    const double s5 = wm1 * (w2 * w2 + w3 + w2 + w + 1.0);                     // w^5 - 1
+    const double s7 = wm1 * (w5 * w + w5 + w2 * w2 + w3 + w2 + w + 1.0);       // w^7 - 1
+    const double ru = 1.0 / std::sqrt(u), ru3 = ru * ru * ru, ru5 = ru3 * ru * ru, ru7 = ru5 * ru * ru;
+    F = -ru3 * s3 / w3;
+    F1 = 1.5 * ru5 * s5 / w5;
+    F2 = -3.75 * ru7 * s7 / w7;
+}
+
+// Softening-difference field of S at xi (no G), to second order.
+inline V3 soft_far_term(const CellMoments &S, const V3 &xi, double eps) {
+    const V3 d = sub(S.z, xi);
+    double F, F1, F2;
+    soft_diff(norm2(d), eps * eps, F, F1, F2);
+    const double *Q = S.Q;
+    const V3 Qd{Q[0] * d.x + Q[3] * d.y + Q[4] * d.z, Q[3] * d.x + Q[1] * d.y + Q[5] * d.z,
+                Q[4] * d.x + Q[5] * d.y + Q[2] * d.z};
+    const double dQd = d.x * Qd.x + d.y * Qd.y + d.z * Qd.z, tr = Q[0] + Q[1] + Q[2];
+    const double a = S.M * F + 2.0 * F2 * dQd + F1 * tr;
+    return {a * d.x + 2.0 * F1 * Qd.x, a * d.y + 2.0 * F1 * Qd.y, a * d.z + 2.0 * F1 * Qd.z};
+}
+
+// Offset (cell units) of same-level cell b from cell a.
+inline void level_offset(const Tree &t, std::size_t a, std::size_t b, int off[3]) {
+    const V3 ca = t.cells[a].center(), cb = t.cells[b].center();
+    const double h[3] = {t.cells[a].mx.x - t.cells[a].mn.x, t.cells[a].mx.y - t.cells[a].mn.y,
+                         t.cells[a].mx.z - t.cells[a].mn.z};
+    const double d[3] = {cb.x - ca.x, cb.y - ca.y, cb.z - ca.z};
+    for (int k = 0; k < 3; ++k) off[k] = static_cast<int>(std::lround(d[k] / h[k]));
+}
+
+inline bool face_slab(const int off[3]) {
+    int twos = 0, big = 0;
+    for (int k = 0; k < 3; ++k) twos += std::abs(off[k]) == 2, big += std::abs(off[k]) > 2;
+    return twos == 1 && big == 0;
+}
+
+// The softening correction of every particle of the leaves at level >= 2,
+// times G, added to a.
+inline void softening_correction(const Tree &t, const Lists &ls, const std::vector<V3> &x, double G, double mass,
+                                 double eps, std::vector<V3> &a) {
+    if (eps == 0) return;
+    const SoftMoments sm = soft_moments(t, x, mass);
+    const std::size_t nc = t.cells.size();
+#pragma omp parallel for schedule(dynamic, 4)
+    for (std::size_t leaf = 0; leaf < nc; ++leaf) {
+        const Cell &L = t.cells[leaf];
+        if (!L.leaf() || L.pts.empty() || L.level < 2) continue;
+        const V3 c = L.center();
+        V3 fc{0, 0, 0};
+        double J[9] = {};
+        std::vector<V3> corr(L.pts.size(), V3{0, 0, 0});
+        auto at_particles = [&](const CellMoments &S) {
+            if (S.M == 0) return;
+            for (std::size_t q = 0; q < L.pts.size(); ++q) {
+                const V3 f = soft_far_term(S, x[static_cast<std::size_t>(L.pts[q])], eps);
+                corr[q].x += f.x, corr[q].y += f.y, corr[q].z += f.z;
+            }
+        };
+        int k = 0;
+        for (long long anc = static_cast<long long>(leaf); anc >= 0 && t.cells[static_cast<std::size_t>(anc)].level >= 2;
+             anc = t.cells[static_cast<std::size_t>(anc)].parent, ++k) {
+            const std::size_t au = static_cast<std::size_t>(anc);
+            for (long long sidx : ls.m2l[au]) {
+                const std::size_t su = static_cast<std::size_t>(sidx);
+                const CellMoments &S = sm.cell[su];
+                if (S.M == 0) continue;
+                if (k == 0) {
+                    int off[3];
+                    level_offset(t, au, su, off);
+                    if (face_slab(off)) {
+                        for (int o = 0; o < 8; ++o)
+                            at_particles(t.cells[su].leaf() ? sm.leaf_oct[8 * su + static_cast<std::size_t>(o)]
+                                                            : sm.cell[static_cast<std::size_t>(t.cells[su].first_child + o)]);
+                        continue;
+                    }
+                }
+                if (k <= 1) {
+                    at_particles(S);
+                } else {
+                    const V3 f = soft_far_term(S, c, eps);
+                    fc.x += f.x, fc.y += f.y, fc.z += f.z;
+                    const V3 d = sub(S.z, c);
+                    double F, F1, F2;
+                    soft_diff(norm2(d), eps * eps, F, F1, F2);
+                    const double dd[3] = {d.x, d.y, d.z};
+                    for (int r = 0; r < 3; ++r)
+                        for (int q = 0; q < 3; ++q) J[3 * r + q] -= S.M * (2.0 * F1 * dd[r] * dd[q] + (r == q ? F : 0.0));
+                }
+            }
+        }
+        for (std::size_t q = 0; q < L.pts.size(); ++q) {
+            const std::size_t i = static_cast<std::size_t>(L.pts[q]);
+            const V3 y = sub(x[i], c);
+            a[i].x += G * (corr[q].x + fc.x + J[0] * y.x + J[1] * y.y + J[2] * y.z);
+            a[i].y += G * (corr[q].y + fc.y + J[3] * y.x + J[4] * y.y + J[5] * y.z);
+            a[i].z += G * (corr[q].z + fc.z + J[6] * y.x + J[7] * y.y + J[8] * y.z);
+        }
+    }
+}
+
 // One force evaluation (solver_ref.hpp:164-232): zero, tree, lists, then
 // P2M (leaves, level >= 2) / M2M (level >= 2) upward; M2L (index > 8, i.e.
 // level >= 2) and P2P (leaves); L2L (level >= 3) / L2P (leaves, level >= 2)
@@ -490,8 +689,10 @@ struct FmmStats {
     int depth = 0;
 };
 
+// mode 0: the reference's method; mode 1: the accurate mode (far field times
+// G plus the softening correction, see softening_correction).
 inline void accel_fmm(const std::vector<V3> &x, std::size_t s, double G, double mass, double eps, unsigned p,
-                      std::vector<V3> &a, FmmStats *st = nullptr) {
+                      std::vector<V3> &a, FmmStats *st = nullptr, int mode = 0) {
     a.assign(x.size(), V3{0, 0, 0});
     Tree t(x, s);
     Lists ls(t);
@@ -519,9 +720,10 @@ inline void accel_fmm(const std::vector<V3> &x, std::size_t s, double G, double 
 #pragma omp parallel for schedule(dynamic, 16)
         for (std::size_t k = 0; k < cl.size(); ++k) {
             if (lv >= 3) l2l(t, cl[k], p);
-            if (t.cells[cl[k]].leaf()) l2p(t.cells[cl[k]], p, x, a);
+            if (t.cells[cl[k]].leaf()) l2p(t.cells[cl[k]], p, x, a, mode == 1 ? G : 1.0);
         }
     }
+    if (mode == 1) softening_correction(t, ls, x, G, mass, eps, a);
     if (st) {
         st->ncells = nc;
         st->depth = t.max_level;

@@ -108,13 +108,13 @@ void orc_tree_lists(long long *m2l, long long *p2p, long long *coll) {
 }
 
 // One FMM force evaluation. stats (may be null): ncells, nleaves, depth, m2l pairs.
-int orc_accel(const double *x_aos, std::size_t n, std::size_t s, double G, double m, double eps, unsigned p, double *a_aos,
-              long long *stats) {
+int orc_accel_mode(const double *x_aos, std::size_t n, std::size_t s, double G, double m, double eps, unsigned p,
+                   int mode, double *a_aos, long long *stats) {
     try {
         auto x = to_v3(x_aos, n);
         std::vector<V3> a;
         FmmStats st;
-        accel_fmm(x, s, G, m, eps, p, a, &st);
+        accel_fmm(x, s, G, m, eps, p, a, &st, mode);
         from_v3(a, a_aos);
         if (stats) {
             stats[0] = static_cast<long long>(st.ncells);
@@ -128,18 +128,29 @@ int orc_accel(const double *x_aos, std::size_t n, std::size_t s, double G, doubl
     }
 }
 
-int orc_rk4(double *x_aos, double *v_aos, std::size_t n, double G, double m, double eps, double dt, std::size_t s, unsigned p,
-            int steps) {
+int orc_accel(const double *x_aos, std::size_t n, std::size_t s, double G, double m, double eps, unsigned p, double *a_aos,
+              long long *stats) {
+    return orc_accel_mode(x_aos, n, s, G, m, eps, p, 0, a_aos, stats);
+}
+
+int orc_rk4_mode(double *x_aos, double *v_aos, std::size_t n, double G, double m, double eps, double dt, std::size_t s,
+                 unsigned p, int steps, int mode) {
     try {
         auto x = to_v3(x_aos, n), v = to_v3(v_aos, n);
         for (int k = 0; k < steps; ++k)
-            rk4_step(x, v, dt, [&](const std::vector<V3> &xx, std::vector<V3> &aa) { accel_fmm(xx, s, G, m, eps, p, aa); });
+            rk4_step(x, v, dt,
+                     [&](const std::vector<V3> &xx, std::vector<V3> &aa) { accel_fmm(xx, s, G, m, eps, p, aa, nullptr, mode); });
         from_v3(x, x_aos);
         from_v3(v, v_aos);
         return 0;
     } catch (...) {
         return 1;
     }
+}
+
+int orc_rk4(double *x_aos, double *v_aos, std::size_t n, double G, double m, double eps, double dt, std::size_t s, unsigned p,
+            int steps) {
+    return orc_rk4_mode(x_aos, v_aos, n, G, m, eps, dt, s, p, steps, 0);
 }
 
 // Direct sum for the listed targets (all when targets == null).
@@ -322,3 +333,55 @@ int orc_accel_sampled(const double *x_aos, std::size_t n, std::size_t s, double 
 }
 
 }  // extern "C"
+
+extern "C" {
+// The accurate mode's softening correction at the listed targets, and the
+// exact sum it approximates: over every particle of the far source cells (the
+// M2L lists of the target's leaf and of its ancestors at level >= 2) of
+// G m F(|d|^2) d, F(u) = (u + eps^2)^-3/2 - u^-3/2.
+int orc_soft_correction_check(const double *x_aos, std::size_t n, std::size_t s, double G, double m, double eps,
+                              const long long *targets, std::size_t nt, double *exact_aos, double *approx_aos) {
+    try {
+        auto x = to_v3(x_aos, n);
+        Tree t(x, s);
+        Lists ls(t);
+        std::vector<V3> a(n, V3{0, 0, 0});
+        softening_correction(t, ls, x, G, m, eps, a);
+        std::vector<long long> leaf_of(n, -1);
+        for (std::size_t c = 0; c < t.cells.size(); ++c)
+            if (t.cells[c].leaf())
+                for (long long i : t.cells[c].pts) leaf_of[static_cast<std::size_t>(i)] = static_cast<long long>(c);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (std::size_t q = 0; q < nt; ++q) {
+            const std::size_t i = static_cast<std::size_t>(targets[q]);
+            approx_aos[3 * q] = a[i].x, approx_aos[3 * q + 1] = a[i].y, approx_aos[3 * q + 2] = a[i].z;
+            V3 acc{0, 0, 0};
+            for (long long anc = leaf_of[i]; anc >= 0 && t.cells[static_cast<std::size_t>(anc)].level >= 2;
+                 anc = t.cells[static_cast<std::size_t>(anc)].parent) {
+                for (long long sidx : ls.m2l[static_cast<std::size_t>(anc)]) {
+                    std::vector<std::size_t> stack{static_cast<std::size_t>(sidx)};
+                    while (!stack.empty()) {
+                        const std::size_t u = stack.back();
+                        stack.pop_back();
+                        if (!t.cells[u].leaf()) {
+                            for (long long w = t.cells[u].first_child; w < t.cells[u].first_child + 8; ++w)
+                                stack.push_back(static_cast<std::size_t>(w));
+                            continue;
+                        }
+                        for (long long j : t.cells[u].pts) {
+                            const V3 d = sub(x[static_cast<std::size_t>(j)], x[i]);
+                            double F, F1, F2;
+                            soft_diff(norm2(d), eps * eps, F, F1, F2);
+                            acc.x += G * m * F * d.x, acc.y += G * m * F * d.y, acc.z += G * m * F * d.z;
+                        }
+                    }
+                }
+            }
+            exact_aos[3 * q] = acc.x, exact_aos[3 * q + 1] = acc.y, exact_aos[3 * q + 2] = acc.z;
+        }
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+}

@@ -258,64 +258,40 @@ def test_reference_method_accuracy_floor_from_softening(orc):
     assert e5[1] > 2e-5
 
 
-def _softening_correction(t, x, m, eps):
-    """Monopole correction of the reference method's unsoftened far field:
-    for every leaf, the field of sum_S M_S [(r^2 + eps^2)^-3/2 - r^-3] d over
-    the leaf's far source cells S (the M2L lists of the leaf and its
-    ancestors; d from the evaluation point to S's centre of mass), taken at
-    the leaf centre with its gradient and applied to the leaf's particles."""
-    nc = len(t["parent"])
-    cnt = np.zeros(nc)
-    sx = np.zeros((nc, 3))
-    for c in range(nc):
-        if t["first_child"][c] < 0 and len(t["pts"][c]):
-            k = c
-            while k >= 0:
-                cnt[k] += len(t["pts"][c])
-                sx[k] += x[t["pts"][c]].sum(0)
-                k = int(t["parent"][k])
-    com = sx / np.maximum(cnt, 1)[:, None]
-    corr = np.zeros_like(x)
-    for leaf in range(nc):
-        if t["first_child"][leaf] >= 0 or not len(t["pts"][leaf]):
-            continue
-        srcs, k = [], leaf
-        while k >= 0:
-            srcs.extend(t["m2l"][k])
-            k = int(t["parent"][k])
-        srcs = np.array([u for u in srcs if cnt[u] > 0], dtype=np.int64)
-        if not len(srcs):
-            continue
-
-        def field(y):
-            d = com[srcs] - y
-            r2 = (d * d).sum(-1)
-            return ((((r2 + eps * eps) ** -1.5 - r2 ** -1.5) * m * cnt[srcs])[:, None] * d).sum(0)
-
-        ctr = 0.5 * (t["mins"][leaf] + t["maxs"][leaf])
-        h = 1e-4 * float(np.max(t["maxs"][leaf] - t["mins"][leaf]))
-        jac = np.stack([(field(ctr + h * e) - field(ctr - h * e)) / (2 * h) for e in np.eye(3)], axis=1)
-        pts = t["pts"][leaf]
-        corr[pts] += field(ctr) + (x[pts] - ctr) @ jac.T
-    return corr
-
-
-def test_monopole_softening_correction_lifts_the_floor(orc):
-    """The floor above is the far field's softening bias: a per-leaf monopole
-    correction (value and gradient at the leaf centre) brings the reference
-    method at p = 10, eps = 0.005 from ~3e-5 to ~1e-5 RMS vs the direct sum on
-    16,384 Plummer particles (the unsoftened method reaches 7.6e-6 there)."""
+def test_accurate_mode_reaches_1e5_against_direct_sum(orc):
+    """The oracle's accurate mode (far field times G plus the second-order
+    softening correction, oracle.hpp softening_correction) at p = 10 on
+    16,384 Plummer particles, s = 64, eps = 0.005: RMS relative error vs the
+    FP64 direct sum <= 1e-5 (measured 7.56e-6, the unsoftened method's own
+    7.55e-6), for G = 1 and G = 2.5 alike; the reference's method stays above
+    2.5e-5 there."""
     import math
     from vipp_gb300.workloads import plummer
     n, eps = 16384, 0.005
     x, _ = plummer(n, 2)
-    t = orc.tree(x, 64)
-    a = orc.accel(x, 64, 1.0, 1.0 / n, eps, 10)
-    ad = O.direct_accel(x, 1.0, 1.0 / n, eps)
+    for G in (1.0, 2.5):
+        ad = O.direct_accel(x, G, 1.0 / n, eps)
+        e = rel_err(orc.accel(x, 64, G, 1.0 / n, eps, 10, mode=1), ad)
+        assert math.sqrt(np.mean(e * e)) <= 1e-5
+    e = rel_err(orc.accel(x, 64, 1.0, 1.0 / n, eps, 10), O.direct_accel(x, 1.0, 1.0 / n, eps))
+    assert math.sqrt(np.mean(e * e)) > 2.5e-5
 
-    def rms(b):
-        e = rel_err(b, ad)
-        return math.sqrt(np.mean(e * e))
 
-    before, after = rms(a), rms(a + _softening_correction(t, x, 1.0 / n, eps))
-    assert before > 2.5e-5 and after < 1.2e-5
+@pytest.mark.parametrize("eps,tol", [(0.005, 5e-7), (0.031, 5e-6)])
+def test_softening_correction_against_exact_far_sum(eps, tol):
+    """The accurate mode's expansion of the softening difference against the
+    exact sum over the far source particles (every particle of the M2L lists
+    of the target's leaf and its ancestors), 2,048 targets of 16,384 Plummer
+    particles, s = 64: RMS error relative to |a| <= tol. eps = 0.031 puts the
+    leaves at ~9 eps, as the 4M sphere's core leaves are at eps = 0.005
+    (measured 6e-8 and 2.6e-6; 3.1e-6 on the 4M sphere itself)."""
+    import math
+    from vipp_gb300.workloads import plummer
+    n = 16384
+    x, _ = plummer(n, 2)
+    tg = np.arange(0, n, 8)
+    ex, ap = O.soft_correction_check(x, 64, 1.0, 1.0 / n, eps, tg)
+    nrm = np.linalg.norm(O.direct_accel(x, 1.0, 1.0 / n, eps, tg), axis=1)
+    e = np.linalg.norm(ex - ap, axis=1) / nrm
+    assert math.sqrt(np.mean(e * e)) <= tol
+    assert math.sqrt(np.mean((np.linalg.norm(ex, axis=1) / nrm) ** 2)) > 20 * tol  # the correction is not small

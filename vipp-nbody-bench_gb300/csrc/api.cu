@@ -91,6 +91,7 @@ int validate(const gb_config *c, std::string &msg) {
     if (!(c->eps >= 0) || !std::isfinite(c->eps)) return msg = "eps must be finite and >= 0", GB_ERR_INVALID;
     if (!std::isfinite(c->G) || !std::isfinite(c->m)) return msg = "G and m must be finite", GB_ERR_INVALID;
     if (c->precision != GB_PREC_FP64 && c->precision != GB_PREC_MIXED) return msg = "unknown precision", GB_ERR_INVALID;
+    if (c->mode != GB_MODE_REF && c->mode != GB_MODE_ACCURATE) return msg = "unknown mode", GB_ERR_INVALID;
     return GB_OK;
 }
 
@@ -107,6 +108,7 @@ void apply_config(gb_ctx *ctx) {
     ws.m2l_tensor = ws.mixed && (ctx->cfg.flags & GB_FLAG_M2L_CUDA_CORES) == 0 && gb::m2l_tc_supported(ws.p);
     ws.m2l_bf16 = (ctx->cfg.flags & GB_FLAG_M2L_BF16) != 0;
     ws.serial = (ctx->cfg.flags & GB_FLAG_SERIAL) != 0;
+    ws.accurate = ctx->cfg.mode == GB_MODE_ACCURATE;
 }
 
 // P2P work items: at most two partial chunks per leaf plus n/32 full ones,
@@ -226,6 +228,20 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
         ++ctx->epoch;
         GB_TRY(dalloc(ws.ranges, r_cap));
         ws.r_cap = r_cap;
+    }
+    if (ws.accurate && (ws.soft_cap != ws.c_cap || ws.soft_mixed != ws.mixed)) {
+        // moment records, octant records and leaf-centre terms of the softening correction
+        ++ctx->epoch;
+        const size_t rec = gb::soften_cell_bytes(ws.mixed), c = ws.c_cap;
+        unsigned char *a = nullptr, *b = nullptr, *t = nullptr;
+        GB_TRY(dalloc(a, rec * c));
+        GB_TRY(dalloc(b, 8 * rec * c));
+        GB_TRY(dalloc(t, 12 * (rec / 16) * c));
+        dfree(ws.smom);
+        dfree(ws.smom_oct);
+        dfree(ws.staylor);
+        ws.smom = a, ws.smom_oct = b, ws.staylor = t;
+        ws.soft_cap = ws.c_cap, ws.soft_mixed = ws.mixed;
     }
     if (ws.m2l_tensor) {
         // split expansions of the tensor-core M2L and their TMA map
@@ -366,6 +382,7 @@ void evaluate(gb_ctx *ctx, bool to_acc = true) {
     else
         gb::m2l_pass(ws);
     gb::downward_pass(ws);
+    if (ws.accurate) gb::soften_pass(ws);
     if (!fork) {
         gb::p2p_pass(ws, full);
     } else {
@@ -497,7 +514,7 @@ void gb_destroy(gb_ctx *ctx) {
                     ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
-                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.m2l_tab, ws.ms_tc, ws.diag, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets,
+                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.m2l_tab, ws.ms_tc, ws.diag, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets, ws.smom, ws.smom_oct, ws.staylor,
                     ctx->d_direct};
     for (void *b : bufs) dfree(b);
     gb::sort_temp_free(ws.sort);

@@ -1,0 +1,468 @@
+// Accurate mode: the far field of the softening difference (no counterpart in
+// the reference).
+//
+// The reference's far field expands the unsoftened 1/r (M2L fmm.hpp:277-304,
+// L2P fmm.hpp:332-374) while its near field is softened (fmm.hpp:531-540), and
+// only the near field carries G; against the softened direct sum its error
+// therefore stops near eps^2/r^2 whatever p is. In the accurate mode the far
+// field is multiplied by G and the field of the softening difference is added:
+// for every leaf and every far source cell S of it (the M2L lists of the leaf
+// and of its ancestors at level >= 2),
+//   da(x) = G sum_{j in S} m_j F(|x_j - x|^2) (x_j - x),
+//   F(u) = (u + eps^2)^{-3/2} - u^{-3/2},
+// expanded about S's centre of mass z to second order in the source offsets
+// (y_j = x_j - z, Q = sum_j m_j y_j y_j^T; the first order vanishes about z):
+//   [M F(u) + F'(u) tr Q + 2 F''(u) d.Qd] d + 2 F'(u) Qd,   d = z - x, u = |d|^2,
+//   F' = -3/2 [(u + e)^{-5/2} - u^{-5/2}],   F'' = 15/4 [(u + e)^{-7/2} - u^{-7/2}].
+// Evaluation:
+//   * k_soft_near: the lists of the leaf and of its parent at every particle;
+//     in the leaf's own list a source at offset o (cell units) with exactly one
+//     |o_a| = 2 and the others <= 1 (the 54 nearest far cells, where the
+//     expansion converges slowest) is taken as its 8 octants: the children of a
+//     non-leaf source, or the leaf's particles split at its mid-planes;
+//   * k_soft_far: the lists of the ancestors two and more levels up, once per
+//     leaf at its centre c (the value above and the first-order change
+//     J (x - c) of its monopole term, J = -M (2 F' d d^T + F I)).
+// The oracle's softening_correction (oracle/oracle.hpp) states the same
+// approximations in FP64; the error of the expansion against the exact sum over
+// the source particles is ~3e-6 of |a| (RMS) on the 4M Plummer sphere with
+// eps = 0.005, below the p = 10 expansion's own ~7e-6.
+//
+// Moments are records of 16 values of T per cell (Mom): the centre of mass
+// relative to the root-box centre (FP32: a hi + lo pair), the mass, tr Q, and
+// the second central moments. Differences d are formed relative to the target
+// leaf's centre, as the near field does, so FP32 keeps ~1e-7 of the
+// neighbourhood size. F, F', F'' are differences of (u + e)^{-k/2} and u^{-k/2};
+// their FP32 rounding is ~1e-7 / (eps^2/u) relative, at most ~1e-3 of a
+// correction that is itself ~eps^2/u of the source's field.
+#include "workspace.cuh"
+
+namespace gb {
+
+namespace {
+
+template <typename T>
+struct Mom {
+    T zh[3], M;   // centre of mass - root-box centre (hi part), mass
+    T zl[3], tr;  // lo part (0 in FP64), trace of Q
+    T Q[6];       // xx yy zz xy xz yz
+    T pad[2];
+};
+static_assert(sizeof(Mom<float>) == 64 && sizeof(Mom<double>) == 128, "Mom layout");
+
+template <typename T>
+__device__ __forceinline__ T rsqrt_t(T x);
+template <>
+__device__ __forceinline__ float rsqrt_t<float>(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+template <>
+__device__ __forceinline__ double rsqrt_t<double>(double x) {
+    return 1.0 / sqrt(x);
+}
+
+// A cell's centre relative to the root-box centre, as (hi, lo) in T.
+template <typename T>
+struct RelC {
+    T h[3], l[3];
+};
+template <typename T>
+__device__ __forceinline__ RelC<T> rel_centre(const double *c_ctr, int c, const TreeInfo *info) {
+    RelC<T> r;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double d = c_ctr[3 * c + a] - info->root_c[a];
+        r.h[a] = static_cast<T>(d);
+        r.l[a] = static_cast<T>(d - static_cast<double>(r.h[a]));
+    }
+    return r;
+}
+
+// Position of tree-order particle j relative to the centre of cell c.
+template <typename T>
+__device__ __forceinline__ void rel_pos(int j, const double *xs, unsigned n, const float4 *ph, const float4 *pl,
+                                        const double *cd, const RelC<T> &cc, T y[3]) {
+    if (sizeof(T) == 4) {
+        const float4 h = ph[j], l = pl[j];
+        y[0] = static_cast<T>((h.x - static_cast<float>(cc.h[0])) + (l.x - static_cast<float>(cc.l[0])));
+        y[1] = static_cast<T>((h.y - static_cast<float>(cc.h[1])) + (l.y - static_cast<float>(cc.l[1])));
+        y[2] = static_cast<T>((h.z - static_cast<float>(cc.h[2])) + (l.z - static_cast<float>(cc.l[2])));
+    } else {
+        y[0] = static_cast<T>(xs[j] - cd[0]);
+        y[1] = static_cast<T>(xs[n + j] - cd[1]);
+        y[2] = static_cast<T>(xs[2 * static_cast<size_t>(n) + j] - cd[2]);
+    }
+}
+
+// Record from sums about a cell centre: count, sum y, sum y y^T (xx yy zz xy xz yz).
+template <typename T>
+__device__ __forceinline__ void make_record(const T *s, T mass, const RelC<T> &cc, Mom<T> &r) {
+    const T cnt = s[0];
+    if (cnt == T(0)) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) r.zh[a] = T(0), r.zl[a] = T(0);
+        r.M = T(0), r.tr = T(0);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) r.Q[k] = T(0);
+        r.pad[0] = r.pad[1] = T(0);
+        return;
+    }
+    const T inv = T(1) / cnt;
+    const T g[3] = {s[1] * inv, s[2] * inv, s[3] * inv};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const T t = cc.l[a] + g[a];
+        r.zh[a] = cc.h[a] + t;
+        r.zl[a] = t - (r.zh[a] - cc.h[a]);
+    }
+    r.M = mass * cnt;
+    r.Q[0] = mass * (s[4] - cnt * g[0] * g[0]);
+    r.Q[1] = mass * (s[5] - cnt * g[1] * g[1]);
+    r.Q[2] = mass * (s[6] - cnt * g[2] * g[2]);
+    r.Q[3] = mass * (s[7] - cnt * g[0] * g[1]);
+    r.Q[4] = mass * (s[8] - cnt * g[0] * g[2]);
+    r.Q[5] = mass * (s[9] - cnt * g[1] * g[2]);
+    r.tr = r.Q[0] + r.Q[1] + r.Q[2];
+    r.pad[0] = r.pad[1] = T(0);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ------------------------------------------------------------ leaf moments
+// One warp per leaf at level >= 2: the moments of the leaf and of its 8
+// octants (coordinate < mid-plane -> lower half, octant bit set; the tree's
+// tie rule). Sums per octant by masked warp reductions (fixed order).
+template <typename T>
+__global__ void __launch_bounds__(128) k_mom_leaf(const int *__restrict__ leaves, const unsigned *counts,
+                                                  const int *__restrict__ c_begin, const int *__restrict__ c_end,
+                                                  const int *__restrict__ c_level, const double *__restrict__ c_ctr,
+                                                  const double *__restrict__ xs, const float4 *__restrict__ ph,
+                                                  const float4 *__restrict__ pl, unsigned n,
+                                                  const TreeInfo *__restrict__ info, T mass, Mom<T> *__restrict__ mom,
+                                                  Mom<T> *__restrict__ moct) {
+    __shared__ T sums[4][9][10];  // 8 octants + the whole leaf
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned NL = counts[3];
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    for (unsigned li = blockIdx.x * (blockDim.x >> 5) + w; li < NL; li += warps) {
+        const int c = leaves[li];
+        if (c_level[c] < 2) continue;  // warp-uniform
+        const RelC<T> cc = rel_centre<T>(c_ctr, c, info);
+        const double cd[3] = {c_ctr[3 * c], c_ctr[3 * c + 1], c_ctr[3 * c + 2]};
+        for (int k = lane; k < 80; k += 32) sums[w][k / 10][k % 10] = T(0);
+        __syncwarp();
+        const int b = c_begin[c], e = c_end[c];
+        for (int j0 = b; j0 < e; j0 += 32) {
+            const int j = j0 + lane;
+            T v[10] = {};
+            int oct = -1;
+            if (j < e) {
+                T y[3];
+                rel_pos<T>(j, xs, n, ph, pl, cd, cc, y);
+                oct = (y[0] < T(0) ? 1 : 0) | (y[1] < T(0) ? 2 : 0) | (y[2] < T(0) ? 4 : 0);
+                v[0] = T(1), v[1] = y[0], v[2] = y[1], v[3] = y[2];
+                v[4] = y[0] * y[0], v[5] = y[1] * y[1], v[6] = y[2] * y[2];
+                v[7] = y[0] * y[1], v[8] = y[0] * y[2], v[9] = y[1] * y[2];
+            }
+            for (int o = 0; o < 8; ++o) {
+                if (!__ballot_sync(0xffffffffu, oct == o)) continue;  // warp-uniform
+#pragma unroll
+                for (int k = 0; k < 10; ++k) {
+                    const T s = warp_sum(oct == o ? v[k] : T(0));
+                    if (lane == 0) sums[w][o][k] += s;
+                }
+            }
+            __syncwarp();
+        }
+        if (lane < 10) {
+            T s = T(0);
+            for (int o = 0; o < 8; ++o) s += sums[w][o][lane];
+            sums[w][8][lane] = s;
+        }
+        __syncwarp();
+        if (lane < 9) {
+            Mom<T> r;
+            make_record<T>(sums[w][lane], mass, cc, r);
+            if (lane < 8)
+                moct[static_cast<size_t>(c) * 8 + lane] = r;
+            else
+                mom[c] = r;
+        }
+        __syncwarp();
+    }
+}
+
+// -------------------------------------------------------- non-leaf moments
+// Non-leaf cells of level L (>= 2) from their 8 children: M = sum M_c,
+// g = sum M_c g_c / M, Q = sum [Q_c + M_c (g_c - g)(g_c - g)^T], with g_c the
+// child's centre of mass relative to the parent's centre.
+template <typename T>
+__global__ void k_mom_up(int L, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell,
+                         const int *__restrict__ c_child, const double *__restrict__ c_ctr, Mom<T> *mom) {
+    const int e0 = info->split_start[L], cnt = info->split_count[L];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += gridDim.x * blockDim.x) {
+        const int P = split_cell[e0 + e];
+        const int fc = c_child[P];
+        const RelC<T> cc = rel_centre<T>(c_ctr, P, info);
+        T gc[8][3], Mc[8];
+        T M = T(0), g[3] = {T(0), T(0), T(0)};
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+            const Mom<T> &r = mom[fc + o];
+            Mc[o] = r.M;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) gc[o][a] = (r.zh[a] - cc.h[a]) + (r.zl[a] - cc.l[a]);
+            M += Mc[o];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) g[a] += Mc[o] * gc[o][a];
+        }
+        Mom<T> out;
+        if (M == T(0)) {
+            T z[10] = {};
+            make_record<T>(z, T(0), cc, out);
+            mom[P] = out;
+            continue;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) g[a] /= M;
+        T Q[6] = {};
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+            const Mom<T> &r = mom[fc + o];
+            const T d0 = gc[o][0] - g[0], d1 = gc[o][1] - g[1], d2 = gc[o][2] - g[2];
+            Q[0] += r.Q[0] + Mc[o] * d0 * d0;
+            Q[1] += r.Q[1] + Mc[o] * d1 * d1;
+            Q[2] += r.Q[2] + Mc[o] * d2 * d2;
+            Q[3] += r.Q[3] + Mc[o] * d0 * d1;
+            Q[4] += r.Q[4] + Mc[o] * d0 * d2;
+            Q[5] += r.Q[5] + Mc[o] * d1 * d2;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const T t = cc.l[a] + g[a];
+            out.zh[a] = cc.h[a] + t;
+            out.zl[a] = t - (out.zh[a] - cc.h[a]);
+        }
+        out.M = M;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) out.Q[k] = Q[k];
+        out.tr = Q[0] + Q[1] + Q[2];
+        out.pad[0] = out.pad[1] = T(0);
+        mom[P] = out;
+    }
+}
+
+// Softening-difference field (no G) of record r at offset d = z - x, added to acc.
+template <typename T>
+__device__ __forceinline__ void soft_term(const Mom<T> &r, T dx, T dy, T dz, T e2, T &ax, T &ay, T &az) {
+    const T u = dx * dx + dy * dy + dz * dz;
+    const T A = rsqrt_t<T>(u + e2), B = rsqrt_t<T>(u);
+    const T A2 = A * A, B2 = B * B;
+    const T A3 = A2 * A, B3 = B2 * B;
+    const T A5 = A3 * A2, B5 = B3 * B2;
+    const T A7 = A5 * A2, B7 = B5 * B2;
+    const T F = A3 - B3;
+    const T F1 = T(-1.5) * (A5 - B5);
+    const T F2 = T(3.75) * (A7 - B7);
+    const T qx = r.Q[0] * dx + r.Q[3] * dy + r.Q[4] * dz;
+    const T qy = r.Q[3] * dx + r.Q[1] * dy + r.Q[5] * dz;
+    const T qz = r.Q[4] * dx + r.Q[5] * dy + r.Q[2] * dz;
+    const T dqd = dx * qx + dy * qy + dz * qz;
+    const T a = r.M * F + F1 * r.tr + T(2) * F2 * dqd;
+    const T b = T(2) * F1;
+    ax += a * dx + b * qx;
+    ay += a * dy + b * qy;
+    az += a * dz + b * qz;
+}
+
+// Offset of the source relative to the target leaf centre: (z - c).
+template <typename T>
+__device__ __forceinline__ void src_offset(const Mom<T> &r, const RelC<T> &cc, T s[3]) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) s[a] = (r.zh[a] - cc.h[a]) + (r.zl[a] - cc.l[a]);
+}
+
+// --------------------------------------------------- far levels (k >= 2)
+// One warp per leaf: the value and first-order change at the leaf centre of
+// the sources in the M2L lists of the ancestors two and more levels up (each
+// lane a fixed subset of slots, then a butterfly sum); 12 values per leaf
+// (value, J row-major). Leaves above level 4 get zeros.
+template <typename T>
+__global__ void __launch_bounds__(128) k_soft_far(const int *__restrict__ leaves, const unsigned *counts,
+                                                  const int *__restrict__ c_level, const int *__restrict__ c_parent,
+                                                  const double *__restrict__ c_ctr, const TreeInfo *__restrict__ info,
+                                                  const int *__restrict__ m2l_src, const Mom<T> *__restrict__ mom, T e2,
+                                                  T *__restrict__ taylor) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned NL = counts[3];
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    for (unsigned li = blockIdx.x * (blockDim.x >> 5) + w; li < NL; li += warps) {
+        const int c = leaves[li];
+        if (c_level[c] < 2) continue;  // warp-uniform
+        const RelC<T> cc = rel_centre<T>(c_ctr, c, info);
+        T v[12] = {};
+        int anc = c_level[c] >= 4 ? c_parent[c_parent[c]] : -1;
+        while (anc >= 0 && c_level[anc] >= 2) {
+            for (int s = lane; s < kM2LSlots; s += 32) {
+                const int src = m2l_src[static_cast<size_t>(anc) * kM2LSlots + s];
+                if (src < 0) continue;
+                const Mom<T> r = mom[src];
+                if (r.M == T(0)) continue;
+                T d[3];
+                src_offset<T>(r, cc, d);
+                soft_term<T>(r, d[0], d[1], d[2], e2, v[0], v[1], v[2]);
+                const T u = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                const T A = rsqrt_t<T>(u + e2), B = rsqrt_t<T>(u);
+                const T A2 = A * A, B2 = B * B, A3 = A2 * A, B3 = B2 * B;
+                const T F = A3 - B3, F1 = T(-1.5) * (A3 * A2 - B3 * B2);
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) v[3 + 3 * a + q] -= r.M * (T(2) * F1 * d[a] * d[q] + (a == q ? F : T(0)));
+            }
+            anc = c_parent[anc];
+        }
+#pragma unroll
+        for (int k = 0; k < 12; ++k) v[k] = warp_sum(v[k]);
+        if (lane < 12) {
+            T out = v[0];
+#pragma unroll
+            for (int k = 1; k < 12; ++k)
+                if (lane == k) out = v[k];
+            taylor[static_cast<size_t>(c) * 12 + lane] = out;
+        }
+    }
+}
+
+// -------------------------------------------- near levels (k = 0, 1) + apply
+// One warp per leaf at level >= 2, lanes over its particles: the per-particle
+// correction of the leaf's and its parent's M2L lists, plus the leaf-centre
+// Taylor part, then far = G (far + correction).
+template <typename T>
+__global__ void __launch_bounds__(128) k_soft_near(const int *__restrict__ leaves, const unsigned *counts,
+                                                   const int *__restrict__ c_begin, const int *__restrict__ c_end,
+                                                   const int *__restrict__ c_level, const int *__restrict__ c_parent,
+                                                   const int *__restrict__ c_child, const double *__restrict__ c_ctr,
+                                                   const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
+                                                   const Mom<T> *__restrict__ mom, const Mom<T> *__restrict__ moct,
+                                                   const T *__restrict__ taylor, const double *__restrict__ xs,
+                                                   const float4 *__restrict__ ph, const float4 *__restrict__ pl,
+                                                   unsigned n, T e2, T G, T *__restrict__ far) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned NL = counts[3];
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    for (unsigned li = blockIdx.x * (blockDim.x >> 5) + w; li < NL; li += warps) {
+        const int c = leaves[li];
+        if (c_level[c] < 2) continue;  // warp-uniform
+        const RelC<T> cc = rel_centre<T>(c_ctr, c, info);
+        const double cd[3] = {c_ctr[3 * c], c_ctr[3 * c + 1], c_ctr[3 * c + 2]};
+        const int P = c_parent[c];
+        const int oc = c - c_child[P];
+        const int uc[3] = {1 - (oc & 1), 1 - ((oc >> 1) & 1), 1 - ((oc >> 2) & 1)};
+        const int P2 = c_level[P] >= 2 ? P : -1;
+        T tl[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) tl[k] = taylor[static_cast<size_t>(c) * 12 + k];
+        const int b = c_begin[c], e = c_end[c];
+        for (int j0 = b; j0 < e; j0 += 32) {
+            const int j = j0 + lane;
+            T y[3] = {T(0), T(0), T(0)};
+            if (j < e) rel_pos<T>(j, xs, n, ph, pl, cd, cc, y);
+            T ax = T(0), ay = T(0), az = T(0);
+            for (int lev = 0; lev < 2; ++lev) {
+                const int tc = lev == 0 ? c : P2;
+                if (tc < 0) break;
+                for (int s = 0; s < kM2LSlots; ++s) {
+                    const int src = m2l_src[static_cast<size_t>(tc) * kM2LSlots + s];
+                    if (src < 0) continue;  // warp-uniform from here on
+                    bool slab = false;
+                    if (lev == 0) {
+                        const int dd = s >> 3, o = s & 7;
+                        const int d[3] = {dd % 3 - 1, (dd / 3) % 3 - 1, dd / 9 - 1};
+                        int twos = 0, big = 0;
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            const int off = 2 * d[a] + (1 - ((o >> a) & 1)) - uc[a];
+                            twos += (off == 2 || off == -2);
+                            big += (off > 2 || off < -2);
+                        }
+                        slab = twos == 1 && big == 0;
+                    }
+                    if (!slab) {
+                        const Mom<T> r = mom[src];
+                        if (r.M == T(0)) continue;
+                        T sd[3];
+                        src_offset<T>(r, cc, sd);
+                        soft_term<T>(r, sd[0] - y[0], sd[1] - y[1], sd[2] - y[2], e2, ax, ay, az);
+                    } else {
+                        const int ch = c_child[src];
+                        const Mom<T> *base = ch >= 0 ? mom + ch : moct + static_cast<size_t>(src) * 8;
+                        for (int o = 0; o < 8; ++o) {
+                            const Mom<T> r = base[o];
+                            if (r.M == T(0)) continue;
+                            T sd[3];
+                            src_offset<T>(r, cc, sd);
+                            soft_term<T>(r, sd[0] - y[0], sd[1] - y[1], sd[2] - y[2], e2, ax, ay, az);
+                        }
+                    }
+                }
+            }
+            if (j < e) {
+                ax += tl[0] + tl[3] * y[0] + tl[4] * y[1] + tl[5] * y[2];
+                ay += tl[1] + tl[6] * y[0] + tl[7] * y[1] + tl[8] * y[2];
+                az += tl[2] + tl[9] * y[0] + tl[10] * y[1] + tl[11] * y[2];
+                far[j] = G * (far[j] + ax);
+                far[n + j] = G * (far[n + j] + ay);
+                far[2 * static_cast<size_t>(n) + j] = G * (far[2 * static_cast<size_t>(n) + j] + az);
+            }
+        }
+    }
+}
+
+template <typename T>
+void launch_soften(Workspace &ws) {
+    const unsigned gw = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));  // a warp per leaf
+    Mom<T> *mom = static_cast<Mom<T> *>(ws.smom);
+    Mom<T> *moct = static_cast<Mom<T> *>(ws.smom_oct);
+    T *taylor = static_cast<T *>(ws.staylor);
+    const T e2 = static_cast<T>(ws.eps * ws.eps);
+    k_mom_leaf<T><<<gw, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.ph,
+                                         ws.pl, ws.n, ws.info, static_cast<T>(ws.m), mom, moct);
+    ws.launches += 1;
+    const unsigned gu = capped_grid(static_cast<unsigned>(ws.num_sms) * 4, ceil_div(ws.s_cap, 256));
+    for (int L = ws.sort_levels - 1; L >= 2; --L) {  // parents lie at levels < sort_levels (tree.cu)
+        k_mom_up<T><<<gu, 256, 0, ws.st>>>(L, ws.info, ws.split_cell, ws.c_child, ws.c_ctr, mom);
+        ws.launches += 1;
+    }
+    k_soft_far<T><<<gw, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_level, ws.c_parent, ws.c_ctr, ws.info, ws.m2l_src,
+                                         mom, e2, taylor);
+    k_soft_near<T><<<gw, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_parent,
+                                          ws.c_child, ws.c_ctr, ws.info, ws.m2l_src, mom, moct, taylor, ws.xs, ws.ph,
+                                          ws.pl, ws.n, e2, static_cast<T>(ws.G), static_cast<T *>(ws.farf));
+    ws.launches += 2;
+}
+
+}  // namespace
+
+size_t soften_cell_bytes(bool mixed) {
+    const size_t t = mixed ? sizeof(float) : sizeof(double);
+    return 16 * t;  // one Mom record
+}
+
+void soften_pass(Workspace &ws) {
+    timer_begin(ws, kTSoft);
+    if (ws.mixed)
+        launch_soften<float>(ws);
+    else
+        launch_soften<double>(ws);
+    timer_end(ws, kTSoft);
+}
+
+}  // namespace gb

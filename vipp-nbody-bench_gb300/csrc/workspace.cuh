@@ -27,7 +27,7 @@
 
 namespace gb {
 
-enum TimerClass { kTTree = 0, kTOps = 1, kTUp = 2, kTM2L = 3, kTDown = 4, kTP2P = 5, kTRK4 = 6, kNumTimers = 7 };
+enum TimerClass { kTTree = 0, kTOps = 1, kTUp = 2, kTM2L = 3, kTDown = 4, kTP2P = 5, kTRK4 = 6, kTSoft = 7, kNumTimers = 8 };
 
 struct Workspace {
     // configuration of the evaluation
@@ -37,6 +37,7 @@ struct Workspace {
     bool p2p_newton = false;  // one Newton step after the FP32 rsqrt
     bool m2l_tensor = false;  // tcgen05 M2L (mixed precision only)
     bool m2l_bf16 = false;    // its split: bf16 hi/lo (kind::f16), else 3 x tf32
+    bool accurate = false;    // accurate mode: far field times G plus the softening correction (soften.cu)
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;         // near field, concurrent with the far field on st
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -86,6 +87,11 @@ struct Workspace {
     void *Mexp = nullptr, *Lexp = nullptr;  // [C][K]
     int *m2l_src = nullptr;     // [C][216]
     int *p2p_own = nullptr, *p2p_cnt = nullptr;  // [C][27], [C]
+    void *smom = nullptr;       // accurate mode: [C] moment records (soften.cu)
+    void *smom_oct = nullptr;   // [C][8] octant moment records of the leaves
+    void *staylor = nullptr;    // [C][12] leaf-centre value and J of the far levels' correction
+    unsigned soft_cap = 0;      // cells the three are sized for (0: not allocated)
+    bool soft_mixed = false;    // their element type
     int *coll = nullptr, *coll_cnt = nullptr;    // [C][27], [C]
     unsigned *flag = nullptr, *flag_off = nullptr;  // [C+1]
 
@@ -157,6 +163,8 @@ size_t m2l_tc_image_floats(int p);
 int m2l_tc_row_floats(int p);
 const char *m2l_tc_encode(Workspace &ws);     // (re)build tmap_ms; nullptr or an error message
 void downward_pass(Workspace &ws);            // L2L + L2P into far
+void soften_pass(Workspace &ws);              // accurate mode: far = G (far + softening correction)
+size_t soften_cell_bytes(bool mixed);         // bytes of one moment record
 void p2p_pass(Workspace &ws, unsigned per_sm); // near-field kernel over the queue, per_sm blocks per SM
 void p2p_finish(Workspace &ws);               // add the slices of split items: near complete
 unsigned p2p_blocks_per_sm(bool concurrent);   // P2P blocks per SM alone / beside the far field

@@ -21,8 +21,9 @@
 //
 // Template parameters are the reference's six types. Arithmetic on the GPU is
 // FP64 (GB_PREC_FP64) by default, or the mixed pipeline (GB_PREC_MIXED) via
-// the seventh parameter; positions and velocities cross the boundary as
-// doubles whatever X and V are.
+// the seventh parameter; the eighth selects the method (GB_MODE_REF, the
+// reference's, by default; GB_MODE_ACCURATE adds the softened far field).
+// Positions and velocities cross the boundary as doubles whatever X and V are.
 #ifndef GRAVITY_SOLVER_GB300_HPP
 #define GRAVITY_SOLVER_GB300_HPP
 
@@ -35,7 +36,7 @@
 
 namespace gravity {
 
-template <class M, class T, class X, class V, class A, class G, int Precision = GB_PREC_FP64>
+template <class M, class T, class X, class V, class A, class G, int Precision = GB_PREC_FP64, int Mode = GB_MODE_REF>
 struct SolverGB300 final {
     SolverGB300() = default;
     explicit SolverGB300(int device) : device_(device) {}
@@ -93,6 +94,7 @@ struct SolverGB300 final {
         c.precision = Precision;
         c.device = device_;
         c.flags = 0;
+        c.mode = Mode;
         if (!ctx_) {
             gb_ctx *h = nullptr;
             const int rc = gb_create(&c, &h);

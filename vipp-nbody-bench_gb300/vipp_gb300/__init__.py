@@ -22,12 +22,13 @@ LIB_PATH = os.path.join(PKG_DIR, "lib", "libvipp_gb300.so")
 
 GB_OK, GB_ERR_INVALID, GB_ERR_NONFINITE, GB_ERR_DEPTH, GB_ERR_CUDA, GB_ERR_NO_DEVICE, GB_ERR_STATE, GB_ERR_CAPACITY = range(8)
 PREC = {"fp64": 0, "mixed": 1}
+MODE = {"ref": 0, "accurate": 1}
 FLAG_P2P_NEWTON = 1
 FLAG_M2L_CUDA_CORES = 2
 FLAG_SERIAL = 4
 FLAG_NO_GRAPH = 8
 FLAG_M2L_BF16 = 16
-TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4")
+TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4", "soften")
 
 # Every symbol include/vipp_gb300.h declares.
 EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_upload", "gb_download", "gb_rk4_step",
@@ -39,7 +40,8 @@ EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_uplo
 
 class GbConfig(ctypes.Structure):
     _fields_ = [("p", ctypes.c_int), ("s", ctypes.c_int), ("eps", ctypes.c_double), ("G", ctypes.c_double),
-                ("m", ctypes.c_double), ("precision", ctypes.c_int), ("device", ctypes.c_int), ("flags", ctypes.c_int)]
+                ("m", ctypes.c_double), ("precision", ctypes.c_int), ("device", ctypes.c_int), ("flags", ctypes.c_int),
+                ("mode", ctypes.c_int)]
 
 
 class GbConserved(ctypes.Structure):
@@ -124,9 +126,9 @@ class Solver:
     """One solver context on one GPU (see include/vipp_gb300.h)."""
 
     def __init__(self, p: int = 4, s: int = 10, eps: float = 0.01, G: float = 1.0, m: float = 1.0,
-                 precision: str = "fp64", device: int = 0, flags: int = 0):
+                 precision: str = "fp64", device: int = 0, flags: int = 0, mode: str = "ref"):
         self.lib = load()
-        self.cfg = GbConfig(p, s, eps, G, m, PREC[precision], device, flags)
+        self.cfg = GbConfig(p, s, eps, G, m, PREC[precision], device, flags, MODE[mode])
         h = ctypes.c_void_p()
         rc = self.lib.gb_create(ctypes.byref(self.cfg), ctypes.byref(h))
         if rc != GB_OK:
@@ -159,6 +161,8 @@ class Solver:
         for k, v in kw.items():
             if k == "precision":
                 v = PREC[v]
+            if k == "mode" and isinstance(v, str):
+                v = MODE[v]
             setattr(self.cfg, k, v)
         self._check(self.lib.gb_set_config(self.h, ctypes.byref(self.cfg)))
 
@@ -288,11 +292,12 @@ class Batch:
     sizes[k] particles of system k, concatenated in x and v; masses[k] is the
     particle mass of system k."""
 
-    def __init__(self, sizes, p=4, s=32, eps=0.01, G=1.0, masses=None, precision="mixed", device=0, flags=0):
+    def __init__(self, sizes, p=4, s=32, eps=0.01, G=1.0, masses=None, precision="mixed", device=0, flags=0,
+                 mode="ref"):
         self.lib = load()
         sizes = np.asarray(sizes, dtype=np.uint64)
         self.off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
-        self.cfg = GbConfig(p, s, eps, G, 1.0, PREC[precision], device, flags)
+        self.cfg = GbConfig(p, s, eps, G, 1.0, PREC[precision], device, flags, MODE[mode])
         m = None if masses is None else np.ascontiguousarray(masses, dtype=np.float64)
         h = ctypes.c_void_p()
         rc = self.lib.gb_batch_create(ctypes.byref(self.cfg), len(sizes), _ptr(self.off), _ptr(m), ctypes.byref(h))

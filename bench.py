@@ -13,6 +13,10 @@ step (four force evaluations, tree rebuilt at every stage).
   e2e     the same through the C-ABI with host buffers: per step, upload of
           x, v from pinned host memory, one RK4 step, download of x, v
   plain_fp64  the same step with every stage in FP64 (the plain form)
+  accurate  the accurate mode (far field times G plus the softening
+          correction) at p = 10: the mixed form and the plain FP64 form, both
+          timed over the same steps, with their errors against the FP64 direct
+          sum and mixed_over_plain
   m2l_other_split  the same step with the other M2L split (value, energy drift)
   batched  512 independent Plummer systems of uneven N (one batch step)
   cpu_baseline  the reference's algorithm on the host cores (oracle port, or
@@ -122,6 +126,72 @@ def batch_measure(steps=4, warmup=2, nsys=512, seed=3, sample=8, flags=0):
             "systems": nsys, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * dt_wall / steps,
             "setup_s": setup, "rms_rel_err_vs_fp64_direct_per_system": errs,
             "timing": "host wall clock per gb_batch_rk4_step (it returns after all systems' steps)"}
+
+
+def timed_steps(sol, steps, dt, local):
+    """Seconds of exactly `steps` RK4 steps by CUDA events on the solver's stream."""
+    import torch
+    st = torch.cuda.ExternalStream(sol.stream_ptr(), device=local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    sol.sync()
+    e0.record(st)
+    for _ in range(steps):
+        sol.solve(dt)
+    e1.record(st)
+    e1.synchronize()
+    sol.sync()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def accurate_measure(x, v, args, local, tg, ad):
+    """The accurate mode (GB_MODE_ACCURATE: far field times G plus the
+    softening correction) on the same workload at p = args.acc_p: the mixed
+    form (3 x TF32 M2L split unless --acc-m2l bf16) and the plain all-FP64
+    form, both timed by CUDA events over the same args.acc_steps steps after
+    one untimed step, both checked against the FP64 direct sum on the same
+    sample (tg, ad)."""
+    import vipp_gb300
+    n = x.shape[0]
+    m = 1.0 / n
+    out = {"p": args.acc_p, "mode": "accurate", "steps": args.acc_steps}
+    forms = (("mixed", vipp_gb300.FLAG_M2L_BF16 if args.acc_m2l == "bf16" else 0), ("fp64", 0))
+    for prec, flags in forms:
+        with vipp_gb300.Solver(p=args.acc_p, s=args.s, eps=args.eps, G=1.0, m=m, precision=prec, device=local,
+                               flags=flags, mode="accurate") as sa:
+            sa.preprocess(x, v)
+            a = sa.accel()
+            e = np.linalg.norm(a[tg] - ad, axis=1) / np.linalg.norm(ad, axis=1)
+            sa.solve(args.dt)  # captures the step graph
+            c0 = sa.conserved() if (prec == "mixed" and not args.no_energy) else None
+            t = timed_steps(sa, args.acc_steps, args.dt, local)
+            drift = None
+            if c0 is not None:
+                c1 = sa.conserved()
+                drift = abs(c1["total"] - c0["total"]) / abs(c0["total"])
+            kt = None
+            if prec == "mixed":
+                sa.enable_timing(True)
+                sa.kernel_times()
+                sa.solve(args.dt)
+                sa.sync()
+                kt = {k: round(val[0], 4) for k, val in sa.kernel_times().items()}
+                sa.enable_timing(False)
+        out[prec] = {"value": n * args.acc_steps / t, "unit": UNIT, "ms_per_step": 1e3 * t / args.acc_steps,
+                     "rms_rel_err_vs_fp64_direct": float(math.sqrt(np.mean(e * e))),
+                     "max_rel_err_vs_fp64_direct": float(e.max()), "error_sample": int(len(tg)),
+                     "m2l_split": ("bf16 hi/lo" if flags else "3 x tf32") if prec == "mixed" else "fp64 cuda cores",
+                     "timing": f"CUDA events around {args.acc_steps} steps on the solver's stream"}
+        if drift is not None:
+            out[prec]["energy_rel_drift"] = drift
+            out[prec]["energy_note"] = ("potential of the reference's far field (unsoftened expansion) times G "
+                                        "plus the FP64 softened near field")
+        if kt:
+            out[prec]["kernel_ms_per_step"] = kt
+    out["mixed_over_plain"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["both_within_1e-5"] = bool(out["mixed"]["rms_rel_err_vs_fp64_direct"] <= 1e-5
+                                   and out["fp64"]["rms_rel_err_vs_fp64_direct"] <= 1e-5)
+    return out
 
 
 class ClockSampler:
@@ -289,6 +359,10 @@ def parse_args(argv=None):
                     help="mixed form's tensor-core M2L split: bf16 hi/lo (the 4M Plummer and batching configurations' "
                          "form, GB_FLAG_M2L_BF16) or 3 x tf32 (the library default)")
     ap.add_argument("--no-alt", action="store_true", help="skip the timing of the other M2L split")
+    ap.add_argument("--no-accurate", action="store_true", help="skip the accurate-mode line (mixed and plain FP64)")
+    ap.add_argument("--acc-p", type=int, default=10, help="expansion order of the accurate-mode line")
+    ap.add_argument("--acc-steps", type=int, default=3, help="timed steps of each accurate-mode form")
+    ap.add_argument("--acc-m2l", default="tf32", choices=["bf16", "tf32"], help="M2L split of the mixed accurate form")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     wdef = {"plummer": (1 << 22, 0.005, 5e-4, 8), "clustered": (1 << 24, 1e-4, 1e-4, 8),
@@ -407,18 +481,16 @@ def main():
     # --- plain FP64 form of the same method --------------------------------------
     plain = None
     if rank == 0 and not args.no_plain and args.precision == "mixed":
+        plain_steps = 2
         with vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, m=m, precision="fp64", device=local) as sp:
             sp.preprocess(x, v)
-            sp.solve(args.dt)
-            sp.sync()
-            t0 = time.perf_counter()
-            sp.solve(args.dt)
-            sp.sync()
-            tp = time.perf_counter() - t0
+            sp.solve(args.dt)  # captures the step graph
+            tp = timed_steps(sp, plain_steps, args.dt, local) / plain_steps
             sp.preprocess(x, v)
             ap64 = sp.accel()
             e = np.linalg.norm(ap64[tg] - ad, axis=1) / np.linalg.norm(ad, axis=1) if acc_info else None
-        plain = {"value": n / tp, "unit": UNIT, "steps": 1, "ms_per_step": 1e3 * tp,
+        plain = {"value": n / tp, "unit": UNIT, "steps": plain_steps, "ms_per_step": 1e3 * tp,
+                 "timing": f"CUDA events around {plain_steps} steps on the solver's stream",
                  "rms_rel_err_vs_fp64_direct": float(math.sqrt(np.mean(e * e))) if e is not None else None,
                  "max_rel_err_vs_fp64_direct": float(e.max()) if e is not None else None,
                  "mixed_over_plain": value / ws / (n / tp)}
@@ -527,6 +599,10 @@ def main():
         alt = {"m2l_split": "bf16 hi/lo" if aflags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32", "value": n * args.steps / ta,
                "unit": UNIT, "steps": args.steps, "ms_per_step": 1e3 * ta / args.steps, "energy_rel_drift": drift}
 
+    accurate = None
+    if rank == 0 and not args.no_accurate and args.precision == "mixed" and acc_info:
+        accurate = accurate_measure(x, v, args, local, tg, ad)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline_sample(x, args.s, args.p, args.eps)
@@ -544,7 +620,8 @@ def main():
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
             "config": cfg, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
-            "roofline_kernels": per, "plain_fp64": plain, "batched": batched, "m2l_other_split": alt, "cpu_baseline": cpu}
+            "roofline_kernels": per, "plain_fp64": plain, "accurate": accurate, "batched": batched, "m2l_other_split": alt,
+            "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

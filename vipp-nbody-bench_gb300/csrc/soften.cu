@@ -35,6 +35,8 @@
 // neighbourhood size. F, F', F'' are differences of (u + e)^{-k/2} and u^{-k/2};
 // their FP32 rounding is ~1e-7 / (eps^2/u) relative, at most ~1e-3 of a
 // correction that is itself ~eps^2/u of the source's field.
+#include <climits>
+
 #include "workspace.cuh"
 
 namespace gb {
@@ -342,19 +344,76 @@ __global__ void __launch_bounds__(128) k_soft_far(const int *__restrict__ leaves
 }
 
 // -------------------------------------------- near levels (k = 0, 1) + apply
-// One warp per leaf at level >= 2, lanes over its particles: the per-particle
-// correction of the leaf's and its parent's M2L lists, plus the leaf-centre
-// Taylor part, then far = G (far + correction).
+// One warp per leaf at level >= 2. The warp first lists the moment records of
+// its sources (the leaf's M2L slots, face-slab sources as their 8 octant
+// records, then the parent's slots) in shared memory, then streams them in
+// batches of 32: each lane stages one record as its offset from the leaf
+// centre plus M, tr Q and Q (the next batch's records are loaded while the
+// current one is computed), and every lane applies the staged batch to up to
+// kTPL of the leaf's particles (targets lane, lane + 32, ...). Last, the
+// leaf-centre Taylor part is added and far = G (far + correction).
+constexpr int kSoftWarps = 4;
+constexpr int kSoftTPL = 4;                     // targets per lane per pass
+constexpr int kSoftMaxSrc = 54 * 8 + 135 + 189;  // 756 records at most
+
 template <typename T>
-__global__ void __launch_bounds__(128) k_soft_near(const int *__restrict__ leaves, const unsigned *counts,
-                                                   const int *__restrict__ c_begin, const int *__restrict__ c_end,
-                                                   const int *__restrict__ c_level, const int *__restrict__ c_parent,
-                                                   const int *__restrict__ c_child, const double *__restrict__ c_ctr,
-                                                   const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
-                                                   const Mom<T> *__restrict__ mom, const Mom<T> *__restrict__ moct,
-                                                   const T *__restrict__ taylor, const double *__restrict__ xs,
-                                                   const float4 *__restrict__ ph, const float4 *__restrict__ pl,
-                                                   unsigned n, T e2, T G, T *__restrict__ far) {
+struct SRec {  // staged record: offset from the target leaf centre, M, tr Q, Q
+    T dx, dy, dz, M, tr, q0, q1, q2, q3, q4, q5, pad;
+};
+
+template <typename T>
+__device__ __forceinline__ void stage(const Mom<T> *__restrict__ mom, const Mom<T> *__restrict__ moct, int code,
+                                      const RelC<T> &cc, SRec<T> &r) {
+    if (code == INT_MIN) {  // padding entry: far away, no mass
+        r.dx = T(1e10), r.dy = T(0), r.dz = T(0), r.M = T(0), r.tr = T(0);
+        r.q0 = r.q1 = r.q2 = r.q3 = r.q4 = r.q5 = T(0);
+        return;
+    }
+    const Mom<T> &m = code >= 0 ? mom[code] : moct[~code];
+    if (m.M == T(0)) {
+        r.dx = T(1e10), r.dy = T(0), r.dz = T(0), r.M = T(0), r.tr = T(0);
+        r.q0 = r.q1 = r.q2 = r.q3 = r.q4 = r.q5 = T(0);
+        return;
+    }
+    T d[3];
+    src_offset<T>(m, cc, d);
+    r.dx = d[0], r.dy = d[1], r.dz = d[2], r.M = m.M, r.tr = m.tr;
+    r.q0 = m.Q[0], r.q1 = m.Q[1], r.q2 = m.Q[2], r.q3 = m.Q[3], r.q4 = m.Q[4], r.q5 = m.Q[5];
+}
+
+template <typename T>
+__device__ __forceinline__ void soft_term_s(const SRec<T> &r, T tx, T ty, T tz, T e2, T &ax, T &ay, T &az) {
+    const T dx = r.dx - tx, dy = r.dy - ty, dz = r.dz - tz;
+    const T u = dx * dx + dy * dy + dz * dz;
+    const T A = rsqrt_t<T>(u + e2), B = rsqrt_t<T>(u);
+    const T A2 = A * A, B2 = B * B;
+    const T A3 = A2 * A, B3 = B2 * B;
+    const T A5 = A3 * A2, B5 = B3 * B2;
+    const T A7 = A5 * A2, B7 = B5 * B2;
+    const T F = A3 - B3;
+    const T F1 = T(-1.5) * (A5 - B5);
+    const T F2 = T(3.75) * (A7 - B7);
+    const T qx = r.q0 * dx + r.q3 * dy + r.q4 * dz;
+    const T qy = r.q3 * dx + r.q1 * dy + r.q5 * dz;
+    const T qz = r.q4 * dx + r.q5 * dy + r.q2 * dz;
+    const T dqd = dx * qx + dy * qy + dz * qz;
+    const T a = r.M * F + F1 * r.tr + T(2) * F2 * dqd;
+    const T b = T(2) * F1;
+    ax += a * dx + b * qx;
+    ay += a * dy + b * qy;
+    az += a * dz + b * qz;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSoftWarps * 32) k_soft_near(
+    const int *__restrict__ leaves, const unsigned *counts, const int *__restrict__ c_begin, const int *__restrict__ c_end,
+    const int *__restrict__ c_level, const int *__restrict__ c_parent, const int *__restrict__ c_child,
+    const double *__restrict__ c_ctr, const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
+    const Mom<T> *__restrict__ mom, const Mom<T> *__restrict__ moct, const T *__restrict__ taylor,
+    const double *__restrict__ xs, const float4 *__restrict__ ph, const float4 *__restrict__ pl, unsigned n, T e2, T G,
+    T *__restrict__ far) {
+    __shared__ int list[kSoftWarps][kSoftMaxSrc + 32];
+    __shared__ SRec<T> batch[kSoftWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned NL = counts[3];
     const unsigned warps = gridDim.x * (blockDim.x >> 5);
@@ -365,64 +424,90 @@ __global__ void __launch_bounds__(128) k_soft_near(const int *__restrict__ leave
         const double cd[3] = {c_ctr[3 * c], c_ctr[3 * c + 1], c_ctr[3 * c + 2]};
         const int P = c_parent[c];
         const int oc = c - c_child[P];
-        const int uc[3] = {1 - (oc & 1), 1 - ((oc >> 1) & 1), 1 - ((oc >> 2) & 1)};
-        const int P2 = c_level[P] >= 2 ? P : -1;
+        // ---- the source list: codes >= 0 index mom, ~k indexes moct
+        int nsrc = 0;
+        for (int lev = 0; lev < 2; ++lev) {
+            const int tc = lev == 0 ? c : (c_level[P] >= 2 ? P : -1);
+            if (tc < 0) break;
+            for (int s0 = 0; s0 < kM2LSlots; s0 += 32) {
+                const int s = s0 + lane;
+                const int src = s < kM2LSlots ? m2l_src[static_cast<size_t>(tc) * kM2LSlots + s] : -1;
+                bool slab = false;
+                if (lev == 0 && src >= 0) {
+                    const int dd = s >> 3, o = s & 7;
+                    const int d[3] = {dd % 3 - 1, (dd / 3) % 3 - 1, dd / 9 - 1};
+                    int twos = 0, big = 0;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const int off = 2 * d[a] + (1 - ((o >> a) & 1)) - (1 - ((oc >> a) & 1));
+                        twos += (off == 2 || off == -2);
+                        big += (off > 2 || off < -2);
+                    }
+                    slab = twos == 1 && big == 0;
+                }
+                const int cnt = src < 0 ? 0 : (slab ? 8 : 1);
+                int incl = cnt;  // inclusive warp scan
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                const int at = nsrc + incl - cnt;
+                if (cnt == 1) {
+                    list[w][at] = src;
+                } else if (cnt == 8) {
+                    const int ch = c_child[src];
+                    for (int o = 0; o < 8; ++o) list[w][at + o] = ch >= 0 ? ch + o : ~(src * 8 + o);
+                }
+                nsrc += __shfl_sync(0xffffffffu, incl, 31);
+            }
+        }
+        if (lane < 32) list[w][nsrc + lane] = INT_MIN;  // pad the last batch
+        __syncwarp();
         T tl[12];
 #pragma unroll
         for (int k = 0; k < 12; ++k) tl[k] = taylor[static_cast<size_t>(c) * 12 + k];
         const int b = c_begin[c], e = c_end[c];
-        for (int j0 = b; j0 < e; j0 += 32) {
-            const int j = j0 + lane;
-            T y[3] = {T(0), T(0), T(0)};
-            if (j < e) rel_pos<T>(j, xs, n, ph, pl, cd, cc, y);
-            T ax = T(0), ay = T(0), az = T(0);
-            for (int lev = 0; lev < 2; ++lev) {
-                const int tc = lev == 0 ? c : P2;
-                if (tc < 0) break;
-                for (int s = 0; s < kM2LSlots; ++s) {
-                    const int src = m2l_src[static_cast<size_t>(tc) * kM2LSlots + s];
-                    if (src < 0) continue;  // warp-uniform from here on
-                    bool slab = false;
-                    if (lev == 0) {
-                        const int dd = s >> 3, o = s & 7;
-                        const int d[3] = {dd % 3 - 1, (dd / 3) % 3 - 1, dd / 9 - 1};
-                        int twos = 0, big = 0;
+        for (int j0 = b; j0 < e; j0 += 32 * kSoftTPL) {
+            const int nq = min(kSoftTPL, (e - j0 + 31) / 32);  // warp-uniform
+            T ty[kSoftTPL][3], acc[kSoftTPL][3];
 #pragma unroll
-                        for (int a = 0; a < 3; ++a) {
-                            const int off = 2 * d[a] + (1 - ((o >> a) & 1)) - uc[a];
-                            twos += (off == 2 || off == -2);
-                            big += (off > 2 || off < -2);
-                        }
-                        slab = twos == 1 && big == 0;
-                    }
-                    if (!slab) {
-                        const Mom<T> r = mom[src];
-                        if (r.M == T(0)) continue;
-                        T sd[3];
-                        src_offset<T>(r, cc, sd);
-                        soft_term<T>(r, sd[0] - y[0], sd[1] - y[1], sd[2] - y[2], e2, ax, ay, az);
-                    } else {
-                        const int ch = c_child[src];
-                        const Mom<T> *base = ch >= 0 ? mom + ch : moct + static_cast<size_t>(src) * 8;
-                        for (int o = 0; o < 8; ++o) {
-                            const Mom<T> r = base[o];
-                            if (r.M == T(0)) continue;
-                            T sd[3];
-                            src_offset<T>(r, cc, sd);
-                            soft_term<T>(r, sd[0] - y[0], sd[1] - y[1], sd[2] - y[2], e2, ax, ay, az);
-                        }
-                    }
+            for (int q = 0; q < kSoftTPL; ++q) {
+                ty[q][0] = ty[q][1] = ty[q][2] = T(0);
+                acc[q][0] = acc[q][1] = acc[q][2] = T(0);
+                const int j = j0 + 32 * q + lane;
+                if (q < nq && j < e) rel_pos<T>(j, xs, n, ph, pl, cd, cc, ty[q]);
+            }
+            SRec<T> nxt;
+            if (nsrc > 0) stage<T>(mom, moct, list[w][lane], cc, nxt);
+            for (int b0 = 0; b0 < nsrc; b0 += 32) {
+                batch[w][lane] = nxt;
+                __syncwarp();
+                if (b0 + 32 < nsrc) stage<T>(mom, moct, list[w][b0 + 32 + lane], cc, nxt);
+                const int nb = min(32, nsrc - b0);
+                for (int k = 0; k < nb; ++k) {
+                    const SRec<T> r = batch[w][k];
+#pragma unroll
+                    for (int q = 0; q < kSoftTPL; ++q)
+                        if (q < nq) soft_term_s<T>(r, ty[q][0], ty[q][1], ty[q][2], e2, acc[q][0], acc[q][1], acc[q][2]);
+                }
+                __syncwarp();
+            }
+#pragma unroll
+            for (int q = 0; q < kSoftTPL; ++q) {
+                const int j = j0 + 32 * q + lane;
+                if (q < nq && j < e) {
+                    const T *y = ty[q];
+                    const T ax = acc[q][0] + tl[0] + tl[3] * y[0] + tl[4] * y[1] + tl[5] * y[2];
+                    const T ay = acc[q][1] + tl[1] + tl[6] * y[0] + tl[7] * y[1] + tl[8] * y[2];
+                    const T az = acc[q][2] + tl[2] + tl[9] * y[0] + tl[10] * y[1] + tl[11] * y[2];
+                    far[j] = G * (far[j] + ax);
+                    far[n + j] = G * (far[n + j] + ay);
+                    far[2 * static_cast<size_t>(n) + j] = G * (far[2 * static_cast<size_t>(n) + j] + az);
                 }
             }
-            if (j < e) {
-                ax += tl[0] + tl[3] * y[0] + tl[4] * y[1] + tl[5] * y[2];
-                ay += tl[1] + tl[6] * y[0] + tl[7] * y[1] + tl[8] * y[2];
-                az += tl[2] + tl[9] * y[0] + tl[10] * y[1] + tl[11] * y[2];
-                far[j] = G * (far[j] + ax);
-                far[n + j] = G * (far[n + j] + ay);
-                far[2 * static_cast<size_t>(n) + j] = G * (far[2 * static_cast<size_t>(n) + j] + az);
-            }
         }
+        __syncwarp();
     }
 }
 
@@ -443,7 +528,7 @@ void launch_soften(Workspace &ws) {
     }
     k_soft_far<T><<<gw, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_level, ws.c_parent, ws.c_ctr, ws.info, ws.m2l_src,
                                          mom, e2, taylor);
-    k_soft_near<T><<<gw, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_parent,
+    k_soft_near<T><<<gw, kSoftWarps * 32, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_parent,
                                           ws.c_child, ws.c_ctr, ws.info, ws.m2l_src, mom, moct, taylor, ws.xs, ws.ph,
                                           ws.pl, ws.n, e2, static_cast<T>(ws.G), static_cast<T *>(ws.farf));
     ws.launches += 2;

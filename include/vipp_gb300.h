@@ -175,8 +175,9 @@ GB_API int gb_rk4_step(gb_ctx *ctx, double dt);
  * doubles). phi may be NULL; when given it receives n potentials per unit mass
  * in the accelerations' convention a = -grad phi: the softened near-field sum
  * -G m sum_{j != i} (r^2 + eps^2)^-1/2 (FP64) plus the far field from the local
- * expansions, which like the reference's far field carries no G. The reference
- * has no potential; this output has no counterpart there. */
+ * expansions, which like the reference's far field carries no G (times G in
+ * GB_MODE_ACCURATE, without the softening correction the accelerations get).
+ * The reference has no potential; this output has no counterpart there. */
 GB_API int gb_accel(gb_ctx *ctx, double *a_aos, double *phi);
 
 /* Conserved quantities of the current state, for energy-drift checks (no

@@ -19,10 +19,10 @@ constexpr int kRBlocks = 256;  // reduction blocks (fixed: the sums are determin
 constexpr int kSums = 8;
 
 __global__ void k_phi_finalize(const unsigned *__restrict__ perm, unsigned n, const double *__restrict__ phis,
-                               double *__restrict__ phi_orig) {
+                               double gfar, double *__restrict__ phi_orig) {
     const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    phi_orig[perm[j]] = -(phis[j] + phis[static_cast<size_t>(n) + j]);
+    phi_orig[perm[j]] = -(phis[j] + gfar * phis[static_cast<size_t>(n) + j]);
 }
 
 // Per block: sum |v|^2, sum phi, sum v (3), sum x cross v (3) over a fixed
@@ -68,7 +68,8 @@ size_t diag_scratch_doubles() { return kSums * kRBlocks + kSums; }
 void potential_orig(Workspace &ws, double *phi_orig) {
     far_potential(ws, ws.phis + ws.n);
     near_potential(ws, ws.phis);
-    k_phi_finalize<<<(ws.n + 255) / 256, 256, 0, ws.st>>>(ws.perm, ws.n, ws.phis, phi_orig);
+    // the far part carries G only in the accurate mode (the reference's far field has none)
+    k_phi_finalize<<<(ws.n + 255) / 256, 256, 0, ws.st>>>(ws.perm, ws.n, ws.phis, ws.accurate ? ws.G : 1.0, phi_orig);
     ws.launches += 1;
 }
 

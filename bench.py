@@ -296,7 +296,7 @@ def cpu_baseline_sample(x, s, p, eps, target_seconds=12.0):
                        f"({times[0]:.2f} s) and upward pass ({times[1]:.2f} s), far/near work of every "
                        f"{stride}th cell ({int(counts[1])} cells, {times[2]:.2f} s) scaled by M2L pairs "
                        f"{int(counts[2])}/{int(counts[3])}; x4 evaluations per RK4 step"),
-            "seconds_per_step_extrapolated": step}
+            "seconds_per_step_extrapolated": step, "extrapolated": True, "samples": 1}
 
 
 def run_reference_arm(args):
@@ -316,13 +316,16 @@ def run_reference_arm(args):
         if time.time() - t_start > 150:
             break
     value = float(np.median(vals))
-    cfg = {"workload": f"{wname} p={args.p} s={args.s} eps={args.eps} (reference algorithm, CPU)",
+    cfg = {"workload": f"{wname} p={args.p} s={args.s} eps={args.eps} {args.precision}",
            "N": args.n, "p": args.p, "s": args.s, "eps": args.eps, "dt": args.dt}
+    # "steps" counts timed samples: each is one extrapolated RK4 step (4 x one
+    # sampled force evaluation), not a run of consecutive steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": len(vals),
+            "samples": len(vals), "extrapolated": True,
             "warmup": args.warmup, "ms_per_step": 1e3 * args.n / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg, "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
-                             "sample": r["sample"]},
+                             "sample": r["sample"], "extrapolated": True, "samples": len(vals)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     del oracle
     print(json.dumps(line), flush=True)
@@ -360,6 +363,8 @@ def parse_args(argv=None):
                          "form, GB_FLAG_M2L_BF16) or 3 x tf32 (the library default)")
     ap.add_argument("--no-alt", action="store_true", help="skip the timing of the other M2L split")
     ap.add_argument("--no-accurate", action="store_true", help="skip the accurate-mode line (mixed and plain FP64)")
+    ap.add_argument("--drift-steps", type=int, default=None,
+                    help="untimed steps of the total-energy drift run (default: the 4M Plummer configuration's 100; 0 skips)")
     ap.add_argument("--acc-p", type=int, default=10, help="expansion order of the accurate-mode line")
     ap.add_argument("--acc-steps", type=int, default=3, help="timed steps of each accurate-mode form")
     ap.add_argument("--acc-m2l", default="tf32", choices=["bf16", "tf32"], help="M2L split of the mixed accurate form")
@@ -371,6 +376,8 @@ def parse_args(argv=None):
     args.eps = wdef[1] if args.eps is None else args.eps
     args.dt = wdef[2] if args.dt is None else args.dt
     args.p = wdef[3] if args.p is None else args.p
+    if args.drift_steps is None:
+        args.drift_steps = 100 if args.workload == "plummer" else 0
     return args
 
 
@@ -599,6 +606,23 @@ def main():
         alt = {"m2l_split": "bf16 hi/lo" if aflags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32", "value": n * args.steps / ta,
                "unit": UNIT, "steps": args.steps, "ms_per_step": 1e3 * ta / args.steps, "energy_rel_drift": drift}
 
+    drift = None
+    if rank == 0 and args.drift_steps > 0 and args.precision == "mixed":
+        # total-energy drift over the configuration's full run (untimed)
+        with vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision="mixed", device=local,
+                               flags=args.flags) as sd:
+            sd.preprocess(x, v)
+            c0 = sd.conserved()
+            t0 = time.perf_counter()
+            for _ in range(args.drift_steps):
+                sd.solve(args.dt)
+            sd.sync()
+            tdr = time.perf_counter() - t0
+            c1 = sd.conserved()
+        drift = {"steps": args.drift_steps, "dt": args.dt, "e_before": c0["total"], "e_after": c1["total"],
+                 "rel_drift": abs(c1["total"] - c0["total"]) / abs(c0["total"]), "wall_s": tdr,
+                 "m2l_split": "bf16 hi/lo" if args.flags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32"}
+
     accurate = None
     if rank == 0 and not args.no_accurate and args.precision == "mixed" and acc_info:
         accurate = accurate_measure(x, v, args, local, tg, ad)
@@ -620,7 +644,8 @@ def main():
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
             "config": cfg, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
-            "roofline_kernels": per, "plain_fp64": plain, "accurate": accurate, "batched": batched, "m2l_other_split": alt,
+            "roofline_kernels": per, "plain_fp64": plain, "accurate": accurate, "energy_drift_run": drift,
+            "batched": batched, "m2l_other_split": alt,
             "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -214,10 +214,14 @@ GB_API int gb_direct_accel(gb_ctx *ctx, const int64_t *targets, size_t ntargets,
  * queued: results are ready once `stream` reaches this point. Its scratch
  * is one fixed 16 MiB device array inside the library, reserved on every
  * GPU that loads it until the process exits; at most 699,050 targets fit
- * (GB_ERR_CAPACITY beyond that). The first call on a device looks up that
- * array's address and should come before any stream capture. All calls share
- * the array, so calls that overlap on the GPU (other streams, other host
- * threads) race; order them on one stream. */
+ * (GB_ERR_CAPACITY beyond that). The first call on a device (and the first
+ * after cudaDeviceReset gave it a new context) looks up that array's address
+ * and should come before any stream capture. All calls share the array, so
+ * calls that overlap on the GPU (other streams, other host threads) race;
+ * order them on one stream. No targets (ntargets == 0 with a list, or n == 0
+ * without one) is a no-op; a target list with n == 0 is GB_ERR_INVALID. A
+ * CUDA error already pending on the calling thread when the call starts is
+ * left pending and the call returns GB_ERR_CUDA without queueing anything. */
 GB_API int gb_direct_accel_noalloc(const double *x_dev, size_t n, const int64_t *targets_dev, size_t ntargets, double G,
                                    double m, double eps, double *a_dev, void *stream);
 

@@ -19,4 +19,6 @@ ${CXX:-g++} -std=c++17 -O2 -fPIC -shared -fopenmp -ffp-contract=off \
   -include chrono -include functional -include algorithm -include iterator -include limits \
   -include variant -include stdexcept \
   -I"$REF/gravity/include" "$HERE/ref_shim.cpp" -o "$HERE/_ref/libvipp_ref.so"
+# where the sources were read, for the tests that compile against the reference's headers
+echo "$REF" > "$HERE/_ref/REFERENCE_DIR"
 echo "built $HERE/_ref/libvipp_ref.so"

@@ -62,6 +62,38 @@ def test_noalloc_direct_sum_matches_context_entry_point():
     assert free_after[1] == free_after[0]  # the second call allocated nothing
 
 
+def test_noalloc_all_particles_and_out_of_range_targets():
+    """targets_dev = NULL computes every particle (against the oracle's sum
+    over all particles); indices outside [0, n) give NaN rows, the valid ones
+    their sums; a target list with n == 0 is rejected."""
+    import torch
+
+    import vipp_gb300
+
+    lib = vipp_gb300.load()
+    n, eps, G = 3000, 0.01, 1.0
+    m = 1.0 / n
+    x, _ = O.plummer_reference(n, eps, 12)
+    dev = torch.device("cuda", 0)
+    x_dev = torch.from_numpy(x).to(dev)
+    a_dev = torch.full((n, 3), float("nan"), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize(dev)
+    assert lib.gb_direct_accel_noalloc(x_dev.data_ptr(), n, None, 0, G, m, eps, a_dev.data_ptr(), None) == 0
+    torch.cuda.synchronize(dev)
+    assert np.max(rel(a_dev.cpu().numpy(), O.direct_accel(x, G, m, eps))) <= TOL
+    t = np.array([-1, n, 5], dtype=np.int64)
+    t_dev = torch.from_numpy(t).to(dev)
+    b_dev = torch.zeros((3, 3), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize(dev)
+    assert lib.gb_direct_accel_noalloc(x_dev.data_ptr(), n, t_dev.data_ptr(), 3, G, m, eps, b_dev.data_ptr(), None) == 0
+    torch.cuda.synchronize(dev)
+    b = b_dev.cpu().numpy()
+    assert np.all(np.isnan(b[0])) and np.all(np.isnan(b[1]))
+    assert np.max(rel(b[2:], O.direct_accel(x, G, m, eps, np.array([5])))) <= TOL
+    rc = lib.gb_direct_accel_noalloc(x_dev.data_ptr(), 0, t_dev.data_ptr(), 3, G, m, eps, b_dev.data_ptr(), None)
+    assert rc == vipp_gb300.GB_ERR_INVALID
+
+
 def test_noalloc_rejects_more_targets_than_its_scratch_holds():
     import torch
 

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <functional>
@@ -109,6 +110,11 @@ void apply_config(gb_ctx *ctx) {
     ws.m2l_bf16 = (ctx->cfg.flags & GB_FLAG_M2L_BF16) != 0;
     ws.serial = (ctx->cfg.flags & GB_FLAG_SERIAL) != 0;
     ws.accurate = ctx->cfg.mode == GB_MODE_ACCURATE;
+    // Failure-detection tests make the radix sort's bounded look-back waits
+    // give up early (0: at the first poll) through this variable; the sort
+    // stays exact and the call reports the timeout.
+    const char *polls = std::getenv("VIPP_GB_SORT_WAIT_POLLS");
+    ws.sort_spin_max = polls && *polls ? static_cast<unsigned>(std::strtoul(polls, nullptr, 10)) : gb::kSortSpinMax;
 }
 
 // P2P work items: at most two partial chunks per leaf plus n/32 full ones,
@@ -333,7 +339,8 @@ int check_device_errors(gb_ctx *ctx, unsigned *need) {
         return GB_ERR_DEPTH;
     }
     if (err & gb::kDevTimeout) {
-        ctx->err = "a pipelined kernel timed out waiting on its barriers";
+        ctx->err = "a bounded device wait gave up (radix-sort look-back or tensor-core M2L barrier); this call's "
+                   "results are discarded";
         return GB_ERR_CUDA;
     }
     if (err & gb::kDevCapacity) {

@@ -16,7 +16,11 @@
 // names a host-side stand-in), so the first call on each device looks up the
 // real address with cudaGetSymbolAddress while that device is current, and
 // caches it; that first call should therefore be made before any stream
-// capture begins.
+// capture begins. The cache is keyed on the device's current CUDA context as
+// well: after cudaDeviceReset the device gets a new context with the module
+// loaded at a new address, and the next call looks the address up again.
+#include <cuda.h>
+
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
@@ -36,16 +40,38 @@ static __device__ __align__(256) double g_direct_scratch[kNoAllocScratchDoubles]
 struct DeviceSlot {
     double *scratch = nullptr;  // device address of g_direct_scratch on this device
     int num_sms = 0;
+    CUcontext ctx = nullptr;    // the context that address belongs to
 };
 DeviceSlot g_slots[kMaxDevices];
 std::mutex g_slots_mu;
 
-// Set-up, once per device, with that device current.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+
+// The calling thread's current CUDA context (the device's primary context once
+// the runtime has set it up), or nullptr when it cannot be read.
+CUcontext current_context() {
+    static CtxGetCurrentFn fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<CtxGetCurrentFn>(f);
+    }();
+    CUcontext c = nullptr;
+    if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
+
+// Set-up, once per device and context, with that device current.
 int device_slot(int dev, DeviceSlot &out) {
     if (dev < 0 || dev >= kMaxDevices) return GB_ERR_INVALID;
+    // null before the runtime has made a context current: then look up (which does that) and read it after
+    const CUcontext ctx = current_context();
     std::lock_guard<std::mutex> lock(g_slots_mu);
     DeviceSlot &s = g_slots[dev];
-    if (!s.scratch) {
+    if (!s.scratch || !ctx || s.ctx != ctx) {
+        s.scratch = nullptr;
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_direct_scratch) != cudaSuccess || !p) return GB_ERR_CUDA;
         int sms = 0;
@@ -53,6 +79,7 @@ int device_slot(int dev, DeviceSlot &out) {
             return GB_ERR_CUDA;
         s.num_sms = sms;
         s.scratch = static_cast<double *>(p);
+        s.ctx = ctx ? ctx : current_context();
     }
     out = s;
     return GB_OK;
@@ -67,11 +94,14 @@ extern "C" int gb_direct_accel_noalloc(const double *x_dev, size_t n, const int6
     if (n > 0x7fffffffu || ntargets > 0x7fffffffu) return GB_ERR_INVALID;
     if (!(eps >= 0) || !std::isfinite(eps) || !std::isfinite(G) || !std::isfinite(m)) return GB_ERR_INVALID;
     const size_t nt = targets_dev ? ntargets : n;
-    if (n == 0 || nt == 0) return GB_OK;
+    if (nt == 0) return GB_OK;
+    if (n == 0) return GB_ERR_INVALID;  // listed targets, but no particle they could index
     if (!x_dev || !a_dev) return GB_ERR_INVALID;
     if (3 * nt > kNoAllocScratchDoubles) return GB_ERR_CAPACITY;  // more than 699,050 targets
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return GB_ERR_NO_DEVICE;
+    // an error the caller left pending stays theirs: report it untouched
+    if (cudaPeekAtLastError() != cudaSuccess) return GB_ERR_CUDA;
     DeviceSlot slot;
     const int rc = device_slot(dev, slot);
     if (rc != GB_OK) return rc;

@@ -45,15 +45,18 @@ struct SortTemp {
     int max_tiles = 0;
 };
 
+constexpr unsigned kSortSpinMax = 1u << 24;  // look-back polls before a wait gives up
+
 // Stable sort of (key, val) pairs by bits [bit_lo, bit_hi) of the key.
 // Ping-pongs between (k0, v0) and (k1, v1); returns 0 if the result is in
 // (k0, v0), 1 if in (k1, v1). vals may be nullptr (keys only). A look-back
-// wait that gives up sets err_bit in *d_err (if d_err is not null).
+// wait that gives up after spin_max polls (at once for 0) sets err_bit in
+// *d_err (if d_err is not null) and counts the missing tile directly.
 // prezeroed: a kernel queued before the sort has run sort_temp_zero over
 // the sort's temporaries (saves two memset nodes per sort).
 int radix_sort_u64(uint64_t *k0, unsigned *v0, uint64_t *k1, unsigned *v1, unsigned n_cap, const unsigned *d_n,
                    int bit_lo, int bit_hi, SortTemp &tmp, cudaStream_t st, int64_t *launches, int *d_err = nullptr,
-                   int err_bit = 0, bool prezeroed = false);
+                   int err_bit = 0, bool prezeroed = false, unsigned spin_max = kSortSpinMax);
 
 // What a sort of n_cap keys over bits [bit_lo, bit_hi) needs zeroed: the
 // histogram and ticket words, and npasses x tiles x 256 look-back words.

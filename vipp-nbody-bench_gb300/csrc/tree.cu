@@ -771,7 +771,7 @@ void build_tree(Workspace &ws) {
                                              sort_zero_plan(ws.sort, n, kbit, 3 * kMaxLevel));
     ws.launches += 4;
     const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, kbit, 3 * kMaxLevel, ws.sort, st,
-                                   &ws.launches, &ws.info->err, kDevTimeout, true);
+                                   &ws.launches, &ws.info->err, kDevTimeout, true, ws.sort_spin_max);
     ws.keys = res ? ws.keys1 : ws.keys0;
     ws.perm = res ? ws.perm1 : ws.perm0;
     // split cells of every level
@@ -781,7 +781,7 @@ void build_tree(Workspace &ws) {
                                                    sort_zero_plan(ws.sort, ws.s_cap, 32, 40));
     ws.launches += 2;
     const int re = radix_sort_u64(ws.ent0, nullptr, ws.ent1, nullptr, ws.s_cap, ws.d_counts + 1, 32, 40, ws.sort, st,
-                                  &ws.launches, &ws.info->err, kDevTimeout, true);
+                                  &ws.launches, &ws.info->err, kDevTimeout, true, ws.sort_spin_max);
     ws.ent = re ? ws.ent1 : ws.ent0;
     k_level_table<<<1, 32, 0, st>>>(ws.ent, ws.d_counts, ws.info, n, ws.T, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child,
                                     ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr, ws.p2p_own, ws.p2p_cnt, ws.coll,

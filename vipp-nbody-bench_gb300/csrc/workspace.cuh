@@ -43,6 +43,7 @@ struct Workspace {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool serial = false;                // near field on st after the far field
     int sort_levels = 10;               // key levels the radix sort orders (grown on demand, up to 21)
+    unsigned sort_spin_max = kSortSpinMax;  // look-back polls before a wait gives up (tests lower it)
     int64_t launches = 0;
     int num_sms = 152;
 

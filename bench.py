@@ -363,6 +363,8 @@ def parse_args(argv=None):
                          "form, GB_FLAG_M2L_BF16) or 3 x tf32 (the library default)")
     ap.add_argument("--no-alt", action="store_true", help="skip the timing of the other M2L split")
     ap.add_argument("--no-accurate", action="store_true", help="skip the accurate-mode line (mixed and plain FP64)")
+    ap.add_argument("--tune", action="store_true", help="run the autotuner on the workload; report tuned vs default")
+    ap.add_argument("--tune-out", default=None, help="append the tuned entry to this tuning cache file")
     ap.add_argument("--drift-steps", type=int, default=None,
                     help="untimed steps of the total-energy drift run (default: the 4M Plummer configuration's 100; 0 skips)")
     ap.add_argument("--acc-p", type=int, default=10, help="expansion order of the accurate-mode line")
@@ -623,6 +625,27 @@ def main():
                  "rel_drift": abs(c1["total"] - c0["total"]) / abs(c0["total"]), "wall_s": tdr,
                  "m2l_split": "bf16 hi/lo" if args.flags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32"}
 
+    tuned = None
+    if rank == 0 and args.tune:
+        # the autotuner on this workload, then the tuned and the default
+        # settings timed alike (CUDA events over --steps steps each)
+        from vipp_gb300 import autotune
+        r = autotune.tune(x, v, p=args.p, s=args.s, eps=args.eps, m=m, precision=args.precision, flags=args.flags,
+                          dt=args.dt, steps=2, device=local)
+        res = {}
+        for label, tset in (("default", vipp_gb300.TUNING_DEFAULT), ("tuned", r["tuning"])):
+            with vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision=args.precision,
+                                   device=local, flags=args.flags) as st_:
+                st_.set_tuning(**tset)
+                st_.preprocess(x, v)
+                st_.solve(args.dt)
+                res[label] = n * args.steps / timed_steps(st_, args.steps, args.dt, local)
+        tuned = {"tuning": r["tuning"], "bucket": r["key"], "trials": r["trials"], "default_value": res["default"],
+                 "tuned_value": res["tuned"], "unit": UNIT, "speedup": res["tuned"] / res["default"]}
+        if args.tune_out:
+            entries = autotune.read_cache(args.tune_out) if os.path.exists(args.tune_out) else []
+            autotune.write_cache(args.tune_out, entries + [(r["key"], r["tuning"])])
+
     accurate = None
     if rank == 0 and not args.no_accurate and args.precision == "mixed" and acc_info:
         accurate = accurate_measure(x, v, args, local, tg, ad)
@@ -644,7 +667,7 @@ def main():
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
             "config": cfg, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
-            "roofline_kernels": per, "plain_fp64": plain, "accurate": accurate, "energy_drift_run": drift,
+            "roofline_kernels": per, "plain_fp64": plain, "accurate": accurate, "energy_drift_run": drift, "autotune": tuned,
             "batched": batched, "m2l_other_split": alt,
             "cpu_baseline": cpu}
     if rank == 0:

@@ -225,6 +225,34 @@ GB_API int gb_direct_accel(gb_ctx *ctx, const int64_t *targets, size_t ntargets,
 GB_API int gb_direct_accel_noalloc(const double *x_dev, size_t n, const int64_t *targets_dev, size_t ntargets, double G,
                                    double m, double eps, double *a_dev, void *stream);
 
+/* Launch and tree parameters a tuner may change (no counterpart in the
+ * reference). None changes the method: the launch shapes give bit-identical
+ * results, the slice length changes only the FP32 summation order of long
+ * near-field lists, and leaf_s applies to GB_MODE_ACCURATE alone (the
+ * reference mode keeps the reference's tree for the config's s).
+ * vipp_gb300/autotune.py measures candidates per size bucket and writes a
+ * cache file; gb_upload applies the cache entry named by the environment
+ * variable VIPP_GB_TUNE_FILE for the context's configuration and the uploaded
+ * particle count, where the file has one. */
+typedef struct gb_tuning {
+    int p2p_blocks;      /* P2P blocks per SM when the near field runs alone, 1..16 (default 8) */
+    int p2p_blocks_conc; /* P2P blocks per SM launched beside the far field, 0..16 (default 8) */
+    int p2p_slice;       /* near-field sources per P2P work item, 1024..65536 (default 8192) */
+    int m2l_ctas_pct;    /* tensor-core M2L CTAs, percent of the SMs, 10..100 (default 100) */
+    int serial;          /* 1: the near field after the far field on one stream (default 0) */
+    int leaf_s;          /* GB_MODE_ACCURATE: leaf parameter used instead of the config's s
+                            (0: the config's s) */
+} gb_tuning;
+GB_API int gb_set_tuning(gb_ctx *ctx, const gb_tuning *t);
+GB_API int gb_get_tuning(const gb_ctx *ctx, gb_tuning *out);
+/* The entry of a tuning cache file for cfg's p, precision, mode and M2L split
+ * (GB_FLAG_M2L_BF16) and n's size bucket floor(log2 n). The file holds one
+ * entry per line as key=value tokens (p, precision, mode, m2l_bf16, log2n,
+ * then the gb_tuning fields by name); '#' starts a comment. GB_OK with *out
+ * filled, GB_ERR_STATE when the file has no matching entry, GB_ERR_INVALID
+ * when it cannot be read or an entry is malformed. No GPU is needed. */
+GB_API int gb_tuning_lookup(const char *path, const gb_config *cfg, size_t n, gb_tuning *out);
+
 /* Block until all queued work finished; reports deferred device errors. */
 GB_API int gb_sync(gb_ctx *ctx);
 GB_API int gb_get_stats(gb_ctx *ctx, gb_stats *out);

@@ -48,6 +48,8 @@ struct gb_ctx {
     long long graph_steps = 0, direct_steps = 0, graph_captures = 0;
     std::vector<gb::PendingTimer> pending;
     std::vector<cudaEvent_t> free_events;
+    gb_tuning tune{8, 8, gb::kSliceSources, 100, 0, 0};
+    int tune_log2n = -1;  // size bucket the tuning cache was last applied for
     long long *d_targets = nullptr;
     size_t targets_cap = 0;
     double *d_direct = nullptr;
@@ -100,7 +102,8 @@ void apply_config(gb_ctx *ctx) {
     gb::Workspace &ws = ctx->ws;
     ws.p = ctx->cfg.p;
     ws.K = (ws.p + 1) * (ws.p + 1);
-    ws.T = static_cast<int>(std::floor(std::sqrt(8.0) * static_cast<double>(ctx->cfg.s)));  // octree.hpp:83
+    const int s_eff = ctx->cfg.mode == GB_MODE_ACCURATE && ctx->tune.leaf_s > 0 ? ctx->tune.leaf_s : ctx->cfg.s;
+    ws.T = static_cast<int>(std::floor(std::sqrt(8.0) * static_cast<double>(s_eff)));  // octree.hpp:83
     ws.eps = ctx->cfg.eps;
     ws.G = ctx->cfg.G;
     ws.m = ctx->cfg.m;
@@ -108,7 +111,11 @@ void apply_config(gb_ctx *ctx) {
     ws.p2p_newton = (ctx->cfg.flags & GB_FLAG_P2P_NEWTON) != 0;
     ws.m2l_tensor = ws.mixed && (ctx->cfg.flags & GB_FLAG_M2L_CUDA_CORES) == 0 && gb::m2l_tc_supported(ws.p);
     ws.m2l_bf16 = (ctx->cfg.flags & GB_FLAG_M2L_BF16) != 0;
-    ws.serial = (ctx->cfg.flags & GB_FLAG_SERIAL) != 0;
+    ws.serial = (ctx->cfg.flags & GB_FLAG_SERIAL) != 0 || ctx->tune.serial != 0;
+    ws.p2p_blocks = static_cast<unsigned>(ctx->tune.p2p_blocks);
+    ws.p2p_blocks_conc = static_cast<unsigned>(ctx->tune.p2p_blocks_conc);
+    ws.p2p_slice = static_cast<unsigned>(ctx->tune.p2p_slice);
+    ws.m2l_ctas_pct = ctx->tune.m2l_ctas_pct;
     ws.accurate = ctx->cfg.mode == GB_MODE_ACCURATE;
     // Failure-detection tests make the radix sort's bounded look-back waits
     // give up early (0: at the first poll) through this variable; the sort
@@ -373,7 +380,7 @@ void evaluate(gb_ctx *ctx, bool to_acc = true) {
     // Near field on the second stream, unless serial or timed: class timers
     // measure each class alone on one stream.
     const bool fork = !ws.serial && !ws.timing;
-    const unsigned conc = gb::p2p_blocks_per_sm(true), full = gb::p2p_blocks_per_sm(false);
+    const unsigned conc = ws.p2p_blocks_conc, full = ws.p2p_blocks;
     if (fork) {
         cudaEventRecord(ws.ev_fork, ws.st);
         cudaStreamWaitEvent(ws.st2, ws.ev_fork, 0);
@@ -442,9 +449,143 @@ int initial_capacity(gb_ctx *ctx) {
 
 }  // namespace
 
+namespace {
+
+int validate_tuning(const gb_tuning *t, std::string &msg) {
+    if (!t) return msg = "null tuning", GB_ERR_INVALID;
+    if (t->p2p_blocks < 1 || t->p2p_blocks > 16) return msg = "p2p_blocks must be in 1..16", GB_ERR_INVALID;
+    if (t->p2p_blocks_conc < 0 || t->p2p_blocks_conc > 16) return msg = "p2p_blocks_conc must be in 0..16", GB_ERR_INVALID;
+    if (t->p2p_slice < 1024 || t->p2p_slice > 65536) return msg = "p2p_slice must be in 1024..65536", GB_ERR_INVALID;
+    if (t->m2l_ctas_pct < 10 || t->m2l_ctas_pct > 100) return msg = "m2l_ctas_pct must be in 10..100", GB_ERR_INVALID;
+    if (t->serial != 0 && t->serial != 1) return msg = "serial must be 0 or 1", GB_ERR_INVALID;
+    if (t->leaf_s < 0) return msg = "leaf_s must be >= 0", GB_ERR_INVALID;
+    return GB_OK;
+}
+
+int floor_log2(size_t n) {
+    int k = -1;
+    while (n) n >>= 1, ++k;
+    return k;
+}
+
+// gb_tuning_lookup's parser: one entry per line of key=value tokens.
+int tuning_from_file(const char *path, const gb_config *cfg, size_t n, gb_tuning *out, std::string &msg) {
+    if (!path || !cfg || !out) return msg = "null argument", GB_ERR_INVALID;
+    FILE *f = std::fopen(path, "r");
+    if (!f) return msg = std::string("cannot open ") + path, GB_ERR_INVALID;
+    const long want[5] = {cfg->p, cfg->precision, cfg->mode, (cfg->flags & GB_FLAG_M2L_BF16) ? 1 : 0,
+                          static_cast<long>(floor_log2(n))};
+    static const char *kKeys[5] = {"p", "precision", "mode", "m2l_bf16", "log2n"};
+    static const char *kFields[6] = {"p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s"};
+    char line[1024];
+    int rc = GB_ERR_STATE;
+    int lineno = 0;
+    while (std::fgets(line, sizeof line, f)) {
+        ++lineno;
+        if (char *h = std::strchr(line, '#')) *h = 0;
+        long key[5] = {-1, -1, -1, -1, -1};
+        gb_tuning t{8, 8, gb::kSliceSources, 100, 0, 0};
+        int *fld[6] = {&t.p2p_blocks, &t.p2p_blocks_conc, &t.p2p_slice, &t.m2l_ctas_pct, &t.serial, &t.leaf_s};
+        bool any = false, bad = false;
+        for (char *tok = std::strtok(line, " \t\r\n"); tok; tok = std::strtok(nullptr, " \t\r\n")) {
+            char *eq = std::strchr(tok, '=');
+            if (!eq) {
+                bad = true;
+                break;
+            }
+            *eq = 0;
+            char *end = nullptr;
+            const long v = std::strtol(eq + 1, &end, 10);
+            if (!end || *end || end == eq + 1) {
+                bad = true;
+                break;
+            }
+            bool known = false;
+            for (int k = 0; k < 5; ++k)
+                if (!std::strcmp(tok, kKeys[k])) key[k] = v, known = true;
+            for (int k = 0; k < 6; ++k)
+                if (!std::strcmp(tok, kFields[k])) *fld[k] = static_cast<int>(v), known = true;
+            if (!known) {
+                bad = true;
+                break;
+            }
+            any = true;
+        }
+        if (!any) continue;
+        std::string m2;
+        if (bad || key[0] < 0 || key[1] < 0 || key[2] < 0 || key[3] < 0 || key[4] < 0 || validate_tuning(&t, m2) != GB_OK) {
+            msg = std::string(path) + ":" + std::to_string(lineno) + ": malformed tuning entry" + (m2.empty() ? "" : " (" + m2 + ")");
+            rc = GB_ERR_INVALID;
+            break;
+        }
+        if (key[0] == want[0] && key[1] == want[1] && key[2] == want[2] && key[3] == want[3] && key[4] == want[4]) {
+            *out = t;  // the last matching entry wins
+            rc = GB_OK;
+        }
+    }
+    std::fclose(f);
+    if (rc == GB_ERR_STATE) msg = "no tuning entry for this configuration and size";
+    return rc;
+}
+
+int apply_tuning(gb_ctx *ctx, const gb_tuning &t);
+
+// The tuning cache named by VIPP_GB_TUNE_FILE, applied when the uploaded n
+// falls into another size bucket than the last one applied. A file without an
+// entry for this configuration and bucket leaves the tuning as it is.
+int apply_tuning_cache(gb_ctx *ctx, size_t n) {
+    const char *path = std::getenv("VIPP_GB_TUNE_FILE");
+    if (!path || !*path || n == 0) return GB_OK;
+    const int b = floor_log2(n);
+    if (b == ctx->tune_log2n) return GB_OK;
+    gb_tuning t{};
+    std::string msg;
+    const int rc = tuning_from_file(path, &ctx->cfg, n, &t, msg);
+    if (rc == GB_ERR_INVALID) return ctx->err = msg, rc;
+    ctx->tune_log2n = b;
+    return rc == GB_OK ? apply_tuning(ctx, t) : GB_OK;
+}
+
+int apply_tuning(gb_ctx *ctx, const gb_tuning &t) {
+    const int oldT = ctx->ws.T;
+    ctx->tune = t;
+    ++ctx->epoch;  // launch shapes are baked into a captured step graph
+    apply_config(ctx);
+    if (ctx->ws.T != oldT && ctx->have_state) {
+        ctx->levels_fitted = false;
+        const int r = initial_capacity(ctx);
+        if (r) return r;
+    }
+    return GB_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *gb_version(void) { return kVersion; }
+
+int gb_set_tuning(gb_ctx *ctx, const gb_tuning *t) {
+    if (!ctx) return GB_ERR_INVALID;
+    std::string msg;
+    const int rc = validate_tuning(t, msg);
+    if (rc) return ctx->err = msg, rc;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    return apply_tuning(ctx, *t);
+}
+
+int gb_get_tuning(const gb_ctx *ctx, gb_tuning *out) {
+    if (!ctx || !out) return GB_ERR_INVALID;
+    *out = ctx->tune;
+    return GB_OK;
+}
+
+int gb_tuning_lookup(const char *path, const gb_config *cfg, size_t n, gb_tuning *out) {
+    std::string msg;
+    const int rc = tuning_from_file(path, cfg, n, out, msg);
+    if (rc != GB_OK) g_create_error = msg;
+    return rc;
+}
 
 int gb_create(const gb_config *cfg, gb_ctx **out) {
     if (!out) return GB_ERR_INVALID;
@@ -581,7 +722,9 @@ int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
     GB_TRY(cudaSetDevice(ctx->cfg.device));
     gb::Workspace &ws = ctx->ws;
     const unsigned nn = static_cast<unsigned>(n);
-    int rc = ensure_particles(ctx, nn);
+    int rc = apply_tuning_cache(ctx, n);
+    if (rc) return rc;
+    rc = ensure_particles(ctx, nn);
     if (rc) return rc;
     ws.n = nn;
     if (nn) {
@@ -607,7 +750,9 @@ int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max) {
     GB_TRY(cudaSetDevice(ctx->cfg.device));
     gb::Workspace &ws = ctx->ws;
     const unsigned nn = static_cast<unsigned>(n);
-    int rc = ensure_particles(ctx, nn);
+    int rc = apply_tuning_cache(ctx, n);
+    if (rc) return rc;
+    rc = ensure_particles(ctx, nn);
     if (rc) return rc;
     ws.n = nn;
     if (nn) {

@@ -101,10 +101,10 @@ GB_HD void chunk_at(int n, int q, int &off, int &len) {
 // A chunk whose leaf has more than kSliceSources near-field sources runs as
 // several work items, each over a slice of the sources; their partial sums
 // are added in slice order afterwards. This bounds the longest work item.
-constexpr int kSliceSources = 8192;
+constexpr int kSliceSources = 8192;  // default; the tuning may pick another length
 constexpr int kMaxSlices = 4095;
-GB_HD int slice_count(unsigned long long srcs) {
-    const unsigned long long s = (srcs + kSliceSources - 1) / kSliceSources;
+GB_HD int slice_count(unsigned long long srcs, unsigned slice = kSliceSources) {
+    const unsigned long long s = (srcs + slice - 1) / slice;
     return s < 1 ? 1 : (s > kMaxSlices ? kMaxSlices : static_cast<int>(s));
 }
 // Work-item field z: targets (6 bits), slice index (12 bits), slices (12 bits).

@@ -56,6 +56,8 @@
 // records kDevTimeout in the status word, stops issuing work, waits (bounded)
 // for its own copies and MMAs, frees its TMEM and returns.
 #include <cuda.h>
+
+#include <algorithm>
 #include <cuda_bf16.h>
 
 #include "workspace.cuh"
@@ -642,7 +644,8 @@ void launch(Workspace &ws) {
     k_split_m<P, BF><<<4 * ws.num_sms, 256, 0, ws.st>>>(ws.info, static_cast<const float *>(ws.Mexp), ws.ms_tc,
                                                         static_cast<int>(ws.ms_rows));
     cudaFuncSetAttribute(k_m2l_tc<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(C::SMEM));
-    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms), 8 * ceil_div(ceil_div(ws.c_cap, 8), kRows));  // tiles
+    const unsigned ctas = std::max(1u, static_cast<unsigned>(ws.num_sms * ws.m2l_ctas_pct / 100));
+    const unsigned gs = capped_grid(ctas, 8 * ceil_div(ceil_div(ws.c_cap, 8), kRows));  // tiles
     k_m2l_tc<P, BF><<<gs, kThreads, C::SMEM, ws.st>>>(ws.tmap_ms, ws.info, ws.m2l_src,
                                                       reinterpret_cast<const unsigned char *>(ws.bimg),
                                                       static_cast<int>(ws.ms_rows), static_cast<float *>(ws.Lexp), ws.info);

@@ -25,12 +25,6 @@
 #ifndef GB_P2P_CARVEOUT_MAX
 #define GB_P2P_CARVEOUT_MAX 0
 #endif
-#ifndef GB_P2P_BLOCKS_PER_SM
-#define GB_P2P_BLOCKS_PER_SM 8
-#endif
-#ifndef GB_P2P_CONCURRENT_PER_SM
-#define GB_P2P_CONCURRENT_PER_SM 8  // blocks per SM of the P2P launch beside the far field
-#endif
 
 namespace gb {
 
@@ -412,8 +406,6 @@ void near_potential(Workspace &ws, double *phiv) {
 // launches (on any streams) may drain the same queue, each item is taken once.
 // p2p_finish adds the slices of split items after all of them.
 
-unsigned p2p_blocks_per_sm(bool concurrent) { return concurrent ? GB_P2P_CONCURRENT_PER_SM : GB_P2P_BLOCKS_PER_SM; }
-
 void p2p_pass(Workspace &ws, unsigned per_sm) {
     if (per_sm == 0) return;
     timer_begin(ws, kTP2P);
@@ -464,7 +456,7 @@ void p2p_pass(Workspace &ws, unsigned per_sm) {
 }
 
 void p2p_finish(Workspace &ws) {
-    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * GB_P2P_BLOCKS_PER_SM, ceil_div(ws.n, 128));
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.n, 128));
     if (ws.mixed)
         k_p2p_combine<float><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, static_cast<const float *>(ws.part),
                                                     static_cast<float>(ws.G * ws.m), static_cast<float *>(ws.nearf), ws.n);

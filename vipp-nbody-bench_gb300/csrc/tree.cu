@@ -621,7 +621,7 @@ __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts
 __global__ void k_rng_count(const int *__restrict__ leaves, const unsigned *counts, const int *__restrict__ c_parent,
                             const int *__restrict__ c_begin, const int *__restrict__ c_end,
                             const int *__restrict__ p2p_own, const int *__restrict__ p2p_cnt, unsigned *rng_cnt,
-                            unsigned *chunk_cnt, unsigned *src_total, unsigned *part_cnt) {
+                            unsigned *chunk_cnt, unsigned *src_total, unsigned *part_cnt, unsigned slice) {
     const unsigned NL = counts[3];
     for (unsigned li = blockIdx.x * blockDim.x + threadIdx.x; li < NL; li += gridDim.x * blockDim.x) {
         const int c = leaves[li];
@@ -637,7 +637,7 @@ __global__ void k_rng_count(const int *__restrict__ leaves, const unsigned *coun
                 }
             }
         rng_cnt[li] = tot;
-        const unsigned ns = nt > 0 ? static_cast<unsigned>(slice_count(srcs)) : 1u;
+        const unsigned ns = nt > 0 ? static_cast<unsigned>(slice_count(srcs, slice)) : 1u;
         chunk_cnt[li] = static_cast<unsigned>(chunk_count(nt)) * ns;
         part_cnt[li] = ns > 1 ? static_cast<unsigned>(chunk_count(nt)) * ns : 0u;
         src_total[li] = static_cast<unsigned>(srcs < 0xffffffffull ? srcs : 0xffffffffull);
@@ -654,7 +654,7 @@ __global__ void k_rng_fill(const int *__restrict__ leaves, unsigned *counts, uns
                            const int *__restrict__ p2p_own, const int *__restrict__ p2p_cnt,
                            const unsigned *__restrict__ rng_off, unsigned *rng_len, uint2 *ranges,
                            const unsigned *__restrict__ chunk_off, int4 *chunks, const unsigned *__restrict__ src_total,
-                           const unsigned *__restrict__ part_off, unsigned part_cap, TreeInfo *info) {
+                           const unsigned *__restrict__ part_off, unsigned part_cap, TreeInfo *info, unsigned slice) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         counts[7] = counts[5];  // requested sizes, kept for the host when they overflow
         const bool over = counts[4] > r_cap || counts[5] > ch_cap || counts[8] > part_cap;
@@ -711,7 +711,7 @@ __global__ void k_rng_fill(const int *__restrict__ leaves, unsigned *counts, uns
         rng_len[li] = overflow ? 0u : k;  // never let P2P read past the buffer
         const unsigned cb = chunk_off[li];
         const int nch = chunk_count(e - b);
-        const int ns = slice_count(src_total[li]);
+        const int ns = slice_count(src_total[li], slice);
         for (int q = 0; q < nch; ++q) {
             int off, len;
             chunk_at(e - b, q, off, len);
@@ -812,7 +812,7 @@ void build_tree(Workspace &ws) {
                                 ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                                 reinterpret_cast<unsigned long long *>(&ws.info->m2l_pairs));
     k_rng_count<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.c_parent, ws.c_begin, ws.c_end, ws.p2p_own, ws.p2p_cnt,
-                                    ws.rng_cnt, ws.chunk_cnt, ws.src_total, ws.part_cnt);
+                                    ws.rng_cnt, ws.chunk_cnt, ws.src_total, ws.part_cnt, ws.p2p_slice);
     {  // range, work-item and partial-slot offsets per leaf, one scan sequence
         ScanSet sc{};
         sc.in[0] = ws.rng_cnt, sc.out[0] = ws.rng_off, sc.total[0] = ws.d_counts + 4;
@@ -822,7 +822,7 @@ void build_tree(Workspace &ws) {
     }
     k_rng_fill<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.r_cap, ws.ch_cap, ws.c_parent, ws.c_begin, ws.c_end,
                                    ws.p2p_own, ws.p2p_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_off, ws.chunks,
-                                   ws.src_total, ws.part_off, ws.part_cap, ws.info);
+                                   ws.src_total, ws.part_off, ws.part_cap, ws.info, ws.p2p_slice);
     ws.launches += 9;
     timer_end(ws, kTTree);
 }

@@ -46,6 +46,11 @@ struct Workspace {
     unsigned sort_spin_max = kSortSpinMax;  // look-back polls before a wait gives up (tests lower it)
     int64_t launches = 0;
     int num_sms = 152;
+    // tuning knobs (gb_set_tuning / the tuning cache; the defaults are the measured best at 4M)
+    unsigned p2p_blocks = 8;        // P2P blocks per SM when it runs alone (or after the far field)
+    unsigned p2p_blocks_conc = 8;   // P2P blocks per SM launched beside the far field
+    unsigned p2p_slice = kSliceSources;  // near-field sources per P2P work item
+    int m2l_ctas_pct = 100;         // tensor-core M2L CTAs, percent of the SMs (one persistent CTA per SM)
 
     // capacities
     unsigned n_cap = 0;   // particles
@@ -168,7 +173,6 @@ void soften_pass(Workspace &ws);              // accurate mode: far = G (far + s
 size_t soften_cell_bytes(bool mixed);         // bytes of one moment record
 void p2p_pass(Workspace &ws, unsigned per_sm); // near-field kernel over the queue, per_sm blocks per SM
 void p2p_finish(Workspace &ws);               // add the slices of split items: near complete
-unsigned p2p_blocks_per_sm(bool concurrent);   // P2P blocks per SM alone / beside the far field
 void finalize_accel(Workspace &ws, double *acc_orig);  // acc[perm] = near + far
 // diagnostics after an evaluation (tree order, FP64): far-field potential of the
 // local expansions (no G, like the far-field acceleration) and the near-field

@@ -35,13 +35,21 @@ EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_uplo
            "gb_accel", "gb_direct_accel", "gb_sync", "gb_get_stats", "gb_tree_dump", "gb_enable_timing",
            "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream", "gb_direct_accel_noalloc",
            "gb_get_conserved", "gb_init_plummer", "gb_batch_create", "gb_batch_destroy", "gb_batch_last_error",
-           "gb_batch_upload", "gb_batch_download", "gb_batch_rk4_step", "gb_batch_size", "gb_batch_system")
+           "gb_batch_upload", "gb_batch_download", "gb_batch_rk4_step", "gb_batch_size", "gb_batch_system",
+           "gb_set_tuning", "gb_get_tuning", "gb_tuning_lookup")
+TUNING_FIELDS = ("p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s")
+TUNING_DEFAULT = {"p2p_blocks": 8, "p2p_blocks_conc": 8, "p2p_slice": 8192, "m2l_ctas_pct": 100, "serial": 0,
+                  "leaf_s": 0}
 
 
 class GbConfig(ctypes.Structure):
     _fields_ = [("p", ctypes.c_int), ("s", ctypes.c_int), ("eps", ctypes.c_double), ("G", ctypes.c_double),
                 ("m", ctypes.c_double), ("precision", ctypes.c_int), ("device", ctypes.c_int), ("flags", ctypes.c_int),
                 ("mode", ctypes.c_int)]
+
+
+class GbTuning(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int) for k in TUNING_FIELDS]
 
 
 class GbConserved(ctypes.Structure):
@@ -104,6 +112,10 @@ def load(path: str | None = None):
     lib.gb_stream.restype = vp
     lib.gb_direct_accel_noalloc.argtypes = [vp, ctypes.c_size_t, vp, ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, vp, vp]
+    lib.gb_set_tuning.argtypes = [vp, ctypes.POINTER(GbTuning)]
+    lib.gb_get_tuning.argtypes = [vp, ctypes.POINTER(GbTuning)]
+    lib.gb_tuning_lookup.argtypes = [ctypes.c_char_p, ctypes.POINTER(GbConfig), ctypes.c_size_t,
+                                     ctypes.POINTER(GbTuning)]
     _LIB = lib
     return lib
 
@@ -114,6 +126,20 @@ def _ptr(a):
 
 def _aos(a):
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1, 3))
+
+
+def tuning_lookup(path: str, n: int, p: int, precision: str = "mixed", mode: str = "ref", flags: int = 0):
+    """The tuning-cache entry (dict) for a configuration and particle count, or
+    None when the file has none (gb_tuning_lookup; no GPU needed)."""
+    lib = load()
+    cfg = GbConfig(p, 1, 0.0, 1.0, 1.0, PREC[precision], 0, flags, MODE[mode])
+    t = GbTuning()
+    rc = lib.gb_tuning_lookup(path.encode(), ctypes.byref(cfg), n, ctypes.byref(t))
+    if rc == GB_ERR_STATE:
+        return None
+    if rc != GB_OK:
+        raise GB300Error(rc, lib.gb_last_error(None).decode())
+    return {k: int(getattr(t, k)) for k in TUNING_FIELDS}
 
 
 class GB300Error(RuntimeError):
@@ -165,6 +191,21 @@ class Solver:
                 v = MODE[v]
             setattr(self.cfg, k, v)
         self._check(self.lib.gb_set_config(self.h, ctypes.byref(self.cfg)))
+
+    def set_tuning(self, **kw):
+        """Change launch/tree parameters (gb_set_tuning); unnamed ones keep their values."""
+        t = GbTuning()
+        self._check(self.lib.gb_get_tuning(self.h, ctypes.byref(t)))
+        for k, v in kw.items():
+            if k not in TUNING_FIELDS:
+                raise KeyError(k)
+            setattr(t, k, int(v))
+        self._check(self.lib.gb_set_tuning(self.h, ctypes.byref(t)))
+
+    def tuning(self) -> dict:
+        t = GbTuning()
+        self._check(self.lib.gb_get_tuning(self.h, ctypes.byref(t)))
+        return {k: int(getattr(t, k)) for k in TUNING_FIELDS}
 
     # Solver concept -------------------------------------------------------
     def preprocess(self, x, v):

@@ -62,10 +62,19 @@ UNIT = "particle-steps/s"
 FP32_LANES_PER_SM = 128
 
 
-def make_workload(args, rank=0):
-    """(x, v, seed, name) of the selected workload; replicas use seed + rank."""
+def make_workload(args, rank=0, device=None):
+    """(x, v, seed, name) of the selected workload; replicas use seed + rank.
+    With a device, the clustered workload is drawn there (gb_init_clustered)
+    and copied back; otherwise on the host (workloads.clustered: the same
+    distribution, other numbers)."""
     if args.workload == "clustered":
         seed = 4 + rank
+        if device is not None:
+            import vipp_gb300
+            with vipp_gb300.Solver(p=4, s=args.s, eps=args.eps, m=1.0 / args.n, device=device) as g:
+                g.init_clustered(args.n, seed)
+                x, v = g.postprocess()
+            return x, v, seed, f"clustered-{args.n} (8 Plummer clusters + 5% background, drawn on the GPU)"
         x, v, _ = clustered(args.n, seed)
         return x, v, seed, f"clustered-{args.n} (8 Plummer clusters + 5% background)"
     if args.workload == "uniform":
@@ -82,7 +91,7 @@ def make_workload(args, rank=0):
 M2L_BF16_TRAFFIC = 139474944 + 19757568
 
 
-def batch_measure(steps=4, warmup=2, nsys=512, seed=3, sample=8, flags=0):
+def batch_measure(steps=50, warmup=2, nsys=512, seed=3, sample=32, flags=0):
     """Batching form: nsys Plummer systems, N log-uniform in [1024, 65536],
     scale radius uniform in [0.5, 2] (positions x R, velocities x R^-1/2), total
     mass 1 each, eps = 0.01, p = 6, s = 32, mixed precision, dt = 1e-3, all
@@ -92,16 +101,9 @@ def batch_measure(steps=4, warmup=2, nsys=512, seed=3, sample=8, flags=0):
     import vipp_gb300
     rng = np.random.default_rng(seed)
     sizes = np.rint(np.exp(rng.uniform(math.log(1024), math.log(65536), nsys))).astype(np.int64)
-    radii = rng.uniform(0.5, 2.0, nsys)
-    xs, vs = [], []
-    for k in range(nsys):
-        x, v = plummer(int(sizes[k]), 1000 + k)
-        xs.append(x * radii[k])
-        vs.append(v / math.sqrt(radii[k]))
-    X, V = np.concatenate(xs), np.concatenate(vs)
     t0 = time.perf_counter()
     b = vipp_gb300.Batch(sizes, p=6, s=32, eps=0.01, masses=1.0 / sizes, precision="mixed", flags=flags)
-    b.upload(X, V)
+    b.init_plummer(seed=seed, r_lo=0.5, r_hi=2.0)  # every system drawn on the GPU
     setup = time.perf_counter() - t0
     for _ in range(warmup):
         b.step(1e-3)
@@ -121,8 +123,8 @@ def batch_measure(steps=4, warmup=2, nsys=512, seed=3, sample=8, flags=0):
         errs.append(float(math.sqrt(np.mean(e * e))))
     b.close()
     n = int(sizes.sum())
-    return {"workload": f"{nsys} Plummer systems, N log-uniform in [1024, 65536] (seed {seed}), R in [0.5, 2], p=6 s=32 "
-                        "eps=0.01 mixed, dt=1e-3", "value": n * steps / dt_wall, "unit": UNIT, "n_total": n,
+    return {"workload": f"{nsys} Plummer systems, N log-uniform in [1024, 65536] (seed {seed}), R in [0.5, 2] (systems "
+                        "drawn on the GPU), p=6 s=32 eps=0.01 mixed, dt=1e-3", "value": n * steps / dt_wall, "unit": UNIT, "n_total": n,
             "systems": nsys, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * dt_wall / steps,
             "setup_s": setup, "rms_rel_err_vs_fp64_direct_per_system": errs,
             "timing": "host wall clock per gb_batch_rk4_step (it returns after all systems' steps)"}
@@ -404,7 +406,9 @@ def main():
     if args.precision == "mixed" and args.m2l == "bf16":
         args.flags |= vipp_gb300.FLAG_M2L_BF16
     n = args.n
-    x, v, seed, wname = make_workload(args, rank)
+    t_ic = time.perf_counter()
+    x, v, seed, wname = make_workload(args, rank, device=local)
+    t_ic = time.perf_counter() - t_ic
     m = 1.0 / n
     sol = vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision=args.precision, device=local,
                             flags=args.flags)
@@ -661,6 +665,7 @@ def main():
            "s": args.s, "eps": args.eps, "dt": args.dt, "precision": args.precision, "m2l_split": m2l_split, "seed": seed,
            "l2": f"inputs larger than L2 (state {48 * n / 1e6:.0f} MB, per-step working set > 1 GB)",
            "tree": {k: st[k] for k in ("ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges")},
+           "initial_conditions_s": round(t_ic, 3),
            "kernel_ms_per_step": kt_ms, **acc_info, "energy": energy, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * elapsed / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,

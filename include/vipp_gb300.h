@@ -146,6 +146,12 @@ GB_API int gb_batch_create(const gb_config *cfg, size_t nsys, const uint64_t *se
 GB_API void gb_batch_destroy(gb_batch *b);
 GB_API const char *gb_batch_last_error(const gb_batch *b);
 GB_API int gb_batch_upload(gb_batch *b, const double *x_aos, const double *v_aos);
+/* Every system of the batch generated on the device instead of uploaded: a
+ * Plummer sphere of total mass 1 (G = 1) with radii capped at r_max scale
+ * radii, scaled to a scale radius R_k uniform in [r_lo, r_hi] (positions
+ * times R_k, velocities times R_k^-1/2); radii (may be NULL) receives the
+ * nsys R_k. Each system's particle mass stays as given at gb_batch_create. */
+GB_API int gb_batch_init_plummer(gb_batch *b, uint64_t seed, double r_lo, double r_hi, double r_max, double *radii);
 GB_API int gb_batch_download(gb_batch *b, double *x_aos, double *v_aos);
 GB_API int gb_batch_rk4_step(gb_batch *b, double dt);
 GB_API int gb_batch_size(const gb_batch *b, size_t *nsys, uint64_t *n_total);
@@ -158,6 +164,19 @@ GB_API gb_ctx *gb_batch_system(gb_batch *b, size_t k);
  * caps radii at r_max instead. Same distribution as the reference, not the
  * same numbers. Replaces the state like gb_upload; gb_download reads it. */
 GB_API int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max);
+
+/* The adaptive-depth stress workload generated on the device (no counterpart
+ * in the reference): `clusters` (1..8) equal-mass Plummer clusters, each with
+ * its scale radius uniform in [0.01, 0.1], its centre uniform in [0, 1)^3, a
+ * Gaussian bulk velocity (sigma 0.3 per component) and internal Plummer
+ * velocities of its own mass and radius (G = 1), radii capped at r_max scale
+ * radii, plus round(background n) particles uniform in [0, 1)^3 at rest;
+ * total mass 1 in equal masses. The same counter-based streams as
+ * gb_init_plummer. params (may be NULL) receives 8 doubles per cluster:
+ * centre[3], scale radius, bulk velocity[3], particle count. Replaces the
+ * state like gb_upload. */
+GB_API int gb_init_clustered(gb_ctx *ctx, size_t n, uint64_t seed, int clusters, double background, double r_max,
+                             double *params);
 
 /* preprocess: copy n particles (AoS doubles) to the device. n may be 0. */
 GB_API int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n);

@@ -770,6 +770,38 @@ int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max) {
     return GB_OK;
 }
 
+int gb_init_clustered(gb_ctx *ctx, size_t n, uint64_t seed, int clusters, double background, double r_max,
+                      double *params) {
+    if (ctx) ctx->levels_fitted = false;
+    if (!ctx) return GB_ERR_INVALID;
+    if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
+    if (clusters < 1 || clusters > 8) return ctx->err = "clusters must be in 1..8", GB_ERR_INVALID;
+    if (!(background >= 0 && background < 1)) return ctx->err = "background must be in [0, 1)", GB_ERR_INVALID;
+    if (!(r_max > 0) || !std::isfinite(r_max)) return ctx->err = "r_max must be finite and > 0", GB_ERR_INVALID;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    gb::Workspace &ws = ctx->ws;
+    const unsigned nn = static_cast<unsigned>(n);
+    int rc = apply_tuning_cache(ctx, n);
+    if (rc) return rc;
+    rc = ensure_particles(ctx, nn);
+    if (rc) return rc;
+    ws.n = nn;
+    if (nn) {
+        if (gb::generate_clustered(ws, nn, seed, clusters, background, r_max, params) != 0)
+            return ctx->err = "bad cluster parameters", GB_ERR_INVALID;
+        GB_TRY(cudaGetLastError());
+        int err = 0;
+        GB_TRY(cudaMemcpyAsync(&err, &ws.info->err, sizeof(int), cudaMemcpyDeviceToHost, ws.st));
+        GB_TRY(cudaStreamSynchronize(ws.st));
+        if (err) return ctx->err = "initial-condition sampling did not converge", GB_ERR_CUDA;
+        rc = initial_capacity(ctx);
+        if (rc) return rc;
+    }
+    GB_TRY(cudaStreamSynchronize(ws.st));
+    ctx->have_state = true;
+    return GB_OK;
+}
+
 int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos) {
     if (!ctx) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
@@ -932,6 +964,51 @@ int gb_batch_upload(gb_batch *b, const double *x_aos, const double *v_aos) {
         const uint64_t o = b->off[k], n = b->off[k + 1] - o;
         const int rc = gb_upload(b->ctx[k], x_aos + 3 * o, v_aos + 3 * o, n);
         if (rc != GB_OK) return batch_fail(b, k, rc);
+    }
+    return GB_OK;
+}
+
+int gb_batch_init_plummer(gb_batch *b, uint64_t seed, double r_lo, double r_hi, double r_max, double *radii) {
+    if (!b) return GB_ERR_INVALID;
+    if (!(r_lo > 0) || !(r_hi >= r_lo) || !std::isfinite(r_hi)) return b->err = "need 0 < r_lo <= r_hi", GB_ERR_INVALID;
+    if (!(r_max > 0) || !std::isfinite(r_max)) return b->err = "r_max must be finite and > 0", GB_ERR_INVALID;
+    auto mix = [](uint64_t z) {  // SplitMix64 output function, as the device streams (ic.cu)
+        z += 0x9e3779b97f4a7c15ull;
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        return z ^ (z >> 31);
+    };
+    for (size_t k = 0; k < b->ctx.size(); ++k) {
+        gb_ctx *ctx = b->ctx[k];
+        const uint64_t n = b->off[k + 1] - b->off[k];
+        const double u = static_cast<double>(mix(mix(seed ^ 0x2545f4914f6cdd1dull) + k) >> 11) * 0x1.0p-53;
+        const double R = r_lo + (r_hi - r_lo) * u;
+        if (radii) radii[k] = R;
+        ctx->levels_fitted = false;
+        if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return batch_fail(b, k, GB_ERR_CUDA);
+        gb::Workspace &ws = ctx->ws;
+        int rc = apply_tuning_cache(ctx, n);
+        if (rc == GB_OK) rc = ensure_particles(ctx, static_cast<unsigned>(n));
+        if (rc != GB_OK) return batch_fail(b, k, rc);
+        ws.n = static_cast<unsigned>(n);
+        if (n) {
+            // total mass 1 and scale radius R (G = 1): positions x R, velocities x R^-1/2
+            gb::generate_plummer(ws, ws.n, mix(seed + k), 1.0, r_max, R, 1.0 / std::sqrt(R));
+            rc = initial_capacity(ctx);
+            if (rc != GB_OK) return batch_fail(b, k, rc);
+        }
+        ctx->have_state = true;
+    }
+    for (size_t k = 0; k < b->ctx.size(); ++k) {
+        gb::Workspace &ws = b->ctx[k]->ws;
+        int err = 0;
+        if (cudaMemcpyAsync(&err, &ws.info->err, sizeof(int), cudaMemcpyDeviceToHost, ws.st) != cudaSuccess ||
+            cudaStreamSynchronize(ws.st) != cudaSuccess)
+            return batch_fail(b, k, GB_ERR_CUDA);
+        if (err) {
+            b->ctx[k]->err = "initial-condition sampling did not converge";
+            return batch_fail(b, k, GB_ERR_CUDA);
+        }
     }
     return GB_OK;
 }

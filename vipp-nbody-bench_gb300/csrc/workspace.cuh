@@ -182,7 +182,12 @@ void near_potential(Workspace &ws, double *nearphi);
 void potential_orig(Workspace &ws, double *phi_orig);    // phi[perm] = -(near + far), needs ws.phis [2N]
 void conserved_sums(Workspace &ws, const double *phi_orig, double *sums8);  // see diag.cu
 size_t diag_scratch_doubles();
-void generate_plummer(Workspace &ws, unsigned n, uint64_t seed, double x0_max, double r_max);  // ic.cu
+void generate_plummer(Workspace &ws, unsigned n, uint64_t seed, double x0_max, double r_max, double x_scale = 1.0,
+                      double v_scale = 1.0);  // ic.cu
+// clusters (<= 8) Plummer clusters + a uniform background fraction (ic.cu);
+// params (may be null): 8 doubles per cluster, centre[3], radius, bulk[3], size
+int generate_clustered(Workspace &ws, unsigned n, uint64_t seed, int clusters, double background, double r_max,
+                       double *params);
 void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, unsigned nt, double *out_soa,
                 double *part, unsigned nsplit);  // part: [nsplit][3][nt] scratch
 

@@ -36,7 +36,7 @@ EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_uplo
            "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream", "gb_direct_accel_noalloc",
            "gb_get_conserved", "gb_init_plummer", "gb_batch_create", "gb_batch_destroy", "gb_batch_last_error",
            "gb_batch_upload", "gb_batch_download", "gb_batch_rk4_step", "gb_batch_size", "gb_batch_system",
-           "gb_set_tuning", "gb_get_tuning", "gb_tuning_lookup")
+           "gb_set_tuning", "gb_get_tuning", "gb_tuning_lookup", "gb_init_clustered", "gb_batch_init_plummer")
 TUNING_FIELDS = ("p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s")
 TUNING_DEFAULT = {"p2p_blocks": 8, "p2p_blocks_conc": 8, "p2p_slice": 8192, "m2l_ctas_pct": 100, "serial": 0,
                   "leaf_s": 0}
@@ -112,6 +112,9 @@ def load(path: str | None = None):
     lib.gb_stream.restype = vp
     lib.gb_direct_accel_noalloc.argtypes = [vp, ctypes.c_size_t, vp, ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, vp, vp]
+    lib.gb_init_clustered.argtypes = [vp, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_double, vp]
+    lib.gb_batch_init_plummer.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
     lib.gb_set_tuning.argtypes = [vp, ctypes.POINTER(GbTuning)]
     lib.gb_get_tuning.argtypes = [vp, ctypes.POINTER(GbTuning)]
     lib.gb_tuning_lookup.argtypes = [ctypes.c_char_p, ctypes.POINTER(GbConfig), ctypes.c_size_t,
@@ -248,6 +251,18 @@ class Solver:
         self._check(self.lib.gb_init_plummer(self.h, int(n), int(seed), float(r_max)))
         self.n = int(n)
 
+    def init_clustered(self, n, seed=4, clusters=8, background=0.05, r_max=10.0):
+        """Generate the adaptive-depth stress workload on the device
+        (gb_init_clustered); returns the clusters' parameters as a dict of
+        arrays: centres, radii, bulk, sizes."""
+        prm = np.zeros(8 * clusters)
+        self._check(self.lib.gb_init_clustered(self.h, int(n), int(seed), int(clusters), float(background),
+                                               float(r_max), _ptr(prm)))
+        self.n = int(n)
+        q = prm.reshape(clusters, 8)
+        return {"centres": q[:, :3].copy(), "radii": q[:, 3].copy(), "bulk": q[:, 4:7].copy(),
+                "sizes": q[:, 7].astype(np.int64)}
+
     def conserved(self) -> dict:
         """Kinetic, potential and total energy, momentum and angular momentum
         of the current state (one FMM evaluation for the potential)."""
@@ -356,6 +371,15 @@ class Batch:
         assert x.shape[0] == self.n and v.shape[0] == self.n
         self._check(self.lib.gb_batch_upload(self.h, _ptr(x), _ptr(v)))
 
+    def init_plummer(self, seed=3, r_lo=0.5, r_hi=2.0, r_max=10.0):
+        """Generate every system on the device (gb_batch_init_plummer): Plummer
+        spheres of total mass 1 scaled to radii uniform in [r_lo, r_hi];
+        returns the radii."""
+        radii = np.zeros(len(self.off) - 1)
+        self._check(self.lib.gb_batch_init_plummer(self.h, int(seed), float(r_lo), float(r_hi), float(r_max),
+                                                   _ptr(radii)))
+        return radii
+
     def step(self, dt):
         self._check(self.lib.gb_batch_rk4_step(self.h, float(dt)))
 
@@ -382,6 +406,16 @@ class Batch:
         if rc != GB_OK:
             raise GB300Error(rc, self.lib.gb_last_error(c).decode())
         return a
+
+    def system_conserved(self, k) -> dict:
+        """Conserved quantities of system k (gb_get_conserved on its context)."""
+        c = self.lib.gb_batch_system(self.h, k)
+        out = GbConserved()
+        rc = self.lib.gb_get_conserved(c, ctypes.byref(out))
+        if rc != GB_OK:
+            raise GB300Error(rc, self.lib.gb_last_error(c).decode())
+        return {"kinetic": out.kinetic, "potential": out.potential, "total": out.total,
+                "momentum": list(out.momentum), "angular_momentum": list(out.angular_momentum)}
 
     def close(self):
         if getattr(self, "h", None):

@@ -404,6 +404,48 @@ __device__ __forceinline__ void soft_term_s(const SRec<T> &r, T tx, T ty, T tz, 
     az += a * dz + b * qz;
 }
 
+// FP32: two staged records per step on paired FP32 instructions (.f32x2, each
+// component rounded as the scalar operation). A batch of 32 records is kept as
+// 16 pairs of 24 floats, field-interleaved ((dx0, dx1, dy0, dy1), ...), so a
+// pair is six 16-byte shared-memory loads.
+__device__ __forceinline__ void put_paired(float *pb, int lane, const SRec<float> &r) {
+    float *q = pb + 24 * (lane >> 1) + (lane & 1);
+    q[0] = r.dx, q[2] = r.dy, q[4] = r.dz, q[6] = r.M, q[8] = r.tr, q[10] = r.q0;
+    q[12] = r.q1, q[14] = r.q2, q[16] = r.q3, q[18] = r.q4, q[20] = r.q5, q[22] = 0.f;
+}
+
+__device__ __forceinline__ float2 rsqrt2(float2 x) { return make_float2(rsqrt_t<float>(x.x), rsqrt_t<float>(x.y)); }
+
+__device__ __forceinline__ void soft_term_pair(const float4 *P, float2 ntx, float2 nty, float2 ntz, float2 e2, float2 &ax,
+                                               float2 &ay, float2 &az) {
+    const float4 a = P[0], b = P[1], c = P[2], d = P[3], e = P[4], f = P[5];
+    const float2 m1 = make_float2(-1.f, -1.f), two = make_float2(2.f, 2.f);
+    const float2 dx = __fadd2_rn(make_float2(a.x, a.y), ntx);
+    const float2 dy = __fadd2_rn(make_float2(a.z, a.w), nty);
+    const float2 dz = __fadd2_rn(make_float2(b.x, b.y), ntz);
+    const float2 M = make_float2(b.z, b.w), tr = make_float2(c.x, c.y);
+    const float2 q0 = make_float2(c.z, c.w), q1 = make_float2(d.x, d.y), q2 = make_float2(d.z, d.w);
+    const float2 q3 = make_float2(e.x, e.y), q4 = make_float2(e.z, e.w), q5 = make_float2(f.x, f.y);
+    const float2 u = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+    const float2 A = rsqrt2(__fadd2_rn(u, e2)), B = rsqrt2(u);
+    const float2 A2 = __fmul2_rn(A, A), B2 = __fmul2_rn(B, B);
+    const float2 A3 = __fmul2_rn(A2, A), B3 = __fmul2_rn(B2, B);
+    const float2 A5 = __fmul2_rn(A3, A2), B5 = __fmul2_rn(B3, B2);
+    const float2 A7 = __fmul2_rn(A5, A2), B7 = __fmul2_rn(B5, B2);
+    const float2 F = __ffma2_rn(B3, m1, A3);
+    const float2 F1 = __fmul2_rn(__ffma2_rn(B5, m1, A5), make_float2(-1.5f, -1.5f));
+    const float2 F2 = __fmul2_rn(__ffma2_rn(B7, m1, A7), make_float2(3.75f, 3.75f));
+    const float2 qx = __ffma2_rn(q0, dx, __ffma2_rn(q3, dy, __fmul2_rn(q4, dz)));
+    const float2 qy = __ffma2_rn(q3, dx, __ffma2_rn(q1, dy, __fmul2_rn(q5, dz)));
+    const float2 qz = __ffma2_rn(q4, dx, __ffma2_rn(q5, dy, __fmul2_rn(q2, dz)));
+    const float2 dqd = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
+    const float2 sa = __ffma2_rn(__fmul2_rn(two, F2), dqd, __ffma2_rn(M, F, __fmul2_rn(F1, tr)));
+    const float2 sb = __fmul2_rn(two, F1);
+    ax = __ffma2_rn(sa, dx, __ffma2_rn(sb, qx, ax));
+    ay = __ffma2_rn(sa, dy, __ffma2_rn(sb, qy, ay));
+    az = __ffma2_rn(sa, dz, __ffma2_rn(sb, qz, az));
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kSoftWarps * 32) k_soft_near(
     const int *__restrict__ leaves, const unsigned *counts, const int *__restrict__ c_begin, const int *__restrict__ c_end,
@@ -413,7 +455,7 @@ __global__ void __launch_bounds__(kSoftWarps * 32) k_soft_near(
     const double *__restrict__ xs, const float4 *__restrict__ ph, const float4 *__restrict__ pl, unsigned n, T e2, T G,
     T *__restrict__ far) {
     __shared__ int list[kSoftWarps][kSoftMaxSrc + 32];
-    __shared__ SRec<T> batch[kSoftWarps][32];
+    __shared__ __align__(16) SRec<T> batch[kSoftWarps][32];  // FP32: the paired layout (put_paired)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned NL = counts[3];
     const unsigned warps = gridDim.x * (blockDim.x >> 5);
@@ -480,18 +522,48 @@ __global__ void __launch_bounds__(kSoftWarps * 32) k_soft_near(
             }
             SRec<T> nxt;
             if (nsrc > 0) stage<T>(mom, moct, list[w][lane], cc, nxt);
-            for (int b0 = 0; b0 < nsrc; b0 += 32) {
-                batch[w][lane] = nxt;
-                __syncwarp();
-                if (b0 + 32 < nsrc) stage<T>(mom, moct, list[w][b0 + 32 + lane], cc, nxt);
-                const int nb = min(32, nsrc - b0);
-                for (int k = 0; k < nb; ++k) {
-                    const SRec<T> r = batch[w][k];
+            if constexpr (sizeof(T) == 4) {
+                float *pb = reinterpret_cast<float *>(batch[w]);
+                const float4 *pb4 = reinterpret_cast<const float4 *>(pb);
+                const float2 e22 = make_float2(e2, e2);
+                float2 nt[kSoftTPL][3], a2[kSoftTPL][3];
 #pragma unroll
-                    for (int q = 0; q < kSoftTPL; ++q)
-                        if (q < nq) soft_term_s<T>(r, ty[q][0], ty[q][1], ty[q][2], e2, acc[q][0], acc[q][1], acc[q][2]);
+                for (int q = 0; q < kSoftTPL; ++q)
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+                        nt[q][a] = make_float2(-ty[q][a], -ty[q][a]), a2[q][a] = make_float2(0.f, 0.f);
+                for (int b0 = 0; b0 < nsrc; b0 += 32) {
+                    put_paired(pb, lane, nxt);
+                    __syncwarp();
+                    if (b0 + 32 < nsrc) stage<T>(mom, moct, list[w][b0 + 32 + lane], cc, nxt);
+                    // a padded batch's tail holds massless records whose terms are exactly zero
+                    const int npairs = (min(32, nsrc - b0) + 1) >> 1;
+                    for (int k = 0; k < npairs; ++k) {
+#pragma unroll
+                        for (int q = 0; q < kSoftTPL; ++q)
+                            if (q < nq)
+                                soft_term_pair(pb4 + 6 * k, nt[q][0], nt[q][1], nt[q][2], e22, a2[q][0], a2[q][1], a2[q][2]);
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < kSoftTPL; ++q)
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) acc[q][a] = a2[q][a].x + a2[q][a].y;
+            } else {
+                for (int b0 = 0; b0 < nsrc; b0 += 32) {
+                    batch[w][lane] = nxt;
+                    __syncwarp();
+                    if (b0 + 32 < nsrc) stage<T>(mom, moct, list[w][b0 + 32 + lane], cc, nxt);
+                    const int nb = min(32, nsrc - b0);
+                    for (int k = 0; k < nb; ++k) {
+                        const SRec<T> r = batch[w][k];
+#pragma unroll
+                        for (int q = 0; q < kSoftTPL; ++q)
+                            if (q < nq) soft_term_s<T>(r, ty[q][0], ty[q][1], ty[q][2], e2, acc[q][0], acc[q][1], acc[q][2]);
+                    }
+                    __syncwarp();
+                }
             }
 #pragma unroll
             for (int q = 0; q < kSoftTPL; ++q) {

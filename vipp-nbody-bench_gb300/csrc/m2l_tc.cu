@@ -81,9 +81,6 @@ constexpr int kDrainThreads = 128;  // warps 0-3
 #ifndef M2L_MIN_BLOCKS
 #define M2L_MIN_BLOCKS 1  // > 1 caps registers so the kernel fits beside P2P blocks
 #endif
-#ifndef M2L_CPASYNC
-#define M2L_CPASYNC 1  // A rows gathered by the loader warps' cp.async (16 B per lane) instead of TMA gather4
-#endif
 #ifndef M2L_WIDE_B
 #define M2L_WIDE_B 1
 #endif
@@ -201,7 +198,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
 
 // Four rows (r0..r3) of a 2-D tensor, columns [x, x + box width), into dst as
 // four consecutive swizzled 128-byte rows.
-#if !M2L_CPASYNC
 __device__ __forceinline__ void tma_gather4(void *dst, const CUtensorMap *map, int x, int r0, int r1, int r2, int r3,
                                             uint64_t *bar) {
     asm volatile(
@@ -209,17 +205,6 @@ __device__ __forceinline__ void tma_gather4(void *dst, const CUtensorMap *map, i
         "%5, %6}], [%7];" ::"r"(saddr(dst)),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(saddr(bar))
         : "memory");
-}
-#endif
-
-// 16 bytes global -> shared by the LSU (cp.async, L2 only), and the arrival on
-// an mbarrier once all of this thread's earlier cp.async copies have landed
-// (.noinc: the barrier's expected count includes these arrivals).
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_arrive(uint64_t *bar) {
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(saddr(bar)) : "memory");
 }
 
 // Shared-memory matrix descriptors. No swizzle: start address >> 4 (bits 0-13),
@@ -302,11 +287,9 @@ __device__ __forceinline__ int next_slot(int cls, int s) {
 template <int P, bool BF>
 __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
     k_m2l_tc(const __grid_constant__ CUtensorMap tmap, const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
-             const unsigned char *__restrict__ bimg, int rows_cap, float *__restrict__ Lx, TreeInfo *info_rw,
-             const unsigned char *__restrict__ ms_bytes, int row_pitch) {
+             const unsigned char *__restrict__ bimg, int rows_cap, float *__restrict__ Lx, TreeInfo *info_rw) {
     using C = TcCfg<P, BF>;
     constexpr int kGW = C::GATHERS / kLoaderWarps;  // gather4 copies per loader warp and step
-    static_assert(!M2L_CPASYNC || kGW <= 32, "the cp.async loaders take a quad's rows from lanes 0..kGW-1");
     extern __shared__ __align__(1024) unsigned char sm_raw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(sm_raw) + 1023) & ~uintptr_t(1023));
     uint64_t *full = reinterpret_cast<uint64_t *>(sm + C::STAGES * C::STAGE);
@@ -325,10 +308,7 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
     if (ntiles == 0 || static_cast<int>(blockIdx.x) >= ntiles) return;  // uniform: no barrier or TMEM touched yet
 
     if (tid == 0) {
-        // full: cp.async form, one arrival per loader thread plus the operator copy's;
-        // TMA form, one expect_tx arrival per loader warp
-        for (int s = 0; s < C::STAGES; ++s)
-            mbar_init(full + s, M2L_CPASYNC ? 32 * kLoaderWarps + 1 : kLoaderWarps), mbar_init(empty + s, 1);
+        for (int s = 0; s < C::STAGES; ++s) mbar_init(full + s, kLoaderWarps), mbar_init(empty + s, 1);
         for (int a = 0; a < 2; ++a) mbar_init(accum + a, 1), mbar_init(tfree + a, kDrainThreads);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -355,10 +335,8 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
         const int g0 = q * kGW + lane;
         const int quad = g0 % 32;
         const bool active = lane < kGW;
-#if !M2L_CPASYNC
         const bool do_hi = active && (kGW >= 64 || g0 < 32);
         const bool do_lo = !BF && active && (kGW >= 64 || g0 >= 32);
-#endif
         // operator bytes of chunk kc: [Bhi; Blo], or (bf16) Bhi alone for a chunk
         // of lo inputs only, whose MMAs read only the first N rows
         auto b_bytes = [](int kc) { return (BF && kc * C::KC >= C::K) ? 1u * C::B_BYTES : 2u * C::B_BYTES; };
@@ -394,43 +372,13 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                     int ok = 1;
                     if (lane == 0) {
                         if (use > 0 && !mbar_wait(empty + st, (use - 1) & 1, abort_flag)) ok = 0;
-                        if (ok && !M2L_CPASYNC)
-                            mbar_expect_tx(full + st, static_cast<unsigned>(kGW) * 512u + (q == 0 ? b_bytes(kc) : 0u));
+                        if (ok) mbar_expect_tx(full + st, static_cast<unsigned>(kGW) * 512u + (q == 0 ? b_bytes(kc) : 0u));
                     }
                     if (!__shfl_sync(0xffffffffu, ok, 0)) {
                         stop = true;
                         break;
                     }
                     unsigned char *stage = sm + st * C::STAGE;
-#if M2L_CPASYNC
-                    // the warp copies its kGW row quads one at a time, lane l the
-                    // 16 bytes c = l % 8 of row l / 8 of the quad, into the
-                    // 128B-swizzled K-major tile (chunk c of row r at c ^ (r % 8))
-                    {
-                        const int ri = lane >> 3, ch = lane & 7;
-                        for (int j = 0; j < kGW; ++j) {
-                            const int g = q * kGW + j;  // the quad lane j owns
-                            const int tq = g % 32;
-                            const bool lo_tile = !BF && g >= 32;  // tf32: quads 32..63 are the lo tile's
-                            int rsel = __shfl_sync(0xffffffffu, cur[0], j);
-#pragma unroll
-                            for (int i = 1; i < 4; ++i) {
-                                const int v = __shfl_sync(0xffffffffu, cur[i], j);
-                                if (ri == i) rsel = v;
-                            }
-                            const int row = rsel + (lo_tile ? rows_cap : 0);
-                            const int tr = 4 * tq + ri;  // row within the A tile
-                            unsigned char *dst = stage + (lo_tile ? C::A_BYTES : 0) + 128 * tr + 16 * (ch ^ (tr & 7));
-                            cp_async16(dst, ms_bytes + static_cast<size_t>(row) * row_pitch + kc * 128 + 16 * ch);
-                        }
-                        cp_async_arrive(full + st);
-                        if (q == 0 && lane == 0) {
-                            mbar_expect_tx(full + st, b_bytes(kc));
-                            bulk_g2s(stage + C::NA * C::A_BYTES,
-                                     bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::B_BYTES), b_bytes(kc), full + st);
-                        }
-                    }
-#else
                     if (do_hi)
                         tma_gather4(stage + 512 * quad, &tmap, kc * C::KC, cur[0], cur[1], cur[2], cur[3], full + st);
                     if (do_lo)
@@ -439,16 +387,12 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                     if (q == 0 && lane == 0)
                         bulk_g2s(stage + C::NA * C::A_BYTES, bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::B_BYTES),
                                  b_bytes(kc), full + st);
-#endif
                 }
 #pragma unroll
                 for (int i = 0; i < 4; ++i) cur[i] = nxt[i];
                 s = sn;
             }
         }
-#if M2L_CPASYNC
-        asm volatile("cp.async.wait_all;" ::: "memory");  // no copy of this thread outlives it
-#endif
     } else if (warp == kMmaWarp) {
         // ------------------------------------------------------------------- MMA
         if (lane == 0) {
@@ -471,10 +415,6 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                             stop = true;
                             break;
                         }
-#if M2L_CPASYNC
-                        // the A tiles were written through the generic proxy (cp.async); the MMAs read them through the async proxy
-                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-#endif
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         const unsigned char *stage = sm + st * C::STAGE;
                         const uint64_t ahi = sdesc_sw128(stage);
@@ -708,9 +648,7 @@ void launch(Workspace &ws) {
     const unsigned gs = capped_grid(ctas, 8 * ceil_div(ceil_div(ws.c_cap, 8), kRows));  // tiles
     k_m2l_tc<P, BF><<<gs, kThreads, C::SMEM, ws.st>>>(ws.tmap_ms, ws.info, ws.m2l_src,
                                                       reinterpret_cast<const unsigned char *>(ws.bimg),
-                                                      static_cast<int>(ws.ms_rows), static_cast<float *>(ws.Lexp), ws.info,
-                                                      reinterpret_cast<const unsigned char *>(ws.ms_tc),
-                                                      ws.ms_kp * static_cast<int>(sizeof(float)));
+                                                      static_cast<int>(ws.ms_rows), static_cast<float *>(ws.Lexp), ws.info);
     ws.launches += 3;
 }
 

@@ -22,9 +22,6 @@
 #include "direct.cuh"
 #include "workspace.cuh"
 
-#ifndef GB_P2P_PAIRED_REST
-#define GB_P2P_PAIRED_REST 1  // paired FP32 also for small chunks' lane groups and partial source batches
-#endif
 #ifndef GB_P2P_CARVEOUT_MAX
 #define GB_P2P_CARVEOUT_MAX 0
 #endif
@@ -194,34 +191,7 @@ __global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(c
                 }
                 bx = ax.x + ax.y, by = ay.x + ay.y, bz = az.x + az.y;
             } else if (tact) {
-#if GB_P2P_PAIRED_REST
-                // the other shapes (lane groups of small chunks, partial
-                // batches): this group's sources k and k + g on the paired
-                // instructions, an odd last one alone
-                float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
-                unsigned k = grp;
-                for (; k + g < now; k += 2 * g) {
-                    const float4 a = src[w][k], c = src[w][k + g];
-                    const float2 dx = __fadd2_rn(make_float2(a.x, c.x), ntx);
-                    const float2 dy = __fadd2_rn(make_float2(a.y, c.y), nty);
-                    const float2 dz = __fadd2_rn(make_float2(a.z, c.z), ntz);
-                    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-                    float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
-                    if (kNewton) {
-                        ri.x = ri.x * fmaf(-0.5f * r2.x * ri.x, ri.x, 1.5f);
-                        ri.y = ri.y * fmaf(-0.5f * r2.y * ri.y, ri.y, 1.5f);
-                    }
-                    if (!kSoft) ri.x = r2.x > 0.f ? ri.x : 0.f, ri.y = r2.y > 0.f ? ri.y : 0.f;
-                    const float2 f = __fmul2_rn(ri, __fmul2_rn(ri, ri));
-                    ax = __ffma2_rn(dx, f, ax);
-                    ay = __ffma2_rn(dy, f, ay);
-                    az = __ffma2_rn(dz, f, az);
-                }
-                bx = ax.x + ax.y, by = ay.x + ay.y, bz = az.x + az.y;
-                if (k < now) pair_f32<kNewton, kSoft>(src[w][k], tx, ty, tz, eps2, bx, by, bz);
-#else
                 for (unsigned k = grp; k < now; k += g) pair_f32<kNewton, kSoft>(src[w][k], tx, ty, tz, eps2, bx, by, bz);
-#endif
             }
             __syncwarp();
             float y = bx - kx, tt = sx + y;

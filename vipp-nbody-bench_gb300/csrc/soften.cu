@@ -352,8 +352,14 @@ __global__ void __launch_bounds__(128) k_soft_far(const int *__restrict__ leaves
 // current one is computed), and every lane applies the staged batch to up to
 // kTPL of the leaf's particles (targets lane, lane + 32, ...). Last, the
 // leaf-centre Taylor part is added and far = G (far + correction).
+#ifndef GB_SOFT_TPL
+#define GB_SOFT_TPL 4  // targets per lane per pass
+#endif
+#ifndef GB_SOFT_MIN_BLOCKS
+#define GB_SOFT_MIN_BLOCKS 1
+#endif
 constexpr int kSoftWarps = 4;
-constexpr int kSoftTPL = 4;                     // targets per lane per pass
+constexpr int kSoftTPL = GB_SOFT_TPL;
 constexpr int kSoftMaxSrc = 54 * 8 + 135 + 189;  // 756 records at most
 
 template <typename T>
@@ -447,7 +453,7 @@ __device__ __forceinline__ void soft_term_pair(const float4 *P, float2 ntx, floa
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kSoftWarps * 32) k_soft_near(
+__global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_near(
     const int *__restrict__ leaves, const unsigned *counts, const int *__restrict__ c_begin, const int *__restrict__ c_end,
     const int *__restrict__ c_level, const int *__restrict__ c_parent, const int *__restrict__ c_child,
     const double *__restrict__ c_ctr, const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,

@@ -249,7 +249,7 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
         unsigned char *a = nullptr, *b = nullptr, *t = nullptr;
         GB_TRY(dalloc(a, rec * c));
         GB_TRY(dalloc(b, 8 * rec * c));
-        GB_TRY(dalloc(t, 12 * (rec / 16) * c));
+        GB_TRY(dalloc(t, gb::soften_taylor_values() * (rec / 16) * c));
         dfree(ws.smom);
         dfree(ws.smom_oct);
         dfree(ws.staylor);

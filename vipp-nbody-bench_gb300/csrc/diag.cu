@@ -67,6 +67,7 @@ size_t diag_scratch_doubles() { return kSums * kRBlocks + kSums; }
 
 void potential_orig(Workspace &ws, double *phi_orig) {
     far_potential(ws, ws.phis + ws.n);
+    if (ws.accurate) soften_phi(ws, ws.phis + ws.n);
     near_potential(ws, ws.phis);
     // the far part carries G only in the accurate mode (the reference's far field has none)
     k_phi_finalize<<<(ws.n + 255) / 256, 256, 0, ws.st>>>(ws.perm, ws.n, ws.phis, ws.accurate ? ws.G : 1.0, phi_orig);

@@ -284,6 +284,27 @@ __device__ __forceinline__ void soft_term(const Mom<T> &r, T dx, T dy, T dz, T e
     az += a * dz + b * qz;
 }
 
+// Per-leaf values of the far levels: the correction's field at the leaf
+// centre (3), its Jacobian (9, row-major) and its potential there (1).
+constexpr int kTaylor = 13;
+
+// Softening-difference potential (no G; the far potential's convention, whose
+// gradient is the far field) of record r at offset d = z - x:
+//   M P(u) + 2 P''(u) d.Qd + P'(u) tr Q,  P = (u + e)^{-1/2} - u^{-1/2},
+//   P' = -F / 2, P'' = -F' / 2.
+template <typename T>
+__device__ __forceinline__ T soft_phi_term(const Mom<T> &r, T dx, T dy, T dz, T e2) {
+    const T u = dx * dx + dy * dy + dz * dz;
+    const T A = rsqrt_t<T>(u + e2), B = rsqrt_t<T>(u);
+    const T A2 = A * A, B2 = B * B, A3 = A2 * A, B3 = B2 * B;
+    const T F = A3 - B3, F1 = T(-1.5) * (A3 * A2 - B3 * B2);
+    const T qx = r.Q[0] * dx + r.Q[3] * dy + r.Q[4] * dz;
+    const T qy = r.Q[3] * dx + r.Q[1] * dy + r.Q[5] * dz;
+    const T qz = r.Q[4] * dx + r.Q[5] * dy + r.Q[2] * dz;
+    const T dqd = dx * qx + dy * qy + dz * qz;
+    return r.M * (A - B) - F1 * dqd - T(0.5) * F * r.tr;
+}
+
 // Offset of the source relative to the target leaf centre: (z - c).
 template <typename T>
 __device__ __forceinline__ void src_offset(const Mom<T> &r, const RelC<T> &cc, T s[3]) {
@@ -309,7 +330,7 @@ __global__ void __launch_bounds__(128) k_soft_far(const int *__restrict__ leaves
         const int c = leaves[li];
         if (c_level[c] < 2) continue;  // warp-uniform
         const RelC<T> cc = rel_centre<T>(c_ctr, c, info);
-        T v[12] = {};
+        T v[kTaylor] = {};
         int anc = c_level[c] >= 4 ? c_parent[c_parent[c]] : -1;
         while (anc >= 0 && c_level[anc] >= 2) {
             for (int s = lane; s < kM2LSlots; s += 32) {
@@ -320,6 +341,7 @@ __global__ void __launch_bounds__(128) k_soft_far(const int *__restrict__ leaves
                 T d[3];
                 src_offset<T>(r, cc, d);
                 soft_term<T>(r, d[0], d[1], d[2], e2, v[0], v[1], v[2]);
+                v[12] += soft_phi_term<T>(r, d[0], d[1], d[2], e2);
                 const T u = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
                 const T A = rsqrt_t<T>(u + e2), B = rsqrt_t<T>(u);
                 const T A2 = A * A, B2 = B * B, A3 = A2 * A, B3 = B2 * B;
@@ -332,13 +354,13 @@ __global__ void __launch_bounds__(128) k_soft_far(const int *__restrict__ leaves
             anc = c_parent[anc];
         }
 #pragma unroll
-        for (int k = 0; k < 12; ++k) v[k] = warp_sum(v[k]);
-        if (lane < 12) {
+        for (int k = 0; k < kTaylor; ++k) v[k] = warp_sum(v[k]);
+        if (lane < kTaylor) {
             T out = v[0];
 #pragma unroll
-            for (int k = 1; k < 12; ++k)
+            for (int k = 1; k < kTaylor; ++k)
                 if (lane == k) out = v[k];
-            taylor[static_cast<size_t>(c) * 12 + lane] = out;
+            taylor[static_cast<size_t>(c) * kTaylor + lane] = out;
         }
     }
 }
@@ -452,14 +474,17 @@ __device__ __forceinline__ void soft_term_pair(const float4 *P, float2 ntx, floa
     az = __ffma2_rn(sa, dz, __ffma2_rn(sb, qz, az));
 }
 
-template <typename T>
+// kPhi: the potential's correction instead (after an evaluation, for the
+// diagnostics): the scalar path, farphi[j] += correction (the far potential
+// is multiplied by G where near and far are added).
+template <typename T, bool kPhi = false>
 __global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_near(
     const int *__restrict__ leaves, const unsigned *counts, const int *__restrict__ c_begin, const int *__restrict__ c_end,
     const int *__restrict__ c_level, const int *__restrict__ c_parent, const int *__restrict__ c_child,
     const double *__restrict__ c_ctr, const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
     const Mom<T> *__restrict__ mom, const Mom<T> *__restrict__ moct, const T *__restrict__ taylor,
     const double *__restrict__ xs, const float4 *__restrict__ ph, const float4 *__restrict__ pl, unsigned n, T e2, T G,
-    T *__restrict__ far) {
+    T *__restrict__ far, double *__restrict__ farphi = nullptr) {
     __shared__ int list[kSoftWarps][kSoftMaxSrc + 32];
     __shared__ __align__(16) SRec<T> batch[kSoftWarps][32];  // FP32: the paired layout (put_paired)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -512,9 +537,9 @@ __global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_ne
         }
         if (lane < 32) list[w][nsrc + lane] = INT_MIN;  // pad the last batch
         __syncwarp();
-        T tl[12];
+        T tl[kTaylor];
 #pragma unroll
-        for (int k = 0; k < 12; ++k) tl[k] = taylor[static_cast<size_t>(c) * 12 + k];
+        for (int k = 0; k < kTaylor; ++k) tl[k] = taylor[static_cast<size_t>(c) * kTaylor + k];
         const int b = c_begin[c], e = c_end[c];
         for (int j0 = b; j0 < e; j0 += 32 * kSoftTPL) {
             const int nq = min(kSoftTPL, (e - j0 + 31) / 32);  // warp-uniform
@@ -528,7 +553,7 @@ __global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_ne
             }
             SRec<T> nxt;
             if (nsrc > 0) stage<T>(mom, moct, list[w][lane], cc, nxt);
-            if constexpr (sizeof(T) == 4) {
+            if constexpr (sizeof(T) == 4 && !kPhi) {
                 float *pb = reinterpret_cast<float *>(batch[w]);
                 const float4 *pb4 = reinterpret_cast<const float4 *>(pb);
                 const float2 e22 = make_float2(e2, e2);
@@ -565,8 +590,17 @@ __global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_ne
                     for (int k = 0; k < nb; ++k) {
                         const SRec<T> r = batch[w][k];
 #pragma unroll
-                        for (int q = 0; q < kSoftTPL; ++q)
-                            if (q < nq) soft_term_s<T>(r, ty[q][0], ty[q][1], ty[q][2], e2, acc[q][0], acc[q][1], acc[q][2]);
+                        for (int q = 0; q < kSoftTPL; ++q) {
+                            if (q >= nq) continue;
+                            if (kPhi) {
+                                Mom<T> m{};
+                                m.M = r.M, m.tr = r.tr;
+                                m.Q[0] = r.q0, m.Q[1] = r.q1, m.Q[2] = r.q2, m.Q[3] = r.q3, m.Q[4] = r.q4, m.Q[5] = r.q5;
+                                acc[q][0] += soft_phi_term<T>(m, r.dx - ty[q][0], r.dy - ty[q][1], r.dz - ty[q][2], e2);
+                            } else {
+                                soft_term_s<T>(r, ty[q][0], ty[q][1], ty[q][2], e2, acc[q][0], acc[q][1], acc[q][2]);
+                            }
+                        }
                     }
                     __syncwarp();
                 }
@@ -574,7 +608,11 @@ __global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_ne
 #pragma unroll
             for (int q = 0; q < kSoftTPL; ++q) {
                 const int j = j0 + 32 * q + lane;
-                if (q < nq && j < e) {
+                if (kPhi && q < nq && j < e) {
+                    const T *y = ty[q];
+                    // far levels: the centre's value and gradient (the field: a = grad phi here)
+                    farphi[j] += static_cast<double>(acc[q][0] + tl[12] + tl[0] * y[0] + tl[1] * y[1] + tl[2] * y[2]);
+                } else if (q < nq && j < e) {
                     const T *y = ty[q];
                     const T ax = acc[q][0] + tl[0] + tl[3] * y[0] + tl[4] * y[1] + tl[5] * y[2];
                     const T ay = acc[q][1] + tl[1] + tl[6] * y[0] + tl[7] * y[1] + tl[8] * y[2];
@@ -613,6 +651,28 @@ void launch_soften(Workspace &ws) {
 }
 
 }  // namespace
+
+template <typename T>
+void launch_soften_phi(Workspace &ws, double *farphi) {
+    const unsigned gw = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));
+    k_soft_near<T, true><<<gw, kSoftWarps * 32, 0, ws.st>>>(
+        ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_parent, ws.c_child, ws.c_ctr, ws.info, ws.m2l_src,
+        static_cast<const Mom<T> *>(ws.smom), static_cast<const Mom<T> *>(ws.smom_oct), static_cast<const T *>(ws.staylor),
+        ws.xs, ws.ph, ws.pl, ws.n, static_cast<T>(ws.eps * ws.eps), static_cast<T>(ws.G), nullptr, farphi);
+    ws.launches += 1;
+}
+
+// Accurate mode, after an evaluation (its moments and leaf-centre terms are
+// still those of the current positions): farphi[j] += the potential's
+// softening correction (tree order, no G).
+void soften_phi(Workspace &ws, double *farphi) {
+    if (ws.mixed)
+        launch_soften_phi<float>(ws, farphi);
+    else
+        launch_soften_phi<double>(ws, farphi);
+}
+
+size_t soften_taylor_values() { return kTaylor; }
 
 size_t soften_cell_bytes(bool mixed) {
     const size_t t = mixed ? sizeof(float) : sizeof(double);

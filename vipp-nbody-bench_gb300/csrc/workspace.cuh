@@ -95,7 +95,7 @@ struct Workspace {
     int *p2p_own = nullptr, *p2p_cnt = nullptr;  // [C][27], [C]
     void *smom = nullptr;       // accurate mode: [C] moment records (soften.cu)
     void *smom_oct = nullptr;   // [C][8] octant moment records of the leaves
-    void *staylor = nullptr;    // [C][12] leaf-centre value and J of the far levels' correction
+    void *staylor = nullptr;    // [C][13] leaf-centre value, J and potential of the far levels' correction
     unsigned soft_cap = 0;      // cells the three are sized for (0: not allocated)
     bool soft_mixed = false;    // their element type
     int *coll = nullptr, *coll_cnt = nullptr;    // [C][27], [C]
@@ -170,6 +170,8 @@ int m2l_tc_row_floats(int p);
 const char *m2l_tc_encode(Workspace &ws);     // (re)build tmap_ms; nullptr or an error message
 void downward_pass(Workspace &ws);            // L2L + L2P into far
 void soften_pass(Workspace &ws);              // accurate mode: far = G (far + softening correction)
+void soften_phi(Workspace &ws, double *farphi); // accurate mode: the far potential's correction (tree order)
+size_t soften_taylor_values();                // per-leaf values of the far levels' correction
 size_t soften_cell_bytes(bool mixed);         // bytes of one moment record
 void p2p_pass(Workspace &ws, unsigned per_sm); // near-field kernel over the queue, per_sm blocks per SM
 void p2p_finish(Workspace &ws);               // add the slices of split items: near complete

@@ -375,13 +375,17 @@ __global__ void __launch_bounds__(128) k_soft_far(const int *__restrict__ leaves
 // kTPL of the leaf's particles (targets lane, lane + 32, ...). Last, the
 // leaf-centre Taylor part is added and far = G (far + correction).
 #ifndef GB_SOFT_TPL
-#define GB_SOFT_TPL 4  // targets per lane per pass
+#define GB_SOFT_TPL 2  // targets per lane per pass (measured at 4M, p = 10: 2 -> 38.4, 4 -> 40.8, 8 -> 51.7 ms per step)
+#endif
+#ifndef GB_SOFT_UNROLL
+#define GB_SOFT_UNROLL 1  // record pairs per unrolled step of the FP32 loop
 #endif
 #ifndef GB_SOFT_MIN_BLOCKS
 #define GB_SOFT_MIN_BLOCKS 1
 #endif
 constexpr int kSoftWarps = 4;
 constexpr int kSoftTPL = GB_SOFT_TPL;
+constexpr int kSoftUnroll = GB_SOFT_UNROLL;
 constexpr int kSoftMaxSrc = 54 * 8 + 135 + 189;  // 756 records at most
 
 template <typename T>
@@ -569,6 +573,7 @@ __global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_ne
                     if (b0 + 32 < nsrc) stage<T>(mom, moct, list[w][b0 + 32 + lane], cc, nxt);
                     // a padded batch's tail holds massless records whose terms are exactly zero
                     const int npairs = (min(32, nsrc - b0) + 1) >> 1;
+#pragma unroll kSoftUnroll
                     for (int k = 0; k < npairs; ++k) {
 #pragma unroll
                         for (int q = 0; q < kSoftTPL; ++q)

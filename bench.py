@@ -48,6 +48,10 @@ import numpy as np
 
 # many concurrent streams in the batching form: one hardware queue each (set before CUDA starts)
 os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+# the library's GB300 tuning cache (vipp_gb300.autotune's measured entries),
+# applied at upload unless the caller names another file or --no-tuning-cache
+SHIPPED_TUNING = os.path.join(os.path.dirname(os.path.abspath(__file__)), "vipp-nbody-bench_gb300", "vipp_gb300",
+                              "tuning_gb300.txt")
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "vipp-nbody-bench_gb300")
@@ -162,6 +166,7 @@ def accurate_measure(x, v, args, local, tg, ad):
         with vipp_gb300.Solver(p=args.acc_p, s=args.s, eps=args.eps, G=1.0, m=m, precision=prec, device=local,
                                flags=flags, mode="accurate") as sa:
             sa.preprocess(x, v)
+            tun = sa.tuning()
             a = sa.accel()
             e = np.linalg.norm(a[tg] - ad, axis=1) / np.linalg.norm(ad, axis=1)
             sa.solve(args.dt)  # captures the step graph
@@ -183,11 +188,11 @@ def accurate_measure(x, v, args, local, tg, ad):
                      "rms_rel_err_vs_fp64_direct": float(math.sqrt(np.mean(e * e))),
                      "max_rel_err_vs_fp64_direct": float(e.max()), "error_sample": int(len(tg)),
                      "m2l_split": ("bf16 hi/lo" if flags else "3 x tf32") if prec == "mixed" else "fp64 cuda cores",
-                     "timing": f"CUDA events around {args.acc_steps} steps on the solver's stream"}
+                     "timing": f"CUDA events around {args.acc_steps} steps on the solver's stream", "tuning": tun}
         if drift is not None:
             out[prec]["energy_rel_drift"] = drift
-            out[prec]["energy_note"] = ("potential of the reference's far field (unsoftened expansion) times G "
-                                        "plus the FP64 softened near field")
+            out[prec]["energy_note"] = ("potential of the accurate mode: far field times G with its softening "
+                                        "correction, plus the FP64 softened near field")
         if kt:
             out[prec]["kernel_ms_per_step"] = kt
     out["mixed_over_plain"] = out["mixed"]["value"] / out["fp64"]["value"]
@@ -366,6 +371,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-alt", action="store_true", help="skip the timing of the other M2L split")
     ap.add_argument("--no-accurate", action="store_true", help="skip the accurate-mode line (mixed and plain FP64)")
     ap.add_argument("--tune", action="store_true", help="run the autotuner on the workload; report tuned vs default")
+    ap.add_argument("--no-tuning-cache", action="store_true",
+                    help="ignore the library's tuning cache (vipp_gb300/tuning_gb300.txt): every line at the defaults")
     ap.add_argument("--tune-out", default=None, help="append the tuned entry to this tuning cache file")
     ap.add_argument("--drift-steps", type=int, default=None,
                     help="untimed steps of the total-energy drift run (default: the 4M Plummer configuration's 100; 0 skips)")
@@ -393,6 +400,10 @@ def main():
         return
 
     ws, rank, local = dist_setup()
+    if args.no_tuning_cache:
+        os.environ.pop("VIPP_GB_TUNE_FILE", None)
+    else:
+        os.environ.setdefault("VIPP_GB_TUNE_FILE", SHIPPED_TUNING)
     import torch
 
     if ws > 1:
@@ -413,6 +424,7 @@ def main():
     sol = vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision=args.precision, device=local,
                             flags=args.flags)
     sol.preprocess(x, v)
+    tuning_used = sol.tuning()
     for _ in range(args.warmup):
         sol.solve(args.dt)
     sol.sync()
@@ -666,6 +678,7 @@ def main():
            "l2": f"inputs larger than L2 (state {48 * n / 1e6:.0f} MB, per-step working set > 1 GB)",
            "tree": {k: st[k] for k in ("ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges")},
            "initial_conditions_s": round(t_ic, 3),
+           "tuning_cache": os.environ.get("VIPP_GB_TUNE_FILE"), "tuning": tuning_used,
            "kernel_ms_per_step": kt_ms, **acc_info, "energy": energy, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * elapsed / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,

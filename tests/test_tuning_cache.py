@@ -62,3 +62,17 @@ def test_missing_file_is_an_error(tmp_path):
     vipp_gb300.load()
     with pytest.raises(vipp_gb300.GB300Error):
         vipp_gb300.tuning_lookup(str(tmp_path / "none.txt"), 1000, 4)
+
+
+def test_shipped_cache_parses():
+    """The library's GB300 cache (vipp_gb300/tuning_gb300.txt, which bench.py
+    applies by default) is well formed and holds the headline buckets."""
+    import os
+    vipp_gb300.load()
+    path = os.path.join(os.path.dirname(vipp_gb300.__file__), "tuning_gb300.txt")
+    entries = autotune.read_cache(path)
+    assert len(entries) >= 3
+    acc = vipp_gb300.tuning_lookup(path, 1 << 22, 10, "mixed", "accurate", 0)
+    assert acc is not None and acc["leaf_s"] >= 64
+    assert vipp_gb300.tuning_lookup(path, 1 << 22, 8, "mixed", "ref", vipp_gb300.FLAG_M2L_BF16) == \
+        vipp_gb300.TUNING_DEFAULT

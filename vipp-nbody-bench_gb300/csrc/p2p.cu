@@ -97,113 +97,6 @@ __device__ __forceinline__ void pair_f32(const float4 s, float tx, float ty, flo
     bz = fmaf(dz, f, bz);
 }
 
-#ifndef GB_P2P_DUAL
-#define GB_P2P_DUAL 0  // a warp takes two work items; two full chunks of one leaf run as one pass, two targets per lane
-#endif
-constexpr unsigned kTake = GB_P2P_DUAL ? 2u : 1u;
-
-// Two full 32-target chunks (wa, wb) of one leaf, each over the leaf's whole
-// source list: the source batches are staged once and every lane accumulates
-// targets wa.t0 + lane and wb.t0 + lane (two independent dependency chains).
-template <bool kNewton, bool kSoft>
-__device__ __forceinline__ void p2p_dual(const int4 wa, const int4 wb, int lane, int w, const int *__restrict__ leaves,
-                                         const double *__restrict__ c_ctr, const TreeInfo *__restrict__ info,
-                                         const unsigned *__restrict__ rng_off, const unsigned *__restrict__ rng_len,
-                                         const uint2 *__restrict__ ranges, const float4 *__restrict__ ph,
-                                         const float4 *__restrict__ pl, const unsigned *__restrict__ src_total,
-                                         float4 *sxy, float2 *sz2, float Gm, float eps2, float *__restrict__ nearv,
-                                         unsigned n) {
-    const int li = wa.x;
-    const RootC cc = leaf_centre(c_ctr, leaves[li], info);
-    const int ia = wa.y + lane, ib = wb.y + lane;
-    float txa, tya, tza, txb, tyb, tzb;
-    {
-        const float4 h = ph[ia], l = pl[ia];
-        txa = (h.x - cc.hx) + (l.x - cc.lx), tya = (h.y - cc.hy) + (l.y - cc.ly), tza = (h.z - cc.hz) + (l.z - cc.lz);
-        const float4 h2 = ph[ib], l2 = pl[ib];
-        txb = (h2.x - cc.hx) + (l2.x - cc.lx), tyb = (h2.y - cc.hy) + (l2.y - cc.ly), tzb = (h2.z - cc.hz) + (l2.z - cc.lz);
-    }
-    float sxa = 0, sya = 0, sza = 0, kxa = 0, kya = 0, kza = 0;
-    float sxb = 0, syb = 0, szb = 0, kxb = 0, kyb = 0, kzb = 0;
-    float *pxy = reinterpret_cast<float *>(sxy);
-    float *pz = reinterpret_cast<float *>(sz2);
-    Cursor cur;
-    cur.start(ranges + rng_off[li], rng_len[li], 0u, src_total[li]);
-    float4 h = make_float4(0, 0, 0, 0), l = h;
-    unsigned cnt = 0;
-    if (cur.valid()) {
-        cnt = cur.count();
-        if (static_cast<unsigned>(lane) < cnt) h = ph[cur.b + lane], l = pl[cur.b + lane];
-    }
-    const float2 ntxa = make_float2(-txa, -txa), ntya = make_float2(-tya, -tya), ntza = make_float2(-tza, -tza);
-    const float2 ntxb = make_float2(-txb, -txb), ntyb = make_float2(-tyb, -tyb), ntzb = make_float2(-tzb, -tzb);
-    const float2 e2 = make_float2(eps2, eps2);
-    auto kahan = [](float b, float &sm, float &k) {
-        const float y = b - k, t = sm + y;
-        k = (t - sm) - y, sm = t;
-    };
-    while (cnt) {
-        // a partial batch is padded with far-away sources whose terms are zero
-        float qx = 1e30f, qy = 0.f, qz = 0.f;
-        if (static_cast<unsigned>(lane) < cnt)
-            qx = (h.x - cc.hx) + (l.x - cc.lx), qy = (h.y - cc.hy) + (l.y - cc.ly), qz = (h.z - cc.hz) + (l.z - cc.lz);
-        pxy[(lane >> 1) * 4 + (lane & 1)] = qx;
-        pxy[(lane >> 1) * 4 + 2 + (lane & 1)] = qy;
-        pz[(lane >> 1) * 2 + (lane & 1)] = qz;
-        __syncwarp();
-        cur.advance();
-        cnt = 0;
-        if (cur.valid()) {
-            cnt = cur.count();
-            if (static_cast<unsigned>(lane) < cnt) h = ph[cur.b + lane], l = pl[cur.b + lane];
-        }
-        float2 axa = make_float2(0.f, 0.f), aya = axa, aza = axa, axb = axa, ayb = axa, azb = axa;
-#pragma unroll
-        for (int m = 0; m < 16; ++m) {
-            const float4 q = sxy[m];
-            const float2 qz2 = sz2[m];
-            {
-                const float2 dx = __fadd2_rn(make_float2(q.x, q.y), ntxa);
-                const float2 dy = __fadd2_rn(make_float2(q.z, q.w), ntya);
-                const float2 dz = __fadd2_rn(qz2, ntza);
-                const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-                float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
-                if (kNewton) {
-                    ri.x = ri.x * fmaf(-0.5f * r2.x * ri.x, ri.x, 1.5f);
-                    ri.y = ri.y * fmaf(-0.5f * r2.y * ri.y, ri.y, 1.5f);
-                }
-                if (!kSoft) ri.x = r2.x > 0.f ? ri.x : 0.f, ri.y = r2.y > 0.f ? ri.y : 0.f;
-                const float2 f = __fmul2_rn(ri, __fmul2_rn(ri, ri));
-                axa = __ffma2_rn(dx, f, axa);
-                aya = __ffma2_rn(dy, f, aya);
-                aza = __ffma2_rn(dz, f, aza);
-            }
-            {
-                const float2 dx = __fadd2_rn(make_float2(q.x, q.y), ntxb);
-                const float2 dy = __fadd2_rn(make_float2(q.z, q.w), ntyb);
-                const float2 dz = __fadd2_rn(qz2, ntzb);
-                const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-                float2 ri = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
-                if (kNewton) {
-                    ri.x = ri.x * fmaf(-0.5f * r2.x * ri.x, ri.x, 1.5f);
-                    ri.y = ri.y * fmaf(-0.5f * r2.y * ri.y, ri.y, 1.5f);
-                }
-                if (!kSoft) ri.x = r2.x > 0.f ? ri.x : 0.f, ri.y = r2.y > 0.f ? ri.y : 0.f;
-                const float2 f = __fmul2_rn(ri, __fmul2_rn(ri, ri));
-                axb = __ffma2_rn(dx, f, axb);
-                ayb = __ffma2_rn(dy, f, ayb);
-                azb = __ffma2_rn(dz, f, azb);
-            }
-        }
-        __syncwarp();
-        kahan(axa.x + axa.y, sxa, kxa), kahan(aya.x + aya.y, sya, kya), kahan(aza.x + aza.y, sza, kza);
-        kahan(axb.x + axb.y, sxb, kxb), kahan(ayb.x + ayb.y, syb, kyb), kahan(azb.x + azb.y, szb, kzb);
-    }
-    sxa -= kxa, sya -= kya, sza -= kza, sxb -= kxb, syb -= kyb, szb -= kzb;
-    nearv[ia] = Gm * sxa, nearv[n + ia] = Gm * sya, nearv[2 * static_cast<size_t>(n) + ia] = Gm * sza;
-    nearv[ib] = Gm * sxb, nearv[n + ib] = Gm * syb, nearv[2 * static_cast<size_t>(n) + ib] = Gm * szb;
-}
-
 #ifndef GB_P2P_MIN_BLOCKS
 #define GB_P2P_MIN_BLOCKS 8  // 8 resident blocks per SM (62 registers, no spills): measured 7% faster than 6
 #endif
@@ -226,24 +119,10 @@ __global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(c
     float *pxy = reinterpret_cast<float *>(srcxy[w]);
     float *pz = reinterpret_cast<float *>(srcz[w]);
     while (true) {
-        unsigned ci0 = 0;
-        if (lane == 0) ci0 = atomicAdd(queue, kTake);
-        ci0 = __shfl_sync(0xffffffffu, ci0, 0);
-        if (ci0 >= nch) break;
-#if GB_P2P_DUAL
-        if (ci0 + 1 < nch) {
-            const int4 wa = chunks[ci0], wb = chunks[ci0 + 1];
-            // two full chunks of one leaf over its whole source list: one pass,
-            // two targets per lane
-            if (wa.x == wb.x && item_nt(wa.z) == 32 && item_nt(wb.z) == 32 && item_nslices(wa.z) == 1 &&
-                item_nslices(wb.z) == 1) {
-                p2p_dual<kNewton, kSoft>(wa, wb, lane, w, leaves, c_ctr, info, rng_off, rng_len, ranges, ph, pl, src_total,
-                                         srcxy[w], srcz[w], Gm, eps2, nearv, n);
-                continue;
-            }
-        }
-#endif
-        for (unsigned ci = ci0; ci < ci0 + kTake && ci < nch; ++ci) {
+        unsigned ci = 0;
+        if (lane == 0) ci = atomicAdd(queue, 1u);
+        ci = __shfl_sync(0xffffffffu, ci, 0);
+        if (ci >= nch) break;
         const Item it(chunks[ci], src_total);
         const int nt = it.nt;
         const int g = 32 / nt;
@@ -339,7 +218,6 @@ __global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(c
                 float *o = part + static_cast<size_t>(it.pslot) * 96;
                 o[t] = sx, o[32 + t] = sy, o[64 + t] = sz;
             }
-        }
         }
     }
 }

@@ -1,8 +1,7 @@
-"""Host input/output paths of gb_upload / gb_download: pinned, mapped host
-buffers (cudaMallocHost-style, here torch's pinned memory) are read and
-written by the layout kernels directly, other host memory goes through the
-device staging buffer. Both must give the same state bit for bit, through a
-few RK4 steps."""
+"""Host buffers of gb_upload / gb_download: pinned host memory (torch's
+pinned tensors through the raw-pointer entry points, as bench.py's e2e line
+uses them) and pageable numpy arrays must give the same state bit for bit,
+through a few RK4 steps with a download and upload between them."""
 import numpy as np
 import pytest
 

@@ -439,20 +439,6 @@ int run_with_capacity(gb_ctx *ctx, F &&f) {
     return GB_ERR_CAPACITY;
 }
 
-// A device address for caller memory the GPU can read and write directly
-// (pinned and mapped host memory: cudaMallocHost / cudaHostAlloc /
-// cudaHostRegister buffers; on a Grace host these are reached over NVLink-C2C),
-// or nullptr for other memory, which goes through the staging buffer.
-double *mapped_host(const double *p) {
-    cudaPointerAttributes at{};
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();  // the query's own error: not a fault of the context
-        return nullptr;
-    }
-    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
-    return static_cast<double *>(at.devicePointer);
-}
-
 int initial_capacity(gb_ctx *ctx) {
     gb::Workspace &ws = ctx->ws;
     const unsigned n = ws.n;
@@ -742,20 +728,10 @@ int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
     if (rc) return rc;
     ws.n = nn;
     if (nn) {
-        // mapped host buffers are read by the layout kernel itself (one pass);
-        // others are copied to the staging buffer first
-        if (const double *mx = mapped_host(x_aos)) {
-            gb::aos_to_soa(ws, mx, ws.x, nn);
-        } else {
-            GB_TRY(cudaMemcpyAsync(ws.staging, x_aos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ws.st));
-            gb::aos_to_soa(ws, ws.staging, ws.x, nn);
-        }
-        if (const double *mv = mapped_host(v_aos)) {
-            gb::aos_to_soa(ws, mv, ws.v, nn);
-        } else {
-            GB_TRY(cudaMemcpyAsync(ws.staging, v_aos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ws.st));
-            gb::aos_to_soa(ws, ws.staging, ws.v, nn);
-        }
+        GB_TRY(cudaMemcpyAsync(ws.staging, x_aos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ws.st));
+        gb::aos_to_soa(ws, ws.staging, ws.x, nn);
+        GB_TRY(cudaMemcpyAsync(ws.staging, v_aos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ws.st));
+        gb::aos_to_soa(ws, ws.staging, ws.v, nn);
         rc = initial_capacity(ctx);
         if (rc) return rc;
     }
@@ -832,25 +808,16 @@ int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos) {
     GB_TRY(cudaSetDevice(ctx->cfg.device));
     gb::Workspace &ws = ctx->ws;
     if (ws.n == 0) return GB_OK;
-    // mapped host buffers are written by the layout kernel itself
     if (x_aos) {
-        if (double *mx = mapped_host(x_aos)) {
-            gb::soa_to_aos(ws, ws.x, mx, ws.n);
-        } else {
-            gb::soa_to_aos(ws, ws.x, ws.staging, ws.n);
-            GB_TRY(cudaMemcpyAsync(x_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
-            GB_TRY(cudaStreamSynchronize(ws.st));
-        }
+        gb::soa_to_aos(ws, ws.x, ws.staging, ws.n);
+        GB_TRY(cudaMemcpyAsync(x_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
+        GB_TRY(cudaStreamSynchronize(ws.st));
     }
     if (v_aos) {
-        if (double *mv = mapped_host(v_aos)) {
-            gb::soa_to_aos(ws, ws.v, mv, ws.n);
-        } else {
-            gb::soa_to_aos(ws, ws.v, ws.staging, ws.n);
-            GB_TRY(cudaMemcpyAsync(v_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
-        }
+        gb::soa_to_aos(ws, ws.v, ws.staging, ws.n);
+        GB_TRY(cudaMemcpyAsync(v_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
+        GB_TRY(cudaStreamSynchronize(ws.st));
     }
-    GB_TRY(cudaStreamSynchronize(ws.st));
     GB_TRY(cudaGetLastError());
     return GB_OK;
 }

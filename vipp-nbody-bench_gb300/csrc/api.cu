@@ -164,7 +164,6 @@ int ensure_particles(gb_ctx *ctx, unsigned n) {
     GB_TRY(dalloc(ws.vo, n3));
     GB_TRY(dalloc(ws.acc, n3));
     GB_TRY(dalloc(ws.staging, n3));
-    GB_TRY(dalloc(ws.staging2, n3));
     GB_TRY(dalloc(ws.keys0, cap));
     GB_TRY(dalloc(ws.keys1, cap));
     GB_TRY(dalloc(ws.perm0, cap));
@@ -658,7 +657,7 @@ void gb_destroy(gb_ctx *ctx) {
     if (ws.st) cudaStreamSynchronize(ws.st);
     collect_timers(ctx);
     for (auto e : ctx->free_events) cudaEventDestroy(e);
-    void *bufs[] = {ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.acc, ws.phi, ws.staging, ws.staging2, ws.bbox_part, ws.keys0, ws.keys1,
+    void *bufs[] = {ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, ws.acc, ws.phi, ws.staging, ws.bbox_part, ws.keys0, ws.keys1,
                     ws.perm0, ws.perm1, ws.inv, ws.xs, ws.ph, ws.pl, ws.nearf, ws.farf, ws.phis, ws.cnt, ws.off, ws.ent0, ws.ent1,
                     ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
@@ -729,18 +728,10 @@ int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
     if (rc) return rc;
     ws.n = nn;
     if (nn) {
-        // positions on the context's stream, velocities on its second one at
-        // the same time (two copy engines), after all earlier work
-        GB_TRY(cudaEventRecord(ws.ev_fork, ws.st));
-        GB_TRY(cudaStreamWaitEvent(ws.st2, ws.ev_fork, 0));
         GB_TRY(cudaMemcpyAsync(ws.staging, x_aos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ws.st));
         gb::aos_to_soa(ws, ws.staging, ws.x, nn);
-        GB_TRY(cudaMemcpyAsync(ws.staging2, v_aos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ws.st2));
-        std::swap(ws.st, ws.st2);
-        gb::aos_to_soa(ws, ws.staging2, ws.v, nn);
-        std::swap(ws.st, ws.st2);
-        GB_TRY(cudaEventRecord(ws.ev_join, ws.st2));
-        GB_TRY(cudaStreamWaitEvent(ws.st, ws.ev_join, 0));
+        GB_TRY(cudaMemcpyAsync(ws.staging, v_aos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ws.st));
+        gb::aos_to_soa(ws, ws.staging, ws.v, nn);
         rc = initial_capacity(ctx);
         if (rc) return rc;
     }
@@ -817,21 +808,16 @@ int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos) {
     GB_TRY(cudaSetDevice(ctx->cfg.device));
     gb::Workspace &ws = ctx->ws;
     if (ws.n == 0) return GB_OK;
-    // positions on the context's stream, velocities on its second one at the same time
-    GB_TRY(cudaEventRecord(ws.ev_fork, ws.st));
-    GB_TRY(cudaStreamWaitEvent(ws.st2, ws.ev_fork, 0));
     if (x_aos) {
         gb::soa_to_aos(ws, ws.x, ws.staging, ws.n);
         GB_TRY(cudaMemcpyAsync(x_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
+        GB_TRY(cudaStreamSynchronize(ws.st));
     }
     if (v_aos) {
-        std::swap(ws.st, ws.st2);
-        gb::soa_to_aos(ws, ws.v, ws.staging2, ws.n);
-        std::swap(ws.st, ws.st2);
-        GB_TRY(cudaMemcpyAsync(v_aos, ws.staging2, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st2));
+        gb::soa_to_aos(ws, ws.v, ws.staging, ws.n);
+        GB_TRY(cudaMemcpyAsync(v_aos, ws.staging, sizeof(double) * 3 * ws.n, cudaMemcpyDeviceToHost, ws.st));
+        GB_TRY(cudaStreamSynchronize(ws.st));
     }
-    GB_TRY(cudaStreamSynchronize(ws.st2));
-    GB_TRY(cudaStreamSynchronize(ws.st));
     GB_TRY(cudaGetLastError());
     return GB_OK;
 }

@@ -64,8 +64,7 @@ struct Workspace {
     // state (original order)
     double *x = nullptr, *v = nullptr, *x0 = nullptr, *v0 = nullptr, *xo = nullptr, *vo = nullptr, *acc = nullptr;
     double *phi = nullptr;  // optional potential (original order)
-    double *staging = nullptr;  // AoS staging [3N] for host copies (positions)
-    double *staging2 = nullptr; // the velocities', copied on the second stream at the same time
+    double *staging = nullptr;  // AoS staging [3N] for host copies
     double *bbox_part = nullptr; // [6 * 2 * num_sms] bounding-box partials
 
     // per evaluation, tree order

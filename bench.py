@@ -95,31 +95,39 @@ def make_workload(args, rank=0, device=None):
 M2L_BF16_TRAFFIC = 139474944 + 19757568
 
 
-def batch_measure(steps=50, warmup=2, nsys=512, seed=3, sample=32, flags=0):
+def batch_measure(steps=50, warmup=2, nsys=512, seed=3, sample=32, flags=0, form="forest"):
     """Batching form: nsys Plummer systems, N log-uniform in [1024, 65536],
     scale radius uniform in [0.5, 2] (positions x R, velocities x R^-1/2), total
     mass 1 each, eps = 0.01, p = 6, s = 32, mixed precision, dt = 1e-3, all
-    advanced together (gb_batch_rk4_step). Wall clock per step (a batch step
-    returns after every system's step has finished); error vs the FP64 direct
-    sum on `sample` systems."""
+    advanced together (gb_batch_rk4_step). form "forest": one context, one
+    launch per kernel class over all systems; "contexts": one context and step
+    graph per system. Wall clock per step (a batch step returns after every
+    system's step has finished); error vs the FP64 direct sum on `sample`
+    systems."""
     import vipp_gb300
     rng = np.random.default_rng(seed)
     sizes = np.rint(np.exp(rng.uniform(math.log(1024), math.log(65536), nsys))).astype(np.int64)
+    if form == "contexts":
+        flags |= vipp_gb300.FLAG_BATCH_CONTEXTS
     t0 = time.perf_counter()
     b = vipp_gb300.Batch(sizes, p=6, s=32, eps=0.01, masses=1.0 / sizes, precision="mixed", flags=flags)
     b.init_plummer(seed=seed, r_lo=0.5, r_hi=2.0)  # every system drawn on the GPU
     setup = time.perf_counter() - t0
     for _ in range(warmup):
         b.step(1e-3)
+    l0 = b.launch_count()
     t0 = time.perf_counter()
     for _ in range(steps):
         b.step(1e-3)
     dt_wall = time.perf_counter() - t0
+    launches = (b.launch_count() - l0) / steps
+    st = b.stats()
     errs = []
     xb, _ = b.download()
+    acc = b.accel() if b.forest else None
     off = np.concatenate([[0], np.cumsum(sizes)])
     for k in np.linspace(0, nsys - 1, sample).astype(int):
-        a = b.system_accel(int(k))
+        a = acc[off[k]:off[k + 1]] if acc is not None else b.system_accel(int(k))
         with vipp_gb300.Solver(p=6, s=32, eps=0.01, m=1.0 / sizes[k], precision="fp64") as sd:
             sd.preprocess(xb[off[k]:off[k + 1]], np.zeros((sizes[k], 3)))
             ad = sd.direct_accel()
@@ -128,8 +136,11 @@ def batch_measure(steps=50, warmup=2, nsys=512, seed=3, sample=32, flags=0):
     b.close()
     n = int(sizes.sum())
     return {"workload": f"{nsys} Plummer systems, N log-uniform in [1024, 65536] (seed {seed}), R in [0.5, 2] (systems "
-                        "drawn on the GPU), p=6 s=32 eps=0.01 mixed, dt=1e-3", "value": n * steps / dt_wall, "unit": UNIT, "n_total": n,
+                        "drawn on the GPU), p=6 s=32 eps=0.01 mixed, dt=1e-3", "form": form,
+            "value": n * steps / dt_wall, "unit": UNIT, "n_total": n,
             "systems": nsys, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * dt_wall / steps,
+            "launches_per_step": launches, "tree": {k: st[k] for k in ("ncells", "nleaves", "depth", "m2l_pairs",
+                                                                        "p2p_pairs")},
             "setup_s": setup, "rms_rel_err_vs_fp64_direct_per_system": errs,
             "timing": "host wall clock per gb_batch_rk4_step (it returns after all systems' steps)"}
 
@@ -594,6 +605,9 @@ def main():
     if rank == 0 and not args.no_batch:
         batched = batch_measure(flags=args.flags & vipp_gb300.FLAG_M2L_BF16)
         batched["m2l_split"] = "bf16 hi/lo" if args.flags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32"
+        # the same batch as one context per system, for comparison
+        ctx_form = batch_measure(steps=10, sample=4, flags=args.flags & vipp_gb300.FLAG_M2L_BF16, form="contexts")
+        batched["contexts_form"] = {k: ctx_form[k] for k in ("value", "ms_per_step", "launches_per_step", "steps")}
 
     # --- the other M2L split on the same workload (value and energy drift) -------
     alt = None

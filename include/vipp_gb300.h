@@ -98,10 +98,12 @@ enum gb_flags {
                                    replaying the step's captured CUDA graph (same
                                    results; graphs are also off while kernel
                                    timing is enabled) */
-    GB_FLAG_M2L_BF16 = 16       /* tensor-core M2L with a BF16 hi/lo split
+    GB_FLAG_M2L_BF16 = 16,      /* tensor-core M2L with a BF16 hi/lo split
                                    (~2^-17 relative per product; half the gathered
                                    bytes and MMA time, ~17% less M2L time) instead
                                    of the default three-term TF32 split (~2^-21) */
+    GB_FLAG_BATCH_CONTEXTS = 32 /* gb_batch_create: one context per system (the
+                                   contexts form) instead of the forest form */
 };
 
 typedef struct gb_ctx gb_ctx;
@@ -135,11 +137,22 @@ GB_API int gb_set_config(gb_ctx *ctx, const gb_config *cfg);
  * Plummer systems of uneven N concatenated with segment offsets). No
  * counterpart in the reference, which runs one Problem per Solver. System k
  * holds particles [seg_offsets[k], seg_offsets[k+1]) of the concatenated AoS
- * arrays, particle mass m_per_system[k] (cfg->m when NULL) and the rest of
- * cfg. A batch step advances every system by one RK4 step; all systems' steps
- * are queued before any is waited for, so they run concurrently on the GPU.
- * gb_batch_system gives system k's context (for gb_accel, gb_get_conserved,
- * gb_get_stats; the batch owns it). */
+ * arrays (seg_offsets[0] = 0), particle mass m_per_system[k] (cfg->m when
+ * NULL) and the rest of cfg. A batch step advances every system by one RK4
+ * step. Two forms, with the same results per system:
+ *   forest (default): one context over all systems; every kernel of a force
+ *     evaluation is one launch over all of them (tiles of the far field hold
+ *     one system's cells each), one step graph per batch step. Each system
+ *     keeps its own root box, tree (the reference's for that system alone),
+ *     operators, mass and G m. A forest holds at most 2^31 - 1 particles, and
+ *     a system's tree at most floor((64 - ceil(log2 nsys)) / 3) levels (18
+ *     for 512 systems); a deeper system fails the step with GB_ERR_DEPTH.
+ *   contexts (cfg->flags & GB_FLAG_BATCH_CONTEXTS, and always for
+ *     GB_MODE_ACCURATE): one context, tree and step graph per system; all
+ *     systems' steps are queued before any is waited for.
+ * gb_batch_system gives system k's context in the contexts form (the batch
+ * owns it) and NULL in the forest form; gb_batch_accel, gb_batch_conserved
+ * and gb_batch_stats work in both. */
 typedef struct gb_batch gb_batch;
 GB_API int gb_batch_create(const gb_config *cfg, size_t nsys, const uint64_t *seg_offsets, const double *m_per_system,
                            gb_batch **out);
@@ -156,6 +169,13 @@ GB_API int gb_batch_download(gb_batch *b, double *x_aos, double *v_aos);
 GB_API int gb_batch_rk4_step(gb_batch *b, double dt);
 GB_API int gb_batch_size(const gb_batch *b, size_t *nsys, uint64_t *n_total);
 GB_API gb_ctx *gb_batch_system(gb_batch *b, size_t k);
+GB_API int gb_batch_is_forest(const gb_batch *b);
+/* The forest form's context (for gb_enable_timing, gb_kernel_times,
+ * gb_launch_count, gb_stream; the batch owns it); NULL in the contexts form. */
+GB_API gb_ctx *gb_batch_forest(gb_batch *b);
+/* Accelerations (AoS, n_total x 3) and optionally potentials (n_total) of
+ * every system at the current positions, concatenated like the state. */
+GB_API int gb_batch_accel(gb_batch *b, double *a_aos, double *phi);
 
 /* Initial state generated on the device: the reference's Plummer sphere
  * (Problem::initialize, problem.hpp:188-211, 245-292; G = M = a = 1) with one
@@ -211,6 +231,9 @@ typedef struct gb_conserved {
     double angular_momentum[3]; /* m sum x cross v */
 } gb_conserved;
 GB_API int gb_get_conserved(gb_ctx *ctx, gb_conserved *out);
+/* The conserved quantities of every system of a batch: out[k] for system k
+ * (nsys entries). */
+GB_API int gb_batch_conserved(gb_batch *b, gb_conserved *out);
 
 /* FP64 direct softened sum on the GPU for the listed targets of the current
  * positions (the accuracy oracle; SolverRefNaive::acceleration,
@@ -275,6 +298,11 @@ GB_API int gb_tuning_lookup(const char *path, const gb_config *cfg, size_t n, gb
 /* Block until all queued work finished; reports deferred device errors. */
 GB_API int gb_sync(gb_ctx *ctx);
 GB_API int gb_get_stats(gb_ctx *ctx, gb_stats *out);
+/* Batch statistics: the forest's (every system's cells, pairs and ranges
+ * together), or the contexts' summed (depth: the deepest). */
+GB_API int gb_batch_stats(gb_batch *b, gb_stats *out);
+/* Kernel launches queued by the batch so far (all its contexts). */
+GB_API int64_t gb_batch_launch_count(const gb_batch *b);
 
 /* Tree dump of the last force evaluation, for the parity tests. Cells are
  * numbered level by level, and within a level in the reference's child order

@@ -1,13 +1,21 @@
-"""Batches of independent systems (gb_batch_*): every system of a batch step
-must equal the same system stepped alone in its own context, bit for bit,
-in both precisions and with either tensor-core M2L split; uneven sizes, an empty and a one-particle system, per-system
-masses, and a system whose first step overflows its buffers (repeated alone)."""
+"""Batches of independent systems (gb_batch_*), in both forms: every system of
+a batch step must equal the same system stepped alone in its own context, bit
+for bit, in both precisions and with each M2L path (tensor cores with either
+split, CUDA cores); uneven sizes, an empty and a one-particle system,
+per-system masses, and a system whose first step overflows its buffers
+(repeated). The forest form (one context, one launch per kernel class over all
+systems) is also compared with the contexts form on many systems: positions,
+velocities, accelerations, potentials, tree totals and initial conditions."""
+import math
+
 import numpy as np
 import pytest
 
 import oracle as O
 
 pytestmark = pytest.mark.gpu
+
+FORMS = ("forest", "contexts")
 
 
 def systems():
@@ -18,16 +26,24 @@ def systems():
     return out
 
 
-@pytest.mark.parametrize("precision,bf16", [("fp64", False), ("mixed", False), ("mixed", True)])
-def test_batch_equals_separate_contexts(precision, bf16):
+def form_flags(form):
     import vipp_gb300
-    flags = vipp_gb300.FLAG_M2L_BF16 if bf16 else 0
+    return vipp_gb300.FLAG_BATCH_CONTEXTS if form == "contexts" else 0
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("precision,m2l", [("fp64", ""), ("mixed", "tf32"), ("mixed", "bf16"), ("mixed", "cuda")])
+def test_batch_equals_separate_contexts(form, precision, m2l):
+    import vipp_gb300
+    flags = {"": 0, "tf32": 0, "bf16": vipp_gb300.FLAG_M2L_BF16, "cuda": vipp_gb300.FLAG_M2L_CUDA_CORES}[m2l]
     sy = systems()
     sizes = [len(x) for x, _ in sy]
     masses = [1.0 / max(n, 1) for n in sizes]
     X = np.concatenate([x for x, _ in sy]) if sum(sizes) else np.zeros((0, 3))
     V = np.concatenate([v for _, v in sy])
-    with vipp_gb300.Batch(sizes, p=5, s=16, eps=0.01, masses=masses, precision=precision, flags=flags) as b:
+    with vipp_gb300.Batch(sizes, p=5, s=16, eps=0.01, masses=masses, precision=precision,
+                          flags=flags | form_flags(form)) as b:
+        assert b.forest == (form == "forest")
         b.upload(X, V)
         for dt in (1e-3, 1e-3, 2e-3):
             b.step(dt)
@@ -47,12 +63,14 @@ def test_batch_equals_separate_contexts(precision, bf16):
         assert np.array_equal(xb[off[k]:off[k + 1]], xs) and np.array_equal(vb[off[k]:off[k + 1]], vs)
 
 
-def test_batch_system_overflow_is_repeated():
+@pytest.mark.parametrize("form", FORMS)
+def test_batch_system_overflow_is_repeated(form):
     import vipp_gb300
     x, v = O.plummer_reference(100_000, 0.01, 0)  # needs 3x the initial partial-sum slots at s = 256
     y, w = O.plummer_reference(4000, 0.01, 1)
     sizes = [len(y), len(x)]
-    with vipp_gb300.Batch(sizes, p=4, s=256, eps=0.01, masses=[1 / len(y), 1 / len(x)], precision="mixed") as b:
+    with vipp_gb300.Batch(sizes, p=4, s=256, eps=0.01, masses=[1 / len(y), 1 / len(x)], precision="mixed",
+                          flags=form_flags(form)) as b:
         b.upload(np.concatenate([y, x]), np.concatenate([w, v]))
         b.step(1e-3)
         xb, vb = b.download()
@@ -61,3 +79,77 @@ def test_batch_system_overflow_is_repeated():
         s.solve(1e-3)
         xs, vs = s.postprocess()
     assert np.array_equal(xb[len(y):], xs) and np.array_equal(vb[len(y):], vs)
+
+
+@pytest.mark.parametrize("precision,flags", [("mixed", 16), ("mixed", 0), ("fp64", 0)])
+def test_forest_equals_contexts_many_systems(precision, flags):
+    """96 Plummer systems drawn on the device (N log-uniform in [16, 6000],
+    radii in [0.5, 2]): the forest and the contexts form give the same initial
+    conditions, the same tree totals and, after two steps, the same state,
+    accelerations and potentials, bit for bit; conserved quantities agree."""
+    import vipp_gb300
+    rng = np.random.default_rng(5)
+    sizes = np.rint(np.exp(rng.uniform(math.log(16), math.log(6000), 96))).astype(np.int64)
+    sizes[7] = 0
+    sizes[11] = 1
+    masses = 1.0 / np.maximum(sizes, 1)
+    res = {}
+    for form in FORMS:
+        with vipp_gb300.Batch(sizes, p=6, s=32, eps=0.01, masses=masses, precision=precision,
+                              flags=flags | form_flags(form)) as b:
+            radii = b.init_plummer(seed=9)
+            x0, v0 = b.download()
+            b.step(1e-3)
+            b.step(1e-3)
+            x, v = b.download()
+            a, phi = b.accel(potential=True)
+            res[form] = dict(radii=radii, x0=x0, v0=v0, x=x, v=v, a=a, phi=phi, stats=b.stats(),
+                             cons=b.conserved())
+    f, c = res["forest"], res["contexts"]
+    for k in ("radii", "x0", "v0", "x", "v", "a", "phi"):
+        assert np.array_equal(f[k], c[k]), k
+    # an empty system's context never evaluates; the forest gives it a root leaf
+    empty = int(np.sum(sizes == 0))
+    for k in ("n", "ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges"):
+        assert f["stats"][k] == c["stats"][k] + (empty if k in ("ncells", "nleaves") else 0), k
+    for cf, cc in zip(f["cons"], c["cons"]):
+        for k in ("kinetic", "potential"):
+            assert cf[k] == pytest.approx(cc[k], rel=1e-12, abs=1e-300)
+
+
+def test_forest_launches_do_not_grow_with_systems():
+    """One forest step queues the same kernels whatever the number of systems
+    (the step graph's launch count; contexts: one graph per system), up to one
+    more radix pass per force evaluation for the wider system index."""
+    import vipp_gb300
+    counts = {}
+    for nsys in (8, 64):
+        sizes = np.full(nsys, 2000)
+        with vipp_gb300.Batch(sizes, p=4, s=32, eps=0.01, masses=1.0 / sizes, precision="mixed") as b:
+            b.init_plummer(seed=1)
+            b.step(1e-3)
+            b.step(1e-3)
+            l0 = b.launch_count()
+            b.step(1e-3)
+            counts[nsys] = b.launch_count() - l0
+    assert counts[8] <= counts[64] <= counts[8] + 16 and counts[64] < 300, counts
+
+
+def test_forest_depth_beyond_its_sort_word_is_reported():
+    """1024 systems leave 18 key levels beside the system index: a system
+    whose tree needs more fails the step with GB_ERR_DEPTH (the contexts form
+    runs it)."""
+    import vipp_gb300
+    sizes = np.zeros(1024, dtype=np.int64)
+    # six particles 4e-7 apart in a unit box: the tree reaches level 20 (the oracle's tree of it)
+    deep = np.array([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0]] + [[0.3 + 4e-7 * i, 0.3, 0.3] for i in range(6)])
+    sizes[5] = len(deep)
+    with vipp_gb300.Batch(sizes, p=3, s=1, eps=0.01, masses=np.ones(1024), precision="mixed") as b:
+        b.upload(deep, np.zeros_like(deep))
+        with pytest.raises(vipp_gb300.GB300Error) as e:
+            b.step(1e-3)
+        assert e.value.code == vipp_gb300.GB_ERR_DEPTH
+    with vipp_gb300.Batch(sizes, p=3, s=1, eps=0.01, masses=np.ones(1024), precision="mixed",
+                          flags=vipp_gb300.FLAG_BATCH_CONTEXTS) as b:
+        b.upload(deep, np.zeros_like(deep))
+        b.step(1e-3)

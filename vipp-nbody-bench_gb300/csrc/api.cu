@@ -194,7 +194,7 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
     const size_t esz = ws.mixed ? sizeof(float) : sizeof(double);
     if (s_cap > ws.s_cap || ws.k_cap != ws.K * static_cast<int>(esz)) {
         ++ctx->epoch;
-        const unsigned c = 1 + 8 * s_cap;
+        const unsigned c = static_cast<unsigned>(ws.forest() ? ws.nsys : 1) + 8 * s_cap;  // roots + 8 per split cell
         GB_TRY(dalloc(ws.ent0, s_cap));
         GB_TRY(dalloc(ws.ent1, s_cap));
         GB_TRY(dalloc(ws.split_cell, s_cap));
@@ -231,6 +231,12 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
         GB_TRY(dalloc(ws.src_total, c + 1));
         GB_TRY(dalloc(ws.part_cnt, c + 1));
         GB_TRY(dalloc(ws.part_off, c + 1));
+        if (ws.forest()) {  // per-cell systems and the one-system tiles (tree.cu: forest_tiles)
+            GB_TRY(dalloc(ws.c_sys, c));
+            GB_TRY(dalloc(ws.etile, s_cap + 1));
+            GB_TRY(dalloc(ws.oct_list, c / 8 + 1));
+            GB_TRY(dalloc(ws.otile, c / 8 + static_cast<size_t>(ws.nsys) + 1));
+        }
         GB_TRY(gb::scan_temp_alloc(ws.scan, std::max(ws.n_cap + 1, c + 1)));
         GB_TRY(gb::sort_temp_alloc(ws.sort, std::max(ws.n_cap, s_cap)));
         ws.s_cap = s_cap;
@@ -259,7 +265,7 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
     if (ws.m2l_tensor) {
         // split expansions of the tensor-core M2L and their TMA map
         const int kp = gb::m2l_tc_row_floats(ws.p);
-        const unsigned rows = ws.c_cap + 1;
+        const unsigned rows = ws.c_cap + gb::kZeroRows;
         if (!ws.ms_tc || ws.ms_rows != rows || ws.ms_kp != kp || ws.ms_bf16 != ws.m2l_bf16) {
             ++ctx->epoch;
             GB_TRY(dalloc(ws.ms_tc, 2 * static_cast<size_t>(rows) * kp));
@@ -345,6 +351,11 @@ int check_device_errors(gb_ctx *ctx, unsigned *need) {
         ctx->err = "tree deeper than 21 levels (more than floor(sqrt(8) s) coincident particles?)";
         return GB_ERR_DEPTH;
     }
+    if (err & gb::kDevForestDepth) {
+        ctx->err = "a system of the forest needs more tree levels than its sort word holds beside the system index "
+                   "(fewer systems per batch, or the contexts form)";
+        return GB_ERR_DEPTH;
+    }
     if (err & gb::kDevTimeout) {
         ctx->err = "a bounded device wait gave up (radix-sort look-back or tensor-core M2L barrier); this call's "
                    "results are discarded";
@@ -390,6 +401,7 @@ void evaluate(gb_ctx *ctx, bool to_acc = true) {
         cudaEventRecord(ws.ev_join, ws.st2);
     }
     gb::build_operators(ws);
+    if (ws.forest()) gb::forest_tiles(ws, ws.m2l_tensor ? gb::kM2LTileTC : gb::kM2LTileCC);
     gb::upward_pass(ws);
     if (ws.m2l_tensor)
         gb::m2l_pass_tc(ws);
@@ -663,7 +675,8 @@ void gb_destroy(gb_ctx *ctx) {
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
                     ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.m2l_tab, ws.ms_tc, ws.diag, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets, ws.smom, ws.smom_oct, ws.staylor,
-                    ctx->d_direct};
+                    ctx->d_direct, ws.seg, ws.psys, ws.c_sys, ws.sys_par, ws.mkeys, ws.etile, ws.oct_list, ws.otile,
+                    ws.ocnt};
     for (void *b : bufs) dfree(b);
     gb::sort_temp_free(ws.sort);
     gb::scan_temp_free(ws.scan);
@@ -899,18 +912,73 @@ int gb_rk4_step(gb_ctx *ctx, double dt) {
 
 // ------------------------------------------------------------------- batches
 // Many independent systems of uneven size (the batching form of the
-// benchmark: systems concatenated with segment offsets). Every system has its
-// own context, tree, operators and step graph on its own stream; a batch step
-// queues all systems' steps before waiting for any, so the GPU runs the small,
-// launch-latency-bound systems concurrently. A system whose buffers overflow is
-// grown and stepped again on its own.
+// benchmark: systems concatenated with segment offsets), in one of two forms.
+//  * Forest (default): one context holds every system. Each kernel class runs
+//    as one launch over all systems (the tree kernels over all particles and
+//    cells; the far-field kernels over tiles that each hold one system's
+//    cells, with that system's operators), so a batch step is one step graph
+//    of the same ~60 launches per force evaluation as a single system's.
+//    Every system keeps its own root box, tree, operators, particle mass and
+//    G m, and gets the results a context of its own computes (the same
+//    operations in the same order per particle and per cell).
+//  * Contexts (GB_FLAG_BATCH_CONTEXTS, and the accurate mode): every system
+//    has its own context, tree, operators and step graph on its own stream;
+//    a batch step queues all systems' steps before waiting for any. A system
+//    whose buffers overflow is grown and stepped again on its own.
 }  // extern "C"
 
 struct gb_batch {
-    std::vector<gb_ctx *> ctx;
+    std::vector<gb_ctx *> ctx;  // contexts form: one per system
+    gb_ctx *forest = nullptr;   // forest form: one context over every system
     std::vector<uint64_t> off;  // nsys + 1 particle offsets
+    std::vector<double> m;      // particle mass of each system
     std::string err;
+    size_t nsys() const { return off.size() - 1; }
 };
+
+namespace {
+
+// Per-system data of a forest context: systems, their TreeInfo entries and
+// operators, the system of every particle position, masses and G m.
+int forest_setup(gb_ctx *ctx, size_t nsys, const uint64_t *off, const std::vector<double> &m) {
+    gb::Workspace &ws = ctx->ws;
+    GB_TRY(cudaSetDevice(ctx->cfg.device));
+    const size_t n = off[nsys];
+    ws.nsys = static_cast<int>(nsys);
+    ws.sys_bits = 0;
+    while ((1ull << ws.sys_bits) < nsys) ++ws.sys_bits;
+    GB_TRY(dalloc(ws.info, nsys));
+    GB_TRY(cudaMemset(ws.info, 0, sizeof(gb::TreeInfo) * nsys));
+    const size_t kk = static_cast<size_t>(ws.K) * ws.K * gb::kNumOps * nsys;
+    GB_TRY(dalloc(ws.ops_d, kk));
+    GB_TRY(dalloc(ws.ops_f, kk));
+    GB_TRY(dalloc(ws.bimg, gb::m2l_tc_image_floats(ws.p) * nsys));
+    std::vector<unsigned> seg(nsys + 1);
+    std::vector<int> ps(n);
+    std::vector<double2> par(nsys);
+    for (size_t k = 0; k <= nsys; ++k) seg[k] = static_cast<unsigned>(off[k]);
+    for (size_t k = 0; k < nsys; ++k) {
+        for (uint64_t i = off[k]; i < off[k + 1]; ++i) ps[i] = static_cast<int>(k);
+        par[k] = make_double2(m[k], ws.G * m[k]);
+    }
+    GB_TRY(dalloc(ws.seg, nsys + 1));
+    GB_TRY(cudaMemcpy(ws.seg, seg.data(), sizeof(unsigned) * (nsys + 1), cudaMemcpyHostToDevice));
+    GB_TRY(dalloc(ws.psys, n));
+    if (n) GB_TRY(cudaMemcpy(ws.psys, ps.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    GB_TRY(dalloc(ws.sys_par, nsys));
+    GB_TRY(cudaMemcpy(ws.sys_par, par.data(), sizeof(double2) * nsys, cudaMemcpyHostToDevice));
+    GB_TRY(dalloc(ws.mkeys, n));
+    GB_TRY(dalloc(ws.ocnt, 3 * nsys + 1));
+    ws.sort_levels = std::min(ws.sort_levels, ws.sort_levels_cap());
+    return GB_OK;
+}
+
+int forest_fail(gb_batch *b, int rc) {
+    b->err = b->forest->err;
+    return rc;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -927,11 +995,45 @@ int gb_batch_create(const gb_config *cfg, size_t nsys, const uint64_t *seg_offse
             g_create_error = "segment offsets must not decrease";
             return GB_ERR_INVALID;
         }
+    if (seg_offsets[0] != 0) {
+        g_create_error = "segment offsets must start at 0";
+        return GB_ERR_INVALID;
+    }
     auto *b = new gb_batch;
     b->off.assign(seg_offsets, seg_offsets + nsys + 1);
+    b->m.resize(nsys);
+    for (size_t k = 0; k < nsys; ++k) b->m[k] = m_per_system ? m_per_system[k] : cfg->m;
+    const bool contexts = (cfg->flags & GB_FLAG_BATCH_CONTEXTS) != 0 || cfg->mode == GB_MODE_ACCURATE;
+    if (!contexts) {
+        if (seg_offsets[nsys] > 0x7fffffffu || nsys > 0x7fffffffu) {
+            g_create_error = "too many particles or systems for one forest";
+            delete b;
+            return GB_ERR_INVALID;
+        }
+        for (size_t k = 0; k < nsys; ++k)
+            if (!std::isfinite(b->m[k])) {
+                g_create_error = "masses must be finite";
+                delete b;
+                return GB_ERR_INVALID;
+            }
+        gb_ctx *h = nullptr;
+        int rc = gb_create(cfg, &h);
+        if (rc == GB_OK) {
+            rc = forest_setup(h, nsys, seg_offsets, b->m);
+            if (rc != GB_OK) g_create_error = h->err;
+        }
+        if (rc != GB_OK) {
+            gb_destroy(h);
+            delete b;
+            return rc;
+        }
+        b->forest = h;
+        *out = b;
+        return GB_OK;
+    }
     for (size_t k = 0; k < nsys; ++k) {
         gb_config c = *cfg;
-        if (m_per_system) c.m = m_per_system[k];
+        c.m = b->m[k];
         gb_ctx *h = nullptr;
         const int rc = gb_create(&c, &h);
         if (rc != GB_OK) {
@@ -948,10 +1050,15 @@ int gb_batch_create(const gb_config *cfg, size_t nsys, const uint64_t *seg_offse
 void gb_batch_destroy(gb_batch *b) {
     if (!b) return;
     for (gb_ctx *x : b->ctx) gb_destroy(x);
+    gb_destroy(b->forest);
     delete b;
 }
 
 const char *gb_batch_last_error(const gb_batch *b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+int gb_batch_is_forest(const gb_batch *b) { return b && b->forest ? 1 : 0; }
+
+gb_ctx *gb_batch_forest(gb_batch *b) { return b ? b->forest : nullptr; }
 
 static int batch_fail(gb_batch *b, size_t k, int rc) {
     b->err = "system " + std::to_string(k) + ": " + b->ctx[k]->err;
@@ -960,6 +1067,10 @@ static int batch_fail(gb_batch *b, size_t k, int rc) {
 
 int gb_batch_upload(gb_batch *b, const double *x_aos, const double *v_aos) {
     if (!b || !x_aos || !v_aos) return GB_ERR_INVALID;
+    if (b->forest) {
+        const int rc = gb_upload(b->forest, x_aos, v_aos, b->off.back());
+        return rc == GB_OK ? rc : forest_fail(b, rc);
+    }
     for (size_t k = 0; k < b->ctx.size(); ++k) {
         const uint64_t o = b->off[k], n = b->off[k + 1] - o;
         const int rc = gb_upload(b->ctx[k], x_aos + 3 * o, v_aos + 3 * o, n);
@@ -978,12 +1089,52 @@ int gb_batch_init_plummer(gb_batch *b, uint64_t seed, double r_lo, double r_hi, 
         z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
         return z ^ (z >> 31);
     };
-    for (size_t k = 0; k < b->ctx.size(); ++k) {
-        gb_ctx *ctx = b->ctx[k];
-        const uint64_t n = b->off[k + 1] - b->off[k];
+    // system k: radius R_k from the batch seed, particle stream family mix(seed + k)
+    const size_t ns = b->nsys();
+    std::vector<uint64_t> seeds(ns);
+    std::vector<double2> scales(ns);
+    for (size_t k = 0; k < ns; ++k) {
         const double u = static_cast<double>(mix(mix(seed ^ 0x2545f4914f6cdd1dull) + k) >> 11) * 0x1.0p-53;
         const double R = r_lo + (r_hi - r_lo) * u;
         if (radii) radii[k] = R;
+        seeds[k] = mix(seed + k);
+        scales[k] = make_double2(R, 1.0 / std::sqrt(R));  // total mass 1, scale radius R (G = 1)
+    }
+    if (b->forest) {
+        gb_ctx *ctx = b->forest;
+        gb::Workspace &ws = ctx->ws;
+        ctx->levels_fitted = false;
+        if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return b->err = "cudaSetDevice failed", GB_ERR_CUDA;
+        const size_t n = b->off.back();
+        int rc = apply_tuning_cache(ctx, n);
+        if (rc == GB_OK) rc = ensure_particles(ctx, static_cast<unsigned>(n));
+        if (rc != GB_OK) return forest_fail(b, rc);
+        ws.n = static_cast<unsigned>(n);
+        uint64_t *d_seeds = nullptr;
+        double2 *d_scales = nullptr;
+        int err = 0;
+        bool ok = dalloc(d_seeds, ns) == cudaSuccess && dalloc(d_scales, ns) == cudaSuccess &&
+                  cudaMemcpy(d_seeds, seeds.data(), sizeof(uint64_t) * ns, cudaMemcpyHostToDevice) == cudaSuccess &&
+                  cudaMemcpy(d_scales, scales.data(), sizeof(double2) * ns, cudaMemcpyHostToDevice) == cudaSuccess;
+        if (ok && n) {
+            gb::generate_plummer_forest(ws, d_seeds, d_scales, 1.0, r_max);
+            ok = cudaMemcpyAsync(&err, &ws.info->err, sizeof(int), cudaMemcpyDeviceToHost, ws.st) == cudaSuccess &&
+                 cudaStreamSynchronize(ws.st) == cudaSuccess;
+        }
+        dfree(d_seeds);
+        dfree(d_scales);
+        if (!ok) return b->err = "initial-condition generation failed", GB_ERR_CUDA;
+        if (err) return b->err = "initial-condition sampling did not converge", GB_ERR_CUDA;
+        if (n) {
+            rc = initial_capacity(ctx);
+            if (rc != GB_OK) return forest_fail(b, rc);
+        }
+        ctx->have_state = true;
+        return GB_OK;
+    }
+    for (size_t k = 0; k < ns; ++k) {
+        gb_ctx *ctx = b->ctx[k];
+        const uint64_t n = b->off[k + 1] - b->off[k];
         ctx->levels_fitted = false;
         if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return batch_fail(b, k, GB_ERR_CUDA);
         gb::Workspace &ws = ctx->ws;
@@ -992,14 +1143,13 @@ int gb_batch_init_plummer(gb_batch *b, uint64_t seed, double r_lo, double r_hi, 
         if (rc != GB_OK) return batch_fail(b, k, rc);
         ws.n = static_cast<unsigned>(n);
         if (n) {
-            // total mass 1 and scale radius R (G = 1): positions x R, velocities x R^-1/2
-            gb::generate_plummer(ws, ws.n, mix(seed + k), 1.0, r_max, R, 1.0 / std::sqrt(R));
+            gb::generate_plummer(ws, ws.n, seeds[k], 1.0, r_max, scales[k].x, scales[k].y);
             rc = initial_capacity(ctx);
             if (rc != GB_OK) return batch_fail(b, k, rc);
         }
         ctx->have_state = true;
     }
-    for (size_t k = 0; k < b->ctx.size(); ++k) {
+    for (size_t k = 0; k < ns; ++k) {
         gb::Workspace &ws = b->ctx[k]->ws;
         int err = 0;
         if (cudaMemcpyAsync(&err, &ws.info->err, sizeof(int), cudaMemcpyDeviceToHost, ws.st) != cudaSuccess ||
@@ -1015,6 +1165,10 @@ int gb_batch_init_plummer(gb_batch *b, uint64_t seed, double r_lo, double r_hi, 
 
 int gb_batch_download(gb_batch *b, double *x_aos, double *v_aos) {
     if (!b || !x_aos || !v_aos) return GB_ERR_INVALID;
+    if (b->forest) {
+        const int rc = gb_download(b->forest, x_aos, v_aos);
+        return rc == GB_OK ? rc : forest_fail(b, rc);
+    }
     for (size_t k = 0; k < b->ctx.size(); ++k) {
         const uint64_t o = b->off[k];
         const int rc = gb_download(b->ctx[k], x_aos + 3 * o, v_aos + 3 * o);
@@ -1026,6 +1180,11 @@ int gb_batch_download(gb_batch *b, double *x_aos, double *v_aos) {
 int gb_batch_rk4_step(gb_batch *b, double dt) {
     if (!b) return GB_ERR_INVALID;
     if (!std::isfinite(dt)) return b->err = "dt must be finite", GB_ERR_INVALID;
+    if (b->forest) {
+        if (!b->forest->have_state) return b->err = "no state uploaded", GB_ERR_STATE;
+        const int rc = gb_rk4_step(b->forest, dt);
+        return rc == GB_OK ? rc : forest_fail(b, rc);
+    }
     const size_t ns = b->ctx.size();
     std::vector<char> live(ns, 0);
     for (size_t k = 0; k < ns; ++k) {
@@ -1076,7 +1235,7 @@ int gb_batch_rk4_step(gb_batch *b, double dt) {
 
 int gb_batch_size(const gb_batch *b, size_t *nsys, uint64_t *n_total) {
     if (!b) return GB_ERR_INVALID;
-    if (nsys) *nsys = b->ctx.size();
+    if (nsys) *nsys = b->nsys();
     if (n_total) *n_total = b->off.back();
     return GB_OK;
 }
@@ -1200,6 +1359,83 @@ int gb_get_stats(gb_ctx *ctx, gb_stats *out) {
     out->graph_captures = ctx->graph_captures;
     out->direct_steps = ctx->direct_steps;
     return GB_OK;
+}
+
+// Batch accessors: the contexts form asks each system's context; the forest
+// form evaluates the whole forest once and splits the results by system.
+int gb_batch_accel(gb_batch *b, double *a_aos, double *phi) {
+    if (!b) return GB_ERR_INVALID;
+    if (b->forest) {
+        const int rc = gb_accel(b->forest, a_aos, phi);
+        return rc == GB_OK ? rc : forest_fail(b, rc);
+    }
+    for (size_t k = 0; k < b->ctx.size(); ++k) {
+        const uint64_t o = b->off[k];
+        if (b->off[k + 1] == o) continue;
+        const int rc = gb_accel(b->ctx[k], a_aos ? a_aos + 3 * o : nullptr, phi ? phi + o : nullptr);
+        if (rc != GB_OK) return batch_fail(b, k, rc);
+    }
+    return GB_OK;
+}
+
+int gb_batch_conserved(gb_batch *b, gb_conserved *out) {
+    if (!b || !out) return GB_ERR_INVALID;
+    const size_t ns = b->nsys();
+    if (!b->forest) {
+        for (size_t k = 0; k < ns; ++k) {
+            const int rc = gb_get_conserved(b->ctx[k], out + k);
+            if (rc != GB_OK) return batch_fail(b, k, rc);
+        }
+        return GB_OK;
+    }
+    // forest: the potentials of one evaluation, then the sums per system in FP64 on the host
+    const size_t n = b->off.back();
+    std::vector<double> x(3 * n), v(3 * n), phi(n);
+    int rc = n ? gb_batch_accel(b, nullptr, phi.data()) : GB_OK;
+    if (rc == GB_OK && n) rc = gb_batch_download(b, x.data(), v.data());
+    if (rc != GB_OK) return rc;
+    for (size_t k = 0; k < ns; ++k) {
+        double h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (uint64_t i = b->off[k]; i < b->off[k + 1]; ++i) {
+            const double *xi = &x[3 * i], *vi = &v[3 * i];
+            h[0] += vi[0] * vi[0] + vi[1] * vi[1] + vi[2] * vi[2];
+            h[1] += phi[i];
+            for (int a = 0; a < 3; ++a) h[2 + a] += vi[a];
+            h[5] += xi[1] * vi[2] - xi[2] * vi[1];
+            h[6] += xi[2] * vi[0] - xi[0] * vi[2];
+            h[7] += xi[0] * vi[1] - xi[1] * vi[0];
+        }
+        const double m = b->m[k];
+        gb_conserved &o = out[k];
+        o.kinetic = 0.5 * m * h[0];
+        o.potential = 0.5 * m * h[1];
+        o.total = o.kinetic + o.potential;
+        for (int a = 0; a < 3; ++a) o.momentum[a] = m * h[2 + a], o.angular_momentum[a] = m * h[5 + a];
+    }
+    return GB_OK;
+}
+
+int gb_batch_stats(gb_batch *b, gb_stats *out) {
+    if (!b || !out) return GB_ERR_INVALID;
+    if (b->forest) return gb_get_stats(b->forest, out);
+    std::memset(out, 0, sizeof(*out));
+    for (gb_ctx *c : b->ctx) {
+        gb_stats t;
+        gb_get_stats(c, &t);
+        out->n += t.n, out->ncells += t.ncells, out->nleaves += t.nleaves, out->depth = std::max(out->depth, t.depth);
+        out->m2l_pairs += t.m2l_pairs, out->p2p_pairs += t.p2p_pairs, out->p2p_ranges += t.p2p_ranges;
+        out->retries += t.retries, out->graph_steps += t.graph_steps, out->direct_steps += t.direct_steps;
+        out->graph_captures += t.graph_captures;
+    }
+    return GB_OK;
+}
+
+int64_t gb_batch_launch_count(const gb_batch *b) {
+    if (!b) return 0;
+    if (b->forest) return b->forest->ws.launches;
+    int64_t t = 0;
+    for (const gb_ctx *c : b->ctx) t += c->ws.launches;
+    return t;
 }
 
 int gb_tree_dump(gb_ctx *ctx, int64_t *ncells, int64_t *list_sizes, int32_t *level, int64_t *parent, int64_t *first_child,

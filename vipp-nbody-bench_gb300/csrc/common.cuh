@@ -45,6 +45,7 @@ enum DevErr : int {
     kDevDepth = 2,
     kDevCapacity = 4,
     kDevTimeout = 8,  // a bounded wait in a pipelined kernel gave up
+    kDevForestDepth = 16,  // a forest system needs more key levels than its sort word holds
 };
 
 // Tree parameters of one force evaluation, produced on the device.
@@ -74,7 +75,19 @@ struct TreeInfo {
     long long m2l_pairs;
     long long p2p_pairs;
     long long p2p_ranges;
+    // Forest of independent systems (the batched form): entry k of the
+    // TreeInfo array holds system k's root box and key fields above, and its
+    // particle mass m and G m below; the level tables and the counters above
+    // are the whole forest's, in entry 0.
+    double m, gm;
+    int etile_start[kMaxLevel + 2];  // M2M/L2L tiles of each level (one system per tile)
+    int etile_end[kMaxLevel + 2];
+    int n_otiles;                    // M2L tiles (one system per tile)
+    int pad_;
 };
+
+// System of cell c in a forest (c_sys null: one tree, system 0).
+GB_HD int cell_system(const int *c_sys, int c) { return c_sys ? c_sys[c] : 0; }
 
 // P2P work chunks of one leaf with n targets. Full chunks hold 32 targets; a
 // chunk of t < 32 targets runs floor(32/t) lane groups that share its sources,

@@ -99,6 +99,7 @@ __device__ __forceinline__ double level_scale(const TreeInfo *info, int L) { ret
 // offset's power of rho and harmonics.
 struct M2LEnt {
     double t[2];        // bracket of the m' = m and m' = -m terms
+    float tf[2];        // the same in FP32 (mixed precision)
     short y[2];         // index of Re Y_{j+n}^{|m'-k|} in yt (Im follows)
     signed char sg[2];  // Y order m' - k: 0 (real), +1, -1 (conjugate)
     unsigned char q;    // j + n
@@ -119,6 +120,7 @@ __global__ void k_m2l_table(int p, M2LEnt *__restrict__ tab) {
             e.t[s] = (s == 1 && m == 0) ? 0.0
                                         : phase_even(iabs(k - mm) - iabs(k) - iabs(mm)) * aco(c_at, n, mm) * aco(c_at, j, k) *
                                               ((n % 2 ? -1.0 : 1.0) * aco_inv(c_at, j + n, o));
+            e.tf[s] = static_cast<float>(e.t[s]);
             e.y[s] = static_cast<short>(ridx(j + n, iabs(o), 0));
             e.sg[s] = static_cast<signed char>(o == 0 ? 0 : (o > 0 ? 1 : -1));
         }
@@ -128,14 +130,34 @@ __global__ void k_m2l_table(int p, M2LEnt *__restrict__ tab) {
     }
 }
 
-// ydir + m2l_coef's last factors from a table entry (same operations, same order)
-__device__ __forceinline__ void m2l_term(const M2LEnt &e, int s, const double *yt, const double *rinv_pow, double &re, double &im) {
-    const double yr = yt[e.y[s]];
-    double yi = e.sg[s] == 0 ? 0.0 : yt[e.y[s] + 1];
+// One term of an M2L operator entry from a table entry: the bracket t times
+// Z = Y_{j+n}^{m'-k} rho^-(j+n+1) (Z precomputed per operator, conjugated for
+// negative orders). T = double: FP64 operators; T = float: the FP32 operators
+// of the mixed forms (t and Z rounded to FP32, one FP32 product: ~2^-23).
+template <typename T>
+__device__ __forceinline__ void m2l_term(const M2LEnt &e, int s, const T *Z, T &re, T &im) {
+    const T yr = Z[e.y[s]];
+    T yi = e.sg[s] == 0 ? T(0) : Z[e.y[s] + 1];
     if (e.sg[s] < 0) yi = -yi;
-    const double c = e.t[s] * rinv_pow[e.q + 1];
+    const T c = sizeof(T) == 4 ? static_cast<T>(e.tf[s]) : static_cast<T>(e.t[s]);
     re = c * yr;
     im = c * yi;
+}
+
+template <typename T>
+__device__ __forceinline__ T m2l_entry(const M2LEnt &e, const T *Z) {
+    T ar, ai, br = 0, bi = 0;
+    m2l_term<T>(e, 0, Z, ar, ai);
+    if (e.f & 1) m2l_term<T>(e, 1, Z, br, bi);
+    T vr, vi;
+    if ((e.f & 2) == 0) {
+        vr = ar + br;
+        vi = ai + bi;
+    } else {
+        vr = -(ai - bi);
+        vi = ar - br;
+    }
+    return (e.f & 4) ? vi : vr;
 }
 // One block per operator: 343 same-level M2L offsets (adjacent ones unused),
 // 8 M2M octants, 8 L2L octants. Shifts are the ideal cell-centre offsets of
@@ -143,11 +165,15 @@ __device__ __forceinline__ void m2l_term(const M2LEnt &e, int s, const double *y
 //   M2L  t = (dx Hx, dy Hy, dz Hz) / S,
 //   M2M  t = child - parent = (+-Hx, +-Hy, +-Hz) / (4 S) (minus for a lower half),
 //   L2L  t = parent - child.
-__global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, const M2LEnt *__restrict__ m2l_tab,
-                            double *__restrict__ ops_d, float *__restrict__ ops_f) {
+// A forest's systems each get their own operators (blockIdx.y: system).
+// Mixed precision writes the M2L operators in FP32 only (ops_f; the
+// tensor-core images are split from them); FP64 writes both.
+__global__ void k_build_ops(const TreeInfo *__restrict__ info_all, int p, const M2LEnt *__restrict__ m2l_tab,
+                            double *__restrict__ ops_d, float *__restrict__ ops_f, bool mixed) {
     extern __shared__ double sm[];
     const int K = (p + 1) * (p + 1);
     const int b = blockIdx.x;
+    const TreeInfo *info = info_all + blockIdx.y;
     int kind;
     double tv[3];
     if (b < 343) {
@@ -205,26 +231,30 @@ __global__ void k_build_ops(const TreeInfo *__restrict__ info, int p, const M2LE
         }
         __syncthreads();
     }
-    double *od = ops_d + static_cast<size_t>(b) * K * K;
-    float *of = ops_f + static_cast<size_t>(b) * K * K;
+    double *od = ops_d + (static_cast<size_t>(blockIdx.y) * kNumOps + b) * K * K;
+    float *of = ops_f + (static_cast<size_t>(blockIdx.y) * kNumOps + b) * K * K;
     if (kind == 0) {
-        // real_entry's combination of the two terms, from the table
-        for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
-            const M2LEnt e = m2l_tab[idx];
-            double ar, ai, br = 0, bi = 0;
-            m2l_term(e, 0, yt, pw, ar, ai);
-            if (e.f & 1) m2l_term(e, 1, yt, pw, br, bi);
-            double vr, vi;
-            if ((e.f & 2) == 0) {
-                vr = ar + br;
-                vi = ai + bi;
-            } else {
-                vr = -(ai - bi);
-                vi = ar - br;
+        // real_entry's combination of the two terms, from the table, with
+        // Z[y] = yt[y] rho^-(deg y + 1) formed once per operator
+        const int ny = (D + 1) * (D + 1);
+        double *Z = pw + 2 * p + 3;
+        float *Zf = reinterpret_cast<float *>(Z + (2 * p + 1) * (2 * p + 1));
+        for (int y = threadIdx.x; y < ny; y += blockDim.x) {
+            int dg = static_cast<int>(sqrtf(static_cast<float>(y)));
+            while (dg * dg > y) --dg;
+            while ((dg + 1) * (dg + 1) <= y) ++dg;
+            Z[y] = yt[y] * pw[dg + 1];
+            Zf[y] = static_cast<float>(Z[y]);
+        }
+        __syncthreads();
+        if (mixed) {
+            for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) of[idx] = m2l_entry<float>(m2l_tab[idx], Zf);
+        } else {
+            for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
+                const double v = m2l_entry<double>(m2l_tab[idx], Z);
+                od[idx] = v;
+                of[idx] = static_cast<float>(v);
             }
-            const double v = (e.f & 4) ? vi : vr;
-            od[idx] = v;
-            of[idx] = static_cast<float>(v);
         }
         return;
     }
@@ -289,8 +319,8 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_P2M_MIN_BLOCKS : GB_F
                                              const int *__restrict__ c_begin, const int *__restrict__ c_end,
                                              const int *__restrict__ c_level, const double *__restrict__ c_ctr,
                                              const double *__restrict__ xs, const float4 *__restrict__ ph,
-                                             const float4 *__restrict__ pl, unsigned n, const TreeInfo *__restrict__ info,
-                                             double mass, T *__restrict__ M) {
+                                             const float4 *__restrict__ pl, unsigned n, const TreeInfo *__restrict__ info_all,
+                                             const int *__restrict__ c_sys, double mass, T *__restrict__ M) {
     constexpr int K = (P + 1) * (P + 1);
     const int lane = threadIdx.x & 31;
     const unsigned NL = counts[3];
@@ -299,12 +329,13 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_P2M_MIN_BLOCKS : GB_F
         const int c = leaves[li];
         const int L = c_level[c];
         if (L < 2) continue;
+        const TreeInfo *info = info_all + cell_system(c_sys, c);
         const CellFrame<T> fr(c_ctr, c, info, 1.0 / level_scale(info, L));
         constexpr int KR = (K + 31) / 32 * 32;
         T acc[KR];
 #pragma unroll
         for (int r = 0; r < KR; ++r) acc[r] = 0;
-        const T q = static_cast<T>(mass);
+        const T q = static_cast<T>(c_sys ? info->m : mass);
         for (int j = c_begin[c] + lane; j < c_end[c]; j += 32) {
             T ux, uy, uz;
             fr.at(j, xs, n, ph, pl, ux, uy, uz);
@@ -334,6 +365,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_P2M_MIN_BLOCKS : GB_F
 // bank groups. 256 threads: ty = 0..15 owns 4 target rows, tx = 0..15 owns the
 // output columns tx + 16 j (j < NJ).
 constexpr int kTile = 64;
+static_assert(kTile == kM2LTileCC, "forest M2L tiles");
 
 constexpr int tile_stride(int K, int esz) {
     int vw = 16 / esz;
@@ -420,24 +452,36 @@ __device__ __forceinline__ void tile_gather(T *A, const int *srcs, const T *__re
 // octant o), so that one tile of 64 targets shares the same 189 source slots
 // (parent-neighbour d, child o') and each slot maps to one offset operator.
 // Per slot: gather the tile's source expansions, multiply by the operator.
+// A forest (otile non-null) takes its tiles from the per-system octet lists
+// (tree.cu: forest_tiles), each tile with its system's operators.
 template <int P, typename T>
 __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
-                                             const T *__restrict__ ops, const T *__restrict__ M, T *__restrict__ Lx) {
+                                             const T *__restrict__ ops_all, const int4 *__restrict__ otile,
+                                             const int *__restrict__ oct_list, const T *__restrict__ M, T *__restrict__ Lx) {
     using C = TileCfg<P, T>;
     extern __shared__ __align__(16) unsigned char smraw[];
     T *A = reinterpret_cast<T *>(smraw);  // [64][KS]
     T *Op = A + kTile * C::KS;             // [KO][KS]
-    __shared__ int srcs[kTile];
+    __shared__ int srcs[kTile], trow[kTile];
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int base = info->level_start[2];
     const int ntgt = info->n_targets_m2l;
     if (ntgt <= 0) return;
     const int per_class = ntgt / 8;
-    const int tiles_per_class = (per_class + kTile - 1) / kTile;
+    const int tiles_per_class = otile ? info->n_otiles : (per_class + kTile - 1) / kTile;
     tile_clear<P, T>(A);
     for (int w = blockIdx.x; w < 8 * tiles_per_class; w += gridDim.x) {
         const int cls = w % 8, tile = w / 8;
-        const int t0 = tile * kTile;
+        const T *ops = ops_all;
+        __syncthreads();  // the previous tile's rows are written out
+        if (otile) {
+            const int4 ot = otile[tile];
+            ops = ops_all + static_cast<size_t>(ot.x) * kNumOps * C::K * C::K;
+            if (tid < kTile) trow[tid] = tid < ot.z ? base + cls + 8 * oct_list[ot.y + tid] : -1;
+        } else if (tid < kTile) {
+            const int t = tile * kTile + tid;
+            trow[tid] = t < per_class ? base + cls + 8 * t : -1;
+        }
         T acc[4][C::NJ];
 #pragma unroll
         for (int a = 0; a < 4; ++a)
@@ -451,8 +495,7 @@ __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, 
             if (off[0] >= -1 && off[0] <= 1 && off[1] >= -1 && off[1] <= 1 && off[2] >= -1 && off[2] <= 1) continue;
             int any = 0;
             if (tid < kTile) {
-                const int t = t0 + tid;
-                const int src = t < per_class ? m2l_src[static_cast<size_t>(base + cls + 8 * t) * kM2LSlots + s] : -1;
+                const int src = trow[tid] >= 0 ? m2l_src[static_cast<size_t>(trow[tid]) * kM2LSlots + s] : -1;
                 srcs[tid] = src;
                 any = src >= 0;
             }
@@ -465,9 +508,8 @@ __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, 
         }
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-            const int t = t0 + ty * 4 + a;
-            if (t >= per_class) continue;
-            const size_t c = static_cast<size_t>(base + cls + 8 * t);
+            if (trow[ty * 4 + a] < 0) continue;
+            const size_t c = static_cast<size_t>(trow[ty * 4 + a]);
 #pragma unroll
             for (int j = 0; j < C::NJ; ++j) {
                 const int r = tx + 16 * j;
@@ -487,7 +529,7 @@ __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, 
 template <int P, typename T>
 __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256, GB_FAR_MIN_BLOCKS)
     k_m2m(int L, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell, const int *__restrict__ c_child,
-          const T *__restrict__ ops, T *M) {
+          const T *__restrict__ ops_all, const int2 *__restrict__ etile, const int *__restrict__ c_sys, T *M) {
     namespace cg = cooperative_groups;
     using C = TileCfg<P, T>;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -498,17 +540,27 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256, GB_FAR_MIN_BLOC
     const int o = static_cast<int>(cluster.block_rank());
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int e0 = info->split_start[L], cnt = info->split_count[L];
-    const int tiles = (cnt + kTile - 1) / kTile;
+    // a forest's tiles: one system each, with that system's operator
+    const int et0 = etile ? info->etile_start[L] : 0;
+    const int tiles = etile ? info->etile_end[L] - et0 : (cnt + kTile - 1) / kTile;
     // uniform over each cluster (it shares blockIdx.x / 8): a cluster without a
     // tile reaches no cluster barrier and skips loading its operator
     if (static_cast<int>(blockIdx.x) / 8 >= tiles) return;
     tile_clear<P, T>(A);
-    tile_load_op<P, T>(Op, ops, kOpM2M + o);
+    int loaded = -1;  // system whose operator is in Op
     const int nclusters = static_cast<int>(gridDim.x) / 8;
     for (int w = static_cast<int>(blockIdx.x) / 8; w < tiles; w += nclusters) {  // same w in all 8 CTAs
+        int first = e0 + w * kTile, count = cnt - w * kTile, sys = 0;
+        if (etile) {
+            const int2 et = etile[et0 + w];
+            first = et.x, count = et.y, sys = c_sys[split_cell[first]];
+        }
+        if (sys != loaded) {  // Op is not read here: the previous tile ended with a cluster barrier
+            tile_load_op<P, T>(Op, ops_all + static_cast<size_t>(sys) * kNumOps * C::K * C::K, kOpM2M + o);
+            loaded = sys;
+        }
         if (tid < kTile) {
-            const int e = w * kTile + tid;
-            par[tid] = e < cnt ? split_cell[e0 + e] : -1;
+            par[tid] = tid < count ? split_cell[first + tid] : -1;
             srcs[tid] = par[tid] >= 0 ? c_child[par[tid]] + o : -1;
         }
         __syncthreads();
@@ -546,7 +598,8 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256, GB_FAR_MIN_BLOC
 // of level Lp; child o of each gets L~ += L2L_o L~_parent.
 template <int P, typename T>
 __global__ void __launch_bounds__(256, GB_FAR_MIN_BLOCKS) k_l2l(int Lp, const TreeInfo *__restrict__ info, const int *__restrict__ split_cell,
-                                             const int *__restrict__ c_child, const T *__restrict__ ops, T *Lx) {
+                                             const int *__restrict__ c_child, const T *__restrict__ ops_all,
+                                             const int2 *__restrict__ etile, const int *__restrict__ c_sys, T *Lx) {
     using C = TileCfg<P, T>;
     extern __shared__ __align__(16) unsigned char smraw[];
     T *A = reinterpret_cast<T *>(smraw);
@@ -554,18 +607,21 @@ __global__ void __launch_bounds__(256, GB_FAR_MIN_BLOCKS) k_l2l(int Lp, const Tr
     __shared__ int par[kTile];
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int e0 = info->split_start[Lp], cnt = info->split_count[Lp];
-    const int tiles = (cnt + kTile - 1) / kTile;
+    const int et0 = etile ? info->etile_start[Lp] : 0;
+    const int tiles = etile ? info->etile_end[Lp] - et0 : (cnt + kTile - 1) / kTile;
     if (static_cast<int>(blockIdx.x) >= 8 * tiles) return;  // no (tile, octant) for this block
     tile_clear<P, T>(A);
     for (int w = blockIdx.x; w < 8 * tiles; w += gridDim.x) {
         const int o = w % 8, tile = w / 8;
-        __syncthreads();
-        if (tid < kTile) {
-            const int e = tile * kTile + tid;
-            par[tid] = e < cnt ? split_cell[e0 + e] : -1;
+        int first = e0 + tile * kTile, count = cnt - tile * kTile, sys = 0;
+        if (etile) {
+            const int2 et = etile[et0 + tile];
+            first = et.x, count = et.y, sys = c_sys[split_cell[first]];
         }
         __syncthreads();
-        tile_load_op<P, T>(Op, ops, kOpL2L + o);
+        if (tid < kTile) par[tid] = tid < count ? split_cell[first + tid] : -1;
+        __syncthreads();
+        tile_load_op<P, T>(Op, ops_all + static_cast<size_t>(sys) * kNumOps * C::K * C::K, kOpL2L + o);
         tile_gather<P, T>(A, par, Lx);
         __syncthreads();
         T acc[4][C::NJ];
@@ -601,8 +657,8 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_L2P_MIN_BLOCKS : GB_F
                                              const int *__restrict__ c_begin, const int *__restrict__ c_end,
                                              const int *__restrict__ c_level, const double *__restrict__ c_ctr,
                                              const double *__restrict__ xs, const float4 *__restrict__ ph,
-                                             const float4 *__restrict__ pl, unsigned n, const TreeInfo *__restrict__ info,
-                                             const T *__restrict__ Lx, T *__restrict__ far) {
+                                             const float4 *__restrict__ pl, unsigned n, const TreeInfo *__restrict__ info_all,
+                                             const int *__restrict__ c_sys, const T *__restrict__ Lx, T *__restrict__ far) {
     constexpr int K = (P + 1) * (P + 1);
     __shared__ T Ls[4][K];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -619,6 +675,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? GB_L2P_MIN_BLOCKS : GB_F
         }
         for (int r = lane; r < K; r += 32) Ls[w][r] = Lx[static_cast<size_t>(c) * K + r];
         __syncwarp();
+        const TreeInfo *info = info_all + cell_system(c_sys, c);
         const double s = level_scale(info, L), inv_s = 1.0 / s;
         const CellFrame<T> fr(c_ctr, c, info, inv_s);
         const T sc = static_cast<T>(inv_s * inv_s);
@@ -683,8 +740,8 @@ template <int P, typename T>
 __global__ void __launch_bounds__(128) k_l2p_phi(const int *__restrict__ leaves, const unsigned *counts,
                                                  const int *__restrict__ c_begin, const int *__restrict__ c_end,
                                                  const int *__restrict__ c_level, const double *__restrict__ c_ctr,
-                                                 const double *__restrict__ xs, unsigned n, const TreeInfo *__restrict__ info,
-                                                 const T *__restrict__ Lx, double *__restrict__ farphi) {
+                                                 const double *__restrict__ xs, unsigned n, const TreeInfo *__restrict__ info_all,
+                                                 const int *__restrict__ c_sys, const T *__restrict__ Lx, double *__restrict__ farphi) {
     constexpr int K = (P + 1) * (P + 1);
     __shared__ T Ls[4][K];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -696,6 +753,7 @@ __global__ void __launch_bounds__(128) k_l2p_phi(const int *__restrict__ leaves,
         if (L < 2) continue;  // warp-uniform
         for (int r = lane; r < K; r += 32) Ls[w][r] = Lx[static_cast<size_t>(c) * K + r];
         __syncwarp();
+        const TreeInfo *info = info_all + cell_system(c_sys, c);
         const double s = level_scale(info, L), inv_s = 1.0 / s;
         const double cx = c_ctr[3 * c], cy = c_ctr[3 * c + 1], cz = c_ctr[3 * c + 2];
         const T *Lc = Ls[w];
@@ -718,7 +776,7 @@ template <int P, typename T>
 void launch_l2p_phi(Workspace &ws, double *farphi) {
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));  // a warp per leaf
     k_l2p_phi<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.n,
-                                           ws.info, static_cast<const T *>(ws.Lexp), farphi);
+                                           ws.info, forest_cells(ws), static_cast<const T *>(ws.Lexp), farphi);
     ws.launches += 1;
 }
 
@@ -726,14 +784,15 @@ template <int P, typename T>
 void launch_p2m(Workspace &ws) {
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));
     k_p2m<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.ph,
-                                       ws.pl, ws.n, ws.info, ws.m, static_cast<T *>(ws.Mexp));
+                                       ws.pl, ws.n, ws.info, forest_cells(ws), ws.m, static_cast<T *>(ws.Mexp));
 }
 
 template <int P, typename T>
 void launch_l2p(Workspace &ws) {
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));
     k_l2p<P, T><<<gs, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.ph,
-                                       ws.pl, ws.n, ws.info, static_cast<const T *>(ws.Lexp), static_cast<T *>(ws.farf));
+                                       ws.pl, ws.n, ws.info, forest_cells(ws), static_cast<const T *>(ws.Lexp),
+                                       static_cast<T *>(ws.farf));
 }
 
 template <int P, typename T>
@@ -745,9 +804,10 @@ template <int P, typename T>
 void launch_m2l(Workspace &ws) {
     const size_t smem = TileCfg<P, T>::smem;
     cudaFuncSetAttribute(k_m2l<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 2, 8 * ceil_div(ceil_div(ws.c_cap, 8), kTile));
-    k_m2l<P, T><<<gs, 256, smem, ws.st>>>(ws.info, ws.m2l_src, ops_of<P, T>(ws), static_cast<const T *>(ws.Mexp),
-                                          static_cast<T *>(ws.Lexp));
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 2,
+                                    8 * (ceil_div(ceil_div(ws.c_cap, 8), kTile) + (ws.forest() ? ws.nsys : 0)));
+    k_m2l<P, T><<<gs, 256, smem, ws.st>>>(ws.info, ws.m2l_src, ops_of<P, T>(ws), ws.forest() ? ws.otile : nullptr,
+                                          ws.oct_list, static_cast<const T *>(ws.Mexp), static_cast<T *>(ws.Lexp));
     ws.launches += 1;
 }
 
@@ -759,7 +819,8 @@ void launch_m2m_levels(Workspace &ws) {
     // no cell is deeper than the key levels the sort ordered (tree.cu), so
     // parents lie at levels < ws.sort_levels
     for (int L = ws.sort_levels - 1; L >= 2; --L) {
-        k_m2m<P, T><<<gs, 256, smem, ws.st>>>(L, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws), static_cast<T *>(ws.Mexp));
+        k_m2m<P, T><<<gs, 256, smem, ws.st>>>(L, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws),
+                                              ws.forest() ? ws.etile : nullptr, ws.c_sys, static_cast<T *>(ws.Mexp));
         ws.launches += 1;
     }
 }
@@ -770,7 +831,8 @@ void launch_l2l_levels(Workspace &ws) {
     cudaFuncSetAttribute(k_l2l<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 2, 8 * ceil_div(ws.s_cap, kTile));
     for (int Lp = 2; Lp <= ws.sort_levels - 1; ++Lp) {
-        k_l2l<P, T><<<gs, 256, smem, ws.st>>>(Lp, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws), static_cast<T *>(ws.Lexp));
+        k_l2l<P, T><<<gs, 256, smem, ws.st>>>(Lp, ws.info, ws.split_cell, ws.c_child, ops_of<P, T>(ws),
+                                              ws.forest() ? ws.etile : nullptr, ws.c_sys, static_cast<T *>(ws.Lexp));
         ws.launches += 1;
     }
 }
@@ -817,8 +879,10 @@ void build_m2l_table(Workspace &ws) {
 
 void build_operators(Workspace &ws) {
     timer_begin(ws, kTOps);
-    const size_t smem = sizeof(double) * ((2 * ws.p + 1) * (2 * ws.p + 1) + 2 * ws.p + 3);
-    k_build_ops<<<kNumOps, 256, smem, ws.st>>>(ws.info, ws.p, static_cast<const M2LEnt *>(ws.m2l_tab), ws.ops_d, ws.ops_f);
+    const size_t ny = static_cast<size_t>(2 * ws.p + 1) * (2 * ws.p + 1);  // yt, pw, Z, Zf
+    const size_t smem = sizeof(double) * (2 * ny + 2 * ws.p + 3) + sizeof(float) * ny;
+    k_build_ops<<<dim3(kNumOps, ws.forest() ? ws.nsys : 1), 256, smem, ws.st>>>(
+        ws.info, ws.p, static_cast<const M2LEnt *>(ws.m2l_tab), ws.ops_d, ws.ops_f, ws.mixed);
     ws.launches += 1;
     timer_end(ws, kTOps);
 }

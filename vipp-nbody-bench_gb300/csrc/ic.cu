@@ -127,7 +127,30 @@ __global__ void k_plummer(unsigned n, uint64_t seed, double x0_max, double r_max
         atomicOr(&info->err, kDevNonFinite);
 }
 
+// Forest: every system's Plummer sphere in one launch. Position j of system
+// s = psys[j] is particle j - seg[s] of stream family seeds[s], scaled by
+// scales[s] (positions, velocities): the draws generate_plummer makes for
+// that system alone.
+__global__ void k_plummer_forest(unsigned n, const int *__restrict__ psys, const unsigned *__restrict__ seg,
+                                 const uint64_t *__restrict__ seeds, const double2 *__restrict__ scales, double x0_max,
+                                 double r_max, double *__restrict__ x, double *__restrict__ v, TreeInfo *info) {
+    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int sidx = psys[j];
+    Stream s(seeds[sidx], j - seg[sidx]);
+    const double zero[3] = {0.0, 0.0, 0.0};
+    if (!plummer_particle(s, x0_max, r_max, scales[sidx].x, zero, scales[sidx].y, zero, x + j, v + j, n))
+        atomicOr(&info->err, kDevNonFinite);
+}
+
 }  // namespace
+
+void generate_plummer_forest(Workspace &ws, const uint64_t *seeds, const double2 *scales, double x0_max, double r_max) {
+    cudaMemsetAsync(ws.info, 0, sizeof(TreeInfo), ws.st);
+    k_plummer_forest<<<(ws.n + 255) / 256, 256, 0, ws.st>>>(ws.n, ws.psys, ws.seg, seeds, scales, x0_max, r_max, ws.x, ws.v,
+                                                            ws.info);
+    ws.launches += 1;
+}
 
 // x, v: SoA [3][n] of the context's state; positions x x_scale, velocities x v_scale.
 void generate_plummer(Workspace &ws, unsigned n, uint64_t seed, double x0_max, double r_max, double x_scale,

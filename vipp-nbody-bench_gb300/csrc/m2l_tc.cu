@@ -67,6 +67,7 @@ namespace gb {
 namespace {
 
 constexpr int kRows = 128;          // targets per tile (MMA M)
+static_assert(kRows == kM2LTileTC, "forest M2L tiles");
 constexpr int kKC32 = 32;           // K chunk in 4-byte units: one 128-byte swizzle row
 constexpr int kDrainThreads = 128;  // warps 0-3
 #ifndef M2L_LOADER_WARPS
@@ -284,10 +285,24 @@ __device__ __forceinline__ int next_slot(int cls, int s) {
     return s;
 }
 
+// Target cell of row r of tile-job w (octant w % 8, tile w / 8), or -1: one
+// tree's tiles take consecutive octets; a forest's take its per-system octet
+// lists (tree.cu: forest_tiles).
+__device__ __forceinline__ int tc_row_cell(int w, int r, int base, int per_class, const int4 *otile, const int *oct_list) {
+    const int cls = w % 8, tile = w / 8;
+    if (otile) {
+        const int4 ot = otile[tile];
+        return r < ot.z ? base + cls + 8 * oct_list[ot.y + r] : -1;
+    }
+    const int t = tile * kRows + r;
+    return t < per_class ? base + cls + 8 * t : -1;
+}
+
 template <int P, bool BF>
 __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
     k_m2l_tc(const __grid_constant__ CUtensorMap tmap, const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
-             const unsigned char *__restrict__ bimg, int rows_cap, float *__restrict__ Lx, TreeInfo *info_rw) {
+             const unsigned char *__restrict__ bimg_all, const int4 *__restrict__ otile, const int *__restrict__ oct_list,
+             int rows_cap, float *__restrict__ Lx, TreeInfo *info_rw) {
     using C = TcCfg<P, BF>;
     constexpr int kGW = C::GATHERS / kLoaderWarps;  // gather4 copies per loader warp and step
     extern __shared__ __align__(1024) unsigned char sm_raw[];
@@ -303,8 +318,8 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
     const int base = info->level_start[2];
     const int ntgt = info->n_targets_m2l;
     const int per_class = ntgt > 0 ? ntgt / 8 : 0;
-    const int tiles_per_class = (per_class + kRows - 1) / kRows;
-    const int ntiles = 8 * tiles_per_class;
+    const int tiles_per_class = otile ? info->n_otiles : (per_class + kRows - 1) / kRows;
+    const int ntiles = ntgt > 0 ? 8 * tiles_per_class : 0;
     if (ntiles == 0 || static_cast<int>(blockIdx.x) >= ntiles) return;  // uniform: no barrier or TMEM touched yet
 
     if (tid == 0) {
@@ -340,17 +355,26 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
         // operator bytes of chunk kc: [Bhi; Blo], or (bf16) Bhi alone for a chunk
         // of lo inputs only, whose MMAs read only the first N rows
         auto b_bytes = [](int kc) { return (BF && kc * C::KC >= C::K) ? 1u * C::B_BYTES : 2u * C::B_BYTES; };
-        const int zrow = rows_cap - 1;
+        // absent sources read a zero row, one per row quad so that the copies
+        // of many CTAs do not all meet on one L2 line
+        const int zrow = rows_cap - kZeroRows + quad;
         unsigned step = 0;
         bool stop = false;
         for (int w = blockIdx.x; w < ntiles && !stop; w += gridDim.x) {
-            const int cls = w % 8, t0 = (w / 8) * kRows;
+            const int cls = w % 8;
+            // a forest tile's operator images are its system's
+            const unsigned char *bimg =
+                otile ? bimg_all + static_cast<size_t>(otile[w / 8].x) * (kNumOffsets * C::NKC * 2 * C::B_BYTES) : bimg_all;
+            // rows past the tile's targets are not copied at all: their stale
+            // shared-memory rows only reach accumulator rows that are never stored
+            const int rows = otile ? otile[w / 8].z : min(kRows, per_class - (w / 8) * kRows);
+            const bool qv = 4 * quad < rows;
+            const bool t_hi = do_hi && qv, t_lo = do_lo && qv;
+            const unsigned tx_bytes =
+                512u * static_cast<unsigned>(__popc(__ballot_sync(0xffffffffu, t_hi)) + __popc(__ballot_sync(0xffffffffu, t_lo)));
             int crow[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int t = t0 + 4 * quad + i;
-                crow[i] = (active && t < per_class) ? base + cls + 8 * t : -1;
-            }
+            for (int i = 0; i < 4; ++i) crow[i] = active ? tc_row_cell(w, 4 * quad + i, base, per_class, otile, oct_list) : -1;
             auto rows_of = [&](int s, int *r) {
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
@@ -372,16 +396,16 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                     int ok = 1;
                     if (lane == 0) {
                         if (use > 0 && !mbar_wait(empty + st, (use - 1) & 1, abort_flag)) ok = 0;
-                        if (ok) mbar_expect_tx(full + st, static_cast<unsigned>(kGW) * 512u + (q == 0 ? b_bytes(kc) : 0u));
+                        if (ok) mbar_expect_tx(full + st, tx_bytes + (q == 0 ? b_bytes(kc) : 0u));
                     }
                     if (!__shfl_sync(0xffffffffu, ok, 0)) {
                         stop = true;
                         break;
                     }
                     unsigned char *stage = sm + st * C::STAGE;
-                    if (do_hi)
+                    if (t_hi)
                         tma_gather4(stage + 512 * quad, &tmap, kc * C::KC, cur[0], cur[1], cur[2], cur[3], full + st);
-                    if (do_lo)
+                    if (t_lo)
                         tma_gather4(stage + C::A_BYTES + 512 * quad, &tmap, kc * C::KC, cur[0] + rows_cap, cur[1] + rows_cap,
                                     cur[2] + rows_cap, cur[3] + rows_cap, full + st);
                     if (q == 0 && lane == 0)
@@ -463,7 +487,6 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
             // running sums in TMEM (columns tcol(k)), added in the same order as
             // the register form below: total, then each half of the group
             for (int w = blockIdx.x; w < ntiles && !stop; w += gridDim.x) {
-                const int cls = w % 8, t0 = (w / 8) * kRows;
                 for (int gi = 0; gi < kGroupsPerTile; ++gi, ++groups) {
                     if (!__all_sync(0xffffffffu, mbar_wait(accum + (groups & 1), (groups >> 1) & 1, abort_flag))) {
                         stop = true;
@@ -493,21 +516,20 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                     mbar_arrive(tfree + (groups & 1));
                 }
                 if (stop) break;
-                const int t = t0 + tid;
-                float *out = Lx + static_cast<size_t>(base + cls + 8 * t) * C::K;
+                const int cell = tc_row_cell(w, tid, base, per_class, otile, oct_list);
+                float *out = Lx + static_cast<size_t>(cell < 0 ? 0 : cell) * C::K;
 #pragma unroll 1
                 for (int k = 0; k < C::NCH; ++k) {
                     float sum[32];
                     tmem_ld32(lanes + C::tcol(k), sum);  // all lanes: the load is warp-collective
 #pragma unroll
                     for (int i = 0; i < 32; ++i)
-                        if (t < per_class && 32 * k + i < C::K) out[32 * k + i] = sum[i];
+                        if (cell >= 0 && 32 * k + i < C::K) out[32 * k + i] = sum[i];
                 }
             }
         } else {
         float acc[C::N];
         for (int w = blockIdx.x; w < ntiles && !stop; w += gridDim.x) {
-            const int cls = w % 8, t0 = (w / 8) * kRows;
 #pragma unroll
             for (int i = 0; i < C::N; ++i) acc[i] = 0.f;
             for (int gi = 0; gi < kGroupsPerTile; ++gi, ++groups) {
@@ -531,9 +553,9 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                 mbar_arrive(tfree + (groups & 1));
             }
             if (stop) break;
-            const int t = t0 + tid;
-            if (t < per_class) {
-                float *out = Lx + static_cast<size_t>(base + cls + 8 * t) * C::K;
+            const int cell = tc_row_cell(w, tid, base, per_class, otile, oct_list);
+            if (cell >= 0) {
+                float *out = Lx + static_cast<size_t>(cell) * C::K;
                 for (int r = 0; r < C::K; ++r) out[r] = acc[r];
             }
         }
@@ -561,16 +583,16 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
     }
 }
 
-// Split expansions for the gather; row rows_cap - 1 is the zero row.
+// Split expansions for the gather; the last kZeroRows rows are zero.
 // bf16: rows [0, rows_cap) of KP elements [hi(0..K-1) | lo(0..K-1) | 0].
 // tf32: rows [0, rows_cap) hold the hi parts, rows [rows_cap, 2 rows_cap) the
 // lo parts, KP floats each, zero beyond K.
 template <int P, bool BF>
 __global__ void k_split_m(const TreeInfo *__restrict__ info, const float *__restrict__ M, void *__restrict__ ms_v, int rows_cap) {
     using C = TcCfg<P, BF>;
-    const int nc = min(info->ncells, rows_cap - 1);
+    const int nc = min(info->ncells, rows_cap - kZeroRows);
     const size_t total = static_cast<size_t>(nc) * C::KP;
-    const size_t zrow = static_cast<size_t>(rows_cap - 1) * C::KP;
+    const size_t zrow = static_cast<size_t>(rows_cap - kZeroRows) * C::KP;
     if (BF) {
         __nv_bfloat16 *ms = static_cast<__nv_bfloat16 *>(ms_v);
         for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
@@ -583,7 +605,7 @@ __global__ void k_split_m(const TreeInfo *__restrict__ info, const float *__rest
             ms[i] = j < C::K ? h : __float2bfloat16_rn(v - __bfloat162float(h));
         }
         if (blockIdx.x == 0)
-            for (int k = threadIdx.x; k < C::KP; k += blockDim.x) ms[zrow + k] = __float2bfloat16_rn(0.f);
+            for (int k = threadIdx.x; k < kZeroRows * C::KP; k += blockDim.x) ms[zrow + k] = __float2bfloat16_rn(0.f);
     } else {
         float *ms = static_cast<float *>(ms_v);
         float *lo = ms + static_cast<size_t>(rows_cap) * C::KP;
@@ -597,7 +619,7 @@ __global__ void k_split_m(const TreeInfo *__restrict__ info, const float *__rest
             lo[i] = v - h;
         }
         if (blockIdx.x == 0)
-            for (int k = threadIdx.x; k < C::KP; k += blockDim.x) ms[zrow + k] = 0.f, lo[zrow + k] = 0.f;
+            for (int k = threadIdx.x; k < kZeroRows * C::KP; k += blockDim.x) ms[zrow + k] = 0.f, lo[zrow + k] = 0.f;
     }
 }
 
@@ -608,10 +630,13 @@ __global__ void k_split_m(const TreeInfo *__restrict__ info, const float *__rest
 // tf32: element k of the chunk is input coefficient KC kc + k.
 // bf16: element j = KC kc + k of the [hi | lo] input row is input coefficient
 // j (j < K) or j - K (K <= j < 2K, the lo inputs: rows N + r are zero there).
+// (A forest: blockIdx.y is the system, with its own operators and images.)
 template <int P, bool BF>
-__global__ void k_build_bimg(const double *__restrict__ ops_d, unsigned char *__restrict__ bimg) {
+__global__ void k_build_bimg(const float *__restrict__ ops_all, unsigned char *__restrict__ bimg_all) {
     using C = TcCfg<P, BF>;
     const int oi = blockIdx.x;
+    const float *ops = ops_all + static_cast<size_t>(blockIdx.y) * kNumOps * C::K * C::K;
+    unsigned char *bimg = bimg_all + static_cast<size_t>(blockIdx.y) * (kNumOffsets * C::NKC * 2 * C::B_BYTES);
     const int d0 = oi % 7 - 3, d1 = (oi / 7) % 7 - 3, d2 = oi / 49 - 3;
     if (d0 >= -1 && d0 <= 1 && d1 >= -1 && d1 <= 1 && d2 >= -1 && d2 <= 1) return;
     for (int kc = 0; kc < C::NKC; ++kc) {
@@ -623,7 +648,7 @@ __global__ void k_build_bimg(const double *__restrict__ ops_d, unsigned char *__
             int ci = j;
             bool use = j < C::K;
             if (BF && j >= C::K && j < 2 * C::K) ci = j - C::K, use = !lo_row;
-            const float v = (use && ro < C::K) ? static_cast<float>(ops_d[(static_cast<size_t>(oi) * C::K + ro) * C::K + ci]) : 0.f;
+            const float v = (use && ro < C::K) ? ops[(static_cast<size_t>(oi) * C::K + ro) * C::K + ci] : 0.f;
             if (BF) {
                 const __nv_bfloat16 h = __float2bfloat16_rn(v);
                 const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
@@ -640,14 +665,17 @@ __global__ void k_build_bimg(const double *__restrict__ ops_d, unsigned char *__
 template <int P, bool BF>
 void launch(Workspace &ws) {
     using C = TcCfg<P, BF>;
-    k_build_bimg<P, BF><<<343, 256, 0, ws.st>>>(ws.ops_d, reinterpret_cast<unsigned char *>(ws.bimg));
+    const bool forest = ws.forest();
+    k_build_bimg<P, BF><<<dim3(kNumOffsets, forest ? ws.nsys : 1), 256, 0, ws.st>>>(ws.ops_f,
+                                                                                 reinterpret_cast<unsigned char *>(ws.bimg));
     k_split_m<P, BF><<<4 * ws.num_sms, 256, 0, ws.st>>>(ws.info, static_cast<const float *>(ws.Mexp), ws.ms_tc,
                                                         static_cast<int>(ws.ms_rows));
     cudaFuncSetAttribute(k_m2l_tc<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(C::SMEM));
     const unsigned ctas = std::max(1u, static_cast<unsigned>(ws.num_sms * ws.m2l_ctas_pct / 100));
-    const unsigned gs = capped_grid(ctas, 8 * ceil_div(ceil_div(ws.c_cap, 8), kRows));  // tiles
+    const unsigned gs = capped_grid(ctas, 8 * (ceil_div(ceil_div(ws.c_cap, 8), kRows) + (forest ? ws.nsys : 0)));  // tiles
     k_m2l_tc<P, BF><<<gs, kThreads, C::SMEM, ws.st>>>(ws.tmap_ms, ws.info, ws.m2l_src,
                                                       reinterpret_cast<const unsigned char *>(ws.bimg),
+                                                      forest ? ws.otile : nullptr, ws.oct_list,
                                                       static_cast<int>(ws.ms_rows), static_cast<float *>(ws.Lexp), ws.info);
     ws.launches += 3;
 }

@@ -105,7 +105,8 @@ template <bool kNewton, bool kSoft>
 __global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(const int4 *__restrict__ chunks, const unsigned *counts,
                                                             unsigned *queue, const int *__restrict__ leaves,
                                                             const double *__restrict__ c_ctr,
-                                                            const TreeInfo *__restrict__ info, const unsigned *__restrict__ rng_off,
+                                                            const TreeInfo *__restrict__ info, const int *__restrict__ c_sys,
+                                                            const unsigned *__restrict__ rng_off,
                                                             const unsigned *__restrict__ rng_len, const uint2 *__restrict__ ranges,
                                                             const float4 *__restrict__ ph, const float4 *__restrict__ pl,
                                                             const unsigned *__restrict__ src_total, float *__restrict__ part,
@@ -130,7 +131,8 @@ __global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(c
         const int t = lane - grp * nt;
         const bool tact = grp < g;
         const int i = it.t0 + t;
-        const RootC cc = leaf_centre(c_ctr, leaves[it.li], info);
+        const int leaf = leaves[it.li];
+        const RootC cc = leaf_centre(c_ctr, leaf, info + cell_system(c_sys, leaf));
         float tx = 0, ty = 0, tz = 0;
         if (tact) {
             const float4 h = ph[i], l = pl[i];
@@ -375,6 +377,17 @@ __global__ void __launch_bounds__(kP2PWarps * 32) k_p2p_phi(const int4 *__restri
     }
 }
 
+// Forest: the near field (or potential) of each particle position times its
+// system's G m (the P2P kernels ran with G m = 1; one rounding either way).
+template <typename T>
+__global__ void k_scale_by_system(T *__restrict__ v, unsigned n, int comps, const int *__restrict__ psys,
+                                  const TreeInfo *__restrict__ info) {
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const T g = static_cast<T>(info[psys[j]].gm);
+        for (int a = 0; a < comps; ++a) v[static_cast<size_t>(a) * n + j] = g * v[static_cast<size_t>(a) * n + j];
+    }
+}
+
 __global__ void k_p2p_phi_combine(const int4 *__restrict__ chunks, const unsigned *counts, const double *__restrict__ part,
                                   double Gm, double *__restrict__ phiv) {
     const unsigned nit = counts[5];
@@ -394,11 +407,15 @@ __global__ void k_p2p_phi_combine(const int4 *__restrict__ chunks, const unsigne
 void near_potential(Workspace &ws, double *phiv) {
     cudaMemsetAsync(ws.queue, 0, sizeof(unsigned), ws.st);
     const unsigned gs = static_cast<unsigned>(ws.num_sms) * 8;
+    const double Gm = ws.forest() ? 1.0 : ws.G * ws.m;
     k_p2p_phi<<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.rng_off, ws.rng_len, ws.ranges, ws.xs,
-                                                ws.src_total, static_cast<double *>(ws.part), ws.G * ws.m, ws.eps * ws.eps,
-                                                phiv, ws.n);
-    k_p2p_phi_combine<<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, static_cast<const double *>(ws.part), ws.G * ws.m, phiv);
+                                                ws.src_total, static_cast<double *>(ws.part), Gm, ws.eps * ws.eps, phiv, ws.n);
+    k_p2p_phi_combine<<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, static_cast<const double *>(ws.part), Gm, phiv);
     ws.launches += 2;
+    if (ws.forest()) {
+        k_scale_by_system<double><<<gs, 256, 0, ws.st>>>(phiv, ws.n, 1, ws.psys, ws.info);
+        ws.launches += 1;
+    }
 }
 
 // Near-field kernel over the work queue, `per_sm` blocks per SM. The queue
@@ -421,12 +438,13 @@ void p2p_pass(Workspace &ws, unsigned per_sm) {
     const bool soft = ws.eps > 0;
     if (ws.mixed) {
         const float eps2 = static_cast<float>(ws.eps * ws.eps);
-        const float Gm = static_cast<float>(ws.G * ws.m);
+        const float Gm = ws.forest() ? 1.0f : static_cast<float>(ws.G * ws.m);  // a forest scales in p2p_finish
         auto *o = static_cast<float *>(ws.nearf);
         auto *pf = static_cast<float *>(ws.part);
 #define GB_P2P32(NW, SF)                                                                                                \
     k_p2p_f32<NW, SF><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.leaves, ws.c_ctr, ws.info, \
-                                                        ws.rng_off, ws.rng_len, ws.ranges, ws.ph, ws.pl, ws.src_total, pf, \
+                                                        forest_cells(ws), ws.rng_off, ws.rng_len, ws.ranges, ws.ph, ws.pl, \
+                                                        ws.src_total, pf, \
                                                         Gm, eps2, o, ws.n)
         if (ws.p2p_newton) {
             if (soft)
@@ -441,7 +459,7 @@ void p2p_pass(Workspace &ws, unsigned per_sm) {
         }
 #undef GB_P2P32
     } else {
-        const double Gm = ws.G * ws.m, eps2 = ws.eps * ws.eps;
+        const double Gm = ws.forest() ? 1.0 : ws.G * ws.m, eps2 = ws.eps * ws.eps;
         auto *o = static_cast<double *>(ws.nearf);
         auto *pd = static_cast<double *>(ws.part);
         if (soft)
@@ -457,13 +475,22 @@ void p2p_pass(Workspace &ws, unsigned per_sm) {
 
 void p2p_finish(Workspace &ws) {
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.n, 128));
+    const bool forest = ws.forest();
+    const double Gm = forest ? 1.0 : ws.G * ws.m;
     if (ws.mixed)
         k_p2p_combine<float><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, static_cast<const float *>(ws.part),
-                                                    static_cast<float>(ws.G * ws.m), static_cast<float *>(ws.nearf), ws.n);
+                                                    static_cast<float>(Gm), static_cast<float *>(ws.nearf), ws.n);
     else
-        k_p2p_combine<double><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, static_cast<const double *>(ws.part), ws.G * ws.m,
+        k_p2p_combine<double><<<gs, 256, 0, ws.st>>>(ws.chunks, ws.d_counts, static_cast<const double *>(ws.part), Gm,
                                                      static_cast<double *>(ws.nearf), ws.n);
     ws.launches += 1;
+    if (forest) {
+        if (ws.mixed)
+            k_scale_by_system<float><<<gs, 256, 0, ws.st>>>(static_cast<float *>(ws.nearf), ws.n, 3, ws.psys, ws.info);
+        else
+            k_scale_by_system<double><<<gs, 256, 0, ws.st>>>(static_cast<double *>(ws.nearf), ws.n, 3, ws.psys, ws.info);
+        ws.launches += 1;
+    }
 }
 
 void direct_sum(Workspace &ws, const double *x_orig, const long long *targets, unsigned nt, double *out_soa,

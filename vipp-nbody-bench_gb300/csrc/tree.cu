@@ -78,6 +78,8 @@ __global__ void k_bbox_partial(const double *__restrict__ x, unsigned n, double 
     }
 }
 
+__device__ void set_root_box(TreeInfo *info, const double *mn, const double *mx);
+
 // One block of kTB threads; min and max do not depend on the order of the
 // partials, so the parallel reduction gives the same box as a serial one.
 __global__ void __launch_bounds__(kTB) k_bbox_final(const double *__restrict__ part, int nb, TreeInfo *info) {
@@ -104,7 +106,13 @@ __global__ void __launch_bounds__(kTB) k_bbox_final(const double *__restrict__ p
         mn[a] = DBL_MAX, mx[a] = -DBL_MAX;
         for (int k = 0; k < static_cast<int>(blockDim.x >> 5); ++k) mn[a] = fmin(mn[a], red[a][k]), mx[a] = fmax(mx[a], red[3 + a][k]);
     }
-    const double pad = 1e-5;  // Problem::OCTREE_WIDTH_PADDING (problem.hpp:167)
+    set_root_box(info, mn, mx);
+}
+
+// Root box (padded by Problem::OCTREE_WIDTH_PADDING, problem.hpp:167) and
+// the key parameters derived from it, from the particles' min and max.
+__device__ void set_root_box(TreeInfo *info, const double *mn, const double *mx) {
+    const double pad = 1e-5;
     double S = 0, margin = 0;
     for (int a = 0; a < 3; ++a) {
         info->root_min[a] = mn[a] - pad;
@@ -128,6 +136,54 @@ __global__ void __launch_bounds__(kTB) k_bbox_final(const double *__restrict__ p
     info->key_mfrac = static_cast<unsigned long long>(ceil(ldexp(margin, 32))) + 1;
 }
 
+// Forest: one block per system, the same box as k_bbox_partial/final give
+// for that system alone (min and max are exact), plus the system's particle
+// mass and G m. An empty system gets the box of the origin (no particle
+// uses it).
+__global__ void __launch_bounds__(kTB) k_bbox_sys(const double *__restrict__ x, unsigned n, const unsigned *__restrict__ seg,
+                                                  const double2 *__restrict__ sys_par, TreeInfo *info) {
+    const int sidx = blockIdx.x;
+    const unsigned b = seg[sidx], e = seg[sidx + 1];
+    const long long kmax = ord_key(__double_as_longlong(DBL_MAX)), kmin = ord_key(__double_as_longlong(-DBL_MAX));
+    long long kn[3] = {kmax, kmax, kmax}, kx[3] = {kmin, kmin, kmin};
+    bool bad = false;
+    for (unsigned i = b + threadIdx.x; i < e; i += blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const long long bits = __double_as_longlong(x[static_cast<size_t>(a) * n + i]);
+            const bool fin = ((bits >> 52) & 0x7ff) != 0x7ff;
+            bad |= !fin;
+            const long long k = ord_key(bits);
+            if (fin) kn[a] = min(kn[a], k), kx[a] = max(kx[a], k);
+        }
+    }
+    if (bad) atomicOr(&info->err, kDevNonFinite);
+    __shared__ long long red[6][kTB / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        for (int o = 16; o; o >>= 1) {
+            kn[a] = min(kn[a], __shfl_xor_sync(0xffffffffu, kn[a], o));
+            kx[a] = max(kx[a], __shfl_xor_sync(0xffffffffu, kx[a], o));
+        }
+        if (lane == 0) red[a][w] = kn[a], red[3 + a][w] = kx[a];
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double mn[3], mx[3];
+    for (int a = 0; a < 3; ++a) {
+        long long lo = red[a][0], hi = red[3 + a][0];
+        for (int k = 1; k < kTB / 32; ++k) lo = min(lo, red[a][k]), hi = max(hi, red[3 + a][k]);
+        // +-0 compare equal as doubles: either is the bound (the padding makes them the same)
+        mn[a] = e > b ? __longlong_as_double(ord_key(lo)) : 0.0;
+        mx[a] = e > b ? __longlong_as_double(ord_key(hi)) : 0.0;
+    }
+    TreeInfo *si = info + sidx;
+    set_root_box(si, mn, mx);
+    si->m = sys_par[sidx].x;
+    si->gm = sys_par[sidx].y;
+}
+
 // Spread the 21 low bits of v to every third bit.
 __device__ __forceinline__ uint64_t spread3(uint64_t v) {
     v &= 0x1fffffull;
@@ -140,12 +196,7 @@ __device__ __forceinline__ uint64_t spread3(uint64_t v) {
 }
 
 // Child offsets of 21 levels of recursive midpoints (see file comment).
-__global__ void k_keys(const double *__restrict__ x, unsigned n, const TreeInfo *__restrict__ info,
-                       uint64_t *__restrict__ keys, unsigned *__restrict__ perm, SortZero z) {
-    sort_temp_zero(z);  // for the key sort that follows
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double p[3] = {x[i], x[static_cast<size_t>(n) + i], x[2 * static_cast<size_t>(n) + i]};
+__device__ __forceinline__ uint64_t morton_key(const double *p, const TreeInfo *__restrict__ info) {
     // Fast path: every split decision of the 21 levels compares x with a
     // midpoint that sits at an integer of u = (x - lo) 2^21 / H up to the
     // rounding bounded by key_margin, so away from integers the child offsets
@@ -165,11 +216,7 @@ __global__ void k_keys(const double *__restrict__ x, unsigned n, const TreeInfo 
             ok &= q >= 0 && q < (1LL << 53) && fr > mf && fr < (1ull << 32) - mf;
             k[a] = ok ? (~static_cast<uint64_t>(q >> 32)) & 0x1fffffull : 0;
         }
-        if (ok) {
-            keys[i] = spread3(k[0]) | (spread3(k[1]) << 1) | (spread3(k[2]) << 2);
-            perm[i] = i;
-            return;
-        }
+        if (ok) return spread3(k[0]) | (spread3(k[1]) << 1) | (spread3(k[2]) << 2);
     }
     double lo[3] = {info->root_min[0], info->root_min[1], info->root_min[2]};
     double hi[3] = {info->root_max[0], info->root_max[1], info->root_max[2]};
@@ -188,24 +235,67 @@ __global__ void k_keys(const double *__restrict__ x, unsigned n, const TreeInfo 
         }
         key = (key << 3) | dig;
     }
-    keys[i] = key;
+    return key;
+}
+
+__global__ void k_keys(const double *__restrict__ x, unsigned n, const TreeInfo *__restrict__ info,
+                       uint64_t *__restrict__ keys, unsigned *__restrict__ perm, SortZero z) {
+    sort_temp_zero(z);  // for the key sort that follows
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double p[3] = {x[i], x[static_cast<size_t>(n) + i], x[2 * static_cast<size_t>(n) + i]};
+    keys[i] = morton_key(p, info);
     perm[i] = i;
+}
+
+// Forest: the Morton key of particle i in its own system's root box (kept in
+// mkeys) and the sort word (system << 3 sorted | top `sorted` levels of the
+// key), so that one stable sort orders every system's particles as a sort of
+// that system alone would, systems in order.
+__global__ void k_keys_forest(const double *__restrict__ x, unsigned n, const TreeInfo *__restrict__ info,
+                              const int *__restrict__ psys, int sorted, uint64_t *__restrict__ words,
+                              unsigned *__restrict__ perm, uint64_t *__restrict__ mkeys, SortZero z) {
+    sort_temp_zero(z);
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double p[3] = {x[i], x[static_cast<size_t>(n) + i], x[2 * static_cast<size_t>(n) + i]};
+    const int sidx = psys[i];
+    const uint64_t key = morton_key(p, info + sidx);
+    mkeys[i] = key;
+    words[i] = (static_cast<uint64_t>(sidx) << (3 * sorted)) | (key >> path_shift(sorted));
+    perm[i] = i;
+}
+
+// Forest: the Morton keys in sorted order.
+__global__ void k_forest_morton(const uint64_t *__restrict__ mkeys, const unsigned *__restrict__ perm, unsigned n,
+                                uint64_t *__restrict__ keys) {
+    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) keys[j] = mkeys[perm[j]];
 }
 
 // Keys are sorted on their top `sorted` levels only (particles inside a leaf
 // are put in index order afterwards, so deeper key bits never matter while no
 // cell of level `sorted` has to split). A run whose level-`sorted` prefix
 // still holds more than T particles asks for a deeper sort through counts[9].
-__global__ void k_split_count(const uint64_t *__restrict__ keys, unsigned n, int T, int sorted, unsigned *__restrict__ cnt,
+// A forest (psys, seg non-null) treats each system's positions [seg[s],
+// seg[s+1]) as a tree of its own: a system's first particle starts runs of
+// every level, and no run reaches into the next system. Its sort words hold
+// at most sorted_cap key levels; a system that needs more is an error.
+__global__ void k_split_count(const uint64_t *__restrict__ keys, unsigned n, int T, int sorted, int sorted_cap,
+                              const int *__restrict__ psys, const unsigned *__restrict__ seg, unsigned *__restrict__ cnt,
                               unsigned *counts, TreeInfo *info) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int Ls = i == 0 ? 0 : first_diff_level(keys[i - 1], keys[i]);
+    const unsigned sb = psys ? seg[psys[i]] : 0u, se = psys ? seg[psys[i] + 1] : n;
+    const int Ls = i == sb ? 0 : first_diff_level(keys[i - 1], keys[i]);
     int Lm = -1;
-    if (static_cast<unsigned long long>(i) + T < n) {
+    if (static_cast<unsigned long long>(i) + T < se) {
         Lm = first_diff_level(keys[i], keys[i + T]) - 1;
-        if (Lm >= sorted && sorted < kMaxLevel) {
-            atomicMax(&counts[9], static_cast<unsigned>(min(sorted + 6, kMaxLevel)));
+        if (Lm >= sorted && sorted < sorted_cap) {
+            atomicMax(&counts[9], static_cast<unsigned>(min(sorted + 6, sorted_cap)));
+            Lm = sorted - 1;
+        } else if (Lm >= sorted && sorted < kMaxLevel) {  // a forest system deeper than its sort word
+            atomicOr(&info->err, kDevForestDepth);
             Lm = sorted - 1;
         } else if (Lm >= kMaxLevel) {  // a deepest-level cell would still split
             atomicOr(&info->err, kDevDepth);
@@ -219,8 +309,9 @@ __global__ void k_split_count(const uint64_t *__restrict__ keys, unsigned n, int
 // an overflow of the split buffer or a too shallow key sort (seen by thread
 // 0, which zeroes the count) the attempt builds a root-only tree (nothing
 // addresses past a buffer) and the host repeats it.
-__global__ void k_split_emit(const uint64_t *__restrict__ keys, unsigned n, int T, const unsigned *__restrict__ off,
-                             unsigned *counts, unsigned s_cap, uint64_t *__restrict__ ent, TreeInfo *info, SortZero z) {
+__global__ void k_split_emit(const uint64_t *__restrict__ keys, unsigned n, int T, int sorted, const int *__restrict__ psys,
+                             const unsigned *__restrict__ seg, const unsigned *__restrict__ off, unsigned *counts,
+                             unsigned s_cap, uint64_t *__restrict__ ent, TreeInfo *info, SortZero z) {
     sort_temp_zero(z);  // for the entry sort that follows (the key sort is done with them)
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned total = counts[1];
@@ -231,9 +322,12 @@ __global__ void k_split_emit(const uint64_t *__restrict__ keys, unsigned n, int 
     }
     // a block that reads counts[1] after thread 0 zeroed it sees 0 and also writes nothing
     if (i >= n || over || total == 0) return;
-    const int Ls = i == 0 ? 0 : first_diff_level(keys[i - 1], keys[i]);
+    const unsigned sb = psys ? seg[psys[i]] : 0u, se = psys ? seg[psys[i] + 1] : n;
+    const int Ls = i == sb ? 0 : first_diff_level(keys[i - 1], keys[i]);
     int Lm = -1;
-    if (static_cast<unsigned long long>(i) + T < n) Lm = min(first_diff_level(keys[i], keys[i + T]) - 1, kMaxLevel - 1);
+    // (sorted - 1 caps Lm only where k_split_count reported an error)
+    if (static_cast<unsigned long long>(i) + T < se)
+        Lm = min(first_diff_level(keys[i], keys[i + T]) - 1, min(kMaxLevel, sorted) - 1);
     unsigned o = off[i];
     for (int L = Ls; L <= Lm; ++L, ++o)
         if (o < s_cap) ent[o] = (static_cast<uint64_t>(L) << 32) | i;
@@ -266,7 +360,9 @@ __device__ void path_geometry(uint64_t path, int L, const TreeInfo *info, double
 
 // One warp: lane L finds level L's split entries (ent is sorted by level),
 // then the cell counts and starts of every level follow by a warp scan.
-__global__ void k_level_table(const uint64_t *__restrict__ ent, unsigned *counts, TreeInfo *info, unsigned n, int T,
+// A forest has nroots roots at level 0 (cells 0 .. nroots-1, set up by
+// k_roots); one tree has the root cell set up here.
+__global__ void k_level_table(const uint64_t *__restrict__ ent, unsigned *counts, TreeInfo *info, unsigned n, int T, int nroots,
                               int *c_begin, int *c_end, int *c_parent, int *c_child, int *c_level, uint64_t *c_path,
                               int *c_coord, double *c_box, double *c_ctr, int *p2p_own, int *p2p_cnt, int *coll,
                               int *coll_cnt) {
@@ -285,7 +381,7 @@ __global__ void k_level_table(const uint64_t *__restrict__ ent, unsigned *counts
     // cells of level L: 1 at the root, 8 per split cell of level L - 1
     const unsigned below = __shfl_up_sync(0xffffffffu, split, 1);
     const bool lv = L <= kMaxLevel + 1;
-    const int cnt = !lv ? 0 : (L == 0 ? 1 : 8 * static_cast<int>(below));
+    const int cnt = !lv ? 0 : (L == 0 ? nroots : 8 * static_cast<int>(below));
     int incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -305,6 +401,7 @@ __global__ void k_level_table(const uint64_t *__restrict__ ent, unsigned *counts
         info->n_targets_m2l = depth >= 2 ? start - start2 : 0;
         counts[2] = static_cast<unsigned>(start);
         counts[3] = static_cast<unsigned>(start) - S;
+        if (nroots != 1) return;
         // the root cell
         c_begin[0] = 0;
         c_end[0] = static_cast<int>(n);
@@ -350,13 +447,50 @@ __device__ void path_geometry(uint64_t path, int L, const TreeInfo *info, double
 }
 
 
+// Forest roots: cell k is system k's root, its particles seg[k] .. seg[k+1],
+// its box the system's root box; calc_link at each root as at a single tree's
+// (solver_ref.hpp:148-154).
+__global__ void k_roots(const uint64_t *__restrict__ ent, const unsigned *__restrict__ seg, int nsys, int T,
+                        const TreeInfo *__restrict__ info, int *c_begin, int *c_end, int *c_parent, int *c_child,
+                        int *c_level, uint64_t *c_path, int *c_coord, double *c_box, double *c_ctr, int *c_sys,
+                        int *p2p_own, int *p2p_cnt, int *coll, int *coll_cnt) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nsys; r += gridDim.x * blockDim.x) {
+        const unsigned b = seg[r], e = seg[r + 1];
+        c_begin[r] = static_cast<int>(b);
+        c_end[r] = static_cast<int>(e);
+        c_parent[r] = -1;
+        c_level[r] = 0;
+        c_path[r] = 0;
+        c_sys[r] = r;
+        const bool split = static_cast<long long>(e) - b > T;
+        int fc = -1;
+        if (split) {  // its level-0 split entry is (0, b); the entries of level 0 are in system order
+            const unsigned a = static_cast<unsigned>(info->split_start[0]);
+            const unsigned rk = lower_bound_ent(ent, a, a + static_cast<unsigned>(info->split_count[0]), b) - a;
+            fc = info->level_start[1] + 8 * static_cast<int>(rk);
+        }
+        c_child[r] = fc;
+        path_geometry(0, 0, info + r, c_box + 6 * static_cast<size_t>(r), c_ctr + 3 * static_cast<size_t>(r),
+                      c_coord + 3 * static_cast<size_t>(r));
+        const size_t o = static_cast<size_t>(r) * kNbrCap;
+        if (split) {
+            coll[o] = r, coll_cnt[r] = 1, p2p_cnt[r] = 0;
+        } else {
+            p2p_own[o] = r, p2p_cnt[r] = 1, coll_cnt[r] = 0;
+        }
+    }
+}
+
 // One thread per (split cell, child octant): the 8 threads of a split cell
 // find its number and particle range (the same searches, in one warp), then
 // each its child's range, links and geometry.
+// In a forest (psys non-null) the searches stay inside the entry's system,
+// whose root is cell psys[i], and every child records its system.
 __global__ void k_cells(const uint64_t *__restrict__ ent, const unsigned *counts, const uint64_t *__restrict__ keys,
-                        unsigned n, int T, const TreeInfo *__restrict__ info, int *split_cell, int *c_begin, int *c_end,
-                        int *c_parent, int *c_child, int *c_level, uint64_t *c_path, int *c_coord, double *c_box,
-                        double *c_ctr) {
+                        unsigned n, int T, const TreeInfo *__restrict__ info, const int *__restrict__ psys,
+                        const unsigned *__restrict__ seg, int *split_cell, int *c_begin, int *c_end, int *c_parent,
+                        int *c_child, int *c_level, uint64_t *c_path, int *c_coord, double *c_box, double *c_ctr,
+                        int *c_sys) {
     const unsigned S = counts[1];
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < 8u * S; t += gridDim.x * blockDim.x) {
         const unsigned e = t >> 3;
@@ -366,17 +500,19 @@ __global__ void k_cells(const uint64_t *__restrict__ ent, const unsigned *counts
         const unsigned r = e - static_cast<unsigned>(info->split_start[L]);
         const int sh = path_shift(L);
         const uint64_t pre = L == 0 ? 0 : (keys[i] >> sh);
-        int own = 0;
+        const int sidx = psys ? psys[i] : 0;
+        const unsigned sb = psys ? seg[sidx] : 0u, se = psys ? seg[sidx + 1] : n;
+        int own = sidx;
         if (L > 0) {
             const int shp = path_shift(L - 1);
-            const unsigned ip = lower_bound_pre(keys, 0, i, shp, keys[i] >> shp);
+            const unsigned ip = lower_bound_pre(keys, sb, i, shp, keys[i] >> shp);
             const unsigned a = static_cast<unsigned>(info->split_start[L - 1]);
             const unsigned b = a + static_cast<unsigned>(info->split_count[L - 1]);
             const unsigned rp = lower_bound_ent(ent, a, b, (static_cast<uint64_t>(L - 1) << 32) | ip) - a;
             own = info->level_start[L] + 8 * static_cast<int>(rp) + static_cast<int>(pre & 7u);
         }
         if (o == 0) split_cell[e] = own;
-        const unsigned pe = L == 0 ? n : lower_bound_pre(keys, i + 1, n, sh, pre + 1);
+        const unsigned pe = L == 0 ? se : lower_bound_pre(keys, i + 1, se, sh, pre + 1);
         const int shc = path_shift(L + 1);
         const unsigned a1 = static_cast<unsigned>(info->split_start[L + 1]);
         const unsigned b1 = a1 + static_cast<unsigned>(info->split_count[L + 1]);
@@ -398,7 +534,8 @@ __global__ void k_cells(const uint64_t *__restrict__ ent, const unsigned *counts
                 fc = info->level_start[L + 2] + 8 * static_cast<int>(rc);
             }
             c_child[c] = fc;
-            path_geometry(cpath, L + 1, info, c_box + 6 * static_cast<size_t>(c), c_ctr + 3 * static_cast<size_t>(c),
+            if (c_sys) c_sys[c] = sidx;
+            path_geometry(cpath, L + 1, info + sidx, c_box + 6 * static_cast<size_t>(c), c_ctr + 3 * static_cast<size_t>(c),
                           c_coord + 3 * static_cast<size_t>(c));
         }
     }
@@ -484,11 +621,15 @@ __global__ void k_leaf_sort(const int *__restrict__ leaves, const unsigned *coun
     }
 }
 
+// Positions in tree order; the FP32 hi/lo pairs relative to the root-box
+// centre (a forest: the system's, with the system's particle mass).
 __global__ void k_gather(const double *__restrict__ x, unsigned n, const unsigned *__restrict__ perm,
-                         const TreeInfo *__restrict__ info, float mass_f, double *__restrict__ xs, float4 *__restrict__ ph,
-                         float4 *__restrict__ pl, unsigned *__restrict__ inv) {
+                         const TreeInfo *__restrict__ info_all, const int *__restrict__ psys, float mass_f,
+                         double *__restrict__ xs, float4 *__restrict__ ph, float4 *__restrict__ pl, unsigned *__restrict__ inv) {
     const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
+    const TreeInfo *info = psys ? info_all + psys[j] : info_all;
+    if (psys) mass_f = static_cast<float>(info->m);
     const unsigned i = perm[j];
     inv[i] = j;
     double d[3];
@@ -505,10 +646,12 @@ __global__ void k_gather(const double *__restrict__ x, unsigned n, const unsigne
 
 // One warp per non-leaf cell P: its 27 same-level neighbours, then for each of
 // its 8 children the colleague, own-p2p and M2L entries (solver_ref.hpp:129-147).
+// In a forest a level holds the systems' cells in system order, path order
+// inside each: neighbours are searched by (system, path).
 __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts, const int *__restrict__ split_cell,
                         const TreeInfo *__restrict__ info, const int *__restrict__ c_child,
-                        const uint64_t *__restrict__ c_path, const int *__restrict__ c_coord, int *m2l_src, int *p2p_own,
-                        int *p2p_cnt, int *coll, int *coll_cnt, unsigned long long *m2l_pairs) {
+                        const uint64_t *__restrict__ c_path, const int *__restrict__ c_coord, const int *__restrict__ c_sys,
+                        int *m2l_src, int *p2p_own, int *p2p_cnt, int *coll, int *coll_cnt, unsigned long long *m2l_pairs) {
     __shared__ int nb[8][32], ord[8][32], nord[8];
     __shared__ int uch[8][27 * 8];  // per neighbour (in order) and octant: child u, or ~u if u is a leaf
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -538,15 +681,19 @@ __global__ void k_lists(const uint64_t *__restrict__ ent, const unsigned *counts
                     for (int a = 0; a < 3; ++a) dig |= static_cast<unsigned>(1 - ((qc[a] >> (L - l)) & 1)) << a;
                     path = (path << 3) | dig;
                 }
+                const int sP = cell_system(c_sys, P);
                 int lo = info->level_start[L], hi = lo + info->level_count[L];
                 while (lo < hi) {
                     const int mid = (lo + hi) >> 1;
-                    if (c_path[mid] < path)
+                    const int sm = cell_system(c_sys, mid);
+                    if (sm < sP || (sm == sP && c_path[mid] < path))
                         lo = mid + 1;
                     else
                         hi = mid;
                 }
-                if (lo < info->level_start[L] + info->level_count[L] && c_path[lo] == path && c_child[lo] >= 0) q = lo;
+                if (lo < info->level_start[L] + info->level_count[L] && cell_system(c_sys, lo) == sP && c_path[lo] == path &&
+                    c_child[lo] >= 0)
+                    q = lo;
             }
         }
         nb[w][lane] = q;
@@ -755,40 +902,194 @@ __global__ void k_eval_begin(TreeInfo *info, unsigned *counts, unsigned n, unsig
 
 inline unsigned grid_for(unsigned n, int tb) { return (n + tb - 1) / tb; }
 
+// ---------------------------------------------------------------- forest tiles
+// The M2M/L2L and M2L kernels apply one operator to a tile of cells, and a
+// forest's operators are per system (each system has its own root box), so
+// every tile holds cells of one system. M2M/L2L tiles: runs of one level's
+// split entries of one system (the entries of a level ascend by particle,
+// hence by system) cut into tiles of kEntTile. M2L tiles: the target octets
+// (8 sibling cells at level >= 2) of one system, listed system by system, cut
+// into tiles of `rows` octets.
+constexpr int kEntTile = 64;
+
+__device__ __forceinline__ int ent_system(const uint64_t *ent, const int *psys, unsigned e) {
+    return psys[static_cast<unsigned>(ent[e] & 0xffffffffu)];
+}
+
+// first e in [lo, hi) whose system is >= sv
+__device__ unsigned lower_bound_system(const uint64_t *ent, const int *psys, unsigned lo, unsigned hi, int sv) {
+    while (lo < hi) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (ent_system(ent, psys, mid) < sv)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_etile_flag(const uint64_t *__restrict__ ent, const unsigned *counts, const int *__restrict__ psys,
+                             const TreeInfo *__restrict__ info, unsigned *flag) {
+    const unsigned S = counts[1];
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < S; e += gridDim.x * blockDim.x) {
+        const int L = static_cast<int>(ent[e] >> 32);
+        const unsigned rs = lower_bound_system(ent, psys, static_cast<unsigned>(info->split_start[L]), e, ent_system(ent, psys, e));
+        flag[e] = (e - rs) % kEntTile == 0 ? 1u : 0u;
+    }
+}
+
+__global__ void k_etile_fill(const uint64_t *__restrict__ ent, const unsigned *counts, const int *__restrict__ psys,
+                             const unsigned *__restrict__ flag, const unsigned *__restrict__ off, TreeInfo *info, int2 *etile) {
+    const unsigned S = counts[1];
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < S; e += gridDim.x * blockDim.x) {
+        const int L = static_cast<int>(ent[e] >> 32);
+        const unsigned a = static_cast<unsigned>(info->split_start[L]), b = a + static_cast<unsigned>(info->split_count[L]);
+        if (flag[e]) {
+            const unsigned re = lower_bound_system(ent, psys, e, b, ent_system(ent, psys, e) + 1);
+            etile[off[e]] = make_int2(static_cast<int>(e), static_cast<int>(min(re - e, static_cast<unsigned>(kEntTile))));
+        }
+        if (e == a) info->etile_start[L] = static_cast<int>(off[e]);
+        if (e + 1 == b) info->etile_end[L] = static_cast<int>(off[e] + flag[e]);
+    }
+}
+
+__global__ void k_oct_count(const TreeInfo *__restrict__ info, const int *__restrict__ c_sys, unsigned *ocnt) {
+    const int base = info->level_start[2], O = info->n_targets_m2l / 8;
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < O; o += gridDim.x * blockDim.x) atomicAdd(&ocnt[c_sys[base + 8 * o]], 1u);
+}
+
+// Exclusive scan of one value per thread over a block of 1024 threads.
+__device__ unsigned block_scan_excl(unsigned v, unsigned *wsum, unsigned &total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        unsigned x = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        wsum[lane] = x;
+    }
+    __syncthreads();
+    const unsigned r = (w ? wsum[w - 1] : 0u) + incl - v;
+    total = wsum[31];
+    __syncthreads();
+    return r;
+}
+
+// One block of 1024 threads, each a contiguous range of systems: list
+// offsets, tiles, and the fill cursors zeroed.
+__global__ void __launch_bounds__(1024) k_oct_plan(int nsys, int rows, unsigned *ocnt, TreeInfo *info, int4 *otile) {
+    __shared__ unsigned wsum[32];
+    const int per = (nsys + 1023) / 1024;
+    const int s0 = min(nsys, static_cast<int>(threadIdx.x) * per), s1 = min(nsys, s0 + per);
+    unsigned octs = 0, tiles = 0;
+    for (int s = s0; s < s1; ++s) octs += ocnt[s], tiles += (ocnt[s] + rows - 1) / rows;
+    unsigned tot_o, tot_t;
+    unsigned oo = block_scan_excl(octs, wsum, tot_o);
+    unsigned to = block_scan_excl(tiles, wsum, tot_t);
+    for (int s = s0; s < s1; ++s) {
+        const unsigned c = ocnt[s];
+        ocnt[nsys + s] = oo;
+        ocnt[2 * nsys + s] = 0;
+        for (unsigned k = 0; k * rows < c; ++k)
+            otile[to++] = make_int4(s, static_cast<int>(oo + k * rows), static_cast<int>(min(static_cast<unsigned>(rows), c - k * rows)), 0);
+        oo += c;
+    }
+    if (threadIdx.x == 0) info->n_otiles = static_cast<int>(tot_t);
+}
+
+__global__ void k_oct_fill(const TreeInfo *__restrict__ info, const int *__restrict__ c_sys, int nsys, unsigned *ocnt,
+                           int *oct_list) {
+    const int base = info->level_start[2], O = info->n_targets_m2l / 8;
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < O; o += gridDim.x * blockDim.x) {
+        const int sidx = c_sys[base + 8 * o];
+        oct_list[ocnt[nsys + sidx] + atomicAdd(&ocnt[2 * nsys + sidx], 1u)] = o;
+    }
+}
+
 }  // namespace
+
+void forest_tiles(Workspace &ws, int rows) {
+    cudaStream_t st = ws.st;
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 4, ceil_div(ws.c_cap, kTB));
+    k_etile_flag<<<gs, kTB, 0, st>>>(ws.ent, ws.d_counts, ws.psys, ws.info, ws.flag);
+    scan_exclusive_u32(ws.flag, ws.flag_off, ws.s_cap, ws.d_counts + 1, ws.d_counts + 10, ws.scan, st, &ws.launches);
+    k_etile_fill<<<gs, kTB, 0, st>>>(ws.ent, ws.d_counts, ws.psys, ws.flag, ws.flag_off, ws.info, ws.etile);
+    cudaMemsetAsync(ws.ocnt, 0, sizeof(unsigned) * ws.nsys, st);
+    k_oct_count<<<gs, kTB, 0, st>>>(ws.info, ws.c_sys, ws.ocnt);
+    k_oct_plan<<<1, 1024, 0, st>>>(ws.nsys, rows, ws.ocnt, ws.info, ws.otile);
+    k_oct_fill<<<gs, kTB, 0, st>>>(ws.info, ws.c_sys, ws.nsys, ws.ocnt, ws.oct_list);
+    ws.launches += 5;
+}
 
 void build_tree(Workspace &ws) {
     const unsigned n = ws.n;
     cudaStream_t st = ws.st;
     timer_begin(ws, kTTree);
     k_eval_begin<<<1, 128, 0, st>>>(ws.info, ws.d_counts, n, ws.queue);
-    const int nb = 2 * ws.num_sms;
-    double *part = ws.bbox_part;
-    k_bbox_partial<<<nb, kTB, 0, st>>>(ws.x, n, part, ws.info);
-    k_bbox_final<<<1, kTB, 0, st>>>(part, nb, ws.info);
-    const int kbit = 3 * (kMaxLevel - ws.sort_levels);
-    k_keys<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.keys0, ws.perm0,
-                                             sort_zero_plan(ws.sort, n, kbit, 3 * kMaxLevel));
-    ws.launches += 4;
-    const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, kbit, 3 * kMaxLevel, ws.sort, st,
-                                   &ws.launches, &ws.info->err, kDevTimeout, true, ws.sort_spin_max);
-    ws.keys = res ? ws.keys1 : ws.keys0;
-    ws.perm = res ? ws.perm1 : ws.perm0;
+    const bool forest = ws.forest();
+    if (!forest) {
+        const int nb = 2 * ws.num_sms;
+        double *part = ws.bbox_part;
+        k_bbox_partial<<<nb, kTB, 0, st>>>(ws.x, n, part, ws.info);
+        k_bbox_final<<<1, kTB, 0, st>>>(part, nb, ws.info);
+        const int kbit = 3 * (kMaxLevel - ws.sort_levels);
+        k_keys<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.keys0, ws.perm0,
+                                                 sort_zero_plan(ws.sort, n, kbit, 3 * kMaxLevel));
+        ws.launches += 4;
+        const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, kbit, 3 * kMaxLevel, ws.sort, st,
+                                       &ws.launches, &ws.info->err, kDevTimeout, true, ws.sort_spin_max);
+        ws.keys = res ? ws.keys1 : ws.keys0;
+        ws.perm = res ? ws.perm1 : ws.perm0;
+    } else {
+        // every system's box, then one sort of (system, key prefix) words and
+        // the Morton keys gathered into sorted order (into the other key buffer)
+        k_bbox_sys<<<ws.nsys, kTB, 0, st>>>(ws.x, n, ws.seg, ws.sys_par, ws.info);
+        const int wbits = 3 * ws.sort_levels + ws.sys_bits;
+        k_keys_forest<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.info, ws.psys, ws.sort_levels, ws.keys0, ws.perm0,
+                                                        ws.mkeys, sort_zero_plan(ws.sort, n, 0, wbits));
+        ws.launches += 3;
+        const int res = radix_sort_u64(ws.keys0, ws.perm0, ws.keys1, ws.perm1, n, nullptr, 0, wbits, ws.sort, st,
+                                       &ws.launches, &ws.info->err, kDevTimeout, true, ws.sort_spin_max);
+        ws.perm = res ? ws.perm1 : ws.perm0;
+        ws.keys = res ? ws.keys0 : ws.keys1;
+        k_forest_morton<<<grid_for(n, kTB), kTB, 0, st>>>(ws.mkeys, ws.perm, n, ws.keys);
+        ws.launches += 1;
+    }
+    const int *psys = forest ? ws.psys : nullptr;
+    const unsigned *seg = forest ? ws.seg : nullptr;
     // split cells of every level
-    k_split_count<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.sort_levels, ws.cnt, ws.d_counts, ws.info);
+    k_split_count<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.sort_levels, forest ? ws.sort_levels_cap() : kMaxLevel,
+                                                    psys, seg, ws.cnt, ws.d_counts, ws.info);
     scan_exclusive_u32(ws.cnt, ws.off, n, nullptr, ws.d_counts + 1, ws.scan, st, &ws.launches);
-    k_split_emit<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.off, ws.d_counts, ws.s_cap, ws.ent0, ws.info,
-                                                   sort_zero_plan(ws.sort, ws.s_cap, 32, 40));
+    k_split_emit<<<grid_for(n, kTB), kTB, 0, st>>>(ws.keys, n, ws.T, ws.sort_levels, psys, seg, ws.off, ws.d_counts,
+                                                   ws.s_cap, ws.ent0, ws.info, sort_zero_plan(ws.sort, ws.s_cap, 32, 40));
     ws.launches += 2;
     const int re = radix_sort_u64(ws.ent0, nullptr, ws.ent1, nullptr, ws.s_cap, ws.d_counts + 1, 32, 40, ws.sort, st,
                                   &ws.launches, &ws.info->err, kDevTimeout, true, ws.sort_spin_max);
     ws.ent = re ? ws.ent1 : ws.ent0;
-    k_level_table<<<1, 32, 0, st>>>(ws.ent, ws.d_counts, ws.info, n, ws.T, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child,
-                                    ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr, ws.p2p_own, ws.p2p_cnt, ws.coll,
-                                    ws.coll_cnt);
+    k_level_table<<<1, 32, 0, st>>>(ws.ent, ws.d_counts, ws.info, n, ws.T, forest ? ws.nsys : 1, ws.c_begin, ws.c_end,
+                                    ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr,
+                                    ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt);
+    if (forest) {
+        k_roots<<<grid_for(ws.nsys, kTB), kTB, 0, st>>>(ws.ent, ws.seg, ws.nsys, ws.T, ws.info, ws.c_begin, ws.c_end,
+                                                        ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord, ws.c_box,
+                                                        ws.c_ctr, ws.c_sys, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt);
+        ws.launches += 1;
+    }
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 4, ceil_div(ws.c_cap, 32));
-    k_cells<<<capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 128)), 128, 0, st>>>(ws.ent, ws.d_counts, ws.keys, n, ws.T, ws.info, ws.split_cell, ws.c_begin, ws.c_end,
-                                ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr);
+    k_cells<<<capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 128)), 128, 0, st>>>(
+        ws.ent, ws.d_counts, ws.keys, n, ws.T, ws.info, psys, seg, ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent,
+        ws.c_child, ws.c_level, ws.c_path, ws.c_coord, ws.c_box, ws.c_ctr, forest ? ws.c_sys : nullptr);
     if (ws.c_cap <= 65536u) {
         k_leaf_list<<<1, 1024, 0, st>>>(ws.c_child, ws.d_counts, ws.leaves);
         ws.launches -= 1;  // one launch in place of the two counted below
@@ -806,10 +1107,10 @@ void build_tree(Workspace &ws) {
         k_leaf_sort<<<capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4)), 32 * nw, smem, st>>>(
             ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.T, ws.perm);
     }
-    k_gather<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.perm, ws.info, static_cast<float>(ws.m), ws.xs, ws.ph, ws.pl,
-                                               ws.inv);
+    k_gather<<<grid_for(n, kTB), kTB, 0, st>>>(ws.x, n, ws.perm, ws.info, psys, static_cast<float>(ws.m), ws.xs, ws.ph,
+                                               ws.pl, ws.inv);
     k_lists<<<gs, 256, 0, st>>>(ws.ent, ws.d_counts, ws.split_cell, ws.info, ws.c_child, ws.c_path, ws.c_coord,
-                                ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
+                                forest ? ws.c_sys : nullptr, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                                 reinterpret_cast<unsigned long long *>(&ws.info->m2l_pairs));
     k_rng_count<<<gs, kTB, 0, st>>>(ws.leaves, ws.d_counts, ws.c_parent, ws.c_begin, ws.c_end, ws.p2p_own, ws.p2p_cnt,
                                     ws.rng_cnt, ws.chunk_cnt, ws.src_total, ws.part_cnt, ws.p2p_slice);

@@ -52,6 +52,26 @@ struct Workspace {
     unsigned p2p_slice = kSliceSources;  // near-field sources per P2P work item
     int m2l_ctas_pct = 100;         // tensor-core M2L CTAs, percent of the SMs (one persistent CTA per SM)
 
+    // forest of independent systems (the batched form; nsys == 1: one tree).
+    // Systems keep their particles contiguous in input and tree order, so
+    // seg[k] .. seg[k+1] are system k's positions in both; cells are numbered
+    // level by level over the whole forest, system by system inside a level
+    // (roots: cells 0 .. nsys-1).
+    int nsys = 1;
+    unsigned *seg = nullptr;        // [nsys + 1] (device)
+    int *psys = nullptr;            // [N] system of each particle position
+    int *c_sys = nullptr;           // [C] system of each cell
+    double2 *sys_par = nullptr;     // [nsys] particle mass and G times it
+    uint64_t *mkeys = nullptr;      // [N] Morton keys in input order (the sort orders (system, key) words)
+    int sys_bits = 0;               // bits of a system index in the sort word
+    int2 *etile = nullptr;          // [s_cap] M2M/L2L tiles: first split entry, entries (<= 64, one system)
+    int *oct_list = nullptr;        // [C / 8] M2L target octets grouped by system
+    int4 *otile = nullptr;          // [C / 8 + nsys] M2L tiles: system, first list entry, octets
+    unsigned *ocnt = nullptr;       // [3 nsys + 1] octets per system, list offsets, fill cursors
+    bool forest() const { return seg != nullptr; }
+    // key levels a sort word holds beside the system index (3 bits a level)
+    int sort_levels_cap() const { return forest() ? (64 - sys_bits) / 3 < kMaxLevel ? (64 - sys_bits) / 3 : kMaxLevel : kMaxLevel; }
+
     // capacities
     unsigned n_cap = 0;   // particles
     unsigned s_cap = 0;   // split entries (non-leaf cells)
@@ -121,7 +141,7 @@ struct Workspace {
     void *m2l_tab = nullptr;  // offset-independent factors of the M2L operator entries (fmm.cu)
     float *bimg = nullptr;    // tensor-core M2L operator images (m2l_tc.cu)
     float *ms_tc = nullptr;   // tensor-core M2L split expansions, 2 ms_rows ms_kp floats (m2l_tc.cu)
-    unsigned ms_rows = 0;     // c_cap + 1: the last row is zero
+    unsigned ms_rows = 0;     // c_cap + kZeroRows: the last rows are zero
     int ms_kp = 0;
     bool ms_bf16 = false;     // the split form tmap_ms was encoded for
     CUtensorMap tmap_ms{};    // TMA map of ms_tc
@@ -152,12 +172,18 @@ inline unsigned capped_grid(unsigned full, size_t work_bound) {
     return b < full ? static_cast<unsigned>(b) : full;
 }
 inline size_t ceil_div(size_t a, size_t b) { return (a + b - 1) / b; }
+// per-cell systems of a forest, or null for one tree
+inline const int *forest_cells(const Workspace &ws) { return ws.forest() ? ws.c_sys : nullptr; }
+constexpr int kM2LTileTC = 128;  // target octets per tensor-core M2L tile (m2l_tc.cu)
+constexpr int kZeroRows = 32;    // zero rows after the split expansions (one per row quad of a tile)
+constexpr int kM2LTileCC = 64;   // per CUDA-core M2L tile (fmm.cu)
 constexpr int kOpM2M = 343;  // op index of M2M octant 0
 constexpr int kOpL2L = 351;  // op index of L2L octant 0
 constexpr int kNumOps = 359;
 
 // stages (all asynchronous on ws.st)
 void build_tree(Workspace &ws);               // bbox, keys, sort, cells, leaves, lists, near-field ranges
+void forest_tiles(Workspace &ws, int rows);   // forest: M2M/L2L tiles and M2L tiles of `rows` octets per system
 void build_operators(Workspace &ws);          // 359 translation matrices for the current root box
 size_t m2l_table_bytes(int p);
 void build_m2l_table(Workspace &ws);          // fill m2l_tab for ws.p (once per p, outside step graphs)
@@ -186,6 +212,8 @@ void conserved_sums(Workspace &ws, const double *phi_orig, double *sums8);  // s
 size_t diag_scratch_doubles();
 void generate_plummer(Workspace &ws, unsigned n, uint64_t seed, double x0_max, double r_max, double x_scale = 1.0,
                       double v_scale = 1.0);  // ic.cu
+// forest: system k's particles are stream family seeds[k] scaled by scales[k] (positions, velocities)
+void generate_plummer_forest(Workspace &ws, const uint64_t *seeds, const double2 *scales, double x0_max, double r_max);
 // clusters (<= 8) Plummer clusters + a uniform background fraction (ic.cu);
 // params (may be null): 8 doubles per cluster, centre[3], radius, bulk[3], size
 int generate_clustered(Workspace &ws, unsigned n, uint64_t seed, int clusters, double background, double r_max,

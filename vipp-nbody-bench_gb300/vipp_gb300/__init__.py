@@ -28,6 +28,7 @@ FLAG_M2L_CUDA_CORES = 2
 FLAG_SERIAL = 4
 FLAG_NO_GRAPH = 8
 FLAG_M2L_BF16 = 16
+FLAG_BATCH_CONTEXTS = 32
 TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4", "soften")
 
 # Every symbol include/vipp_gb300.h declares.
@@ -36,7 +37,8 @@ EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_uplo
            "gb_kernel_times", "gb_launch_count", "gb_version", "gb_stream", "gb_direct_accel_noalloc",
            "gb_get_conserved", "gb_init_plummer", "gb_batch_create", "gb_batch_destroy", "gb_batch_last_error",
            "gb_batch_upload", "gb_batch_download", "gb_batch_rk4_step", "gb_batch_size", "gb_batch_system",
-           "gb_set_tuning", "gb_get_tuning", "gb_tuning_lookup", "gb_init_clustered", "gb_batch_init_plummer")
+           "gb_set_tuning", "gb_get_tuning", "gb_tuning_lookup", "gb_init_clustered", "gb_batch_init_plummer",
+           "gb_batch_is_forest", "gb_batch_forest", "gb_batch_accel", "gb_batch_conserved", "gb_batch_stats", "gb_batch_launch_count")
 TUNING_FIELDS = ("p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s")
 TUNING_DEFAULT = {"p2p_blocks": 8, "p2p_blocks_conc": 8, "p2p_slice": 8192, "m2l_ctas_pct": 100, "serial": 0,
                   "leaf_s": 0}
@@ -108,6 +110,14 @@ def load(path: str | None = None):
     lib.gb_batch_rk4_step.argtypes = [vp, ctypes.c_double]
     lib.gb_batch_system.argtypes = [vp, ctypes.c_size_t]
     lib.gb_batch_system.restype = vp
+    lib.gb_batch_is_forest.argtypes = [vp]
+    lib.gb_batch_forest.argtypes = [vp]
+    lib.gb_batch_forest.restype = vp
+    lib.gb_batch_accel.argtypes = [vp, vp, vp]
+    lib.gb_batch_conserved.argtypes = [vp, vp]
+    lib.gb_batch_stats.argtypes = [vp, ctypes.POINTER(GbStats)]
+    lib.gb_batch_launch_count.argtypes = [vp]
+    lib.gb_batch_launch_count.restype = ctypes.c_int64
     lib.gb_stream.argtypes = [vp]
     lib.gb_stream.restype = vp
     lib.gb_direct_accel_noalloc.argtypes = [vp, ctypes.c_size_t, vp, ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
@@ -346,7 +356,9 @@ def version() -> str:
 class Batch:
     """Independent systems of uneven N advanced together (gb_batch_*):
     sizes[k] particles of system k, concatenated in x and v; masses[k] is the
-    particle mass of system k."""
+    particle mass of system k. The forest form (default) runs every system in
+    one context and one launch per kernel class; flags |= FLAG_BATCH_CONTEXTS
+    gives every system a context of its own (same results)."""
 
     def __init__(self, sizes, p=4, s=32, eps=0.01, G=1.0, masses=None, precision="mixed", device=0, flags=0,
                  mode="ref"):
@@ -383,6 +395,55 @@ class Batch:
     def step(self, dt):
         self._check(self.lib.gb_batch_rk4_step(self.h, float(dt)))
 
+    @property
+    def forest(self) -> bool:
+        return bool(self.lib.gb_batch_is_forest(self.h))
+
+    def accel(self, potential=False):
+        """Accelerations (and potentials) of every system, concatenated."""
+        a = np.zeros((self.n, 3))
+        phi = np.zeros(self.n) if potential else None
+        self._check(self.lib.gb_batch_accel(self.h, _ptr(a), _ptr(phi)))
+        return (a, phi) if potential else a
+
+    def conserved(self) -> list:
+        """Conserved quantities of every system (gb_batch_conserved)."""
+        out = (GbConserved * (len(self.off) - 1))()
+        self._check(self.lib.gb_batch_conserved(self.h, out))
+        return [{"kinetic": c.kinetic, "potential": c.potential, "total": c.total, "momentum": list(c.momentum),
+                 "angular_momentum": list(c.angular_momentum)} for c in out]
+
+    def stats(self) -> dict:
+        st = GbStats()
+        self._check(self.lib.gb_batch_stats(self.h, ctypes.byref(st)))
+        return {f: int(getattr(st, f)) for f, _ in GbStats._fields_}
+
+    def launch_count(self) -> int:
+        return int(self.lib.gb_batch_launch_count(self.h))
+
+    def _forest_ctx(self):
+        c = self.lib.gb_batch_forest(self.h)
+        if not c:
+            raise GB300Error(GB_ERR_INVALID, "kernel timing of a batch needs the forest form")
+        return c
+
+    def enable_timing(self, on=True):
+        """Per-class kernel timers of the forest's context (Solver.enable_timing)."""
+        c = self._forest_ctx()
+        rc = self.lib.gb_enable_timing(c, 1 if on else 0)
+        if rc != GB_OK:
+            raise GB300Error(rc, self.lib.gb_last_error(c).decode())
+
+    def kernel_times(self) -> dict:
+        """{class: (ms, launches)} accumulated since the last call (forest form)."""
+        c = self._forest_ctx()
+        ms = np.zeros(len(TIMER_CLASSES))
+        nl = np.zeros(len(TIMER_CLASSES), dtype=np.int64)
+        rc = self.lib.gb_kernel_times(c, _ptr(ms), _ptr(nl), len(TIMER_CLASSES))
+        if rc != GB_OK:
+            raise GB300Error(rc, self.lib.gb_last_error(c).decode())
+        return {k: (float(ms[i]), int(nl[i])) for i, k in enumerate(TIMER_CLASSES)}
+
     def download(self):
         x = np.zeros((self.n, 3))
         v = np.zeros((self.n, 3))
@@ -390,7 +451,10 @@ class Batch:
         return x, v
 
     def system_stats(self, k) -> dict:
+        """Statistics of system k's own context (contexts form only)."""
         c = self.lib.gb_batch_system(self.h, k)
+        if not c:
+            raise GB300Error(GB_ERR_INVALID, "system_stats needs the contexts form (forest: stats())")
         st = GbStats()
         rc = self.lib.gb_get_stats(c, ctypes.byref(st))
         if rc != GB_OK:
@@ -400,6 +464,8 @@ class Batch:
     def system_accel(self, k):
         """Accelerations of system k at its current positions."""
         c = self.lib.gb_batch_system(self.h, k)
+        if not c:
+            return self.accel()[int(self.off[k]):int(self.off[k + 1])]
         n = int(self.off[k + 1] - self.off[k])
         a = np.zeros((n, 3))
         rc = self.lib.gb_accel(c, _ptr(a), None)
@@ -408,8 +474,11 @@ class Batch:
         return a
 
     def system_conserved(self, k) -> dict:
-        """Conserved quantities of system k (gb_get_conserved on its context)."""
+        """Conserved quantities of system k (gb_get_conserved on its context;
+        the forest form: gb_batch_conserved)."""
         c = self.lib.gb_batch_system(self.h, k)
+        if not c:
+            return self.conserved()[k]
         out = GbConserved()
         rc = self.lib.gb_get_conserved(c, ctypes.byref(out))
         if rc != GB_OK:

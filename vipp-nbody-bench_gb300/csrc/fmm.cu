@@ -106,14 +106,49 @@ struct M2LEnt {
     unsigned char f;    // bit 0: m > 0 (second term), bit 1: input Im part, bit 2: output Im part
 };
 
+// Entries [kind K^2 + ro K + ri]: kind 0 M2L (m2l_coef without rho^-(j+n+1)
+// and Y), 1 M2M and 2 L2L (m2m_coef / l2l_coef without |t|^deg and Y), so
+// that an operator entry is t Z[y] with Z = Y rho^(-deg-1) (M2L) or Y |t|^deg.
+__device__ void shift_entry(int kind, int j, int k, int n, int mm, double &t, int &deg, int &order) {
+    t = 0, deg = 0, order = 0;
+    if (kind == 1) {  // M2M: child (n, mm) into parent (j, k)
+        const int nn = j - n, m_ = k - mm;
+        if (nn < 0 || iabs(m_) > nn) return;
+        deg = nn, order = -m_;
+        t = phase_even(iabs(k) - iabs(m_) - iabs(mm)) * aco(c_at, nn, m_) * aco(c_at, n, mm) * aco_inv(c_at, j, k) *
+            ldexp(1.0, -n);
+    } else {  // L2L: parent (n, mm) into child (j, k)
+        if (n < j || iabs(mm - k) > n - j) return;
+        deg = n - j, order = mm - k;
+        t = phase_even(iabs(mm) - iabs(mm - k) - iabs(k)) * aco(c_at, n - j, mm - k) * aco(c_at, j, k) *
+            (((n + j) % 2 ? -1.0 : 1.0) * aco_inv(c_at, n, mm)) * ldexp(1.0, -(j + 1));
+    }
+}
+
 __global__ void k_m2l_table(int p, M2LEnt *__restrict__ tab) {
     const int K = (p + 1) * (p + 1);
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < K * K; idx += gridDim.x * blockDim.x) {
-        const int ro = idx / K, ri = idx % K;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < 3 * K * K; idx += gridDim.x * blockDim.x) {
+        const int kind = idx / (K * K), ro = (idx % (K * K)) / K, ri = idx % K;
         int j, k, po, n, m, pi;
         rdecode(ro, j, k, po);
         rdecode(ri, n, m, pi);
         M2LEnt e;
+        if (kind > 0) {
+            for (int s = 0; s < 2; ++s) {
+                double t;
+                int deg, order;
+                shift_entry(kind, j, k, n, s == 0 ? m : -m, t, deg, order);
+                if (s == 1 && m == 0) t = 0;
+                e.t[s] = t;
+                e.tf[s] = static_cast<float>(t);
+                e.y[s] = static_cast<short>(ridx(deg, iabs(order), 0));
+                e.sg[s] = static_cast<signed char>(order == 0 ? 0 : (order > 0 ? 1 : -1));
+            }
+            e.q = 0;
+            e.f = static_cast<unsigned char>((m > 0 ? 1 : 0) | (pi ? 2 : 0) | (po ? 4 : 0));
+            tab[idx] = e;
+            continue;
+        }
         for (int s = 0; s < 2; ++s) {
             const int mm = s == 0 ? m : -m;
             const int o = mm - k;
@@ -169,10 +204,10 @@ __device__ __forceinline__ T m2l_entry(const M2LEnt &e, const T *Z) {
 // Mixed precision writes the M2L operators in FP32 only (ops_f; the
 // tensor-core images are split from them); FP64 writes both.
 __global__ void k_build_ops(const TreeInfo *__restrict__ info_all, int p, const M2LEnt *__restrict__ m2l_tab,
-                            double *__restrict__ ops_d, float *__restrict__ ops_f, bool mixed) {
+                            double *__restrict__ ops_d, float *__restrict__ ops_f, bool mixed, int b0) {
     extern __shared__ double sm[];
     const int K = (p + 1) * (p + 1);
-    const int b = blockIdx.x;
+    const int b = b0 + static_cast<int>(blockIdx.x);
     const TreeInfo *info = info_all + blockIdx.y;
     int kind;
     double tv[3];
@@ -266,6 +301,97 @@ __global__ void k_build_ops(const TreeInfo *__restrict__ info_all, int p, const 
         const double v = real_entry(kind, c_at, yt, pw, j, k, po, n, m, pi);
         od[idx] = v;
         of[idx] = static_cast<float>(v);
+    }
+}
+
+// The FP32 operators of the mixed forms for kSysPerBlock systems at once
+// (blockIdx.x: operator, as in k_build_ops; blockIdx.y: group of systems):
+// warp g forms system g's Z table (k_build_ops's harmonics), then every
+// thread reads each table entry once for all the group's systems (the table
+// is the main traffic: one read per operator made a forest's 512 x 359
+// operators cost ~8 ms per evaluation). M2L entries: the values of
+// k_build_ops's mixed branch; M2M and L2L: t Z[y] from the same kind of table.
+constexpr int kSysPerBlock = 8;
+
+__global__ void __launch_bounds__(32 * kSysPerBlock) k_build_ops_f(const TreeInfo *__restrict__ info_all, int nsys, int p,
+                                                               const M2LEnt *__restrict__ tabs, float *__restrict__ ops_f) {
+    extern __shared__ double sm[];
+    const int K = (p + 1) * (p + 1), nmax = (2 * p + 1) * (2 * p + 1);
+    const int b = blockIdx.x;
+    int kind = 0, oct = 0;
+    int dd[3] = {b % 7 - 3, (b / 7) % 7 - 3, b / 49 - 3};
+    if (b < kOpM2M) {
+        if (abs(dd[0]) <= 1 && abs(dd[1]) <= 1 && abs(dd[2]) <= 1) return;
+    } else {
+        kind = b < kOpL2L ? 1 : 2;
+        oct = (b - kOpM2M) & 7;
+    }
+    const int D = kind == 0 ? 2 * p : p, ny = (D + 1) * (D + 1);
+    const M2LEnt *tab = tabs + static_cast<size_t>(kind) * K * K;
+    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sys0 = blockIdx.y * kSysPerBlock;
+    const int per = nmax + 2 * p + 3;  // doubles per system: yt, pw
+    double *yt = sm + g * per, *pw = yt + nmax;
+    float *Zf = reinterpret_cast<float *>(sm + kSysPerBlock * per) + g * nmax;
+    if (sys0 + g < nsys) {
+        const TreeInfo *info = info_all + sys0 + g;
+        double tv[3];
+        if (kind == 0) {
+            for (int a = 0; a < 3; ++a) tv[a] = dd[a] * info->H[a] / info->S;
+        } else {
+            for (int a = 0; a < 3; ++a) {
+                const double sg = ((oct >> a) & 1) ? -1.0 : 1.0;
+                tv[a] = (kind == 1 ? sg : -sg) * info->H[a] / (4.0 * info->S);
+            }
+        }
+        const double rho = sqrt(tv[0] * tv[0] + tv[1] * tv[1] + tv[2] * tv[2]);
+        const double x = tv[0] / rho, y = tv[1] / rho, z = tv[2] / rho;
+        const HTab<double> &t = c_htd;
+        if (lane == 0) {
+            double cre = 1, cim = 0;
+            for (int m = 0; m <= D; ++m) {
+                if (m > 0) {
+                    const double nre = t.mm[m] * (x * cre - y * cim);
+                    const double nim = t.mm[m] * (x * cim + y * cre);
+                    cre = nre, cim = nim;
+                }
+                yt[ridx(m, m, 0)] = cre;
+                if (m > 0) yt[ridx(m, m, 1)] = cim;
+            }
+        } else if (lane == 31) {
+            double a = 1;
+            const double f = kind == 0 ? 1.0 / rho : rho;
+            for (int i = 0; i < 2 * p + 3; ++i) pw[i] = a, a *= f;
+        }
+        __syncwarp();
+        const int m = lane;
+        if (m <= D) {
+            const double r2 = x * x + y * y + z * z;
+            const double cre = yt[ridx(m, m, 0)], cim = m > 0 ? yt[ridx(m, m, 1)] : 0.0;
+            if (m + 1 <= D) {
+                yt[ridx(m + 1, m, 0)] = t.m1[m] * z * cre;
+                if (m > 0) yt[ridx(m + 1, m, 1)] = t.m1[m] * z * cim;
+            }
+            for (int n = m + 2; n <= D; ++n) {
+                yt[ridx(n, m, 0)] = t.ra[n][m] * z * yt[ridx(n - 1, m, 0)] - t.rb[n][m] * r2 * yt[ridx(n - 2, m, 0)];
+                if (m > 0) yt[ridx(n, m, 1)] = t.ra[n][m] * z * yt[ridx(n - 1, m, 1)] - t.rb[n][m] * r2 * yt[ridx(n - 2, m, 1)];
+            }
+        }
+        __syncwarp();
+        for (int yy = lane; yy < ny; yy += 32) {
+            int dg = static_cast<int>(sqrtf(static_cast<float>(yy)));
+            while (dg * dg > yy) --dg;
+            while ((dg + 1) * (dg + 1) <= yy) ++dg;
+            Zf[yy] = static_cast<float>(yt[yy] * pw[kind == 0 ? dg + 1 : dg]);
+        }
+    }
+    __syncthreads();
+    const int ng = min(kSysPerBlock, nsys - sys0);
+    const float *Zs = reinterpret_cast<const float *>(sm + kSysPerBlock * per);
+    for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
+        const M2LEnt e = tab[idx];
+        for (int q = 0; q < ng; ++q)
+            ops_f[((static_cast<size_t>(sys0 + q)) * kNumOps + b) * K * K + idx] = m2l_entry<float>(e, Zs + q * nmax);
     }
 }
 
@@ -867,9 +993,9 @@ void dispatch_p(Workspace &ws, int which, double *farphi = nullptr) {
 
 }  // namespace
 
-size_t m2l_table_bytes(int p) {
+size_t m2l_table_bytes(int p) {  // M2L, M2M and L2L tables
     const size_t K = static_cast<size_t>(p + 1) * (p + 1);
-    return sizeof(M2LEnt) * K * K;
+    return 3 * sizeof(M2LEnt) * K * K;
 }
 
 void build_m2l_table(Workspace &ws) {
@@ -881,8 +1007,16 @@ void build_operators(Workspace &ws) {
     timer_begin(ws, kTOps);
     const size_t ny = static_cast<size_t>(2 * ws.p + 1) * (2 * ws.p + 1);  // yt, pw, Z, Zf
     const size_t smem = sizeof(double) * (2 * ny + 2 * ws.p + 3) + sizeof(float) * ny;
-    k_build_ops<<<dim3(kNumOps, ws.forest() ? ws.nsys : 1), 256, smem, ws.st>>>(
-        ws.info, ws.p, static_cast<const M2LEnt *>(ws.m2l_tab), ws.ops_d, ws.ops_f, ws.mixed);
+    const int nsys = ws.forest() ? ws.nsys : 1;
+    if (ws.mixed) {
+        // M2L offsets: FP32 operators, kSysPerBlock systems per block; then M2M and L2L
+        const size_t smem_f = kSysPerBlock * (sizeof(double) * (ny + 2 * ws.p + 3) + sizeof(float) * ny);
+        k_build_ops_f<<<dim3(kNumOps, (nsys + kSysPerBlock - 1) / kSysPerBlock), 32 * kSysPerBlock, smem_f, ws.st>>>(
+            ws.info, nsys, ws.p, static_cast<const M2LEnt *>(ws.m2l_tab), ws.ops_f);
+    } else {
+        k_build_ops<<<dim3(kNumOps, nsys), 256, smem, ws.st>>>(ws.info, ws.p, static_cast<const M2LEnt *>(ws.m2l_tab), ws.ops_d,
+                                                              ws.ops_f, false, 0);
+    }
     ws.launches += 1;
     timer_end(ws, kTOps);
 }

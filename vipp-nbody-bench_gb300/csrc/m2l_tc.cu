@@ -639,24 +639,42 @@ __global__ void k_build_bimg(const float *__restrict__ ops_all, unsigned char *_
     unsigned char *bimg = bimg_all + static_cast<size_t>(blockIdx.y) * (kNumOffsets * C::NKC * 2 * C::B_BYTES);
     const int d0 = oi % 7 - 3, d1 = (oi / 7) % 7 - 3, d2 = oi / 49 - 3;
     if (d0 >= -1 && d0 <= 1 && d1 >= -1 && d1 <= 1 && d2 >= -1 && d2 <= 1) return;
+    // one 16-byte store per thread and step: 8 bf16 or 4 tf32 consecutive K elements of a row
+    constexpr int VE = BF ? 8 : 4;
+    constexpr int RUNS = C::KC / VE;
     for (int kc = 0; kc < C::NKC; ++kc) {
         unsigned char *blk = bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::B_BYTES);
-        for (int i = threadIdx.x; i < 2 * C::N * C::KC; i += blockDim.x) {
-            const int r = i / C::KC, k = i % C::KC, j = kc * C::KC + k;
+        for (int u = threadIdx.x; u < 2 * C::N * RUNS; u += blockDim.x) {
+            const int r = u / RUNS, k0 = (u % RUNS) * VE;
             const bool lo_row = r >= C::N;
             const int ro = lo_row ? r - C::N : r;
-            int ci = j;
-            bool use = j < C::K;
-            if (BF && j >= C::K && j < 2 * C::K) ci = j - C::K, use = !lo_row;
-            const float v = (use && ro < C::K) ? ops[(static_cast<size_t>(oi) * C::K + ro) * C::K + ci] : 0.f;
+            float v[VE];
+#pragma unroll
+            for (int e = 0; e < VE; ++e) {
+                const int j = kc * C::KC + k0 + e;
+                int ci = j;
+                bool use = j < C::K;
+                if (BF && j >= C::K && j < 2 * C::K) ci = j - C::K, use = !lo_row;
+                v[e] = (use && ro < C::K) ? ops[(static_cast<size_t>(oi) * C::K + ro) * C::K + ci] : 0.f;
+            }
             if (BF) {
-                const __nv_bfloat16 h = __float2bfloat16_rn(v);
-                const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
-                reinterpret_cast<__nv_bfloat16 *>(blk)[canon16(r, k)] = lo_row ? l : h;
+                __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+                for (int e = 0; e < VE; ++e) {
+                    const __nv_bfloat16 h = __float2bfloat16_rn(v[e]);
+                    o[e] = lo_row ? __float2bfloat16_rn(v[e] - __bfloat162float(h)) : h;
+                }
+                *reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(blk) + canon16(r, k0)) = *reinterpret_cast<const uint4 *>(o);
             } else {
-                const float h = tf32_hi(v);
+                float4 o;
+                float *of = &o.x;
+#pragma unroll
+                for (int e = 0; e < VE; ++e) {
+                    const float h = tf32_hi(v[e]);
+                    of[e] = lo_row ? v[e] - h : h;
+                }
                 float *f = reinterpret_cast<float *>(blk) + (lo_row ? C::N * C::KC : 0);
-                f[canon(ro, k)] = lo_row ? v - h : h;
+                *reinterpret_cast<float4 *>(f + canon(ro, k0)) = o;
             }
         }
     }

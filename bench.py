@@ -95,7 +95,7 @@ def make_workload(args, rank=0, device=None):
 M2L_BF16_TRAFFIC = 139474944 + 19757568
 
 
-def batch_measure(steps=50, warmup=2, nsys=512, seed=3, sample=32, flags=0, form="forest"):
+def batch_measure(steps=50, warmup=2, nsys=512, seed=3, sample=32, flags=0, form="forest", rank=0, ws=1, device=0):
     """Batching form: nsys Plummer systems, N log-uniform in [1024, 65536],
     scale radius uniform in [0.5, 2] (positions x R, velocities x R^-1/2), total
     mass 1 each, eps = 0.01, p = 6, s = 32, mixed precision, dt = 1e-3, all
@@ -103,42 +103,51 @@ def batch_measure(steps=50, warmup=2, nsys=512, seed=3, sample=32, flags=0, form
     launch per kernel class over all systems; "contexts": one context and step
     graph per system. Wall clock per step (a batch step returns after every
     system's step has finished); error vs the FP64 direct sum on `sample`
+    systems. With ws > 1 ranks the systems are split into contiguous runs of
+    about equal particle count (vipp_gb300.shard_systems), each rank runs its
+    run as one batch (the same systems the whole batch draws), and the timed
+    steps are bracketed by barriers, max over ranks; errors come from rank 0's
     systems."""
     import vipp_gb300
     rng = np.random.default_rng(seed)
-    sizes = np.rint(np.exp(rng.uniform(math.log(1024), math.log(65536), nsys))).astype(np.int64)
+    sizes_all = np.rint(np.exp(rng.uniform(math.log(1024), math.log(65536), nsys))).astype(np.int64)
+    first, last = vipp_gb300.shard_systems(sizes_all, ws)[rank]
+    sizes = sizes_all[first:last]
+    nsys = len(sizes)
     if form == "contexts":
         flags |= vipp_gb300.FLAG_BATCH_CONTEXTS
     t0 = time.perf_counter()
-    b = vipp_gb300.Batch(sizes, p=6, s=32, eps=0.01, masses=1.0 / sizes, precision="mixed", flags=flags)
-    b.init_plummer(seed=seed, r_lo=0.5, r_hi=2.0)  # every system drawn on the GPU
+    b = vipp_gb300.Batch(sizes, p=6, s=32, eps=0.01, masses=1.0 / sizes, precision="mixed", flags=flags, device=device)
+    b.init_plummer(seed=seed, r_lo=0.5, r_hi=2.0, first=first)  # every system drawn on the GPU
     setup = time.perf_counter() - t0
     for _ in range(warmup):
         b.step(1e-3)
     l0 = b.launch_count()
+    barrier(ws)
     t0 = time.perf_counter()
     for _ in range(steps):
         b.step(1e-3)
-    dt_wall = time.perf_counter() - t0
+    dt_wall = max_over_ranks(time.perf_counter() - t0, ws)
     launches = (b.launch_count() - l0) / steps
     st = b.stats()
     errs = []
     xb, _ = b.download()
     acc = b.accel() if b.forest else None
     off = np.concatenate([[0], np.cumsum(sizes)])
-    for k in np.linspace(0, nsys - 1, sample).astype(int):
+    for k in (np.linspace(0, nsys - 1, sample).astype(int) if rank == 0 and nsys else []):
         a = acc[off[k]:off[k + 1]] if acc is not None else b.system_accel(int(k))
-        with vipp_gb300.Solver(p=6, s=32, eps=0.01, m=1.0 / sizes[k], precision="fp64") as sd:
+        with vipp_gb300.Solver(p=6, s=32, eps=0.01, m=1.0 / sizes[k], precision="fp64", device=device) as sd:
             sd.preprocess(xb[off[k]:off[k + 1]], np.zeros((sizes[k], 3)))
             ad = sd.direct_accel()
         e = np.linalg.norm(a - ad, axis=1) / np.linalg.norm(ad, axis=1)
         errs.append(float(math.sqrt(np.mean(e * e))))
     b.close()
-    n = int(sizes.sum())
-    return {"workload": f"{nsys} Plummer systems, N log-uniform in [1024, 65536] (seed {seed}), R in [0.5, 2] (systems "
-                        "drawn on the GPU), p=6 s=32 eps=0.01 mixed, dt=1e-3", "form": form,
-            "value": n * steps / dt_wall, "unit": UNIT, "n_total": n,
-            "systems": nsys, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * dt_wall / steps,
+    n = int(sizes_all.sum())
+    return {"workload": f"{len(sizes_all)} Plummer systems, N log-uniform in [1024, 65536] (seed {seed}), R in [0.5, 2] "
+                        "(systems drawn on the GPU), p=6 s=32 eps=0.01 mixed, dt=1e-3", "form": form,
+            "value": n * steps / dt_wall, "unit": UNIT, "n_total": n, "n_gpus": ws,
+            "scaling": "strong (the 512 systems split over the ranks)" if ws > 1 else None,
+            "systems": len(sizes_all), "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * dt_wall / steps,
             "launches_per_step": launches, "tree": {k: st[k] for k in ("ncells", "nleaves", "depth", "m2l_pairs",
                                                                         "p2p_pairs")},
             "setup_s": setup, "rms_rel_err_vs_fp64_direct_per_system": errs,
@@ -376,6 +385,9 @@ def parse_args(argv=None):
     ap.add_argument("--flags", type=int, default=0, help="gb_config flags (vipp_gb300.FLAG_*)")
     ap.add_argument("--no-energy", action="store_true", help="skip the total-energy drift (two extra evaluations)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching form (512 independent systems)")
+    ap.add_argument("--batch-steps", type=int, default=50, help="timed steps of the batching form (the configuration's 50)")
+    ap.add_argument("--no-contexts", action="store_true",
+                    help="skip the batching form's comparison run with one context per system")
     ap.add_argument("--m2l", default="bf16", choices=["bf16", "tf32"],
                     help="mixed form's tensor-core M2L split: bf16 hi/lo (the 4M Plummer and batching configurations' "
                          "form, GB_FLAG_M2L_BF16) or 3 x tf32 (the library default)")
@@ -602,12 +614,14 @@ def main():
                         if roof["bound"] == "fp32" else f"{src} hbm_gbs")
 
     batched = None
-    if rank == 0 and not args.no_batch:
-        batched = batch_measure(flags=args.flags & vipp_gb300.FLAG_M2L_BF16)
+    if not args.no_batch:  # every rank takes its run of the batch's systems
+        batched = batch_measure(steps=args.batch_steps, flags=args.flags & vipp_gb300.FLAG_M2L_BF16, rank=rank, ws=ws,
+                                device=local)
         batched["m2l_split"] = "bf16 hi/lo" if args.flags & vipp_gb300.FLAG_M2L_BF16 else "3 x tf32"
-        # the same batch as one context per system, for comparison
-        ctx_form = batch_measure(steps=10, sample=4, flags=args.flags & vipp_gb300.FLAG_M2L_BF16, form="contexts")
-        batched["contexts_form"] = {k: ctx_form[k] for k in ("value", "ms_per_step", "launches_per_step", "steps")}
+        if ws == 1 and not args.no_contexts:
+            # the same batch as one context per system, for comparison
+            ctx_form = batch_measure(steps=10, sample=4, flags=args.flags & vipp_gb300.FLAG_M2L_BF16, form="contexts")
+            batched["contexts_form"] = {k: ctx_form[k] for k in ("value", "ms_per_step", "launches_per_step", "steps")}
 
     # --- the other M2L split on the same workload (value and energy drift) -------
     alt = None

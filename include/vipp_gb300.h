@@ -165,6 +165,11 @@ GB_API int gb_batch_upload(gb_batch *b, const double *x_aos, const double *v_aos
  * times R_k, velocities times R_k^-1/2); radii (may be NULL) receives the
  * nsys R_k. Each system's particle mass stays as given at gb_batch_create. */
 GB_API int gb_batch_init_plummer(gb_batch *b, uint64_t seed, double r_lo, double r_hi, double r_max, double *radii);
+/* The same with this batch's system k drawn as system first + k of the seeded
+ * family: a batch split over ranks into contiguous runs of systems draws
+ * exactly the systems of the whole batch. */
+GB_API int gb_batch_init_plummer_at(gb_batch *b, uint64_t seed, uint64_t first, double r_lo, double r_hi, double r_max,
+                                    double *radii);
 GB_API int gb_batch_download(gb_batch *b, double *x_aos, double *v_aos);
 GB_API int gb_batch_rk4_step(gb_batch *b, double dt);
 GB_API int gb_batch_size(const gb_batch *b, size_t *nsys, uint64_t *n_total);

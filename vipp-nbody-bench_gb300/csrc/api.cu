@@ -1080,6 +1080,11 @@ int gb_batch_upload(gb_batch *b, const double *x_aos, const double *v_aos) {
 }
 
 int gb_batch_init_plummer(gb_batch *b, uint64_t seed, double r_lo, double r_hi, double r_max, double *radii) {
+    return gb_batch_init_plummer_at(b, seed, 0, r_lo, r_hi, r_max, radii);
+}
+
+int gb_batch_init_plummer_at(gb_batch *b, uint64_t seed, uint64_t first, double r_lo, double r_hi, double r_max,
+                             double *radii) {
     if (!b) return GB_ERR_INVALID;
     if (!(r_lo > 0) || !(r_hi >= r_lo) || !std::isfinite(r_hi)) return b->err = "need 0 < r_lo <= r_hi", GB_ERR_INVALID;
     if (!(r_max > 0) || !std::isfinite(r_max)) return b->err = "r_max must be finite and > 0", GB_ERR_INVALID;
@@ -1094,10 +1099,11 @@ int gb_batch_init_plummer(gb_batch *b, uint64_t seed, double r_lo, double r_hi, 
     std::vector<uint64_t> seeds(ns);
     std::vector<double2> scales(ns);
     for (size_t k = 0; k < ns; ++k) {
-        const double u = static_cast<double>(mix(mix(seed ^ 0x2545f4914f6cdd1dull) + k) >> 11) * 0x1.0p-53;
+        const uint64_t id = first + k;  // the system's index in the seeded family
+        const double u = static_cast<double>(mix(mix(seed ^ 0x2545f4914f6cdd1dull) + id) >> 11) * 0x1.0p-53;
         const double R = r_lo + (r_hi - r_lo) * u;
         if (radii) radii[k] = R;
-        seeds[k] = mix(seed + k);
+        seeds[k] = mix(seed + id);
         scales[k] = make_double2(R, 1.0 / std::sqrt(R));  // total mass 1, scale radius R (G = 1)
     }
     if (b->forest) {

@@ -38,7 +38,7 @@ EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_uplo
            "gb_get_conserved", "gb_init_plummer", "gb_batch_create", "gb_batch_destroy", "gb_batch_last_error",
            "gb_batch_upload", "gb_batch_download", "gb_batch_rk4_step", "gb_batch_size", "gb_batch_system",
            "gb_set_tuning", "gb_get_tuning", "gb_tuning_lookup", "gb_init_clustered", "gb_batch_init_plummer",
-           "gb_batch_is_forest", "gb_batch_forest", "gb_batch_accel", "gb_batch_conserved", "gb_batch_stats", "gb_batch_launch_count")
+           "gb_batch_is_forest", "gb_batch_forest", "gb_batch_init_plummer_at", "gb_batch_accel", "gb_batch_conserved", "gb_batch_stats", "gb_batch_launch_count")
 TUNING_FIELDS = ("p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s")
 TUNING_DEFAULT = {"p2p_blocks": 8, "p2p_blocks_conc": 8, "p2p_slice": 8192, "m2l_ctas_pct": 100, "serial": 0,
                   "leaf_s": 0}
@@ -125,6 +125,8 @@ def load(path: str | None = None):
     lib.gb_init_clustered.argtypes = [vp, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_int, ctypes.c_double,
                                       ctypes.c_double, vp]
     lib.gb_batch_init_plummer.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
+    lib.gb_batch_init_plummer_at.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_double, vp]
     lib.gb_set_tuning.argtypes = [vp, ctypes.POINTER(GbTuning)]
     lib.gb_get_tuning.argtypes = [vp, ctypes.POINTER(GbTuning)]
     lib.gb_tuning_lookup.argtypes = [ctypes.c_char_p, ctypes.POINTER(GbConfig), ctypes.c_size_t,
@@ -353,6 +355,25 @@ def version() -> str:
     return load().gb_version().decode()
 
 
+def shard_systems(sizes, world: int) -> list:
+    """Contiguous runs of systems for `world` ranks, balanced by particle count
+    (the work of a force evaluation grows with N): rank r gets systems
+    [start_r, end_r). Rank r's run ends at the system boundary nearest to
+    (r + 1) / world of the total particle count."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    pre = np.concatenate([[0], np.cumsum(sizes)])
+    total = int(pre[-1])
+    bounds = [0]
+    for r in range(1, world):
+        target = total * r / world
+        cut = min(int(np.searchsorted(pre, target, side="left")), len(sizes))
+        if cut > 0 and abs(pre[cut - 1] - target) <= abs(pre[cut] - target):
+            cut -= 1
+        bounds.append(max(bounds[-1], cut))
+    bounds.append(len(sizes))
+    return [(bounds[r], bounds[r + 1]) for r in range(world)]
+
+
 class Batch:
     """Independent systems of uneven N advanced together (gb_batch_*):
     sizes[k] particles of system k, concatenated in x and v; masses[k] is the
@@ -383,13 +404,13 @@ class Batch:
         assert x.shape[0] == self.n and v.shape[0] == self.n
         self._check(self.lib.gb_batch_upload(self.h, _ptr(x), _ptr(v)))
 
-    def init_plummer(self, seed=3, r_lo=0.5, r_hi=2.0, r_max=10.0):
-        """Generate every system on the device (gb_batch_init_plummer): Plummer
-        spheres of total mass 1 scaled to radii uniform in [r_lo, r_hi];
-        returns the radii."""
+    def init_plummer(self, seed=3, r_lo=0.5, r_hi=2.0, r_max=10.0, first=0):
+        """Generate every system on the device (gb_batch_init_plummer_at): Plummer
+        spheres of total mass 1 scaled to radii uniform in [r_lo, r_hi]; system
+        k is system first + k of the seeded family. Returns the radii."""
         radii = np.zeros(len(self.off) - 1)
-        self._check(self.lib.gb_batch_init_plummer(self.h, int(seed), float(r_lo), float(r_hi), float(r_max),
-                                                   _ptr(radii)))
+        self._check(self.lib.gb_batch_init_plummer_at(self.h, int(seed), int(first), float(r_lo), float(r_hi),
+                                                      float(r_max), _ptr(radii)))
         return radii
 
     def step(self, dt):

@@ -92,7 +92,7 @@ def make_workload(args, rank=0, device=None):
 
 # DRAM bytes (read + write) per launch of the BF16-split M2L on the 4M
 # workload, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum)
-M2L_BF16_TRAFFIC = 139474944 + 19757568
+M2L_BF16_TRAFFIC = 135549184 + 14860544
 
 
 def batch_measure(steps=50, warmup=2, nsys=512, seed=3, sample=32, flags=0, form="forest", rank=0, ws=1, device=0):
@@ -388,6 +388,9 @@ def parse_args(argv=None):
     ap.add_argument("--batch-steps", type=int, default=50, help="timed steps of the batching form (the configuration's 50)")
     ap.add_argument("--no-contexts", action="store_true",
                     help="skip the batching form's comparison run with one context per system")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the batching form (warm-up --warmup steps, --batch-steps timed) and print its line")
+    ap.add_argument("--no-error", action="store_true", help="with --batch-only: skip the per-system error check")
     ap.add_argument("--m2l", default="bf16", choices=["bf16", "tf32"],
                     help="mixed form's tensor-core M2L split: bf16 hi/lo (the 4M Plummer and batching configurations' "
                          "form, GB_FLAG_M2L_BF16) or 3 x tf32 (the library default)")
@@ -439,6 +442,13 @@ def main():
     base_flags = args.flags
     if args.precision == "mixed" and args.m2l == "bf16":
         args.flags |= vipp_gb300.FLAG_M2L_BF16
+    if args.batch_only:
+        # the batching form alone (profiling runs); its own line, not the bench contract's
+        b = batch_measure(steps=args.batch_steps, warmup=args.warmup, sample=4 if not args.no_error else 0,
+                          flags=args.flags & vipp_gb300.FLAG_M2L_BF16, rank=rank, ws=ws, device=local)
+        if rank == 0:
+            print(json.dumps({"metric": "batching form " + METRIC, "value": b["value"], "unit": UNIT, "batched": b}))
+        return
     n = args.n
     t_ic = time.perf_counter()
     x, v, seed, wname = make_workload(args, rank, device=local)
@@ -606,7 +616,7 @@ def main():
         default_cfg = (args.workload == "plummer" and n == 1 << 22 and args.p == 8 and args.s == 64 and args.eps == 0.005
                        and args.precision == "mixed" and args.flags & ~vipp_gb300.FLAG_M2L_BF16 == 0)
         bf = bool(args.flags & vipp_gb300.FLAG_M2L_BF16)
-        traffic = {"p2p": 293120768 + 40724736, "m2l": (M2L_BF16_TRAFFIC if bf else 188582656 + 19934464)} if default_cfg else {}
+        traffic = {"p2p": 292350208 + 41266688, "m2l": (M2L_BF16_TRAFFIC if bf else 195950592 + 21233664)} if default_cfg else {}
         for k in per:
             per[k]["traffic"] = traffic.get(k)
         roof.update({"kernel": dom, "traffic": traffic.get(dom), "traffic_unit": "B per launch"})

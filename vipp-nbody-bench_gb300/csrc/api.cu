@@ -654,6 +654,7 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     const size_t kk = static_cast<size_t>(ws.K) * ws.K * gb::kNumOps;
     if ((e = cudaMalloc(&ws.ops_d, sizeof(double) * kk)) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.ops_f, sizeof(float) * kk)) != cudaSuccess) return fail("ops", e);
+    if ((e = cudaMalloc(&ws.zf, sizeof(float) * gb::zf_table_floats(ws.p))) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.bimg, sizeof(float) * gb::m2l_tc_image_floats(ws.p))) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.m2l_tab, gb::m2l_table_bytes(ws.p))) != cudaSuccess) return fail("ops", e);
     gb::build_m2l_table(ws);
@@ -674,7 +675,7 @@ void gb_destroy(gb_ctx *ctx) {
                     ws.split_cell, ws.c_begin, ws.c_end, ws.c_parent, ws.c_child, ws.c_level, ws.c_path, ws.c_coord,
                     ws.c_box, ws.c_ctr, ws.Mexp, ws.Lexp, ws.m2l_src, ws.p2p_own, ws.p2p_cnt, ws.coll, ws.coll_cnt,
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
-                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.m2l_tab, ws.ms_tc, ws.diag, ws.ops_f, ws.info, ws.d_counts, ctx->d_targets, ws.smom, ws.smom_oct, ws.staylor,
+                    ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.m2l_tab, ws.ms_tc, ws.diag, ws.ops_f, ws.zf, ws.info, ws.d_counts, ctx->d_targets, ws.smom, ws.smom_oct, ws.staylor,
                     ctx->d_direct, ws.seg, ws.psys, ws.c_sys, ws.sys_par, ws.mkeys, ws.etile, ws.oct_list, ws.otile,
                     ws.ocnt};
     for (void *b : bufs) dfree(b);
@@ -709,6 +710,7 @@ int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
         const size_t kk = static_cast<size_t>(ctx->ws.K) * ctx->ws.K * gb::kNumOps;
         GB_TRY(dalloc(ctx->ws.ops_d, kk));
         GB_TRY(dalloc(ctx->ws.ops_f, kk));
+        GB_TRY(dalloc(ctx->ws.zf, gb::zf_table_floats(ctx->ws.p)));
         GB_TRY(dalloc(ctx->ws.bimg, gb::m2l_tc_image_floats(ctx->ws.p)));
         unsigned char *t = nullptr;
         GB_TRY(dalloc(t, gb::m2l_table_bytes(ctx->ws.p)));
@@ -952,6 +954,7 @@ int forest_setup(gb_ctx *ctx, size_t nsys, const uint64_t *off, const std::vecto
     const size_t kk = static_cast<size_t>(ws.K) * ws.K * gb::kNumOps * nsys;
     GB_TRY(dalloc(ws.ops_d, kk));
     GB_TRY(dalloc(ws.ops_f, kk));
+    GB_TRY(dalloc(ws.zf, gb::zf_table_floats(ws.p) * nsys));
     GB_TRY(dalloc(ws.bimg, gb::m2l_tc_image_floats(ws.p) * nsys));
     std::vector<unsigned> seg(nsys + 1);
     std::vector<int> ps(n);

@@ -304,94 +304,119 @@ __global__ void k_build_ops(const TreeInfo *__restrict__ info_all, int p, const 
     }
 }
 
-// The FP32 operators of the mixed forms for kSysPerBlock systems at once
-// (blockIdx.x: operator, as in k_build_ops; blockIdx.y: group of systems):
-// warp g forms system g's Z table (k_build_ops's harmonics), then every
-// thread reads each table entry once for all the group's systems (the table
-// is the main traffic: one read per operator made a forest's 512 x 359
-// operators cost ~8 ms per evaluation). M2L entries: the values of
-// k_build_ops's mixed branch; M2M and L2L: t Z[y] from the same kind of table.
-constexpr int kSysPerBlock = 8;
-
-__global__ void __launch_bounds__(32 * kSysPerBlock) k_build_ops_f(const TreeInfo *__restrict__ info_all, int nsys, int p,
-                                                               const M2LEnt *__restrict__ tabs, float *__restrict__ ops_f) {
-    extern __shared__ double sm[];
-    const int K = (p + 1) * (p + 1), nmax = (2 * p + 1) * (2 * p + 1);
-    const int b = blockIdx.x;
+// Z tables of the mixed forms' FP32 operators, one thread per (system,
+// operator), or per (system, operator, order m) when there are few systems
+// (cols = 2p + 1: shorter serial chains, the prologue repeated per order), so
+// that every lane of the FP64 pipe works (spread over a warp's lanes as
+// k_build_ops does, most FP64 issue slots went to idle lanes and the tables
+// cost ~2 ms per evaluation for 512 systems). The harmonics follow
+// k_build_ops's recurrences value by value: the diagonal up to (m, m), then
+// column m down with two running values.
+// Z[y] = Y(y) rho^-(deg y + 1) (M2L) or Y(y) |t|^deg y (M2M, L2L), stride nmax.
+__global__ void k_zf_tables(const TreeInfo *__restrict__ info_all, int nsys, int p, int cols, float *__restrict__ zf) {
+    const long long gid = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    if (gid >= static_cast<long long>(nsys) * kNumOps * cols) return;
+    const int mcol = static_cast<int>(gid % cols);
+    const int sidx = static_cast<int>(gid / cols / kNumOps), b = static_cast<int>((gid / cols) % kNumOps);
+    const int nmax = (2 * p + 1) * (2 * p + 1);
     int kind = 0, oct = 0;
-    int dd[3] = {b % 7 - 3, (b / 7) % 7 - 3, b / 49 - 3};
+    const int dd[3] = {b % 7 - 3, (b / 7) % 7 - 3, b / 49 - 3};
     if (b < kOpM2M) {
         if (abs(dd[0]) <= 1 && abs(dd[1]) <= 1 && abs(dd[2]) <= 1) return;
     } else {
         kind = b < kOpL2L ? 1 : 2;
         oct = (b - kOpM2M) & 7;
     }
-    const int D = kind == 0 ? 2 * p : p, ny = (D + 1) * (D + 1);
-    const M2LEnt *tab = tabs + static_cast<size_t>(kind) * K * K;
-    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sys0 = blockIdx.y * kSysPerBlock;
-    const int per = nmax + 2 * p + 3;  // doubles per system: yt, pw
-    double *yt = sm + g * per, *pw = yt + nmax;
-    float *Zf = reinterpret_cast<float *>(sm + kSysPerBlock * per) + g * nmax;
-    if (sys0 + g < nsys) {
-        const TreeInfo *info = info_all + sys0 + g;
-        double tv[3];
-        if (kind == 0) {
-            for (int a = 0; a < 3; ++a) tv[a] = dd[a] * info->H[a] / info->S;
-        } else {
-            for (int a = 0; a < 3; ++a) {
-                const double sg = ((oct >> a) & 1) ? -1.0 : 1.0;
-                tv[a] = (kind == 1 ? sg : -sg) * info->H[a] / (4.0 * info->S);
-            }
-        }
-        const double rho = sqrt(tv[0] * tv[0] + tv[1] * tv[1] + tv[2] * tv[2]);
-        const double x = tv[0] / rho, y = tv[1] / rho, z = tv[2] / rho;
-        const HTab<double> &t = c_htd;
-        if (lane == 0) {
-            double cre = 1, cim = 0;
-            for (int m = 0; m <= D; ++m) {
-                if (m > 0) {
-                    const double nre = t.mm[m] * (x * cre - y * cim);
-                    const double nim = t.mm[m] * (x * cim + y * cre);
-                    cre = nre, cim = nim;
-                }
-                yt[ridx(m, m, 0)] = cre;
-                if (m > 0) yt[ridx(m, m, 1)] = cim;
-            }
-        } else if (lane == 31) {
-            double a = 1;
-            const double f = kind == 0 ? 1.0 / rho : rho;
-            for (int i = 0; i < 2 * p + 3; ++i) pw[i] = a, a *= f;
-        }
-        __syncwarp();
-        const int m = lane;
-        if (m <= D) {
-            const double r2 = x * x + y * y + z * z;
-            const double cre = yt[ridx(m, m, 0)], cim = m > 0 ? yt[ridx(m, m, 1)] : 0.0;
-            if (m + 1 <= D) {
-                yt[ridx(m + 1, m, 0)] = t.m1[m] * z * cre;
-                if (m > 0) yt[ridx(m + 1, m, 1)] = t.m1[m] * z * cim;
-            }
-            for (int n = m + 2; n <= D; ++n) {
-                yt[ridx(n, m, 0)] = t.ra[n][m] * z * yt[ridx(n - 1, m, 0)] - t.rb[n][m] * r2 * yt[ridx(n - 2, m, 0)];
-                if (m > 0) yt[ridx(n, m, 1)] = t.ra[n][m] * z * yt[ridx(n - 1, m, 1)] - t.rb[n][m] * r2 * yt[ridx(n - 2, m, 1)];
-            }
-        }
-        __syncwarp();
-        for (int yy = lane; yy < ny; yy += 32) {
-            int dg = static_cast<int>(sqrtf(static_cast<float>(yy)));
-            while (dg * dg > yy) --dg;
-            while ((dg + 1) * (dg + 1) <= yy) ++dg;
-            Zf[yy] = static_cast<float>(yt[yy] * pw[kind == 0 ? dg + 1 : dg]);
+    const int D = kind == 0 ? 2 * p : p;
+    if (mcol > D) return;
+    const int m_end = cols == 1 ? D : mcol;  // orders mcol .. m_end
+    const TreeInfo *info = info_all + sidx;
+    double tv[3];
+    if (kind == 0) {
+        for (int a = 0; a < 3; ++a) tv[a] = dd[a] * info->H[a] / info->S;
+    } else {
+        for (int a = 0; a < 3; ++a) {
+            const double sg = ((oct >> a) & 1) ? -1.0 : 1.0;
+            tv[a] = (kind == 1 ? sg : -sg) * info->H[a] / (4.0 * info->S);
         }
     }
-    __syncthreads();
+    const double rho = sqrt(tv[0] * tv[0] + tv[1] * tv[1] + tv[2] * tv[2]);
+    const double x = tv[0] / rho, y = tv[1] / rho, z = tv[2] / rho;
+    const double r2 = x * x + y * y + z * z;
+    double pw[2 * kMaxP + 3];
+    {
+        double a = 1;
+        const double f = kind == 0 ? 1.0 / rho : rho;
+        for (int i = 0; i < 2 * p + 3; ++i) pw[i] = a, a *= f;
+    }
+    const int sh = kind == 0 ? 1 : 0;  // Z's power of rho: deg + 1 (M2L), deg (M2M, L2L)
+    float *Z = zf + (static_cast<size_t>(sidx) * kNumOps + b) * nmax;
+    const HTab<double> &t = c_htd;
+    double cre = 1, cim = 0;  // Y(m, m)
+    for (int m = 1; m <= mcol; ++m) {
+        const double nre = t.mm[m] * (x * cre - y * cim);
+        const double nim = t.mm[m] * (x * cim + y * cre);
+        cre = nre, cim = nim;
+    }
+    for (int m = mcol; m <= m_end; ++m) {
+        if (m > mcol) {
+            const double nre = t.mm[m] * (x * cre - y * cim);
+            const double nim = t.mm[m] * (x * cim + y * cre);
+            cre = nre, cim = nim;
+        }
+        Z[ridx(m, m, 0)] = static_cast<float>(cre * pw[m + sh]);
+        if (m > 0) Z[ridx(m, m, 1)] = static_cast<float>(cim * pw[m + sh]);
+        if (m + 1 > D) continue;
+        double ar = cre, ai = cim;  // Y(n - 2, m)
+        double br = t.m1[m] * z * cre, bi = m > 0 ? t.m1[m] * z * cim : 0.0;  // Y(n - 1, m)
+        Z[ridx(m + 1, m, 0)] = static_cast<float>(br * pw[m + 1 + sh]);
+        if (m > 0) Z[ridx(m + 1, m, 1)] = static_cast<float>(bi * pw[m + 1 + sh]);
+        for (int n = m + 2; n <= D; ++n) {
+            const double vr = t.ra[n][m] * z * br - t.rb[n][m] * r2 * ar;
+            Z[ridx(n, m, 0)] = static_cast<float>(vr * pw[n + sh]);
+            ar = br, br = vr;
+            if (m > 0) {
+                const double vi = t.ra[n][m] * z * bi - t.rb[n][m] * r2 * ai;
+                Z[ridx(n, m, 1)] = static_cast<float>(vi * pw[n + sh]);
+                ai = bi, bi = vi;
+            }
+        }
+    }
+}
+
+// The FP32 operators of the mixed forms for kSysPerBlock systems at once
+// (blockIdx.x: operator, as in k_build_ops; blockIdx.y: group of systems),
+// from the Z tables of k_zf_tables: every thread reads each table entry once
+// for all the group's systems (the entry table is the main traffic: one read
+// per operator made a forest's 512 x 359 operators cost ~8 ms per
+// evaluation). Entries t Z[y] (M2LEnt tables: M2L, M2M, L2L).
+constexpr int kSysPerBlock = 8;
+
+__global__ void __launch_bounds__(32 * kSysPerBlock) k_build_ops_f(int nsys, int p, const M2LEnt *__restrict__ tabs,
+                                                               const float *__restrict__ zf, float *__restrict__ ops_f) {
+    extern __shared__ float smf[];
+    const int K = (p + 1) * (p + 1), nmax = (2 * p + 1) * (2 * p + 1);
+    const int b = blockIdx.x;
+    int kind = 0;
+    const int dd[3] = {b % 7 - 3, (b / 7) % 7 - 3, b / 49 - 3};
+    if (b < kOpM2M) {
+        if (abs(dd[0]) <= 1 && abs(dd[1]) <= 1 && abs(dd[2]) <= 1) return;
+    } else {
+        kind = b < kOpL2L ? 1 : 2;
+    }
+    const int D = kind == 0 ? 2 * p : p, ny = (D + 1) * (D + 1);
+    const M2LEnt *tab = tabs + static_cast<size_t>(kind) * K * K;
+    const int sys0 = blockIdx.y * kSysPerBlock;
     const int ng = min(kSysPerBlock, nsys - sys0);
-    const float *Zs = reinterpret_cast<const float *>(sm + kSysPerBlock * per);
+    for (int i = threadIdx.x; i < ng * ny; i += blockDim.x) {
+        const int q = i / ny, yy = i - q * ny;
+        smf[q * nmax + yy] = zf[(static_cast<size_t>(sys0 + q) * kNumOps + b) * nmax + yy];
+    }
+    __syncthreads();
     for (int idx = threadIdx.x; idx < K * K; idx += blockDim.x) {
         const M2LEnt e = tab[idx];
         for (int q = 0; q < ng; ++q)
-            ops_f[((static_cast<size_t>(sys0 + q)) * kNumOps + b) * K * K + idx] = m2l_entry<float>(e, Zs + q * nmax);
+            ops_f[((static_cast<size_t>(sys0 + q)) * kNumOps + b) * K * K + idx] = m2l_entry<float>(e, smf + q * nmax);
     }
 }
 
@@ -1010,9 +1035,14 @@ void build_operators(Workspace &ws) {
     const int nsys = ws.forest() ? ws.nsys : 1;
     if (ws.mixed) {
         // M2L offsets: FP32 operators, kSysPerBlock systems per block; then M2M and L2L
-        const size_t smem_f = kSysPerBlock * (sizeof(double) * (ny + 2 * ws.p + 3) + sizeof(float) * ny);
+        // few systems: a thread per order (latency); many: a thread per operator (FP64 work)
+        const int cols = nsys < 16 ? 2 * ws.p + 1 : 1;
+        k_zf_tables<<<static_cast<unsigned>(ceil_div(static_cast<size_t>(nsys) * kNumOps * cols, 128)), 128, 0, ws.st>>>(
+            ws.info, nsys, ws.p, cols, ws.zf);
+        const size_t smem_f = kSysPerBlock * sizeof(float) * ny;
         k_build_ops_f<<<dim3(kNumOps, (nsys + kSysPerBlock - 1) / kSysPerBlock), 32 * kSysPerBlock, smem_f, ws.st>>>(
-            ws.info, nsys, ws.p, static_cast<const M2LEnt *>(ws.m2l_tab), ws.ops_f);
+            nsys, ws.p, static_cast<const M2LEnt *>(ws.m2l_tab), ws.zf, ws.ops_f);
+        ws.launches += 1;
     } else {
         k_build_ops<<<dim3(kNumOps, nsys), 256, smem, ws.st>>>(ws.info, ws.p, static_cast<const M2LEnt *>(ws.m2l_tab), ws.ops_d,
                                                               ws.ops_f, false, 0);

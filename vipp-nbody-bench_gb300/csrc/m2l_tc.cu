@@ -92,7 +92,13 @@ constexpr int kLoaderWarps = M2L_LOADER_WARPS;  // warps 4 .. 3 + kLoaderWarps
 constexpr int kMmaWarp = 4 + kLoaderWarps;
 constexpr int kThreads = 32 * (kMmaWarp + 1);
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
-constexpr int kGroup = 4;           // slots per TMEM accumulation group
+#ifndef M2L_PREFETCH2
+#define M2L_PREFETCH2 1  // source rows of two slots ahead in flight instead of one (~1% faster at 4M)
+#endif
+#ifndef M2L_GROUP
+#define M2L_GROUP 4
+#endif
+constexpr int kGroup = M2L_GROUP;   // slots per TMEM accumulation group
 constexpr int kSlotsPerTile = 189;  // M2L slots of every octant: 216 minus the 27 adjacent ones
 constexpr int kGroupsPerTile = (kSlotsPerTile + kGroup - 1) / kGroup;
 constexpr int kSmemMax = 232448;    // opt-in shared memory per block
@@ -385,11 +391,24 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
             int s = next_slot(cls, 0);
             int cur[4];
             rows_of(s, cur);
+#if M2L_PREFETCH2
+            // source rows two slots ahead: the loads of slot s + 2 are in flight
+            // while slots s and s + 1 are posted
+            int sn = s < kM2LSlots ? next_slot(cls, s + 1) : kM2LSlots;
+            int nxt[4] = {zrow, zrow, zrow, zrow};
+            if (sn < kM2LSlots) rows_of(sn, nxt);
+            while (s < kM2LSlots && !stop) {
+                const int oi = slot_operator(cls, s);
+                const int snn = sn < kM2LSlots ? next_slot(cls, sn + 1) : kM2LSlots;
+                int nxt2[4] = {zrow, zrow, zrow, zrow};
+                if (snn < kM2LSlots) rows_of(snn, nxt2);
+#else
             while (s < kM2LSlots && !stop) {
                 const int oi = slot_operator(cls, s);
                 const int sn = next_slot(cls, s + 1);
                 int nxt[4] = {zrow, zrow, zrow, zrow};
                 if (sn < kM2LSlots) rows_of(sn, nxt);  // in flight while this slot's copies are posted
+#endif
                 for (int kc = 0; kc < C::NKC; ++kc, ++step) {
                     const int st = step % C::STAGES;
                     const unsigned use = step / C::STAGES;
@@ -412,9 +431,16 @@ __global__ void __launch_bounds__(kThreads, M2L_MIN_BLOCKS)
                         bulk_g2s(stage + C::NA * C::A_BYTES, bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::B_BYTES),
                                  b_bytes(kc), full + st);
                 }
+#if M2L_PREFETCH2
+#pragma unroll
+                for (int i = 0; i < 4; ++i) cur[i] = nxt[i], nxt[i] = nxt2[i];
+                s = sn;
+                sn = snn;
+#else
 #pragma unroll
                 for (int i = 0; i < 4; ++i) cur[i] = nxt[i];
                 s = sn;
+#endif
             }
         }
     } else if (warp == kMmaWarp) {
@@ -639,7 +665,11 @@ __global__ void k_build_bimg(const float *__restrict__ ops_all, unsigned char *_
     unsigned char *bimg = bimg_all + static_cast<size_t>(blockIdx.y) * (kNumOffsets * C::NKC * 2 * C::B_BYTES);
     const int d0 = oi % 7 - 3, d1 = (oi / 7) % 7 - 3, d2 = oi / 49 - 3;
     if (d0 >= -1 && d0 <= 1 && d1 >= -1 && d1 <= 1 && d2 >= -1 && d2 <= 1) return;
-    // one 16-byte store per thread and step: 8 bf16 or 4 tf32 consecutive K elements of a row
+    // the operator staged in shared memory by coalesced loads, then one 16-byte
+    // store per thread and step: 8 bf16 or 4 tf32 consecutive K elements of a row
+    extern __shared__ float op[];  // [K * K]
+    for (int i = threadIdx.x; i < C::K * C::K; i += blockDim.x) op[i] = ops[static_cast<size_t>(oi) * C::K * C::K + i];
+    __syncthreads();
     constexpr int VE = BF ? 8 : 4;
     constexpr int RUNS = C::KC / VE;
     for (int kc = 0; kc < C::NKC; ++kc) {
@@ -655,7 +685,7 @@ __global__ void k_build_bimg(const float *__restrict__ ops_all, unsigned char *_
                 int ci = j;
                 bool use = j < C::K;
                 if (BF && j >= C::K && j < 2 * C::K) ci = j - C::K, use = !lo_row;
-                v[e] = (use && ro < C::K) ? ops[(static_cast<size_t>(oi) * C::K + ro) * C::K + ci] : 0.f;
+                v[e] = (use && ro < C::K) ? op[ro * C::K + ci] : 0.f;
             }
             if (BF) {
                 __align__(16) __nv_bfloat16 o[8];
@@ -684,7 +714,10 @@ template <int P, bool BF>
 void launch(Workspace &ws) {
     using C = TcCfg<P, BF>;
     const bool forest = ws.forest();
-    k_build_bimg<P, BF><<<dim3(kNumOffsets, forest ? ws.nsys : 1), 256, 0, ws.st>>>(ws.ops_f,
+    const int op_smem = static_cast<int>(sizeof(float) * C::K * C::K);
+    if (op_smem > 48 * 1024)
+        cudaFuncSetAttribute(k_build_bimg<P, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, op_smem);
+    k_build_bimg<P, BF><<<dim3(kNumOffsets, forest ? ws.nsys : 1), 256, op_smem, ws.st>>>(ws.ops_f,
                                                                                  reinterpret_cast<unsigned char *>(ws.bimg));
     k_split_m<P, BF><<<4 * ws.num_sms, 256, 0, ws.st>>>(ws.info, static_cast<const float *>(ws.Mexp), ws.ms_tc,
                                                         static_cast<int>(ws.ms_rows));

@@ -138,6 +138,7 @@ struct Workspace {
     // operators
     double *ops_d = nullptr;  // [(343+16) K K]
     float *ops_f = nullptr;
+    float *zf = nullptr;      // mixed forms: [nsys][359][(2p+1)^2] Z tables of the FP32 operators (fmm.cu)
     void *m2l_tab = nullptr;  // offset-independent factors of the M2L operator entries (fmm.cu)
     float *bimg = nullptr;    // tensor-core M2L operator images (m2l_tc.cu)
     float *ms_tc = nullptr;   // tensor-core M2L split expansions, 2 ms_rows ms_kp floats (m2l_tc.cu)
@@ -186,6 +187,7 @@ void build_tree(Workspace &ws);               // bbox, keys, sort, cells, leaves
 void forest_tiles(Workspace &ws, int rows);   // forest: M2M/L2L tiles and M2L tiles of `rows` octets per system
 void build_operators(Workspace &ws);          // 359 translation matrices for the current root box
 size_t m2l_table_bytes(int p);
+inline size_t zf_table_floats(int p) { return static_cast<size_t>(kNumOps) * (2 * p + 1) * (2 * p + 1); }  // per system
 void build_m2l_table(Workspace &ws);          // fill m2l_tab for ws.p (once per p, outside step graphs)
 void upward_pass(Workspace &ws);              // P2M + M2M
 void m2l_pass(Workspace &ws);                 // M2L into L (CUDA cores)

@@ -153,3 +153,19 @@ def test_forest_depth_beyond_its_sort_word_is_reported():
                           flags=vipp_gb300.FLAG_BATCH_CONTEXTS) as b:
         b.upload(deep, np.zeros_like(deep))
         b.step(1e-3)
+
+
+def test_accurate_mode_batch_runs_as_contexts():
+    """The accurate mode's batches take the contexts form (the forest builds
+    the reference mode's tree only), with the same per-system results."""
+    import vipp_gb300
+    sy = systems()[:2]
+    sizes = [len(x) for x, _ in sy]
+    masses = [1.0 / n for n in sizes]
+    with vipp_gb300.Batch(sizes, p=6, s=16, eps=0.01, masses=masses, precision="mixed", mode="accurate") as b:
+        assert not b.forest
+        b.upload(np.concatenate([x for x, _ in sy]), np.concatenate([v for _, v in sy]))
+        a = b.accel()
+    with vipp_gb300.Solver(p=6, s=16, eps=0.01, m=masses[1], precision="mixed", mode="accurate") as s:
+        s.preprocess(*sy[1])
+        assert np.array_equal(s.accel(), a[sizes[0]:])

@@ -169,3 +169,46 @@ def test_accurate_mode_batch_runs_as_contexts():
     with vipp_gb300.Solver(p=6, s=16, eps=0.01, m=masses[1], precision="mixed", mode="accurate") as s:
         s.preprocess(*sy[1])
         assert np.array_equal(s.accel(), a[sizes[0]:])
+
+
+def test_forest_equals_contexts_on_the_benchmark_batch():
+    """bench.py's batching form (512 Plummer systems, N log-uniform in
+    [1024, 65536], 7.5 M particles, BF16 split): one batch step of the forest
+    and of one context per system give the same positions and velocities, bit
+    for bit."""
+    import vipp_gb300
+    rng = np.random.default_rng(3)
+    sizes = np.rint(np.exp(rng.uniform(math.log(1024), math.log(65536), 512))).astype(np.int64)
+    out = {}
+    for form in FORMS:
+        with vipp_gb300.Batch(sizes, p=6, s=32, eps=0.01, masses=1.0 / sizes, precision="mixed",
+                              flags=vipp_gb300.FLAG_M2L_BF16 | form_flags(form)) as b:
+            b.init_plummer(seed=3)
+            b.step(1e-3)
+            out[form] = b.download()
+    assert np.array_equal(out["forest"][0], out["contexts"][0])
+    assert np.array_equal(out["forest"][1], out["contexts"][1])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_step_repeated_after_overflow_equals_step_without(precision):
+    """A step whose first attempt overflows a buffer is grown and run again
+    from the step's start: the same result as a step that needed no repeat
+    (the RK4 sums start over at stage 0)."""
+    import vipp_gb300
+    x, v = O.plummer_reference(100_000, 0.01, 0)  # needs 3x the initial partial-sum slots at s = 256
+    n = len(x)
+    with vipp_gb300.Solver(p=4, s=256, eps=0.01, m=1 / n, precision=precision) as a:
+        a.preprocess(x, v)
+        a.solve(1e-3)
+        xa, va = a.postprocess()
+        ra = a.stats()["retries"]
+    with vipp_gb300.Solver(p=4, s=256, eps=0.01, m=1 / n, precision=precision) as b:
+        b.preprocess(x, v)
+        b.accel()  # grows the buffers outside the step
+        rb0 = b.stats()["retries"]
+        b.solve(1e-3)
+        xb, vb = b.postprocess()
+        rb = b.stats()["retries"] - rb0
+    assert ra >= 1 and rb == 0
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)

@@ -625,13 +625,18 @@ __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, 
         const int cls = w % 8, tile = w / 8;
         const T *ops = ops_all;
         __syncthreads();  // the previous tile's rows are written out
+        int rows;  // targets of the tile (rows past them skip the GEMM)
         if (otile) {
             const int4 ot = otile[tile];
             ops = ops_all + static_cast<size_t>(ot.x) * kNumOps * C::K * C::K;
+            rows = ot.z;
             if (tid < kTile) trow[tid] = tid < ot.z ? base + cls + 8 * oct_list[ot.y + tid] : -1;
-        } else if (tid < kTile) {
-            const int t = tile * kTile + tid;
-            trow[tid] = t < per_class ? base + cls + 8 * t : -1;
+        } else {
+            rows = per_class - tile * kTile;
+            if (tid < kTile) {
+                const int t = tile * kTile + tid;
+                trow[tid] = t < per_class ? base + cls + 8 * t : -1;
+            }
         }
         T acc[4][C::NJ];
 #pragma unroll
@@ -654,7 +659,7 @@ __global__ void __launch_bounds__(256) k_m2l(const TreeInfo *__restrict__ info, 
             tile_load_op<P, T>(Op, ops, (off[0] + 3) + 7 * (off[1] + 3) + 49 * (off[2] + 3));
             tile_gather<P, T>(A, srcs, M);
             __syncthreads();
-            tile_gemm<P, T>(A, Op, acc, ty, tx);
+            if (ty * 4 < rows) tile_gemm<P, T>(A, Op, acc, ty, tx);
             __syncthreads();
         }
 #pragma unroll
@@ -722,7 +727,7 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256, GB_FAR_MIN_BLOC
         for (int a = 0; a < 4; ++a)
 #pragma unroll
             for (int j = 0; j < C::NJ; ++j) acc[a][j] = 0;
-        tile_gemm<P, T>(A, Op, acc, ty, tx);
+        if (ty * 4 < count) tile_gemm<P, T>(A, Op, acc, ty, tx);  // rows past the tile's parents are not stored
         __syncthreads();
 #pragma unroll
         for (int a = 0; a < 4; ++a)
@@ -780,7 +785,7 @@ __global__ void __launch_bounds__(256, GB_FAR_MIN_BLOCKS) k_l2l(int Lp, const Tr
         for (int a = 0; a < 4; ++a)
 #pragma unroll
             for (int j = 0; j < C::NJ; ++j) acc[a][j] = 0;
-        tile_gemm<P, T>(A, Op, acc, ty, tx);
+        if (ty * 4 < count) tile_gemm<P, T>(A, Op, acc, ty, tx);
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const int pc = par[ty * 4 + a];

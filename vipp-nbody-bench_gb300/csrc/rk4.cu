@@ -3,7 +3,8 @@
 //
 // After force evaluation k (k = 0..3) of a step, with v the stage velocity
 // and a the stage acceleration:
-//   xo += w_k v,  vo += w_k a            (w = dt/6, dt/3, dt/3, dt/6)
+//   xo += w_k v,  vo += w_k a            (w = dt/6, dt/3, dt/3, dt/6;
+//                                         k = 0 starts them: xo = x0 + w_0 v)
 //   k < 3: x = x0 + v c_k, v = v0 + a c_k (c = dt/2, dt/2, dt; x uses the old v)
 //   k = 3: x = xo, v = vo
 // Products and sums are issued as separate round-to-nearest operations
@@ -15,12 +16,14 @@ namespace gb {
 
 namespace {
 
+// The step's start state. The accumulators xo, vo are started by stage 0
+// from x0, v0 (not here), so a step repeated after a capacity overflow, which
+// restores x, v from x0, v0 and runs all four stages again, does not add its
+// stage sums to the failed attempt's.
 __global__ void k_rk4_begin(const double *__restrict__ x, const double *__restrict__ v, double *__restrict__ x0,
-                            double *__restrict__ v0, double *__restrict__ xo, double *__restrict__ vo, size_t n3) {
-    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n3; e += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const double xe = x[e], ve = v[e];
-        x0[e] = xe, xo[e] = xe, v0[e] = ve, vo[e] = ve;
-    }
+                            double *__restrict__ v0, size_t n3) {
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n3; e += static_cast<size_t>(gridDim.x) * blockDim.x)
+        x0[e] = x[e], v0[e] = v[e];
 }
 
 // The stage's acceleration is read where the force evaluation left it, in
@@ -49,8 +52,8 @@ __global__ void k_rk4_stage(int stage, double w, double c, double *__restrict__ 
         for (int k = 0; k < 3; ++k) {
             const size_t e = k * n + i;
             const double ve = v[e], ae = static_cast<double>(av[k]);
-            const double xoe = __dadd_rn(xo[e], __dmul_rn(w, ve));
-            const double voe = __dadd_rn(vo[e], __dmul_rn(w, ae));
+            const double xoe = __dadd_rn(stage == 0 ? x0[e] : xo[e], __dmul_rn(w, ve));
+            const double voe = __dadd_rn(stage == 0 ? v0[e] : vo[e], __dmul_rn(w, ae));
             xo[e] = xoe, vo[e] = voe;
             if (stage < 3) {
                 x[e] = __dadd_rn(x0[e], __dmul_rn(ve, c));
@@ -108,7 +111,7 @@ constexpr unsigned kPackedStageMin = 1u << 16;
 }  // namespace
 
 void rk4_begin(Workspace &ws) {
-    k_rk4_begin<<<grid_stride_blocks(ws), 256, 0, ws.st>>>(ws.x, ws.v, ws.x0, ws.v0, ws.xo, ws.vo, 3 * static_cast<size_t>(ws.n));
+    k_rk4_begin<<<grid_stride_blocks(ws), 256, 0, ws.st>>>(ws.x, ws.v, ws.x0, ws.v0, 3 * static_cast<size_t>(ws.n));
     ws.launches += 1;
 }
 

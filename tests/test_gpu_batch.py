@@ -212,3 +212,38 @@ def test_step_repeated_after_overflow_equals_step_without(precision):
         rb = b.stats()["retries"] - rb0
     assert ra >= 1 and rb == 0
     assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
+@pytest.mark.parametrize("sizes", [[3000], [5, 10, 0, 3, 90], [91, 1, 2000]])
+def test_forest_edge_batches(sizes):
+    """Forests of one system, of systems that are single leaves (no far
+    field at all: every root holds at most floor(sqrt(8) s) particles), and
+    of a system just over one leaf beside tiny ones: each system equals its own
+    context after two steps, and its accelerations match."""
+    import vipp_gb300
+    sy = []
+    for k, n in enumerate(sizes):
+        x, v = O.plummer_reference(n, 0.01, 40 + k) if n > 1 else (np.full((n, 3), 0.5), np.zeros((n, 3)))
+        sy.append((x, v))
+    masses = [1.0 / max(n, 1) for n in sizes]
+    X = np.concatenate([x for x, _ in sy])
+    V = np.concatenate([v for _, v in sy])
+    with vipp_gb300.Batch(sizes, p=5, s=32, eps=0.01, masses=masses, precision="mixed") as b:
+        assert b.forest
+        b.upload(X, V)
+        b.step(1e-3)
+        b.step(1e-3)
+        xb, vb = b.download()
+        ab = b.accel()
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for k, (x, v) in enumerate(sy):
+        if len(x) == 0:
+            continue
+        with vipp_gb300.Solver(p=5, s=32, eps=0.01, m=masses[k], precision="mixed") as s:
+            s.preprocess(x, v)
+            s.solve(1e-3)
+            s.solve(1e-3)
+            xs, vs = s.postprocess()
+            a = s.accel()
+        sl = slice(off[k], off[k + 1])
+        assert np.array_equal(xb[sl], xs) and np.array_equal(vb[sl], vs) and np.array_equal(ab[sl], a)

@@ -439,11 +439,15 @@ __device__ __forceinline__ void soft_term_s(const SRec<T> &r, T tx, T ty, T tz, 
 // FP32: two staged records per step on paired FP32 instructions (.f32x2, each
 // component rounded as the scalar operation). A batch of 32 records is kept as
 // 16 pairs of 24 floats, field-interleaved ((dx0, dx1, dy0, dy1), ...), so a
-// pair is six 16-byte shared-memory loads.
+// pair is six 16-byte shared-memory loads. The records are staged with the
+// term's constants folded in (tr' = -3/2 tr, Q' = 15/2 Q), so that
+//   a = M F + F1 tr + 2 F2 d.Qd = M (A^3 - B^3) + tr' (A^5 - B^5) + d.Q'd (A^7 - B^7),
+//   2 F1 Qd = -2/5 (A^5 - B^5) Q'd,
+// three pipe operations per record fewer than soft_term_s.
 __device__ __forceinline__ void put_paired(float *pb, int lane, const SRec<float> &r) {
     float *q = pb + 24 * (lane >> 1) + (lane & 1);
-    q[0] = r.dx, q[2] = r.dy, q[4] = r.dz, q[6] = r.M, q[8] = r.tr, q[10] = r.q0;
-    q[12] = r.q1, q[14] = r.q2, q[16] = r.q3, q[18] = r.q4, q[20] = r.q5, q[22] = 0.f;
+    q[0] = r.dx, q[2] = r.dy, q[4] = r.dz, q[6] = r.M, q[8] = -1.5f * r.tr, q[10] = 7.5f * r.q0;
+    q[12] = 7.5f * r.q1, q[14] = 7.5f * r.q2, q[16] = 7.5f * r.q3, q[18] = 7.5f * r.q4, q[20] = 7.5f * r.q5, q[22] = 0.f;
 }
 
 __device__ __forceinline__ float2 rsqrt2(float2 x) { return make_float2(rsqrt_t<float>(x.x), rsqrt_t<float>(x.y)); }
@@ -451,7 +455,7 @@ __device__ __forceinline__ float2 rsqrt2(float2 x) { return make_float2(rsqrt_t<
 __device__ __forceinline__ void soft_term_pair(const float4 *P, float2 ntx, float2 nty, float2 ntz, float2 e2, float2 &ax,
                                                float2 &ay, float2 &az) {
     const float4 a = P[0], b = P[1], c = P[2], d = P[3], e = P[4], f = P[5];
-    const float2 m1 = make_float2(-1.f, -1.f), two = make_float2(2.f, 2.f);
+    const float2 m1 = make_float2(-1.f, -1.f);
     const float2 dx = __fadd2_rn(make_float2(a.x, a.y), ntx);
     const float2 dy = __fadd2_rn(make_float2(a.z, a.w), nty);
     const float2 dz = __fadd2_rn(make_float2(b.x, b.y), ntz);
@@ -465,14 +469,14 @@ __device__ __forceinline__ void soft_term_pair(const float4 *P, float2 ntx, floa
     const float2 A5 = __fmul2_rn(A3, A2), B5 = __fmul2_rn(B3, B2);
     const float2 A7 = __fmul2_rn(A5, A2), B7 = __fmul2_rn(B5, B2);
     const float2 F = __ffma2_rn(B3, m1, A3);
-    const float2 F1 = __fmul2_rn(__ffma2_rn(B5, m1, A5), make_float2(-1.5f, -1.5f));
-    const float2 F2 = __fmul2_rn(__ffma2_rn(B7, m1, A7), make_float2(3.75f, 3.75f));
-    const float2 qx = __ffma2_rn(q0, dx, __ffma2_rn(q3, dy, __fmul2_rn(q4, dz)));
+    const float2 G5 = __ffma2_rn(B5, m1, A5);  // A^5 - B^5
+    const float2 G7 = __ffma2_rn(B7, m1, A7);  // A^7 - B^7
+    const float2 qx = __ffma2_rn(q0, dx, __ffma2_rn(q3, dy, __fmul2_rn(q4, dz)));  // Q'd
     const float2 qy = __ffma2_rn(q3, dx, __ffma2_rn(q1, dy, __fmul2_rn(q5, dz)));
     const float2 qz = __ffma2_rn(q4, dx, __ffma2_rn(q5, dy, __fmul2_rn(q2, dz)));
     const float2 dqd = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
-    const float2 sa = __ffma2_rn(__fmul2_rn(two, F2), dqd, __ffma2_rn(M, F, __fmul2_rn(F1, tr)));
-    const float2 sb = __fmul2_rn(two, F1);
+    const float2 sa = __ffma2_rn(G7, dqd, __ffma2_rn(tr, G5, __fmul2_rn(M, F)));
+    const float2 sb = __fmul2_rn(make_float2(-0.4f, -0.4f), G5);
     ax = __ffma2_rn(sa, dx, __ffma2_rn(sb, qx, ax));
     ay = __ffma2_rn(sa, dy, __ffma2_rn(sb, qy, ay));
     az = __ffma2_rn(sa, dz, __ffma2_rn(sb, qz, az));

@@ -23,7 +23,7 @@
 #include "workspace.cuh"
 
 #ifndef GB_P2P_CARVEOUT_MAX
-#define GB_P2P_CARVEOUT_MAX 0
+#define GB_P2P_CARVEOUT_MAX 1  // P2P SMs keep full shared memory, so the tensor-core M2L can start beside P2P blocks
 #endif
 
 namespace gb {
@@ -428,7 +428,7 @@ void p2p_pass(Workspace &ws, unsigned per_sm) {
     timer_begin(ws, kTP2P);
 #if GB_P2P_CARVEOUT_MAX
     // keep the SMs that run P2P configured for full shared memory, so far-field
-    // kernels (M2L: 173 KB) can start beside the P2P blocks
+    // kernels (the tensor-core M2L: up to 206 KB) can start beside the P2P blocks
     cudaFuncSetAttribute(k_p2p_f32<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(k_p2p_f32<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(k_p2p_f32<true, true>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);

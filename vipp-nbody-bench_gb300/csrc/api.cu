@@ -184,6 +184,13 @@ int ensure_particles(gb_ctx *ctx, unsigned n) {
     GB_TRY(dalloc(ws.off, cap + 1));
     GB_TRY(gb::sort_temp_alloc(ws.sort, cap));
     GB_TRY(gb::scan_temp_alloc(ws.scan, std::max(cap + 1, ws.c_cap + 1)));
+    if (ws.accurate) {  // the softening correction computed beside the far field
+        double *c = nullptr;
+        GB_TRY(dalloc(c, n3));
+        dfree(ws.soft_corr);
+        ws.soft_corr = c;
+        ws.soft_corr_cap = cap;
+    }
     ws.n_cap = cap;
     return ensure_chunks(ctx);
 }
@@ -261,6 +268,14 @@ int ensure_cells(gb_ctx *ctx, unsigned s_cap, unsigned r_cap) {
         dfree(ws.staylor);
         ws.smom = a, ws.smom_oct = b, ws.staylor = t;
         ws.soft_cap = ws.c_cap, ws.soft_mixed = ws.mixed;
+    }
+    if (ws.accurate && (!ws.soft_corr || ws.soft_corr_cap < ws.n_cap)) {
+        ++ctx->epoch;
+        double *c = nullptr;
+        GB_TRY(dalloc(c, 3 * static_cast<size_t>(ws.n_cap)));  // doubles: either precision fits
+        dfree(ws.soft_corr);
+        ws.soft_corr = c;
+        ws.soft_corr_cap = ws.n_cap;
     }
     if (ws.m2l_tensor) {
         // split expansions of the tensor-core M2L and their TMA map
@@ -400,6 +415,18 @@ void evaluate(gb_ctx *ctx, bool to_acc = true) {
         std::swap(ws.st, ws.st2);
         cudaEventRecord(ws.ev_join, ws.st2);
     }
+    // accurate mode: the softening correction needs only the tree and the
+    // particles, so it runs on a third stream beside the far field and is
+    // folded into the far field after L2P
+    const bool soft_fork = ws.accurate && fork && ws.soft_corr && ws.soft_corr_cap >= ws.n;
+    if (soft_fork) {
+        cudaEventRecord(ws.ev_fork3, ws.st);
+        cudaStreamWaitEvent(ws.st3, ws.ev_fork3, 0);
+        std::swap(ws.st, ws.st3);
+        gb::soften_corr(ws);
+        std::swap(ws.st, ws.st3);
+        cudaEventRecord(ws.ev_join3, ws.st3);
+    }
     gb::build_operators(ws);
     if (ws.forest()) gb::forest_tiles(ws, ws.m2l_tensor ? gb::kM2LTileTC : gb::kM2LTileCC);
     gb::upward_pass(ws);
@@ -408,7 +435,12 @@ void evaluate(gb_ctx *ctx, bool to_acc = true) {
     else
         gb::m2l_pass(ws);
     gb::downward_pass(ws);
-    if (ws.accurate) gb::soften_pass(ws);
+    if (soft_fork) {
+        cudaStreamWaitEvent(ws.st, ws.ev_join3, 0);
+        gb::soften_apply(ws);
+    } else if (ws.accurate) {
+        gb::soften_pass(ws);
+    }
     if (!fork) {
         gb::p2p_pass(ws, full);
     } else {
@@ -644,6 +676,9 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     if ((e = cudaStreamCreateWithFlags(&ws.st2, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream", e);
     if ((e = cudaEventCreateWithFlags(&ws.ev_fork, cudaEventDisableTiming)) != cudaSuccess) return fail("event", e);
     if ((e = cudaEventCreateWithFlags(&ws.ev_join, cudaEventDisableTiming)) != cudaSuccess) return fail("event", e);
+    if ((e = cudaStreamCreateWithFlags(&ws.st3, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream", e);
+    if ((e = cudaEventCreateWithFlags(&ws.ev_fork3, cudaEventDisableTiming)) != cudaSuccess) return fail("event", e);
+    if ((e = cudaEventCreateWithFlags(&ws.ev_join3, cudaEventDisableTiming)) != cudaSuccess) return fail("event", e);
     if ((e = gb::upload_tables()) != cudaSuccess) return fail("tables", e);
     if ((e = cudaMalloc(&ws.info, sizeof(gb::TreeInfo))) != cudaSuccess) return fail("info", e);
     if ((e = cudaMalloc(&ws.d_counts, gb::kNumCounts * sizeof(unsigned))) != cudaSuccess) return fail("counts", e);
@@ -677,7 +712,7 @@ void gb_destroy(gb_ctx *ctx) {
                     ws.flag, ws.flag_off, ws.leaves, ws.rng_cnt, ws.rng_off, ws.rng_len, ws.ranges, ws.chunk_cnt,
                     ws.chunk_off, ws.chunks, ws.src_total, ws.part_cnt, ws.part_off, ws.part, ws.queue, ws.ops_d, ws.bimg, ws.m2l_tab, ws.ms_tc, ws.diag, ws.ops_f, ws.zf, ws.info, ws.d_counts, ctx->d_targets, ws.smom, ws.smom_oct, ws.staylor,
                     ctx->d_direct, ws.seg, ws.psys, ws.c_sys, ws.sys_par, ws.mkeys, ws.etile, ws.oct_list, ws.otile,
-                    ws.ocnt};
+                    ws.ocnt, ws.soft_corr};
     for (void *b : bufs) dfree(b);
     gb::sort_temp_free(ws.sort);
     gb::scan_temp_free(ws.scan);
@@ -685,6 +720,9 @@ void gb_destroy(gb_ctx *ctx) {
     if (ctx->step_exec) cudaGraphExecDestroy(ctx->step_exec);
     if (ws.ev_fork) cudaEventDestroy(ws.ev_fork);
     if (ws.ev_join) cudaEventDestroy(ws.ev_join);
+    if (ws.ev_fork3) cudaEventDestroy(ws.ev_fork3);
+    if (ws.ev_join3) cudaEventDestroy(ws.ev_join3);
+    if (ws.st3) cudaStreamDestroy(ws.st3);
     if (ws.st2) cudaStreamDestroy(ws.st2);
     if (ws.st) cudaStreamDestroy(ws.st);
     if (g_timer_ctx == ctx) g_timer_ctx = nullptr;

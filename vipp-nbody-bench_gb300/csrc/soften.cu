@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_ne
     const double *__restrict__ c_ctr, const TreeInfo *__restrict__ info, const int *__restrict__ m2l_src,
     const Mom<T> *__restrict__ mom, const Mom<T> *__restrict__ moct, const T *__restrict__ taylor,
     const double *__restrict__ xs, const float4 *__restrict__ ph, const float4 *__restrict__ pl, unsigned n, T e2, T G,
-    T *__restrict__ far, double *__restrict__ farphi = nullptr) {
+    T *__restrict__ far, double *__restrict__ farphi = nullptr, T *__restrict__ corr = nullptr) {
     __shared__ int list[kSoftWarps][kSoftMaxSrc + 32];
     __shared__ __align__(16) SRec<T> batch[kSoftWarps][32];  // FP32: the paired layout (put_paired)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -626,9 +626,13 @@ __global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_ne
                     const T ax = acc[q][0] + tl[0] + tl[3] * y[0] + tl[4] * y[1] + tl[5] * y[2];
                     const T ay = acc[q][1] + tl[1] + tl[6] * y[0] + tl[7] * y[1] + tl[8] * y[2];
                     const T az = acc[q][2] + tl[2] + tl[9] * y[0] + tl[10] * y[1] + tl[11] * y[2];
-                    far[j] = G * (far[j] + ax);
-                    far[n + j] = G * (far[n + j] + ay);
-                    far[2 * static_cast<size_t>(n) + j] = G * (far[2 * static_cast<size_t>(n) + j] + az);
+                    if (corr) {  // kept apart; soften_apply folds it into the far field
+                        corr[j] = ax, corr[n + j] = ay, corr[2 * static_cast<size_t>(n) + j] = az;
+                    } else {
+                        far[j] = G * (far[j] + ax);
+                        far[n + j] = G * (far[n + j] + ay);
+                        far[2 * static_cast<size_t>(n) + j] = G * (far[2 * static_cast<size_t>(n) + j] + az);
+                    }
                 }
             }
         }
@@ -636,13 +640,24 @@ __global__ void __launch_bounds__(kSoftWarps * 32, GB_SOFT_MIN_BLOCKS) k_soft_ne
     }
 }
 
+// far = G (far + corr) for every particle (tree order): the particles the
+// correction kernel skips have corr = 0 and far = 0 (leaves above level 2).
 template <typename T>
-void launch_soften(Workspace &ws) {
+__global__ void k_soft_apply(T *__restrict__ far, const T *__restrict__ corr, T G, size_t n3) {
+    for (size_t e = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; e < n3; e += static_cast<size_t>(gridDim.x) * blockDim.x)
+        far[e] = G * (far[e] + corr[e]);
+}
+
+// corr: null writes far = G (far + correction) after L2P; non-null writes the
+// correction there (zeroed first), independent of the far-field chain.
+template <typename T>
+void launch_soften(Workspace &ws, T *corr) {
     const unsigned gw = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(ws.c_cap, 4));  // a warp per leaf
     Mom<T> *mom = static_cast<Mom<T> *>(ws.smom);
     Mom<T> *moct = static_cast<Mom<T> *>(ws.smom_oct);
     T *taylor = static_cast<T *>(ws.staylor);
     const T e2 = static_cast<T>(ws.eps * ws.eps);
+    if (corr) cudaMemsetAsync(corr, 0, sizeof(T) * 3 * static_cast<size_t>(ws.n), ws.st);
     k_mom_leaf<T><<<gw, 128, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_ctr, ws.xs, ws.ph,
                                          ws.pl, ws.n, ws.info, static_cast<T>(ws.m), mom, moct);
     ws.launches += 1;
@@ -655,7 +670,7 @@ void launch_soften(Workspace &ws) {
                                          mom, e2, taylor);
     k_soft_near<T><<<gw, kSoftWarps * 32, 0, ws.st>>>(ws.leaves, ws.d_counts, ws.c_begin, ws.c_end, ws.c_level, ws.c_parent,
                                           ws.c_child, ws.c_ctr, ws.info, ws.m2l_src, mom, moct, taylor, ws.xs, ws.ph,
-                                          ws.pl, ws.n, e2, static_cast<T>(ws.G), static_cast<T *>(ws.farf));
+                                          ws.pl, ws.n, e2, static_cast<T>(ws.G), static_cast<T *>(ws.farf), nullptr, corr);
     ws.launches += 2;
 }
 
@@ -691,10 +706,29 @@ size_t soften_cell_bytes(bool mixed) {
 void soften_pass(Workspace &ws) {
     timer_begin(ws, kTSoft);
     if (ws.mixed)
-        launch_soften<float>(ws);
+        launch_soften<float>(ws, nullptr);
     else
-        launch_soften<double>(ws);
+        launch_soften<double>(ws, nullptr);
     timer_end(ws, kTSoft);
+}
+
+void soften_corr(Workspace &ws) {
+    if (ws.mixed)
+        launch_soften<float>(ws, static_cast<float *>(ws.soft_corr));
+    else
+        launch_soften<double>(ws, static_cast<double *>(ws.soft_corr));
+}
+
+void soften_apply(Workspace &ws) {
+    const size_t n3 = 3 * static_cast<size_t>(ws.n);
+    const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * 8, ceil_div(n3, 256));
+    if (ws.mixed)
+        k_soft_apply<float><<<gs, 256, 0, ws.st>>>(static_cast<float *>(ws.farf), static_cast<const float *>(ws.soft_corr),
+                                                   static_cast<float>(ws.G), n3);
+    else
+        k_soft_apply<double><<<gs, 256, 0, ws.st>>>(static_cast<double *>(ws.farf), static_cast<const double *>(ws.soft_corr),
+                                                    ws.G, n3);
+    ws.launches += 1;
 }
 
 }  // namespace gb

@@ -41,6 +41,8 @@ struct Workspace {
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;         // near field, concurrent with the far field on st
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t st3 = nullptr;         // accurate mode: the softening correction, concurrent with the far field
+    cudaEvent_t ev_fork3 = nullptr, ev_join3 = nullptr;
     bool serial = false;                // near field on st after the far field
     int sort_levels = 10;               // key levels the radix sort orders (grown on demand, up to 21)
     unsigned sort_spin_max = kSortSpinMax;  // look-back polls before a wait gives up (tests lower it)
@@ -116,6 +118,8 @@ struct Workspace {
     void *smom = nullptr;       // accurate mode: [C] moment records (soften.cu)
     void *smom_oct = nullptr;   // [C][8] octant moment records of the leaves
     void *staylor = nullptr;    // [C][13] leaf-centre value, J and potential of the far levels' correction
+    void *soft_corr = nullptr;  // [3][N] the correction, tree order (computed beside the far field)
+    unsigned soft_corr_cap = 0; // particles soft_corr is sized for (doubles)
     unsigned soft_cap = 0;      // cells the three are sized for (0: not allocated)
     bool soft_mixed = false;    // their element type
     int *coll = nullptr, *coll_cnt = nullptr;    // [C][27], [C]
@@ -198,6 +202,8 @@ int m2l_tc_row_floats(int p);
 const char *m2l_tc_encode(Workspace &ws);     // (re)build tmap_ms; nullptr or an error message
 void downward_pass(Workspace &ws);            // L2L + L2P into far
 void soften_pass(Workspace &ws);              // accurate mode: far = G (far + softening correction)
+void soften_corr(Workspace &ws);              // the same correction into soft_corr (no far-field input)
+void soften_apply(Workspace &ws);             // far = G (far + soft_corr)
 void soften_phi(Workspace &ws, double *farphi); // accurate mode: the far potential's correction (tree order)
 size_t soften_taylor_values();                // per-leaf values of the far levels' correction
 size_t soften_cell_bytes(bool mixed);         // bytes of one moment record

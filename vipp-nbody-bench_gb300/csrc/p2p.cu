@@ -69,6 +69,35 @@ struct Cursor {
     }
 };
 
+// The same walk in full batches: up to 32 sources taken across range
+// boundaries, lane l getting the l-th (a batch is cut only at the slice's end,
+// so every batch but the last is full and takes the paired path). The state
+// is uniform over the warp; the loop runs once per range the batch touches.
+struct BatchCursor {
+    const uint2 *rng;
+    unsigned nr, r, b, end, rem;
+    __device__ __forceinline__ void start(const uint2 *ranges, unsigned n, unsigned v0, unsigned len) {
+        Cursor c;
+        c.start(ranges, n, v0, len);
+        rng = c.rng, nr = c.nr, r = c.r, b = c.b, end = c.end, rem = c.rem;
+    }
+    // the next batch: its size, and this lane's source index (lane < size)
+    __device__ __forceinline__ unsigned next(unsigned lane, unsigned &idx) {
+        unsigned filled = 0;
+        idx = 0;
+        while (filled < 32u && rem > 0 && r < nr) {
+            const unsigned take = min(min(32u - filled, end - b), rem);
+            if (lane >= filled && lane < filled + take) idx = b + (lane - filled);
+            filled += take, rem -= take, b += take;
+            if (b >= end && ++r < nr) {
+                const uint2 g = rng[r];
+                b = g.x, end = g.y;
+            }
+        }
+        return filled;
+    }
+};
+
 // Work item -> (leaf, first target, targets, slice, slices, partial slot,
 // source slice [v0, v0 + len)).
 struct Item {
@@ -141,14 +170,12 @@ __global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(c
             tz = (h.z - cc.hz) + (l.z - cc.lz);
         }
         float sx = 0, sy = 0, sz = 0, kx = 0, ky = 0, kz = 0;  // Kahan sums and compensations
-        Cursor cur;
+        BatchCursor cur;
         cur.start(ranges + rng_off[it.li], rng_len[it.li], it.v0, it.len);
         float4 h = make_float4(0, 0, 0, 0), l = h;
-        unsigned cnt = 0;
-        if (cur.valid()) {
-            cnt = cur.count();
-            if (static_cast<unsigned>(lane) < cnt) h = ph[cur.b + lane], l = pl[cur.b + lane];
-        }
+        unsigned sidx;
+        unsigned cnt = cur.next(static_cast<unsigned>(lane), sidx);
+        if (static_cast<unsigned>(lane) < cnt) h = ph[sidx], l = pl[sidx];
         const float2 ntx = make_float2(-tx, -tx), nty = make_float2(-ty, -ty), ntz = make_float2(-tz, -tz);
         const float2 e2 = make_float2(eps2, eps2);
         while (cnt) {
@@ -162,12 +189,8 @@ __global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(c
             }
             __syncwarp();
             const unsigned now = cnt;
-            cur.advance();
-            cnt = 0;
-            if (cur.valid()) {  // prefetch the next batch while this one is computed
-                cnt = cur.count();
-                if (static_cast<unsigned>(lane) < cnt) h = ph[cur.b + lane], l = pl[cur.b + lane];
-            }
+            cnt = cur.next(static_cast<unsigned>(lane), sidx);  // prefetch the next batch while this one is computed
+            if (static_cast<unsigned>(lane) < cnt) h = ph[sidx], l = pl[sidx];
             float bx = 0, by = 0, bz = 0;
             if (g == 1 && now == 32) {
                 // two sources per step on paired FP32 instructions (.f32x2);

@@ -616,7 +616,7 @@ def main():
         default_cfg = (args.workload == "plummer" and n == 1 << 22 and args.p == 8 and args.s == 64 and args.eps == 0.005
                        and args.precision == "mixed" and args.flags & ~vipp_gb300.FLAG_M2L_BF16 == 0)
         bf = bool(args.flags & vipp_gb300.FLAG_M2L_BF16)
-        traffic = {"p2p": 292350208 + 41266688, "m2l": (M2L_BF16_TRAFFIC if bf else 195950592 + 21233664)} if default_cfg else {}
+        traffic = {"p2p": 301173760 + 40833536, "m2l": (M2L_BF16_TRAFFIC if bf else 195950592 + 21233664)} if default_cfg else {}
         for k in per:
             per[k]["traffic"] = traffic.get(k)
         roof.update({"kernel": dom, "traffic": traffic.get(dom), "traffic_unit": "B per launch"})

@@ -381,12 +381,15 @@ int check_device_errors(gb_ctx *ctx, unsigned *need) {
         return GB_ERR_CAPACITY;
     }
     // After the first good evaluation of an upload, sort only the key levels
-    // the tree uses plus two (never more than now): shallow trees get fewer
-    // sort passes and M2M/L2L level launches. A tree that deepens later asks
-    // for more through counts[9].
+    // the tree uses plus one, rounded up to what the same number of 8-bit
+    // radix passes holds (never more than now): shallow trees get fewer sort
+    // passes and M2M/L2L level launches, and the margin costs no pass. A tree
+    // that deepens past it later asks for more through counts[9].
     if (!ctx->levels_fitted) {
         ctx->levels_fitted = true;
-        const int want = std::max(3, ws.h_info->depth + 2);
+        const int sb = ws.forest() ? ws.sys_bits : 0;  // a forest's sort word also holds the system
+        const int passes = (3 * std::max(3, ws.h_info->depth + 1) + sb + 7) / 8;
+        const int want = std::min((8 * passes - sb) / 3, ws.sort_levels_cap());
         if (want < ws.sort_levels) ws.sort_levels = want, ++ctx->epoch;
     }
     return GB_OK;

@@ -674,7 +674,10 @@ __global__ void k_build_bimg(const float *__restrict__ ops_all, unsigned char *_
     constexpr int RUNS = C::KC / VE;
     for (int kc = 0; kc < C::NKC; ++kc) {
         unsigned char *blk = bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::B_BYTES);
-        for (int u = threadIdx.x; u < 2 * C::N * RUNS; u += blockDim.x) {
+        // bf16: a chunk of lo inputs only is copied without its Blo rows (they
+        // would be zero there), so they are not written either
+        const int rows = (BF && kc * C::KC >= C::K) ? C::N : 2 * C::N;
+        for (int u = threadIdx.x; u < rows * RUNS; u += blockDim.x) {
             const int r = u / RUNS, k0 = (u % RUNS) * VE;
             const bool lo_row = r >= C::N;
             const int ro = lo_row ? r - C::N : r;

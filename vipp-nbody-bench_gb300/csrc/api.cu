@@ -694,6 +694,8 @@ int gb_create(const gb_config *cfg, gb_ctx **out) {
     if ((e = cudaMalloc(&ws.ops_f, sizeof(float) * kk)) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.zf, sizeof(float) * gb::zf_table_floats(ws.p))) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.bimg, sizeof(float) * gb::m2l_tc_image_floats(ws.p))) != cudaSuccess) return fail("ops", e);
+    // image rows past K are never written (k_build_bimg): zero once
+    if ((e = cudaMemset(ws.bimg, 0, sizeof(float) * gb::m2l_tc_image_floats(ws.p))) != cudaSuccess) return fail("ops", e);
     if ((e = cudaMalloc(&ws.m2l_tab, gb::m2l_table_bytes(ws.p))) != cudaSuccess) return fail("ops", e);
     gb::build_m2l_table(ws);
     if ((e = cudaStreamSynchronize(ws.st)) != cudaSuccess) return fail("ops table", e);
@@ -753,6 +755,7 @@ int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
         GB_TRY(dalloc(ctx->ws.ops_f, kk));
         GB_TRY(dalloc(ctx->ws.zf, gb::zf_table_floats(ctx->ws.p)));
         GB_TRY(dalloc(ctx->ws.bimg, gb::m2l_tc_image_floats(ctx->ws.p)));
+        GB_TRY(cudaMemset(ctx->ws.bimg, 0, sizeof(float) * gb::m2l_tc_image_floats(ctx->ws.p)));
         unsigned char *t = nullptr;
         GB_TRY(dalloc(t, gb::m2l_table_bytes(ctx->ws.p)));
         dfree(ctx->ws.m2l_tab);
@@ -997,6 +1000,7 @@ int forest_setup(gb_ctx *ctx, size_t nsys, const uint64_t *off, const std::vecto
     GB_TRY(dalloc(ws.ops_f, kk));
     GB_TRY(dalloc(ws.zf, gb::zf_table_floats(ws.p) * nsys));
     GB_TRY(dalloc(ws.bimg, gb::m2l_tc_image_floats(ws.p) * nsys));
+    GB_TRY(cudaMemset(ws.bimg, 0, sizeof(float) * gb::m2l_tc_image_floats(ws.p) * nsys));
     std::vector<unsigned> seg(nsys + 1);
     std::vector<int> ps(n);
     std::vector<double2> par(nsys);

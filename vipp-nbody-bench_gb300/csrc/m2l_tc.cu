@@ -675,12 +675,15 @@ __global__ void k_build_bimg(const float *__restrict__ ops_all, unsigned char *_
     for (int kc = 0; kc < C::NKC; ++kc) {
         unsigned char *blk = bimg + (static_cast<size_t>(oi) * C::NKC + kc) * (2 * C::B_BYTES);
         // bf16: a chunk of lo inputs only is copied without its Blo rows (they
-        // would be zero there), so they are not written either
-        const int rows = (BF && kc * C::KC >= C::K) ? C::N : 2 * C::N;
+        // would be zero there), so they are not written either. Rows of output
+        // coefficients past K are not written (they only reach accumulator
+        // columns the drain never stores); the K columns are all written.
+        const int rows = (BF && kc * C::KC >= C::K) ? C::K : 2 * C::K;
         for (int u = threadIdx.x; u < rows * RUNS; u += blockDim.x) {
-            const int r = u / RUNS, k0 = (u % RUNS) * VE;
-            const bool lo_row = r >= C::N;
-            const int ro = lo_row ? r - C::N : r;
+            const int vr = u / RUNS, k0 = (u % RUNS) * VE;
+            const bool lo_row = vr >= C::K;
+            const int ro = lo_row ? vr - C::K : vr;
+            const int r = lo_row ? C::N + ro : ro;
             float v[VE];
 #pragma unroll
             for (int e = 0; e < VE; ++e) {

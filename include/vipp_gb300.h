@@ -121,6 +121,9 @@ typedef struct gb_stats {
     int64_t graph_steps;  /* RK4 steps run by replaying the captured step graph */
     int64_t direct_steps; /* RK4 steps run by launching every kernel */
     int64_t graph_captures; /* step graphs captured (a new n, dt or buffer set) */
+    int64_t steps;        /* RK4 steps taken since the state was set (upload or
+                             initial conditions; a checkpoint load restores the
+                             saved count) */
 } gb_stats;
 
 /* Create a context on cfg->device. Validates cfg (p in 1..10, s >= 1). */
@@ -299,6 +302,65 @@ GB_API int gb_get_tuning(const gb_ctx *ctx, gb_tuning *out);
  * filled, GB_ERR_STATE when the file has no matching entry, GB_ERR_INVALID
  * when it cannot be read or an entry is malformed. No GPU is needed. */
 GB_API int gb_tuning_lookup(const char *path, const gb_config *cfg, size_t n, gb_tuning *out);
+
+/* Checkpoints: the state that restarts a run. The reference keeps none (its
+ * ENABLE_PRINT build writes the positions of a run as text,
+ * gravity/include/benchmark.hpp:15-20, 46-58). A step depends only on the
+ * positions, velocities and configuration, so a run restarted from a
+ * checkpoint continues bit-identically to the run that wrote it.
+ * File layout (little-endian; 8-byte words after the header):
+ *   header, 128 bytes: 0 char[8] "VIPPGBCK", 8 uint32 version (1),
+ *     12 uint32 header bytes (128), 16 uint64 n, 24 uint64 nsys,
+ *     32 int64 steps, 40 double t, 48 int32 p, 52 int32 s, 56 int32 precision,
+ *     60 int32 mode, 64 int32 flags, 68 int32 leaf_s, 72 double eps,
+ *     80 double G, 88 double m, 96..127 zero;
+ *   uint64 seg_offsets[nsys + 1]; double m_per_system[nsys];
+ *   double x[3n]; double v[3n] (AoS, the caller's particle order);
+ *   uint64 check word: FNV-1a over every preceding 8-byte word, one word per
+ *     round (offset basis 0xcbf29ce484222325, prime 0x100000001b3).
+ * Files are written under path + ".tmp" and renamed over path. */
+typedef struct gb_checkpoint_info {
+    uint64_t n;      /* particles of all systems */
+    uint64_t nsys;   /* systems (1 for a context) */
+    int64_t steps;   /* RK4 steps taken since the state was set */
+    double t;        /* simulated time, as given to the save */
+    gb_config cfg;   /* the writer's p, s, eps, G, m, precision, flags and mode
+                        (device: 0 on read) */
+    int32_t leaf_s;  /* leaf parameter in effect (s, or the tuning's leaf_s in
+                        accurate mode) */
+} gb_checkpoint_info;
+
+enum gb_checkpoint_flags {
+    GB_CHECKPOINT_ANY_CONFIG = 1  /* load: skip the configuration check */
+};
+
+/* Host only (no GPU). Write a checkpoint from host arrays: seg_offsets
+ * (nsys + 1 entries from 0 to n, not decreasing; NULL for one system),
+ * m_per_system (NULL: info->cfg.m for every system), x_aos and v_aos (3n
+ * each). Read fills *info from the header; when any array is given it reads
+ * the whole body, verifies the check word and fills the arrays given:
+ * seg_offsets (nsys + 1) and m_per_system (nsys) when nsys <= nsys_cap, x_aos
+ * and v_aos (3n) when n <= n_cap. A malformed, truncated or corrupt file or a
+ * bad argument is GB_ERR_INVALID, described by gb_last_error(NULL). */
+GB_API int gb_checkpoint_write(const char *path, const gb_checkpoint_info *info, const uint64_t *seg_offsets,
+                               const double *m_per_system, const double *x_aos, const double *v_aos);
+GB_API int gb_checkpoint_read(const char *path, gb_checkpoint_info *info, uint64_t *seg_offsets,
+                              double *m_per_system, size_t nsys_cap, double *x_aos, double *v_aos, size_t n_cap);
+
+/* Save the context's state, its step count and the time t (GB_ERR_STATE
+ * before an upload). Load replaces the context's state as gb_upload does and
+ * restores the step count; *t (may be NULL) receives the saved time. The file
+ * must hold one system, and unless flags has GB_CHECKPOINT_ANY_CONFIG its p,
+ * s, eps, G, m, precision, mode, leaf_s and result-changing flags
+ * (GB_FLAG_P2P_NEWTON, GB_FLAG_M2L_CUDA_CORES, GB_FLAG_M2L_BF16) must equal
+ * the context's (GB_ERR_INVALID otherwise; the state is then unchanged). */
+GB_API int gb_checkpoint_save(gb_ctx *ctx, const char *path, double t);
+GB_API int gb_checkpoint_load(gb_ctx *ctx, const char *path, int flags, double *t);
+/* The same for a batch: the file holds the batch's systems. Load requires the
+ * batch's segment offsets, and (unless GB_CHECKPOINT_ANY_CONFIG) its masses
+ * and configuration. */
+GB_API int gb_batch_checkpoint_save(gb_batch *b, const char *path, double t);
+GB_API int gb_batch_checkpoint_load(gb_batch *b, const char *path, int flags, double *t);
 
 /* Block until all queued work finished; reports deferred device errors. */
 GB_API int gb_sync(gb_ctx *ctx);

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 #include <gravity/solver_gb300.hpp>
@@ -51,7 +52,8 @@ void expect(bool ok, const char *what) {
 
 }  // namespace
 
-int main() {
+int main(int argc, char **argv) {
+    const std::string dir = argc > 1 ? argv[1] : ".";  // where the checkpoint test writes its file
     using Solver = gravity::SolverGB300<double, double, double, double, double, double>;
     {  // two-body RK4 step against its closed form, via the FMM solver (root leaf: direct P2P)
         const double eps = 1e-4, d = 10.0, t = eps / std::sqrt(2.0);  // delta_t()/t == 1
@@ -95,6 +97,34 @@ int main() {
         expect(dx <= 1e-13 * xs && dv <= 1e-10 * vs, "Plummer RK4 trajectory vs oracle");
         const auto a = s.acceleration();
         expect(a.size() == 3 * n, "acceleration size");
+    }
+    {  // checkpoint: a solver restarted from the file written after two steps
+       // continues bit-identically to the solver that wrote it
+        const std::size_t n = 2000;
+        Problem pr{n, 16, 0.01, 1.0, 1.0, 5};
+        std::vector<vipp_oracle::V3> x3, v3;
+        vipp_oracle::plummer_reference(n, pr.eps, 4, x3, v3);
+        std::vector<Vec> x(n), v(n), xb(n), vb(n);
+        for (std::size_t i = 0; i < n; ++i) x[i] = {x3[i].x, x3[i].y, x3[i].z}, v[i] = {v3[i].x, v3[i].y, v3[i].z};
+        const std::string path = dir + "/solver_gb300.ckpt";
+        const double t = 10.0, t_saved = 2 * pr.delta_t() / t;
+        Solver a;
+        a.preprocess(pr, x, v);
+        a.solve(pr, t, x, v);
+        a.solve(pr, t, x, v);
+        a.save_checkpoint(path, t_saved);
+        a.solve(pr, t, x, v);
+        a.postprocess(pr, x, v);
+        Solver b;
+        const double t_loaded = b.load_checkpoint(pr, path);
+        b.solve(pr, t, xb, vb);
+        b.postprocess(pr, xb, vb);
+        bool same = t_loaded == t_saved;
+        for (std::size_t i = 0; i < n; ++i)
+            same = same && x[i].x() == xb[i].x() && x[i].y() == xb[i].y() && x[i].z() == xb[i].z() &&
+                   v[i].x() == vb[i].x() && v[i].y() == vb[i].y() && v[i].z() == vb[i].z();
+        expect(same, "checkpoint restart bit-identical");
+        std::remove(path.c_str());
     }
     {  // errors surface as std::runtime_error, like the reference's exceptions
         Problem bad{10, 0, 0.01, 1.0, 1.0, 4};  // s = 0 (problem.hpp:182-184)

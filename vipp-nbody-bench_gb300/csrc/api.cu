@@ -11,7 +11,9 @@
 #include <vector>
 
 #include "../../include/vipp_gb300.h"
+#include "checkpoint.h"
 #include "direct.cuh"
+#include "trace.h"
 #include "workspace.cuh"
 
 namespace gb {
@@ -34,6 +36,7 @@ struct gb_ctx {
     gb::Workspace ws;
     std::string err;
     bool have_state = false;
+    long long state_steps = 0;  // RK4 steps since the state was set
     long long retries = 0;  // evaluations repeated after a capacity overflow
     size_t phi_cap = 0;     // particles ws.phi / ws.phis are sized for
     // CUDA graph of one RK4 step, valid for (n, dt, buffer epoch)
@@ -62,7 +65,8 @@ struct gb_ctx {
 
 namespace {
 
-std::string g_create_error;
+// message of the last failed call without a context (per host thread)
+thread_local std::string g_create_error;
 
 const char *kVersion = "vipp-gb300 0.1 (sm_103a)";
 
@@ -310,13 +314,19 @@ void collect_timers(gb_ctx *ctx) {
     ctx->pending.clear();
 }
 
-gb_ctx *g_timer_ctx = nullptr;  // context whose stream the timer hooks record on
+// context whose stream the timer hooks record on (set by each evaluation on
+// its own host thread: a batch queues its contexts from several threads)
+thread_local gb_ctx *g_timer_ctx = nullptr;
+
+const char *const kClassNames[gb::kNumTimers] = {"tree", "operators", "p2m_m2m", "m2l",
+                                                 "l2l_l2p", "p2p", "rk4", "soften"};
 
 }  // namespace
 
 namespace gb {
 
 void timer_begin(Workspace &ws, int cls) {
+    nvtx_push(kClassNames[cls]);
     if (!ws.timing || !g_timer_ctx) return;
     gb_ctx *ctx = g_timer_ctx;
     auto take = [&]() {
@@ -335,6 +345,7 @@ void timer_begin(Workspace &ws, int cls) {
 }
 
 void timer_end(Workspace &ws, int cls) {
+    nvtx_pop();
     if (!ws.timing || !g_timer_ctx) return;
     gb_ctx *ctx = g_timer_ctx;
     for (auto it = ctx->pending.rbegin(); it != ctx->pending.rend(); ++it)
@@ -774,6 +785,7 @@ int gb_set_config(gb_ctx *ctx, const gb_config *cfg) {
 }
 
 int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
+    gb::NvtxRange nvtx_("gb_upload");
     if (ctx) ctx->levels_fitted = false;
     if (!ctx) return GB_ERR_INVALID;
     if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
@@ -796,10 +808,12 @@ int gb_upload(gb_ctx *ctx, const double *x_aos, const double *v_aos, size_t n) {
     }
     GB_TRY(cudaStreamSynchronize(ws.st));
     ctx->have_state = true;
+    ctx->state_steps = 0;
     return GB_OK;
 }
 
 int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max) {
+    gb::NvtxRange nvtx_("gb_init_plummer");
     if (ctx) ctx->levels_fitted = false;
     if (!ctx) return GB_ERR_INVALID;
     if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
@@ -826,11 +840,13 @@ int gb_init_plummer(gb_ctx *ctx, size_t n, uint64_t seed, double r_max) {
     }
     GB_TRY(cudaStreamSynchronize(ws.st));
     ctx->have_state = true;
+    ctx->state_steps = 0;
     return GB_OK;
 }
 
 int gb_init_clustered(gb_ctx *ctx, size_t n, uint64_t seed, int clusters, double background, double r_max,
                       double *params) {
+    gb::NvtxRange nvtx_("gb_init_clustered");
     if (ctx) ctx->levels_fitted = false;
     if (!ctx) return GB_ERR_INVALID;
     if (n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
@@ -858,10 +874,12 @@ int gb_init_clustered(gb_ctx *ctx, size_t n, uint64_t seed, int clusters, double
     }
     GB_TRY(cudaStreamSynchronize(ws.st));
     ctx->have_state = true;
+    ctx->state_steps = 0;
     return GB_OK;
 }
 
 int gb_download(gb_ctx *ctx, double *x_aos, double *v_aos) {
+    gb::NvtxRange nvtx_("gb_download");
     if (!ctx) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
     GB_TRY(cudaSetDevice(ctx->cfg.device));
@@ -940,18 +958,21 @@ static void step_enqueue(gb_ctx *ctx, double dt) {
 }
 
 int gb_rk4_step(gb_ctx *ctx, double dt) {
+    gb::NvtxRange nvtx_("gb_rk4_step");
     if (!ctx) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
     if (!std::isfinite(dt)) return ctx->err = "dt must be finite", GB_ERR_INVALID;
     GB_TRY(cudaSetDevice(ctx->cfg.device));
     gb::Workspace &ws = ctx->ws;
-    if (ws.n == 0) return GB_OK;
+    if (ws.n == 0) return ++ctx->state_steps, GB_OK;
     gb::rk4_begin(ws);
     const int rc = run_with_capacity(ctx, [&]() { step_enqueue(ctx, dt); });
     if (rc != GB_OK) {
         // leave the state as it was before the step
         gb::rk4_restore(ws);
         cudaStreamSynchronize(ws.st);
+    } else {
+        ++ctx->state_steps;
     }
     return rc;
 }
@@ -978,6 +999,7 @@ struct gb_batch {
     gb_ctx *forest = nullptr;   // forest form: one context over every system
     std::vector<uint64_t> off;  // nsys + 1 particle offsets
     std::vector<double> m;      // particle mass of each system
+    long long steps = 0;        // batch steps since the state was set
     std::string err;
     size_t nsys() const { return off.size() - 1; }
 };
@@ -1114,7 +1136,9 @@ static int batch_fail(gb_batch *b, size_t k, int rc) {
 }
 
 int gb_batch_upload(gb_batch *b, const double *x_aos, const double *v_aos) {
+    gb::NvtxRange nvtx_("gb_batch_upload");
     if (!b || !x_aos || !v_aos) return GB_ERR_INVALID;
+    b->steps = 0;
     if (b->forest) {
         const int rc = gb_upload(b->forest, x_aos, v_aos, b->off.back());
         return rc == GB_OK ? rc : forest_fail(b, rc);
@@ -1133,6 +1157,7 @@ int gb_batch_init_plummer(gb_batch *b, uint64_t seed, double r_lo, double r_hi, 
 
 int gb_batch_init_plummer_at(gb_batch *b, uint64_t seed, uint64_t first, double r_lo, double r_hi, double r_max,
                              double *radii) {
+    gb::NvtxRange nvtx_("gb_batch_init_plummer_at");
     if (!b) return GB_ERR_INVALID;
     if (!(r_lo > 0) || !(r_hi >= r_lo) || !std::isfinite(r_hi)) return b->err = "need 0 < r_lo <= r_hi", GB_ERR_INVALID;
     if (!(r_max > 0) || !std::isfinite(r_max)) return b->err = "r_max must be finite and > 0", GB_ERR_INVALID;
@@ -1184,6 +1209,8 @@ int gb_batch_init_plummer_at(gb_batch *b, uint64_t seed, uint64_t first, double 
             if (rc != GB_OK) return forest_fail(b, rc);
         }
         ctx->have_state = true;
+        ctx->state_steps = 0;
+        b->steps = 0;
         return GB_OK;
     }
     for (size_t k = 0; k < ns; ++k) {
@@ -1202,6 +1229,7 @@ int gb_batch_init_plummer_at(gb_batch *b, uint64_t seed, uint64_t first, double 
             if (rc != GB_OK) return batch_fail(b, k, rc);
         }
         ctx->have_state = true;
+        ctx->state_steps = 0;
     }
     for (size_t k = 0; k < ns; ++k) {
         gb::Workspace &ws = b->ctx[k]->ws;
@@ -1214,10 +1242,12 @@ int gb_batch_init_plummer_at(gb_batch *b, uint64_t seed, uint64_t first, double 
             return batch_fail(b, k, GB_ERR_CUDA);
         }
     }
+    b->steps = 0;
     return GB_OK;
 }
 
 int gb_batch_download(gb_batch *b, double *x_aos, double *v_aos) {
+    gb::NvtxRange nvtx_("gb_batch_download");
     if (!b || !x_aos || !v_aos) return GB_ERR_INVALID;
     if (b->forest) {
         const int rc = gb_download(b->forest, x_aos, v_aos);
@@ -1232,11 +1262,13 @@ int gb_batch_download(gb_batch *b, double *x_aos, double *v_aos) {
 }
 
 int gb_batch_rk4_step(gb_batch *b, double dt) {
+    gb::NvtxRange nvtx_("gb_batch_rk4_step");
     if (!b) return GB_ERR_INVALID;
     if (!std::isfinite(dt)) return b->err = "dt must be finite", GB_ERR_INVALID;
     if (b->forest) {
         if (!b->forest->have_state) return b->err = "no state uploaded", GB_ERR_STATE;
         const int rc = gb_rk4_step(b->forest, dt);
+        if (rc == GB_OK) ++b->steps;
         return rc == GB_OK ? rc : forest_fail(b, rc);
     }
     const size_t ns = b->ctx.size();
@@ -1282,8 +1314,13 @@ int gb_batch_rk4_step(gb_batch *b, double dt) {
             gb::rk4_restore(c->ws);
             cudaStreamSynchronize(c->ws.st);
             if (first_rc == GB_OK) first_rc = batch_fail(b, k, rc);
+        } else {
+            ++c->state_steps;
         }
     }
+    for (size_t k = 0; k < ns; ++k)
+        if (!live[k]) ++b->ctx[k]->state_steps;
+    if (first_rc == GB_OK) ++b->steps;
     return first_rc;
 }
 
@@ -1309,6 +1346,7 @@ int ensure_potential(gb_ctx *ctx) {
 }
 
 int gb_accel(gb_ctx *ctx, double *a_aos, double *phi) {
+    gb::NvtxRange nvtx_("gb_accel");
     if (!ctx) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
     GB_TRY(cudaSetDevice(ctx->cfg.device));
@@ -1331,6 +1369,7 @@ int gb_accel(gb_ctx *ctx, double *a_aos, double *phi) {
 }
 
 int gb_get_conserved(gb_ctx *ctx, gb_conserved *out) {
+    gb::NvtxRange nvtx_("gb_get_conserved");
     if (!ctx || !out) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
     GB_TRY(cudaSetDevice(ctx->cfg.device));
@@ -1356,6 +1395,7 @@ int gb_get_conserved(gb_ctx *ctx, gb_conserved *out) {
 }
 
 int gb_direct_accel(gb_ctx *ctx, const int64_t *targets, size_t ntargets, double *a_aos) {
+    gb::NvtxRange nvtx_("gb_direct_accel");
     if (!ctx) return GB_ERR_INVALID;
     if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
     if (!a_aos) return ctx->err = "null output", GB_ERR_INVALID;
@@ -1391,6 +1431,7 @@ int gb_direct_accel(gb_ctx *ctx, const int64_t *targets, size_t ntargets, double
 }
 
 int gb_sync(gb_ctx *ctx) {
+    gb::NvtxRange nvtx_("gb_sync");
     if (!ctx) return GB_ERR_INVALID;
     GB_TRY(cudaSetDevice(ctx->cfg.device));
     GB_TRY(cudaStreamSynchronize(ctx->ws.st));
@@ -1412,12 +1453,14 @@ int gb_get_stats(gb_ctx *ctx, gb_stats *out) {
     out->graph_steps = ctx->graph_steps;
     out->graph_captures = ctx->graph_captures;
     out->direct_steps = ctx->direct_steps;
+    out->steps = ctx->state_steps;
     return GB_OK;
 }
 
 // Batch accessors: the contexts form asks each system's context; the forest
 // form evaluates the whole forest once and splits the results by system.
 int gb_batch_accel(gb_batch *b, double *a_aos, double *phi) {
+    gb::NvtxRange nvtx_("gb_batch_accel");
     if (!b) return GB_ERR_INVALID;
     if (b->forest) {
         const int rc = gb_accel(b->forest, a_aos, phi);
@@ -1433,6 +1476,7 @@ int gb_batch_accel(gb_batch *b, double *a_aos, double *phi) {
 }
 
 int gb_batch_conserved(gb_batch *b, gb_conserved *out) {
+    gb::NvtxRange nvtx_("gb_batch_conserved");
     if (!b || !out) return GB_ERR_INVALID;
     const size_t ns = b->nsys();
     if (!b->forest) {
@@ -1471,7 +1515,11 @@ int gb_batch_conserved(gb_batch *b, gb_conserved *out) {
 
 int gb_batch_stats(gb_batch *b, gb_stats *out) {
     if (!b || !out) return GB_ERR_INVALID;
-    if (b->forest) return gb_get_stats(b->forest, out);
+    if (b->forest) {
+        gb_get_stats(b->forest, out);
+        out->steps = b->steps;
+        return GB_OK;
+    }
     std::memset(out, 0, sizeof(*out));
     for (gb_ctx *c : b->ctx) {
         gb_stats t;
@@ -1481,6 +1529,7 @@ int gb_batch_stats(gb_batch *b, gb_stats *out) {
         out->retries += t.retries, out->graph_steps += t.graph_steps, out->direct_steps += t.direct_steps;
         out->graph_captures += t.graph_captures;
     }
+    out->steps = b->steps;
     return GB_OK;
 }
 
@@ -1490,6 +1539,171 @@ int64_t gb_batch_launch_count(const gb_batch *b) {
     int64_t t = 0;
     for (const gb_ctx *c : b->ctx) t += c->ws.launches;
     return t;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Leaf parameter a context builds its trees with.
+int leaf_param(const gb_ctx *ctx) {
+    return ctx->cfg.mode == GB_MODE_ACCURATE && ctx->tune.leaf_s > 0 ? ctx->tune.leaf_s : ctx->cfg.s;
+}
+
+gb_checkpoint_info info_of(const gb_ctx *ctx, uint64_t n, uint64_t nsys, long long steps, double t) {
+    gb_checkpoint_info in{};
+    in.n = n;
+    in.nsys = nsys;
+    in.steps = steps;
+    in.t = t;
+    in.cfg = ctx->cfg;
+    in.cfg.device = 0;
+    in.leaf_s = leaf_param(ctx);
+    return in;
+}
+
+// Empty when a checkpoint written with f's configuration continues in ctx
+// with the same results; else what differs. Batches compare their masses
+// per system instead of m, and leave out the leaf parameter (their contexts
+// take it from the tuning cache per system size, the same on a reload).
+std::string config_mismatch(const gb_checkpoint_info &f, const gb_ctx *ctx, bool one_system) {
+    const gb_config &c = ctx->cfg;
+    constexpr int kResultFlags = GB_FLAG_P2P_NEWTON | GB_FLAG_M2L_CUDA_CORES | GB_FLAG_M2L_BF16;
+    auto num = [](double v) {
+        char buf[40];
+        std::snprintf(buf, sizeof buf, "%.17g", v);
+        return std::string(buf);
+    };
+    auto differs = [](const char *what, const std::string &a, const std::string &b) {
+        return std::string(what) + " " + a + " (context " + b + ")";
+    };
+    if (f.cfg.p != c.p) return differs("p", std::to_string(f.cfg.p), std::to_string(c.p));
+    if (f.cfg.s != c.s) return differs("s", std::to_string(f.cfg.s), std::to_string(c.s));
+    if (f.cfg.precision != c.precision)
+        return differs("precision", std::to_string(f.cfg.precision), std::to_string(c.precision));
+    if (f.cfg.mode != c.mode) return differs("mode", std::to_string(f.cfg.mode), std::to_string(c.mode));
+    if ((f.cfg.flags ^ c.flags) & kResultFlags)
+        return differs("flags", std::to_string(f.cfg.flags & kResultFlags), std::to_string(c.flags & kResultFlags));
+    if (f.cfg.eps != c.eps) return differs("eps", num(f.cfg.eps), num(c.eps));
+    if (f.cfg.G != c.G) return differs("G", num(f.cfg.G), num(c.G));
+    if (one_system && f.cfg.m != c.m) return differs("m", num(f.cfg.m), num(c.m));
+    if (one_system && f.leaf_s != leaf_param(ctx))
+        return differs("leaf_s", std::to_string(f.leaf_s), std::to_string(leaf_param(ctx)));
+    return std::string();
+}
+
+}  // namespace
+
+extern "C" {
+
+int gb_checkpoint_write(const char *path, const gb_checkpoint_info *info, const uint64_t *seg_offsets,
+                        const double *m_per_system, const double *x_aos, const double *v_aos) {
+    std::string err;
+    const int rc = gb::checkpoint_write(path, info, seg_offsets, m_per_system, x_aos, v_aos, err);
+    if (rc != GB_OK) g_create_error = err;
+    return rc;
+}
+
+int gb_checkpoint_read(const char *path, gb_checkpoint_info *info, uint64_t *seg_offsets, double *m_per_system,
+                       size_t nsys_cap, double *x_aos, double *v_aos, size_t n_cap) {
+    std::string err;
+    const int rc = gb::checkpoint_read(path, info, seg_offsets, m_per_system, nsys_cap, x_aos, v_aos, n_cap, err);
+    if (rc != GB_OK) g_create_error = err;
+    return rc;
+}
+
+int gb_checkpoint_save(gb_ctx *ctx, const char *path, double t) {
+    gb::NvtxRange nvtx_("gb_checkpoint_save");
+    if (!ctx) return GB_ERR_INVALID;
+    if (ctx->ws.forest()) return ctx->err = "a forest context is saved through its batch", GB_ERR_INVALID;
+    if (!ctx->have_state) return ctx->err = "no state uploaded", GB_ERR_STATE;
+    const uint64_t n = ctx->ws.n;
+    std::vector<double> x(3 * n + 1), v(3 * n + 1);
+    int rc = gb_download(ctx, x.data(), v.data());
+    if (rc != GB_OK) return rc;
+    const gb_checkpoint_info info = info_of(ctx, n, 1, ctx->state_steps, t);
+    std::string err;
+    rc = gb::checkpoint_write(path, &info, nullptr, nullptr, x.data(), v.data(), err);
+    if (rc != GB_OK) ctx->err = err;
+    return rc;
+}
+
+int gb_checkpoint_load(gb_ctx *ctx, const char *path, int flags, double *t) {
+    gb::NvtxRange nvtx_("gb_checkpoint_load");
+    if (!ctx) return GB_ERR_INVALID;
+    if (ctx->ws.forest()) return ctx->err = "a forest context is loaded through its batch", GB_ERR_INVALID;
+    gb_checkpoint_info info;
+    std::string err;
+    int rc = gb::checkpoint_read(path, &info, nullptr, nullptr, 0, nullptr, nullptr, 0, err);
+    if (rc != GB_OK) return ctx->err = err, rc;
+    if (info.nsys != 1)
+        return ctx->err = "the checkpoint holds " + std::to_string(info.nsys) + " systems; load it into a batch",
+               GB_ERR_INVALID;
+    if (info.n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
+    if (!(flags & GB_CHECKPOINT_ANY_CONFIG)) {
+        GB_TRY(cudaSetDevice(ctx->cfg.device));
+        rc = apply_tuning_cache(ctx, info.n);  // the leaf parameter the upload will use
+        if (rc != GB_OK) return rc;
+        const std::string d = config_mismatch(info, ctx, true);
+        if (!d.empty()) return ctx->err = "checkpoint configuration differs: " + d, GB_ERR_INVALID;
+    }
+    std::vector<double> x(3 * info.n + 1), v(3 * info.n + 1);
+    double m = 0;
+    rc = gb::checkpoint_read(path, &info, nullptr, &m, 1, x.data(), v.data(), info.n, err);
+    if (rc != GB_OK) return ctx->err = err, rc;
+    rc = gb_upload(ctx, x.data(), v.data(), info.n);
+    if (rc != GB_OK) return rc;
+    ctx->state_steps = info.steps;
+    if (t) *t = info.t;
+    return GB_OK;
+}
+
+int gb_batch_checkpoint_save(gb_batch *b, const char *path, double t) {
+    gb::NvtxRange nvtx_("gb_batch_checkpoint_save");
+    if (!b) return GB_ERR_INVALID;
+    const uint64_t n = b->off.back();
+    std::vector<double> x(3 * n + 1), v(3 * n + 1);
+    int rc = gb_batch_download(b, x.data(), v.data());
+    if (rc != GB_OK) return rc;
+    const gb_ctx *rep = b->forest ? b->forest : b->ctx[0];
+    const gb_checkpoint_info info = info_of(rep, n, b->nsys(), b->steps, t);
+    std::string err;
+    rc = gb::checkpoint_write(path, &info, b->off.data(), b->m.data(), x.data(), v.data(), err);
+    if (rc != GB_OK) b->err = err;
+    return rc;
+}
+
+int gb_batch_checkpoint_load(gb_batch *b, const char *path, int flags, double *t) {
+    gb::NvtxRange nvtx_("gb_batch_checkpoint_load");
+    if (!b) return GB_ERR_INVALID;
+    gb_checkpoint_info info;
+    std::string err;
+    int rc = gb::checkpoint_read(path, &info, nullptr, nullptr, 0, nullptr, nullptr, 0, err);
+    if (rc != GB_OK) return b->err = err, rc;
+    const size_t ns = b->nsys();
+    const uint64_t n = b->off.back();
+    if (info.nsys != ns || info.n != n)
+        return b->err = "the checkpoint holds " + std::to_string(info.nsys) + " systems and " + std::to_string(info.n) +
+                        " particles; the batch " + std::to_string(ns) + " and " + std::to_string(n),
+               GB_ERR_INVALID;
+    std::vector<uint64_t> seg(ns + 1);
+    std::vector<double> m(ns), x(3 * n + 1), v(3 * n + 1);
+    rc = gb::checkpoint_read(path, &info, seg.data(), m.data(), ns, x.data(), v.data(), n, err);
+    if (rc != GB_OK) return b->err = err, rc;
+    if (seg != b->off) return b->err = "checkpoint segment offsets differ from the batch's", GB_ERR_INVALID;
+    if (!(flags & GB_CHECKPOINT_ANY_CONFIG)) {
+        for (size_t k = 0; k < ns; ++k)
+            if (m[k] != b->m[k]) return b->err = "checkpoint mass of system " + std::to_string(k) + " differs", GB_ERR_INVALID;
+        const std::string d = config_mismatch(info, b->forest ? b->forest : b->ctx[0], false);
+        if (!d.empty()) return b->err = "checkpoint configuration differs: " + d, GB_ERR_INVALID;
+    }
+    rc = gb_batch_upload(b, x.data(), v.data());
+    if (rc != GB_OK) return rc;
+    b->steps = info.steps;
+    if (b->forest) b->forest->state_steps = info.steps;
+    for (gb_ctx *c : b->ctx) c->state_steps = info.steps;
+    if (t) *t = info.t;
+    return GB_OK;
 }
 
 int gb_tree_dump(gb_ctx *ctx, int64_t *ncells, int64_t *list_sizes, int32_t *level, int64_t *parent, int64_t *first_child,

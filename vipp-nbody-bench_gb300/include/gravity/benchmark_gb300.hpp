@@ -15,12 +15,22 @@
 // Problem requirements: N(), and initialize(x, v) filling the initial state
 // (the reference's Problem::initialize, problem.hpp:188-211); plus what the
 // two solvers read (p, s, epsilon, get_G, m, delta_t).
+//
+// Built with ENABLE_PRINT, run() writes the evaluated solver's positions as
+// the reference's ENABLE_PRINT build does (benchmark.hpp:15-20, 46-58):
+// before.csv from the initial state and after<T>.csv after each solve, one
+// "x,y,z" line per particle in the stream's default format.
 #pragma once
 
 #include <chrono>
 #include <cmath>
 #include <tuple>
 #include <vector>
+#ifdef ENABLE_PRINT
+#include <fstream>
+#include <sstream>
+#include <string>
+#endif
 
 namespace gravity {
 
@@ -76,6 +86,14 @@ struct BenchmarkGB300 {
         return {num / den, c};
     }
 
+#ifdef ENABLE_PRINT
+    template <class X>
+    static void print(const std::string &filename, const std::vector<X> &x) {
+        std::ofstream out(filename);
+        for (const auto &q : x) out << q.x() << "," << q.y() << "," << q.z() << "\n";
+    }
+#endif
+
     // The evaluated and comparator states may use different vector types
     // (the reference's benchmark_different_precision, benchmark.hpp:33-87).
     template <class EvalSolver, class RefSolver, class ProblemEval, class ProblemRef, class XE, class VE, class XR, class VR>
@@ -87,12 +105,20 @@ struct BenchmarkGB300 {
         r.t_set = t_set;
         for (const double t : t_set) {
             problem.initialize(x_eval, v_eval);
+#ifdef ENABLE_PRINT
+            print("before.csv", x_eval);
+#endif
             eval.preprocess(problem, x_eval, v_eval);
             const auto t0 = std::chrono::high_resolution_clock::now();
             eval.solve(problem, t, x_eval, v_eval);
             const auto t1 = std::chrono::high_resolution_clock::now();
             eval.postprocess(problem, x_eval, v_eval);
             r.eval_seconds += std::chrono::duration<double>(t1 - t0).count();
+#ifdef ENABLE_PRINT
+            std::ostringstream name;
+            name << "after" << t << ".csv";
+            print(name.str(), x_eval);
+#endif
 
             problem_ref.initialize(x_ref, v_ref);
             ref.preprocess(problem_ref, x_ref, v_ref);

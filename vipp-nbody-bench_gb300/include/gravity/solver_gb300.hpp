@@ -80,6 +80,27 @@ struct SolverGB300 final {
         return a;
     }
 
+    // Checkpoint of the current state with simulated time t (gb_checkpoint_save).
+    void save_checkpoint(const std::string &path, double t = 0) {
+        if (!ctx_) throw std::runtime_error("save_checkpoint before preprocess");
+        check(gb_checkpoint_save(ctx_, path.c_str(), t));
+    }
+
+    // Restart from a checkpoint: configures the context from problem, as
+    // preprocess does, and loads the saved state and step count (the file's
+    // configuration must match); returns the saved time. postprocess then
+    // gives the saved state.
+    template <class Problem>
+    double load_checkpoint(const Problem &problem, const std::string &path) {
+        configure(problem);
+        double t = 0;
+        check(gb_checkpoint_load(ctx_, path.c_str(), 0, &t));
+        gb_stats st{};
+        check(gb_get_stats(ctx_, &st));
+        n_ = static_cast<std::size_t>(st.n);
+        return t;
+    }
+
     gb_ctx *context() const { return ctx_; }
 
   private:

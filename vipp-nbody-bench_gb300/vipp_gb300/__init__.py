@@ -29,6 +29,7 @@ FLAG_SERIAL = 4
 FLAG_NO_GRAPH = 8
 FLAG_M2L_BF16 = 16
 FLAG_BATCH_CONTEXTS = 32
+CHECKPOINT_ANY_CONFIG = 1
 TIMER_CLASSES = ("tree", "operators", "p2m_m2m", "m2l", "l2l_l2p", "p2p", "rk4", "soften")
 
 # Every symbol include/vipp_gb300.h declares.
@@ -38,7 +39,9 @@ EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_uplo
            "gb_get_conserved", "gb_init_plummer", "gb_batch_create", "gb_batch_destroy", "gb_batch_last_error",
            "gb_batch_upload", "gb_batch_download", "gb_batch_rk4_step", "gb_batch_size", "gb_batch_system",
            "gb_set_tuning", "gb_get_tuning", "gb_tuning_lookup", "gb_init_clustered", "gb_batch_init_plummer",
-           "gb_batch_is_forest", "gb_batch_forest", "gb_batch_init_plummer_at", "gb_batch_accel", "gb_batch_conserved", "gb_batch_stats", "gb_batch_launch_count")
+           "gb_batch_is_forest", "gb_batch_forest", "gb_batch_init_plummer_at", "gb_batch_accel", "gb_batch_conserved", "gb_batch_stats", "gb_batch_launch_count",
+           "gb_checkpoint_write", "gb_checkpoint_read", "gb_checkpoint_save", "gb_checkpoint_load",
+           "gb_batch_checkpoint_save", "gb_batch_checkpoint_load")
 TUNING_FIELDS = ("p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s")
 TUNING_DEFAULT = {"p2p_blocks": 8, "p2p_blocks_conc": 8, "p2p_slice": 8192, "m2l_ctas_pct": 100, "serial": 0,
                   "leaf_s": 0}
@@ -61,7 +64,12 @@ class GbConserved(ctypes.Structure):
 
 class GbStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int64) for k in ("n", "ncells", "nleaves", "depth", "m2l_pairs", "p2p_pairs", "p2p_ranges", "retries",
-                                                        "graph_steps", "direct_steps", "graph_captures")]
+                                                        "graph_steps", "direct_steps", "graph_captures", "steps")]
+
+
+class GbCheckpointInfo(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint64), ("nsys", ctypes.c_uint64), ("steps", ctypes.c_int64), ("t", ctypes.c_double),
+                ("cfg", GbConfig), ("leaf_s", ctypes.c_int32)]
 
 
 _LIB = None
@@ -127,6 +135,13 @@ def load(path: str | None = None):
     lib.gb_batch_init_plummer.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
     lib.gb_batch_init_plummer_at.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
                                              ctypes.c_double, vp]
+    ci = ctypes.POINTER(GbCheckpointInfo)
+    lib.gb_checkpoint_write.argtypes = [ctypes.c_char_p, ci, vp, vp, vp, vp]
+    lib.gb_checkpoint_read.argtypes = [ctypes.c_char_p, ci, vp, vp, ctypes.c_size_t, vp, vp, ctypes.c_size_t]
+    lib.gb_checkpoint_save.argtypes = [vp, ctypes.c_char_p, ctypes.c_double]
+    lib.gb_checkpoint_load.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.gb_batch_checkpoint_save.argtypes = [vp, ctypes.c_char_p, ctypes.c_double]
+    lib.gb_batch_checkpoint_load.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     lib.gb_set_tuning.argtypes = [vp, ctypes.POINTER(GbTuning)]
     lib.gb_get_tuning.argtypes = [vp, ctypes.POINTER(GbTuning)]
     lib.gb_tuning_lookup.argtypes = [ctypes.c_char_p, ctypes.POINTER(GbConfig), ctypes.c_size_t,
@@ -161,6 +176,54 @@ class GB300Error(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"gb error {code}: {msg}")
         self.code = code
+
+
+def _config_dict(c: GbConfig) -> dict:
+    return {"p": c.p, "s": c.s, "eps": c.eps, "G": c.G, "m": c.m, "precision": c.precision, "flags": c.flags,
+            "mode": c.mode}
+
+
+def checkpoint_write(path: str, x, v, p=4, s=10, eps=0.01, G=1.0, m=1.0, precision="fp64", flags=0, mode="ref",
+                     seg=None, masses=None, steps=0, t=0.0, leaf_s=None):
+    """Write a checkpoint from host arrays (gb_checkpoint_write; no GPU
+    needed): x, v (n, 3), the configuration, segment offsets (nsys + 1, None
+    for one system), per-system masses, the step count and time."""
+    lib = load()
+    x, v = _aos(x), _aos(v)
+    n = x.shape[0]
+    seg_a = None if seg is None else np.ascontiguousarray(seg, dtype=np.uint64)
+    m_a = None if masses is None else np.ascontiguousarray(masses, dtype=np.float64)
+    info = GbCheckpointInfo()
+    info.n, info.nsys = n, 1 if seg_a is None else len(seg_a) - 1
+    info.steps, info.t = int(steps), float(t)
+    info.cfg = GbConfig(p, s, eps, G, m, PREC.get(precision, precision), 0, flags, MODE.get(mode, mode))
+    info.leaf_s = s if leaf_s is None else int(leaf_s)
+    rc = lib.gb_checkpoint_write(os.fsencode(path), ctypes.byref(info), _ptr(seg_a), _ptr(m_a), _ptr(x), _ptr(v))
+    if rc != GB_OK:
+        raise GB300Error(rc, lib.gb_last_error(None).decode())
+
+
+def checkpoint_read(path: str, arrays: bool = True) -> dict:
+    """Read a checkpoint (gb_checkpoint_read; no GPU needed): a dict with n,
+    nsys, steps, t, config, leaf_s and, with arrays=True (check word
+    verified), seg, masses, x and v."""
+    lib = load()
+    info = GbCheckpointInfo()
+    fpath = os.fsencode(path)
+    rc = lib.gb_checkpoint_read(fpath, ctypes.byref(info), None, None, 0, None, None, 0)
+    if rc != GB_OK:
+        raise GB300Error(rc, lib.gb_last_error(None).decode())
+    out = {"n": int(info.n), "nsys": int(info.nsys), "steps": int(info.steps), "t": float(info.t),
+           "config": _config_dict(info.cfg), "leaf_s": int(info.leaf_s)}
+    if arrays:
+        n, ns = out["n"], out["nsys"]
+        seg, masses = np.zeros(ns + 1, np.uint64), np.zeros(ns)
+        x, v = np.zeros((n, 3)), np.zeros((n, 3))
+        rc = lib.gb_checkpoint_read(fpath, ctypes.byref(info), _ptr(seg), _ptr(masses), ns, _ptr(x), _ptr(v), n)
+        if rc != GB_OK:
+            raise GB300Error(rc, lib.gb_last_error(None).decode())
+        out.update(seg=seg, masses=masses, x=x, v=v)
+    return out
 
 
 class Solver:
@@ -304,6 +367,19 @@ class Solver:
     def enable_timing(self, on=True):
         self._check(self.lib.gb_enable_timing(self.h, int(on)))
 
+    def save_checkpoint(self, path: str, t: float = 0.0):
+        """Write the state, step count and time t to a checkpoint file."""
+        self._check(self.lib.gb_checkpoint_save(self.h, os.fsencode(path), float(t)))
+
+    def load_checkpoint(self, path: str, any_config: bool = False) -> float:
+        """Replace the state from a checkpoint (configuration checked unless
+        any_config); returns the saved time."""
+        t = ctypes.c_double()
+        self._check(self.lib.gb_checkpoint_load(self.h, os.fsencode(path), CHECKPOINT_ANY_CONFIG if any_config else 0,
+                                                ctypes.byref(t)))
+        self.n = checkpoint_read(path, arrays=False)["n"]
+        return t.value
+
     def kernel_times(self) -> dict:
         n = len(TIMER_CLASSES)
         ms = np.zeros(n)
@@ -415,6 +491,17 @@ class Batch:
 
     def step(self, dt):
         self._check(self.lib.gb_batch_rk4_step(self.h, float(dt)))
+
+    def save_checkpoint(self, path: str, t: float = 0.0):
+        """Write every system's state, the step count and time t to a checkpoint file."""
+        self._check(self.lib.gb_batch_checkpoint_save(self.h, os.fsencode(path), float(t)))
+
+    def load_checkpoint(self, path: str, any_config: bool = False) -> float:
+        """Replace the state from a checkpoint of this batch's systems; returns the saved time."""
+        t = ctypes.c_double()
+        self._check(self.lib.gb_batch_checkpoint_load(self.h, os.fsencode(path),
+                                                      CHECKPOINT_ANY_CONFIG if any_config else 0, ctypes.byref(t)))
+        return t.value
 
     @property
     def forest(self) -> bool:

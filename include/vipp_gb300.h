@@ -292,6 +292,9 @@ typedef struct gb_tuning {
     int serial;          /* 1: the near field after the far field on one stream (default 0) */
     int leaf_s;          /* GB_MODE_ACCURATE: leaf parameter used instead of the config's s
                             (0: the config's s) */
+    int p2p_occupancy;   /* mixed P2P kernel build: 8 (registers budgeted for 8 blocks
+                            per SM, default; 0 means 8) or 6 (80 registers, more work
+                            in flight per warp); same results either way */
 } gb_tuning;
 GB_API int gb_set_tuning(gb_ctx *ctx, const gb_tuning *t);
 GB_API int gb_get_tuning(const gb_ctx *ctx, gb_tuning *out);

@@ -45,7 +45,8 @@ CFG = dict(p=8, s=64, eps=0.005, precision="mixed")
 
 
 @pytest.mark.parametrize("tune", [{"p2p_blocks": 4}, {"p2p_blocks_conc": 0}, {"p2p_blocks_conc": 3, "m2l_ctas_pct": 50},
-                                  {"serial": 1}, {"m2l_ctas_pct": 10}])
+                                  {"serial": 1}, {"m2l_ctas_pct": 10}, {"p2p_occupancy": 6},
+                                  {"p2p_occupancy": 6, "p2p_blocks_conc": 2}])
 def test_launch_shapes_are_bit_identical(plummer64k, tune):
     import vipp_gb300
     x, v = plummer64k

@@ -48,7 +48,8 @@ def test_last_entry_wins_and_comments(tmp_path):
 @pytest.mark.parametrize("line", ["p=8 precision=1 mode=0 m2l_bf16=1 log2n=22 p2p_slice=100",  # out of range
                                   "p=8 precision=1 mode=0 m2l_bf16=1 log2n=22 bogus=3",         # unknown key
                                   "p=8 precision=1 mode=0 m2l_bf16=1 p2p_blocks=4",            # no bucket
-                                  "p=8 precision=1 mode=0 m2l_bf16=1 log2n=22 p2p_blocks=x"])  # not a number
+                                  "p=8 precision=1 mode=0 m2l_bf16=1 log2n=22 p2p_blocks=x",   # not a number
+                                  "p=8 precision=1 mode=0 m2l_bf16=1 log2n=22 p2p_occupancy=7"])  # no such build
 def test_malformed_entries_are_rejected(tmp_path, line):
     vipp_gb300.load()
     path = tmp_path / "tune.txt"
@@ -76,3 +77,4 @@ def test_shipped_cache_parses():
     assert acc is not None and acc["leaf_s"] >= 64
     ref = vipp_gb300.tuning_lookup(path, 1 << 22, 8, "mixed", "ref", vipp_gb300.FLAG_M2L_BF16)
     assert ref is not None and ref["p2p_blocks_conc"] < ref["p2p_blocks"]  # P2P beside the M2L on a share of the SMs
+    assert ref["p2p_occupancy"] == 6 and acc["p2p_occupancy"] == 8

@@ -51,7 +51,7 @@ struct gb_ctx {
     long long graph_steps = 0, direct_steps = 0, graph_captures = 0;
     std::vector<gb::PendingTimer> pending;
     std::vector<cudaEvent_t> free_events;
-    gb_tuning tune{8, 8, gb::kSliceSources, 100, 0, 0};
+    gb_tuning tune{8, 8, gb::kSliceSources, 100, 0, 0, 8};
     int tune_log2n = -1;  // size bucket the tuning cache was last applied for
     long long *d_targets = nullptr;
     size_t targets_cap = 0;
@@ -118,6 +118,7 @@ void apply_config(gb_ctx *ctx) {
     ws.serial = (ctx->cfg.flags & GB_FLAG_SERIAL) != 0 || ctx->tune.serial != 0;
     ws.p2p_blocks = static_cast<unsigned>(ctx->tune.p2p_blocks);
     ws.p2p_blocks_conc = static_cast<unsigned>(ctx->tune.p2p_blocks_conc);
+    ws.p2p_occ = ctx->tune.p2p_occupancy == 6 ? 6 : 8;
     ws.p2p_slice = static_cast<unsigned>(ctx->tune.p2p_slice);
     ws.m2l_ctas_pct = ctx->tune.m2l_ctas_pct;
     ws.accurate = ctx->cfg.mode == GB_MODE_ACCURATE;
@@ -517,6 +518,8 @@ int validate_tuning(const gb_tuning *t, std::string &msg) {
     if (t->m2l_ctas_pct < 10 || t->m2l_ctas_pct > 100) return msg = "m2l_ctas_pct must be in 10..100", GB_ERR_INVALID;
     if (t->serial != 0 && t->serial != 1) return msg = "serial must be 0 or 1", GB_ERR_INVALID;
     if (t->leaf_s < 0) return msg = "leaf_s must be >= 0", GB_ERR_INVALID;
+    if (t->p2p_occupancy != 0 && t->p2p_occupancy != 6 && t->p2p_occupancy != 8)
+        return msg = "p2p_occupancy must be 6 or 8 (0: 8)", GB_ERR_INVALID;
     return GB_OK;
 }
 
@@ -534,7 +537,8 @@ int tuning_from_file(const char *path, const gb_config *cfg, size_t n, gb_tuning
     const long want[5] = {cfg->p, cfg->precision, cfg->mode, (cfg->flags & GB_FLAG_M2L_BF16) ? 1 : 0,
                           static_cast<long>(floor_log2(n))};
     static const char *kKeys[5] = {"p", "precision", "mode", "m2l_bf16", "log2n"};
-    static const char *kFields[6] = {"p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s"};
+    static const char *kFields[7] = {"p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s",
+                                     "p2p_occupancy"};
     char line[1024];
     int rc = GB_ERR_STATE;
     int lineno = 0;
@@ -542,8 +546,9 @@ int tuning_from_file(const char *path, const gb_config *cfg, size_t n, gb_tuning
         ++lineno;
         if (char *h = std::strchr(line, '#')) *h = 0;
         long key[5] = {-1, -1, -1, -1, -1};
-        gb_tuning t{8, 8, gb::kSliceSources, 100, 0, 0};
-        int *fld[6] = {&t.p2p_blocks, &t.p2p_blocks_conc, &t.p2p_slice, &t.m2l_ctas_pct, &t.serial, &t.leaf_s};
+        gb_tuning t{8, 8, gb::kSliceSources, 100, 0, 0, 8};
+        int *fld[7] = {&t.p2p_blocks, &t.p2p_blocks_conc, &t.p2p_slice, &t.m2l_ctas_pct, &t.serial, &t.leaf_s,
+                       &t.p2p_occupancy};
         bool any = false, bad = false;
         for (char *tok = std::strtok(line, " \t\r\n"); tok; tok = std::strtok(nullptr, " \t\r\n")) {
             char *eq = std::strchr(tok, '=');
@@ -561,7 +566,7 @@ int tuning_from_file(const char *path, const gb_config *cfg, size_t n, gb_tuning
             bool known = false;
             for (int k = 0; k < 5; ++k)
                 if (!std::strcmp(tok, kKeys[k])) key[k] = v, known = true;
-            for (int k = 0; k < 6; ++k)
+            for (int k = 0; k < 7; ++k)
                 if (!std::strcmp(tok, kFields[k])) *fld[k] = static_cast<int>(v), known = true;
             if (!known) {
                 bad = true;

@@ -126,12 +126,15 @@ __device__ __forceinline__ void pair_f32(const float4 s, float tx, float ty, flo
     bz = fmaf(dz, f, bz);
 }
 
-#ifndef GB_P2P_MIN_BLOCKS
-#define GB_P2P_MIN_BLOCKS 8  // 8 resident blocks per SM (62 registers, no spills): measured 7% faster than 6
-#endif
-
-template <bool kNewton, bool kSoft>
-__global__ void __launch_bounds__(kP2PWarps * 32, GB_P2P_MIN_BLOCKS) k_p2p_f32(const int4 *__restrict__ chunks, const unsigned *counts,
+// Register budgets of the mixed-precision kernel (tuning knob p2p_occupancy):
+// compiled for 8 resident blocks per SM (64 registers) or for 6 (80
+// registers: more pair terms in flight per warp, which pays while P2P shares
+// the SMs with the far field on 2 blocks per SM). Both fit beside the far
+// field's kernels (a 96-register build kept the cluster M2M from starting
+// beside P2P and serialised the two). The same arithmetic either way, so
+// the same results bit for bit.
+template <bool kNewton, bool kSoft, int kMinBlocks>
+__global__ void __launch_bounds__(kP2PWarps * 32, kMinBlocks) k_p2p_f32(const int4 *__restrict__ chunks, const unsigned *counts,
                                                             unsigned *queue, const int *__restrict__ leaves,
                                                             const double *__restrict__ c_ctr,
                                                             const TreeInfo *__restrict__ info, const int *__restrict__ c_sys,
@@ -446,16 +449,26 @@ void near_potential(Workspace &ws, double *phiv) {
 // launches (on any streams) may drain the same queue, each item is taken once.
 // p2p_finish adds the slices of split items after all of them.
 
+template <int kMinBlocks>
+void p2p_f32_carveout() {
+    // keep the SMs that run P2P configured for full shared memory, so far-field
+    // kernels (the tensor-core M2L: up to 206 KB) can start beside the P2P blocks
+    cudaFuncSetAttribute(k_p2p_f32<false, true, kMinBlocks>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_p2p_f32<false, false, kMinBlocks>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_p2p_f32<true, true, kMinBlocks>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_p2p_f32<true, false, kMinBlocks>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+}
+
 void p2p_pass(Workspace &ws, unsigned per_sm) {
     if (per_sm == 0) return;
     timer_begin(ws, kTP2P);
 #if GB_P2P_CARVEOUT_MAX
-    // keep the SMs that run P2P configured for full shared memory, so far-field
-    // kernels (the tensor-core M2L: up to 206 KB) can start beside the P2P blocks
-    cudaFuncSetAttribute(k_p2p_f32<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_p2p_f32<false, false>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_p2p_f32<true, true>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_p2p_f32<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    p2p_f32_carveout<8>();
+    p2p_f32_carveout<6>();
 #endif
     const unsigned gs = capped_grid(static_cast<unsigned>(ws.num_sms) * per_sm, ceil_div(ws.n, 128));
     const bool soft = ws.eps > 0;
@@ -464,11 +477,17 @@ void p2p_pass(Workspace &ws, unsigned per_sm) {
         const float Gm = ws.forest() ? 1.0f : static_cast<float>(ws.G * ws.m);  // a forest scales in p2p_finish
         auto *o = static_cast<float *>(ws.nearf);
         auto *pf = static_cast<float *>(ws.part);
-#define GB_P2P32(NW, SF)                                                                                                \
-    k_p2p_f32<NW, SF><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.leaves, ws.c_ctr, ws.info, \
-                                                        forest_cells(ws), ws.rng_off, ws.rng_len, ws.ranges, ws.ph, ws.pl, \
-                                                        ws.src_total, pf, \
-                                                        Gm, eps2, o, ws.n)
+#define GB_P2P32_MB(NW, SF, MB)                                                                                  \
+    k_p2p_f32<NW, SF, MB><<<gs, kP2PWarps * 32, 0, ws.st>>>(ws.chunks, ws.d_counts, ws.queue, ws.leaves, ws.c_ctr,    \
+                                                            ws.info, forest_cells(ws), ws.rng_off, ws.rng_len,        \
+                                                            ws.ranges, ws.ph, ws.pl, ws.src_total, pf, Gm, eps2, o, ws.n)
+#define GB_P2P32(NW, SF)             \
+    do {                             \
+        if (ws.p2p_occ == 6)         \
+            GB_P2P32_MB(NW, SF, 6);  \
+        else                         \
+            GB_P2P32_MB(NW, SF, 8);  \
+    } while (0)
         if (ws.p2p_newton) {
             if (soft)
                 GB_P2P32(true, true);
@@ -481,6 +500,7 @@ void p2p_pass(Workspace &ws, unsigned per_sm) {
                 GB_P2P32(false, false);
         }
 #undef GB_P2P32
+#undef GB_P2P32_MB
     } else {
         const double Gm = ws.forest() ? 1.0 : ws.G * ws.m, eps2 = ws.eps * ws.eps;
         auto *o = static_cast<double *>(ws.nearf);

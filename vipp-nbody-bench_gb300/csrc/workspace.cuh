@@ -51,6 +51,7 @@ struct Workspace {
     // tuning knobs (gb_set_tuning / the tuning cache; the defaults are the measured best at 4M)
     unsigned p2p_blocks = 8;        // P2P blocks per SM when it runs alone (or after the far field)
     unsigned p2p_blocks_conc = 8;   // P2P blocks per SM launched beside the far field
+    int p2p_occ = 8;                // blocks per SM the mixed P2P kernel's registers are budgeted for (8 or 6)
     unsigned p2p_slice = kSliceSources;  // near-field sources per P2P work item
     int m2l_ctas_pct = 100;         // tensor-core M2L CTAs, percent of the SMs (one persistent CTA per SM)
 

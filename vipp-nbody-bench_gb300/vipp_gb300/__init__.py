@@ -42,9 +42,9 @@ EXPORTS = ("gb_create", "gb_destroy", "gb_last_error", "gb_set_config", "gb_uplo
            "gb_batch_is_forest", "gb_batch_forest", "gb_batch_init_plummer_at", "gb_batch_accel", "gb_batch_conserved", "gb_batch_stats", "gb_batch_launch_count",
            "gb_checkpoint_write", "gb_checkpoint_read", "gb_checkpoint_save", "gb_checkpoint_load",
            "gb_batch_checkpoint_save", "gb_batch_checkpoint_load")
-TUNING_FIELDS = ("p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s")
+TUNING_FIELDS = ("p2p_blocks", "p2p_blocks_conc", "p2p_slice", "m2l_ctas_pct", "serial", "leaf_s", "p2p_occupancy")
 TUNING_DEFAULT = {"p2p_blocks": 8, "p2p_blocks_conc": 8, "p2p_slice": 8192, "m2l_ctas_pct": 100, "serial": 0,
-                  "leaf_s": 0}
+                  "leaf_s": 0, "p2p_occupancy": 8}
 
 
 class GbConfig(ctypes.Structure):

@@ -10,6 +10,8 @@ The knobs are the gb_tuning fields of include/vipp_gb300.h:
   m2l_ctas_pct     tensor-core M2L CTAs as a percent of the SMs (its tile
                    schedule: how many persistent CTAs share the 128-target tiles)
   serial           near field after the far field instead of beside it
+  p2p_occupancy    mixed P2P kernel build: registers budgeted for 8 or for
+                   6 resident blocks per SM
   leaf_s           leaf capacity, in the accurate mode only (the reference
                    mode keeps the reference's s so its trees stay the
                    reference's); candidates are >= the configured s, whose
@@ -40,6 +42,7 @@ CANDIDATES = {
     "p2p_slice": (2048, 4096, 8192, 16384, 32768),
     "m2l_ctas_pct": (50, 75, 100),
     "serial": (0, 1),
+    "p2p_occupancy": (8, 6),
 }
 
 

@@ -400,6 +400,9 @@ def parse_args(argv=None):
     ap.add_argument("--no-tuning-cache", action="store_true",
                     help="ignore the library's tuning cache (vipp_gb300/tuning_gb300.txt): every line at the defaults")
     ap.add_argument("--tune-out", default=None, help="append the tuned entry to this tuning cache file")
+    ap.add_argument("--p2p-occupancy", type=int, default=None, choices=[6, 8],
+                    help="override the tuning's mixed P2P kernel build for the main line (registers budgeted for "
+                         "8 or for 6 blocks per SM)")
     ap.add_argument("--drift-steps", type=int, default=None,
                     help="untimed steps of the total-energy drift run (default: the 4M Plummer configuration's 100; 0 skips)")
     ap.add_argument("--acc-p", type=int, default=10, help="expansion order of the accurate-mode line")
@@ -457,6 +460,8 @@ def main():
     sol = vipp_gb300.Solver(p=args.p, s=args.s, eps=args.eps, G=1.0, m=m, precision=args.precision, device=local,
                             flags=args.flags)
     sol.preprocess(x, v)
+    if args.p2p_occupancy is not None:
+        sol.set_tuning(p2p_occupancy=args.p2p_occupancy)
     tuning_used = sol.tuning()
     for _ in range(args.warmup):
         sol.solve(args.dt)

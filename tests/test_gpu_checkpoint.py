@@ -56,11 +56,12 @@ def test_configuration_is_checked_and_a_refused_load_keeps_the_state(tmp_path):
         with solver(**kw) as b:
             b.init_plummer(1000, seed=9)
             x0, v0 = b.postprocess()
+            t0 = b.tuning()
             with pytest.raises(vipp_gb300.GB300Error) as ei:
                 b.load_checkpoint(path)
             assert ei.value.code == vipp_gb300.GB_ERR_INVALID and word in str(ei.value), str(ei.value)
             x1, v1 = b.postprocess()
-            assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
+            assert np.array_equal(x0, x1) and np.array_equal(v0, v1) and b.tuning() == t0
     with solver(p=4) as b:  # any_config: the state loads into another configuration
         b.load_checkpoint(path, any_config=True)
         assert b.n == 4000 and b.stats()["steps"] == 1

@@ -1555,6 +1555,20 @@ int leaf_param(const gb_ctx *ctx) {
     return ctx->cfg.mode == GB_MODE_ACCURATE && ctx->tune.leaf_s > 0 ? ctx->tune.leaf_s : ctx->cfg.s;
 }
 
+// The leaf parameter an upload of n particles would give the context (the
+// tuning cache's entry for n's bucket, when the upload would apply one),
+// without applying anything.
+int leaf_param_for(const gb_ctx *ctx, size_t n) {
+    gb_tuning t = ctx->tune;
+    const char *path = std::getenv("VIPP_GB_TUNE_FILE");
+    if (path && *path && n && floor_log2(n) != ctx->tune_log2n) {
+        gb_tuning ft{};
+        std::string msg;
+        if (tuning_from_file(path, &ctx->cfg, n, &ft, msg) == GB_OK) t = ft;
+    }
+    return ctx->cfg.mode == GB_MODE_ACCURATE && t.leaf_s > 0 ? t.leaf_s : ctx->cfg.s;
+}
+
 gb_checkpoint_info info_of(const gb_ctx *ctx, uint64_t n, uint64_t nsys, long long steps, double t) {
     gb_checkpoint_info in{};
     in.n = n;
@@ -1571,7 +1585,7 @@ gb_checkpoint_info info_of(const gb_ctx *ctx, uint64_t n, uint64_t nsys, long lo
 // with the same results; else what differs. Batches compare their masses
 // per system instead of m, and leave out the leaf parameter (their contexts
 // take it from the tuning cache per system size, the same on a reload).
-std::string config_mismatch(const gb_checkpoint_info &f, const gb_ctx *ctx, bool one_system) {
+std::string config_mismatch(const gb_checkpoint_info &f, const gb_ctx *ctx, bool one_system, int leaf_now) {
     const gb_config &c = ctx->cfg;
     constexpr int kResultFlags = GB_FLAG_P2P_NEWTON | GB_FLAG_M2L_CUDA_CORES | GB_FLAG_M2L_BF16;
     auto num = [](double v) {
@@ -1592,8 +1606,7 @@ std::string config_mismatch(const gb_checkpoint_info &f, const gb_ctx *ctx, bool
     if (f.cfg.eps != c.eps) return differs("eps", num(f.cfg.eps), num(c.eps));
     if (f.cfg.G != c.G) return differs("G", num(f.cfg.G), num(c.G));
     if (one_system && f.cfg.m != c.m) return differs("m", num(f.cfg.m), num(c.m));
-    if (one_system && f.leaf_s != leaf_param(ctx))
-        return differs("leaf_s", std::to_string(f.leaf_s), std::to_string(leaf_param(ctx)));
+    if (one_system && f.leaf_s != leaf_now) return differs("leaf_s", std::to_string(f.leaf_s), std::to_string(leaf_now));
     return std::string();
 }
 
@@ -1646,10 +1659,7 @@ int gb_checkpoint_load(gb_ctx *ctx, const char *path, int flags, double *t) {
                GB_ERR_INVALID;
     if (info.n > 0x7fffffffu) return ctx->err = "too many particles", GB_ERR_INVALID;
     if (!(flags & GB_CHECKPOINT_ANY_CONFIG)) {
-        GB_TRY(cudaSetDevice(ctx->cfg.device));
-        rc = apply_tuning_cache(ctx, info.n);  // the leaf parameter the upload will use
-        if (rc != GB_OK) return rc;
-        const std::string d = config_mismatch(info, ctx, true);
+        const std::string d = config_mismatch(info, ctx, true, leaf_param_for(ctx, info.n));
         if (!d.empty()) return ctx->err = "checkpoint configuration differs: " + d, GB_ERR_INVALID;
     }
     std::vector<double> x(3 * info.n + 1), v(3 * info.n + 1);
@@ -1699,7 +1709,7 @@ int gb_batch_checkpoint_load(gb_batch *b, const char *path, int flags, double *t
     if (!(flags & GB_CHECKPOINT_ANY_CONFIG)) {
         for (size_t k = 0; k < ns; ++k)
             if (m[k] != b->m[k]) return b->err = "checkpoint mass of system " + std::to_string(k) + " differs", GB_ERR_INVALID;
-        const std::string d = config_mismatch(info, b->forest ? b->forest : b->ctx[0], false);
+        const std::string d = config_mismatch(info, b->forest ? b->forest : b->ctx[0], false, 0);
         if (!d.empty()) return b->err = "checkpoint configuration differs: " + d, GB_ERR_INVALID;
     }
     rc = gb_batch_upload(b, x.data(), v.data());

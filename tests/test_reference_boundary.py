@@ -4,8 +4,9 @@ linked (no GPU needed; the programs are not run):
   * tests/cpp/test_reference_types.cpp: gravity::SolverGB300 instantiated with
     gravity::Problem and gravity::Vector (gravity/include/problem.hpp:32-302);
   * the reference's own gravity/src/main.cpp, unmodified, with the Solver
-    alias (gravity/include/solver.hpp:6-9) pointed at SolverGB300 the way
-    INTEGRATION.md section 1 describes, so Benchmark::benchmark
+    alias (gravity/include/solver.hpp:6-9) pointed at SolverGB300 by a
+    replacement solver.hpp found first on the include path (SHIM below), so
+    Benchmark::benchmark
     (benchmark.hpp:91-175) drives it; also with GRAVITY_FLOAT and with
     ENABLE_DIFFERENT_PRECISION (benchmark_different_precision, benchmark.hpp:33-87).
 
